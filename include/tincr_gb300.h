@@ -1,0 +1,157 @@
+/*
+ * tincr_gb300 — C ABI of the GB300 (sm_103a) linear-response excited-state path of tincr.
+ *
+ * One context owns one GPU and the device-resident state of one molecular system (MO coefficients,
+ * overlap, gamma matrices, Davidson subspace).  Every array crossing this boundary is a HOST
+ * pointer to C-order (row-major) float64 data unless stated otherwise; the library copies in and
+ * out.  Every call returns a tincr_status; tincr_last_error() gives a message for the last failure.
+ *
+ * Each entry point names the tincr interface it replaces (file:line inside the tincr project).
+ * Calls on one context are not thread safe; distinct contexts are independent (the per-instance
+ * reentrancy that tincr's rayon-parallel `Monomer::run_tda` calls need, src/fmo/lcmo/basis.rs:462).
+ */
+#ifndef TINCR_GB300_H
+#define TINCR_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct tincr_ctx tincr_ctx;
+
+typedef enum {
+    TINCR_OK = 0,
+    TINCR_NOT_CONVERGED = 1, /* Davidson reached max_iter (DavidsonError, solvers/davidson.rs:28-37) */
+    TINCR_NONFINITE = 2,     /* NaN/Inf found in inputs or in an iterate                          */
+    TINCR_BAD_ARG = 3,       /* wrong sizes, null pointers, call order                            */
+    TINCR_CUDA_ERR = 4,      /* CUDA runtime error                                                 */
+    TINCR_NO_DEVICE = 5,     /* no usable sm_103 device                                            */
+    TINCR_CG_MAXITER = 6     /* Z-vector CG hit its iteration cap (helpers.rs:1146 stops silently) */
+} tincr_status;
+
+/* Arithmetic of the two-electron contractions (Coulomb + long-range exchange) of A.X.
+ * Subspace Rayleigh-Ritz, orthogonalisation, residual norms and CG scalars are always FP64. */
+typedef enum {
+    TINCR_PREC_FP64 = 0,      /* plain FP64 drop-in                                             */
+    TINCR_PREC_BF16X3 = 1     /* split-BF16 (hi*hi + hi*lo + lo*hi) tensor cores, FP32 accumulate */
+} tincr_precision;
+
+/* ---- context --------------------------------------------------------------------------------- */
+
+/* Create a context on CUDA device `device`.  Fails with TINCR_NO_DEVICE if it is not sm_103. */
+int tincr_ctx_create(tincr_ctx **out, int device);
+int tincr_ctx_destroy(tincr_ctx *ctx);
+const char *tincr_last_error(const tincr_ctx *ctx);
+/* Device time (ms, CUDA events) of the last tincr_tda_solve / tincr_tda_products call and the
+ * number of kernels it launched. */
+int tincr_last_timing(const tincr_ctx *ctx, double *ms, long long *kernel_launches);
+
+/* Statistics of the last tincr_tda_solve: A.X products evaluated (tincr's compute_products
+ * columns), subspace collapses and the final largest residual norm. */
+int tincr_last_solve_stats(const tincr_ctx *ctx, long long *n_products, int *n_collapses, double *max_residual);
+
+/* Kernel families timed with CUDA events when profiling is on. */
+typedef enum {
+    TINCR_KF_AO_EXCHANGE = 0,  /* the two n^2 v contractions of the LC exchange (A.X steps 2 and 4) */
+    TINCR_KF_AO_TRANSFORM = 1, /* MO<->AO half transforms of A.X (steps 1 and 5)                    */
+    TINCR_KF_SUBSPACE = 2,     /* Davidson projections, Ritz vectors, residuals, orthogonalisation  */
+    TINCR_KF_OTHER = 3,        /* Coulomb, packing, transition charges, small kernels              */
+    TINCR_KF_COUNT = 4
+} tincr_kernel_family;
+
+/* Turn per-family kernel timing on (1) or off (0); turning it on clears the statistics. */
+int tincr_set_profiling(tincr_ctx *ctx, int enable);
+/* Accumulated device ms, launches, algorithmic FLOPs and algorithmic bytes of one family. */
+int tincr_kernel_stats(const tincr_ctx *ctx, int family, double *ms, long long *launches, double *flops,
+                       double *bytes);
+
+/* ---- transition charges ---------------------------------------------------------------------- */
+
+/* Replaces `trans_charges(n_atoms, atoms, orbs, s, occ_indices, virt_indices)`
+ * (src/excited_states/transition_charges.rs:8-98).  Occupied and virtual orbitals are the
+ * contiguous MO ranges [occ0, occ0+n_occ) and [virt0, virt0+n_virt).
+ *   orbs_per_atom [n_atoms]; C, S [n_orb*n_orb];
+ *   q_ov [n_atoms*n_occ*n_virt] (index A*o*v + i*v + a), q_oo [n_atoms*o*o], q_vv [n_atoms*v*v];
+ *   any of q_ov/q_oo/q_vv may be NULL when not wanted. */
+int tincr_trans_charges(tincr_ctx *ctx, int n_atoms, const int *orbs_per_atom, int n_orb,
+                        const double *C, const double *S, int occ0, int n_occ, int virt0, int n_virt,
+                        double *q_ov, double *q_oo, double *q_vv);
+
+/* ---- TDA / LC-TDA ------------------------------------------------------------------------------ */
+
+/* Load one system's ground state onto the device: the inputs `System::prepare_tda`
+ * (src/excited_states/tda/system.rs:10-52) reads from Properties.
+ *   C, S [n_orb*n_orb]; orbe [n_orb]; gamma [n_atoms*n_atoms];
+ *   gamma_lr [n_atoms*n_atoms] or NULL for a calculation without long-range correction;
+ *   xyz [n_atoms*3] bohr (for transition dipoles, src/excited_states/tda/moments.rs:7-15).
+ * The occupied block is MOs [0, n_occ), the virtual block [n_occ, n_occ+n_virt)
+ * (src/initialization/system.rs:132-140). */
+int tincr_tda_setup(tincr_ctx *ctx, int n_atoms, const int *orbs_per_atom, int n_orb,
+                    const double *C, const double *S, const double *orbe, int n_occ, int n_virt,
+                    const double *gamma, const double *gamma_lr, const double *xyz);
+
+/* Replaces `DavidsonEngine::compute_products` for a System/Monomer
+ * (src/excited_states/solvers/mod.rs:280-369, :59-148):
+ *   AX = omega o X + 2 q_ov^T gamma q_ov X - K_lr X
+ * X and AX are [n_occ*n_virt, k] (column j = trial vector j, tincr's guess layout).  Unlike the
+ * trait, no product cache is kept here: the caller passes exactly the vectors to multiply. */
+int tincr_tda_products(tincr_ctx *ctx, int k, const double *X, double *AX, int precision);
+
+/* Replaces `System::run_tda(n_roots, max_iter, tolerance)` (src/excited_states/tda/mod.rs:74-131)
+ * with `Davidson::new` (src/excited_states/solvers/davidson.rs:53-185) and `initial_subspace`
+ * (solvers/utils.rs:17-26) on the device.
+ *   energies [n_roots]; coefficients [n_occ*n_virt, n_roots] (tincr's ci_coefficients layout);
+ *   osc [n_roots] oscillator strengths; tr_dip [3*n_roots] (row c = x,y,z component);
+ *   q_trans [n_atoms*n_roots] or NULL; iterations: Davidson iterations done.
+ * Returns TINCR_NOT_CONVERGED when max_iter is reached (tincr unwraps a DavidsonError). */
+int tincr_tda_solve(tincr_ctx *ctx, int n_roots, int max_iter, double tolerance, int precision,
+                    double *energies, double *coefficients, double *osc, double *tr_dip,
+                    double *q_trans, int *iterations);
+
+/* ---- analytic gradients ---------------------------------------------------------------------- */
+
+typedef enum {
+    /* tincr's formulas: Z-vector with the TDA matrix A for LC (mult_av_lc, helpers.rs:1384-1438),
+     * Hav for W_ij[Z], same-element SK derivatives with the moving atom as centre 1 (h0_and_s.rs:218) */
+    TINCR_GRAD_REFERENCE = 0,
+    /* derivative of the energies tincr computes: (A+B) Z-vector and H+[Z] for LC, SK derivatives
+     * in the centre order H0 is built with (lower index first for same-element pairs) */
+    TINCR_GRAD_EXACT = 1
+} tincr_grad_variant;
+
+/* Parameter tables for the gradient kernels (the SK splines, gamma and repulsion tincr's
+ * SlaterKoster / RepulsivePotential / GammaFunction hold; src/initialization/parameters.rs:127-372).
+ *   kind_z [n_kinds] atomic numbers; kind_norb [n_kinds] (1 or 4); kind_l, kind_m [n_kinds*4]
+ *   quantum numbers of each orbital (s, p_y, p_z, p_x order); kind_hubbard [n_kinds];
+ *   kind_occ [n_kinds*4] reference (neutral atom) occupations per orbital (P0);
+ *   sk_knots [n_knots] common FITPACK knot vector of every SK spline;
+ *   sk_coef [n_kinds][n_kinds][2 (S, H0)][5 (ss_s, sp_s, ps_s, pp_p, pp_s)][n_knots]: entry (a, b)
+ *   has centre 1 of kind a (used for z_a <= z_b), unused integrals zero;
+ *   rep_nt [n_kinds*n_kinds], rep_knots / rep_coef [n_kinds*n_kinds*rep_ntmax], rep_dmax
+ *   [n_kinds*n_kinds]: repulsive spline per kind pair (both orders filled); may be NULL. */
+int tincr_set_parameters(tincr_ctx *ctx, int n_kinds, const int *kind_z, const int *kind_norb,
+                         const int *kind_l, const int *kind_m, const double *kind_hubbard,
+                         const double *kind_occ, int n_knots, const double *sk_knots,
+                         const double *sk_coef, int rep_ntmax, const int *rep_nt,
+                         const double *rep_knots, const double *rep_coef, const double *rep_dmax);
+
+/* Replaces `System::ground_state_gradient(true)` (src/gradients/ground_state.rs:12-137) and
+ * `System::tda_gradient_lc(state)` / `tda_gradient_nolc(state)` (src/gradients/excited_state.rs:
+ * 56-487) for the system of the last tincr_tda_setup and the roots of the last tincr_tda_solve.
+ * LC is on when tincr_tda_setup got gamma_lr; r_lr is its long-range radius (bohr).
+ *   atom_kind [n_atoms] index into the parameter tables; P [n_orb*n_orb] SCC density matrix;
+ *   h_coul_x [n_orb*n_orb] final SCC Hamiltonian (for the energy-weighted density, ground_state.rs:77);
+ *   dq [n_atoms] Mulliken charge differences; state: root index;
+ *   grad_gs [3*n_atoms] ground-state gradient or NULL; grad_exc [3*n_atoms] gradient of the
+ *   excitation energy of `state` or NULL (total S_n gradient = grad_gs + grad_exc);
+ *   cg_iterations: Z-vector CG iterations (or NULL).  Returns TINCR_CG_MAXITER when the CG did
+ *   not reach r.r <= 1e-19 in 10000 iterations (gradient still written). */
+int tincr_gradient(tincr_ctx *ctx, const int *atom_kind, double r_lr, const double *P,
+                   const double *h_coul_x, const double *dq, int state, int variant,
+                   double *grad_gs, double *grad_exc, int *cg_iterations);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* TINCR_GB300_H */

@@ -8,7 +8,9 @@ the value rules with respect to the inter-centre vector r = pos2 - pos1:
     d/dr_c [P(u) V(r)] = (grad_u P . (e_c - u_c u)) V / r + P V'(r) u_c,   u = r/|r|
 
 which is what tincr's hard-coded expressions evaluate.  Splines are FITPACK cubic splines
-(SciPy's FITPACK binding, `splev` with ext=0) from the shipped parameter set.
+(SciPy's FITPACK binding) from the shipped parameter set, evaluated as zero beyond the last grid
+point (10 bohr): tincr's behaviour there comes from Rusty-FITPACK's `splev_uniform`, which no
+fixture pins, and FITPACK's polynomial extrapolation would make S indefinite beyond ~15 bohr.
 
 Test infrastructure only (see oracle/__init__.py).
 """
@@ -59,8 +61,8 @@ def sk_block(knots, coef, present, l_a, m_a, l_b, m_b, rvec, grad=False):
     slot_of = {0: 0, 2: 1, 4: 2, 5: 3, 6: 4}
     for idx in present:
         s = slot_of[idx]
-        v[s] = splev(r, (knots, coef[s], 3))
-        dv[s] = splev(r, (knots, coef[s], 3), der=1)
+        v[s] = splev(r, (knots, coef[s], 3), ext=1)
+        dv[s] = splev(r, (knots, coef[s], 3), der=1, ext=1)
     na, nb = len(l_a), len(l_b)
     val = np.zeros((n, na, nb))
     g = np.zeros((n, 3, na, nb)) if grad else None

@@ -1,0 +1,74 @@
+"""Input cases shared by the tests: golden-fixture ground states and seeded synthetic systems."""
+
+import os
+
+import numpy as np
+
+from tincr_gb300 import geometry as G
+from tincr_gb300 import groundstate as gs
+from tincr_gb300.params import NUMBERS
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+# the fixtures of tincr's tests/data were generated with this bohr radius
+FIXTURE_BOHR = 0.529177249
+
+
+def golden(name):
+    return np.load(os.path.join(GOLDEN, name + ".npz"))
+
+
+def fixture_case(mol, lc=True):
+    """Ground state exactly as stored in tincr's tests/data/<mol> fixtures."""
+    d = golden(mol)
+    numbers = np.array([NUMBERS[s] for s in d["symbols"]], dtype=np.int32)
+    sy = gs.build_system(numbers, d["xyz_angstrom"] / FIXTURE_BOHR, lc=lc)
+    n_occ = int(np.sum(d["occupation"][:, 0] > 0))
+    return dict(
+        name=mol, numbers=numbers, xyz=sy.xyz, opa=d["orbs_per_atom"][:, 0].astype(np.int32),
+        ao_offset=np.concatenate([[0], np.cumsum(d["orbs_per_atom"][:, 0].astype(np.int64))]),
+        orbs=np.ascontiguousarray(d["orbs_after_scc"]), s=np.ascontiguousarray(d["S"]),
+        orbe=d["orbe_after_scc"][:, 0].copy(), n_occ=n_occ, n_virt=sy.n_orbs - n_occ,
+        gamma=np.ascontiguousarray(d["gamma_atomwise"]),
+        gamma_lr=np.ascontiguousarray(d["gamma_atomwise_lc"]) if lc else None)
+
+
+_SYN = {}
+
+
+def synthetic_case(name, lc=True, r_lr=gs.LONG_RANGE_RADIUS):
+    """Seeded synthetic system with a host SCC ground state (cached per process)."""
+    key = (name, lc, r_lr)
+    if key in _SYN:
+        return _SYN[key]
+    if name == "polyene":
+        z, x = G.polyene(20)
+    elif name == "polyene8":
+        z, x = G.polyene(8)
+    elif name == "decacene":
+        z, x = G.acene(10)
+    elif name == "naphthalene":
+        z, x = G.acene(2)
+    elif name.startswith("water"):
+        n = {"water8": (2, 2, 2), "water27": (3, 3, 3), "water128": (8, 4, 4)}[name]
+        z, x = G.water_cluster(*n)
+    else:
+        raise KeyError(name)
+    sy = gs.build_system(z, G.to_bohr(x), lc=lc, r_lr=r_lr)
+    g = gs.run_scc(sy)
+    case = dict(name=name, numbers=sy.numbers, xyz=sy.xyz, opa=sy.orbs_per_atom.astype(np.int32),
+                ao_offset=sy.ao_offset, orbs=g.orbs, s=g.s, orbe=g.orbe, n_occ=sy.n_occ, n_virt=sy.n_virt,
+                gamma=g.gamma, gamma_lr=g.gamma_lr if lc else None, system=sy, ground=g)
+    _SYN[key] = case
+    return case
+
+
+def oracle_inputs(case):
+    """q's, omega and engine arguments of the oracle for a case."""
+    from oracle import tda
+    no, nv = case["n_occ"], case["n_virt"]
+    occ = np.arange(no)
+    virt = np.arange(no, no + nv)
+    qov, qoo, qvv = tda.trans_charges(case["ao_offset"], case["orbs"], case["s"], occ, virt)
+    om = tda.orbe_differences(case["orbe"][occ], case["orbe"][virt])
+    return dict(omega=om, q_ov=qov, q_oo=qoo, q_vv=qvv, gamma=case["gamma"], gamma_lr=case["gamma_lr"],
+                n_occ=no, n_virt=nv)

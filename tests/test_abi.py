@@ -1,0 +1,52 @@
+"""CPU tests of the C-ABI library: it builds for sm_103a, loads, and exports exactly the entry
+points that include/tincr_gb300.h declares.  No compute call is made here."""
+
+import ctypes
+import os
+import re
+import shutil
+import subprocess
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(ROOT, "include", "tincr_gb300.h")
+
+
+def declared_symbols():
+    text = open(HEADER).read()
+    return sorted(set(re.findall(r"^\s*(?:const\s+)?\w+\s*\*?\s*(tincr_\w+)\s*\(", text, re.M)))
+
+
+@pytest.fixture(scope="module")
+def libpath():
+    if shutil.which("nvcc") is None and not os.path.exists("/usr/local/cuda/bin/nvcc"):
+        pytest.skip("nvcc not available")
+    from tincr_gb300 import build
+    return build.build()
+
+
+def test_header_declares_entry_points():
+    syms = declared_symbols()
+    for s in ("tincr_ctx_create", "tincr_ctx_destroy", "tincr_trans_charges", "tincr_tda_setup",
+              "tincr_tda_products", "tincr_tda_solve"):
+        assert s in syms
+
+
+def test_library_exports_every_declared_symbol(libpath):
+    out = subprocess.run(["nm", "-D", "--defined-only", libpath], capture_output=True, text=True).stdout
+    exported = set(re.findall(r"\bT\s+(tincr_\w+)", out))
+    assert set(declared_symbols()) <= exported, set(declared_symbols()) - exported
+    lib = ctypes.CDLL(libpath)
+    for s in declared_symbols():
+        assert getattr(lib, s) is not None
+
+
+def test_binding_signatures_cover_header(libpath):
+    from tincr_gb300 import _lib
+    assert set(declared_symbols()) == set(_lib.SIGNATURES)
+
+
+def test_build_targets_sm103a_only():
+    from tincr_gb300 import build
+    assert build.ARCH == ["-gencode", "arch=compute_103a,code=sm_103a"]

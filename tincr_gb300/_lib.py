@@ -1,0 +1,137 @@
+"""ctypes binding of the C ABI declared in include/tincr_gb300.h.
+
+The shared library is built in-tree (`tincr_gb300/lib/libtincr_gb300.so`, see build.py).  There
+is no CPU fallback: if the library cannot be loaded every entry point raises.
+"""
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "lib", "libtincr_gb300.so")
+
+OK, NOT_CONVERGED, NONFINITE, BAD_ARG, CUDA_ERR, NO_DEVICE, CG_MAXITER = range(7)
+STATUS_NAMES = {0: "OK", 1: "NOT_CONVERGED", 2: "NONFINITE", 3: "BAD_ARG", 4: "CUDA_ERR", 5: "NO_DEVICE",
+                6: "CG_MAXITER"}
+PREC_FP64, PREC_BF16X3 = 0, 1
+KF_AO_EXCHANGE, KF_AO_TRANSFORM, KF_SUBSPACE, KF_OTHER = range(4)
+GRAD_REFERENCE, GRAD_EXACT = 0, 1
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int)
+
+# name -> (restype, argtypes); must match include/tincr_gb300.h
+SIGNATURES = {
+    "tincr_ctx_create": (C.c_int, [C.POINTER(C.c_void_p), C.c_int]),
+    "tincr_ctx_destroy": (C.c_int, [C.c_void_p]),
+    "tincr_last_error": (C.c_char_p, [C.c_void_p]),
+    "tincr_last_timing": (C.c_int, [C.c_void_p, _dp, C.POINTER(C.c_longlong)]),
+    "tincr_last_solve_stats": (C.c_int, [C.c_void_p, C.POINTER(C.c_longlong), _ip, _dp]),
+    "tincr_set_profiling": (C.c_int, [C.c_void_p, C.c_int]),
+    "tincr_kernel_stats": (C.c_int, [C.c_void_p, C.c_int, _dp, C.POINTER(C.c_longlong), _dp, _dp]),
+    "tincr_trans_charges": (C.c_int, [C.c_void_p, C.c_int, _ip, C.c_int, _dp, _dp, C.c_int, C.c_int, C.c_int,
+                                      C.c_int, _dp, _dp, _dp]),
+    "tincr_tda_setup": (C.c_int, [C.c_void_p, C.c_int, _ip, C.c_int, _dp, _dp, _dp, C.c_int, C.c_int, _dp, _dp,
+                                  _dp]),
+    "tincr_tda_products": (C.c_int, [C.c_void_p, C.c_int, _dp, _dp, C.c_int]),
+    "tincr_tda_solve": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_double, C.c_int, _dp, _dp, _dp, _dp, _dp,
+                                  _ip]),
+    "tincr_set_parameters": (C.c_int, [C.c_void_p, C.c_int, _ip, _ip, _ip, _ip, _dp, _dp, C.c_int, _dp, _dp,
+                                       C.c_int, _ip, _dp, _dp, _dp]),
+    "tincr_gradient": (C.c_int, [C.c_void_p, _ip, C.c_double, _dp, _dp, _dp, C.c_int, C.c_int, _dp, _dp, _ip]),
+}
+
+_lib = None
+
+
+class TincrError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__("%s: %s" % (STATUS_NAMES.get(status, status), msg))
+        self.status = status
+
+
+def load(path=LIB_PATH):
+    """Load the CUDA library (raises OSError when it is missing: no fallback)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise OSError("tincr_gb300 CUDA library not built: %s (run tincr_gb300.build.build())" % path)
+    lib = C.CDLL(path)
+    for name, (res, args) in SIGNATURES.items():
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = lib
+    return lib
+
+
+def dptr(a):
+    if a is None:
+        return None
+    assert a.dtype == np.float64 and a.flags["C_CONTIGUOUS"]
+    return a.ctypes.data_as(_dp)
+
+
+def iptr(a):
+    if a is None:
+        return None
+    assert a.dtype == np.int32 and a.flags["C_CONTIGUOUS"]
+    return a.ctypes.data_as(_ip)
+
+
+def f64(a):
+    return None if a is None else np.ascontiguousarray(a, dtype=np.float64)
+
+
+class Context:
+    """Owns one `tincr_ctx` (one GPU, one system)."""
+
+    def __init__(self, device=0):
+        self.lib = load()
+        h = C.c_void_p()
+        rc = self.lib.tincr_ctx_create(C.byref(h), int(device))
+        if rc != OK:
+            raise TincrError(rc, "tincr_ctx_create(device=%d) failed" % device)
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.tincr_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def check(self, rc, allow=(OK,)):
+        if rc not in allow:
+            raise TincrError(rc, (self.lib.tincr_last_error(self.h) or b"").decode())
+        return rc
+
+    def set_profiling(self, on=True):
+        self.check(self.lib.tincr_set_profiling(self.h, 1 if on else 0))
+
+    def kernel_stats(self, family):
+        ms, fl, by = C.c_double(), C.c_double(), C.c_double()
+        n = C.c_longlong()
+        self.check(self.lib.tincr_kernel_stats(self.h, int(family), C.byref(ms), C.byref(n), C.byref(fl),
+                                               C.byref(by)))
+        return dict(ms=ms.value, launches=n.value, flops=fl.value, bytes=by.value)
+
+    def last_solve_stats(self):
+        n = C.c_longlong()
+        k = C.c_int()
+        r = C.c_double()
+        self.check(self.lib.tincr_last_solve_stats(self.h, C.byref(n), C.byref(k), C.byref(r)))
+        return dict(n_products=n.value, n_collapses=k.value, max_residual=r.value)
+
+    def last_timing(self):
+        ms = C.c_double()
+        n = C.c_longlong()
+        self.lib.tincr_last_timing(self.h, C.byref(ms), C.byref(n))
+        return ms.value, n.value

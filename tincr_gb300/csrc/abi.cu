@@ -1,0 +1,148 @@
+// extern "C" boundary: turns tincr::Error exceptions into tincr_status codes.
+#include <cstring>
+#include <new>
+
+#include "tda.cuh"
+
+struct tincr_ctx {
+    tincr::Ctx *impl = nullptr;
+    std::string err;
+};
+
+namespace {
+
+template <class F>
+int guarded(tincr_ctx *ctx, F &&f) {
+    if (!ctx || !ctx->impl) return TINCR_BAD_ARG;
+    try {
+        TINCR_CUDA(cudaSetDevice(ctx->impl->device));
+        int rc = f(*ctx->impl);
+        if (rc == TINCR_OK) ctx->err.clear();
+        return rc;
+    } catch (const tincr::Error &e) {
+        ctx->err = e.msg;
+        return e.status;
+    } catch (const std::bad_alloc &) {
+        ctx->err = "host allocation failed";
+        return TINCR_BAD_ARG;
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+int tincr_ctx_create(tincr_ctx **out, int device) {
+    if (!out) return TINCR_BAD_ARG;
+    *out = nullptr;
+    try {
+        auto *c = new tincr_ctx;
+        c->impl = new tincr::Ctx(device);
+        *out = c;
+        return TINCR_OK;
+    } catch (const tincr::Error &e) {
+        return e.status;
+    } catch (...) {
+        return TINCR_BAD_ARG;
+    }
+}
+
+int tincr_ctx_destroy(tincr_ctx *ctx) {
+    if (!ctx) return TINCR_BAD_ARG;
+    delete ctx->impl;
+    delete ctx;
+    return TINCR_OK;
+}
+
+const char *tincr_last_error(const tincr_ctx *ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+int tincr_last_timing(const tincr_ctx *ctx, double *ms, long long *kernel_launches) {
+    if (!ctx || !ctx->impl) return TINCR_BAD_ARG;
+    if (ms) *ms = ctx->impl->last_ms;
+    if (kernel_launches) *kernel_launches = ctx->impl->last_launches;
+    return TINCR_OK;
+}
+
+int tincr_last_solve_stats(const tincr_ctx *ctx, long long *n_products, int *n_collapses, double *max_residual) {
+    if (!ctx || !ctx->impl) return TINCR_BAD_ARG;
+    if (n_products) *n_products = ctx->impl->last_products;
+    if (n_collapses) *n_collapses = ctx->impl->last_collapses;
+    if (max_residual) *max_residual = ctx->impl->last_max_residual;
+    return TINCR_OK;
+}
+
+int tincr_set_profiling(tincr_ctx *ctx, int enable) {
+    return guarded(ctx, [&](tincr::Ctx &c) {
+        c.sync();
+        c.prof_resolve();
+        c.profiling = enable != 0;
+        if (c.profiling)
+            for (auto &s : c.stats) s = tincr::KernelStats{};
+        return TINCR_OK;
+    });
+}
+
+int tincr_kernel_stats(const tincr_ctx *ctx, int family, double *ms, long long *launches, double *flops,
+                       double *bytes) {
+    if (!ctx || !ctx->impl || family < 0 || family >= TINCR_KF_COUNT) return TINCR_BAD_ARG;
+    const tincr::KernelStats &s = ctx->impl->stats[family];
+    if (ms) *ms = s.ms;
+    if (launches) *launches = s.launches;
+    if (flops) *flops = s.flops;
+    if (bytes) *bytes = s.bytes;
+    return TINCR_OK;
+}
+
+int tincr_trans_charges(tincr_ctx *ctx, int n_atoms, const int *orbs_per_atom, int n_orb, const double *C,
+                        const double *S, int occ0, int n_occ, int virt0, int n_virt, double *q_ov, double *q_oo,
+                        double *q_vv) {
+    return guarded(ctx, [&](tincr::Ctx &c) {
+        c.trans_charges(n_atoms, orbs_per_atom, n_orb, C, S, occ0, n_occ, virt0, n_virt, q_ov, q_oo, q_vv);
+        return TINCR_OK;
+    });
+}
+
+int tincr_tda_setup(tincr_ctx *ctx, int n_atoms, const int *orbs_per_atom, int n_orb, const double *C,
+                    const double *S, const double *orbe, int n_occ, int n_virt, const double *gamma,
+                    const double *gamma_lr, const double *xyz) {
+    return guarded(ctx, [&](tincr::Ctx &c) {
+        c.tda_setup(n_atoms, orbs_per_atom, n_orb, C, S, orbe, n_occ, n_virt, gamma, gamma_lr, xyz);
+        return TINCR_OK;
+    });
+}
+
+int tincr_tda_products(tincr_ctx *ctx, int k, const double *X, double *AX, int precision) {
+    return guarded(ctx, [&](tincr::Ctx &c) {
+        c.products(k, X, AX, precision);
+        return TINCR_OK;
+    });
+}
+
+int tincr_tda_solve(tincr_ctx *ctx, int n_roots, int max_iter, double tolerance, int precision, double *energies,
+                    double *coefficients, double *osc, double *tr_dip, double *q_trans, int *iterations) {
+    return guarded(ctx, [&](tincr::Ctx &c) {
+        c.last_history.clear();
+        return c.solve(n_roots, max_iter, tolerance, precision, energies, coefficients, osc, tr_dip, q_trans,
+                       iterations);
+    });
+}
+
+int tincr_set_parameters(tincr_ctx *ctx, int n_kinds, const int *kind_z, const int *kind_norb, const int *kind_l,
+                         const int *kind_m, const double *kind_hubbard, const double *kind_occ, int n_knots,
+                         const double *sk_knots, const double *sk_coef, int rep_ntmax, const int *rep_nt,
+                         const double *rep_knots, const double *rep_coef, const double *rep_dmax) {
+    return guarded(ctx, [&](tincr::Ctx &c) {
+        c.set_parameters(n_kinds, kind_z, kind_norb, kind_l, kind_m, kind_hubbard, kind_occ, n_knots, sk_knots, sk_coef,
+                         rep_ntmax, rep_nt, rep_knots, rep_coef, rep_dmax);
+        return TINCR_OK;
+    });
+}
+
+int tincr_gradient(tincr_ctx *ctx, const int *atom_kind, double r_lr, const double *P, const double *h_coul_x,
+                   const double *dq, int state, int variant, double *grad_gs, double *grad_exc, int *cg_iterations) {
+    return guarded(ctx, [&](tincr::Ctx &c) {
+        return c.gradient(atom_kind, r_lr, P, h_coul_x, dq, state, variant, grad_gs, grad_exc, cg_iterations);
+    });
+}
+
+}  // extern "C"

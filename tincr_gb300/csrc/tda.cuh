@@ -1,0 +1,117 @@
+// Device context of one molecular system (see tda.cu).
+#pragma once
+
+#include <vector>
+
+#include "common.cuh"
+
+namespace tincr {
+
+struct DavidsonStep {
+    int iter;
+    int n_sub;
+    double max_residual;
+    int roots_left;
+};
+
+// Per-kernel-family device timing (CUDA events on the library stream), enabled on request.
+struct KernelStats {
+    double ms = 0.0;
+    long long launches = 0;
+    double flops = 0.0;
+    double bytes = 0.0;
+};
+
+enum Blk { BLK_OCC = 0, BLK_VIRT = 1 };
+
+struct Ctx {
+    int device = 0;
+    int n_sm = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    std::string err;
+    double last_ms = 0.0;
+    long long last_launches = 0;
+    std::vector<DavidsonStep> last_history;
+    long long last_products = 0;
+    int last_collapses = 0;
+    double last_max_residual = 0.0;
+
+    // profiling
+    bool profiling = false;
+    struct Pending {
+        int family;
+        cudaEvent_t a, b;
+        double flops, bytes;
+    };
+    std::vector<Pending> pending;
+    std::vector<cudaEvent_t> event_pool;
+    KernelStats stats[8];
+    int prof_begin(int family);                 // returns slot or -1
+    void prof_end(int slot, double flops, double bytes);
+    void prof_resolve();                        // after a sync: fold pending events into stats
+
+    // system
+    bool ready = false;
+    bool lc = false;
+    int n_atoms = 0, n_orb = 0, n_occ = 0, n_virt = 0;
+    long long ov = 0;
+    std::vector<int> h_ao_off;
+    std::vector<double> h_xyz, h_omega;
+    DevBuf<int> d_ao_off, d_ao_atom;
+    DevBuf<double> dC, dSC, d_omega, d_gamma, d_glr_ao;
+    DevBuf<double> dLst, dRv, dLsw, dRsw;     // [Co;SCo], [Cv;SCv], [SCo;Co], [SCv;Cv]
+
+    std::vector<double> h_gamma, h_orbe, h_energies;
+    int solved_roots = 0;
+    DevBuf<double> dS_, d_xyz;
+
+    // parameters for the gradient (SK splines, gamma, repulsion)
+    bool params_ready = false;
+    int n_kinds = 0, n_knots = 0, rep_ntmax = 0;
+    std::vector<int> h_kind_z, h_kind_norb;
+    std::vector<double> h_kind_occ;
+    DevBuf<int> d_kind_z, d_kind_norb, d_kind_l, d_kind_m, d_rep_nt;
+    DevBuf<double> d_sigma, d_knots, d_coef, d_rep_knots, d_rep_coef, d_rep_dmax;
+    DevBuf<double> gw, gv, gcg;            // gradient workspaces
+    int last_cg_status = TINCR_OK;
+
+    // product workspace
+    DevBuf<double> wsH, wsF, wsG, wsd3, wsd2, wsz;
+    // Davidson state
+    DevBuf<double> dV, dAV, dR, dRk, dT;
+
+    explicit Ctx(int dev);
+    ~Ctx();
+    void sync();
+    void launch_transpose(int rows, int cols, const double *in, double *out);
+    void set_atoms(int n_atoms, const int *orbs_per_atom, int n_orb);
+    void upload_mo(int n, const double *C, const double *S);
+    int product_chunk() const;
+
+    void trans_charges(int n_atoms, const int *opa, int n, const double *C, const double *S, int occ0, int no,
+                       int virt0, int nv, double *q_ov, double *q_oo, double *q_vv);
+    void tda_setup(int n_atoms, const int *opa, int n, const double *C, const double *S, const double *orbe, int no,
+                   int nv, const double *gamma, const double *gamma_lr, const double *xyz);
+    const double *stk(int b) const { return b == BLK_OCC ? dLst.p : dRv.p; }    // [C_B; SC_B]
+    const double *swp(int b) const { return b == BLK_OCC ? dLsw.p : dRsw.p; }   // [SC_B; C_B]
+    int bsz(int b) const { return b == BLK_OCC ? n_occ : n_virt; }
+    void ao_contract(int k, int R, int S, const double *V, int P, int Q, double ax, double ac, double *out,
+                     double alpha, double beta, const double *Xomega);
+    void products_dev(int k, const double *X, double *AX, double *y_out);
+    void qtrans_dev(int k, const double *X, double *y_out);
+    void products(int k, const double *X, double *AX, int precision);
+    void set_parameters(int n_kinds, const int *kind_z, const int *kind_norb, const int *kind_l, const int *kind_m,
+                        const double *kind_hubbard, const double *kind_occ, int n_knots, const double *knots,
+                        const double *coef, int rep_ntmax, const int *rep_nt, const double *rep_knots,
+                        const double *rep_coef, const double *rep_dmax);
+    void plr_adjoint(const double *v, const double *Y, double scale_p, double scale_q, double *PS, double *QLblk);
+    void pv_adjoint(const double *V, const double *Y, double scale, double *PS, double *QGblk);
+    int zvector_cg(int variant, const double *R, double *Z, int max_iter, double conv, int *iters);
+    int gradient(const int *atom_kind, double r_lr, const double *P, const double *h_coul_x, const double *dq,
+                 int state, int variant, double *grad_gs, double *grad_exc, int *cg_iters);
+    int solve(int n_roots, int max_iter, double tol, int precision, double *energies, double *coefficients,
+              double *osc, double *tr_dip, double *q_trans, int *iterations);
+};
+
+}  // namespace tincr

@@ -10,6 +10,12 @@ timed path.
 Conventions follow tincr:
 * orbitals per atom in the order of `Atom::from` (s, then p with m = -1, 0, +1 i.e. y, z, x);
 * occupied orbitals are the first n_elec/2 MOs (`system.rs:132-140`);
+* SK integrals are zero beyond the last grid point of the table (10 bohr).  tincr evaluates its
+  splines up to PROXIMITY_CUTOFF = 30 bohr (`h0_and_s.rs:110`) through Rusty-FITPACK's
+  `splev_uniform`, whose behaviour outside the knot range no tincr fixture pins (all fixture
+  distances are below 9.6 bohr).  Polynomial extrapolation of the end piece (FITPACK ext=0) grows
+  to O(0.1-1) at 20-30 bohr and makes S indefinite for extended molecules, so the tail is taken as
+  zero, the rule tincr itself applies to its repulsive splines (`parameters.rs:345-372`);
 * S and H0 by the Slater-Koster rules of `src/param/slako_transformations.rs:57-680` (s and p
   orbitals) on the pair ordering of `src/scc/h0_and_s.rs:92-182`: the atom with the smaller atomic
   number is centre 1 and the direction vector points from centre 1 to centre 2;
@@ -164,8 +170,8 @@ def h0_and_s(sysm):
             ch = ps.sk_coef[(int(zA), int(zB), "h")]
             for slot, idx in enumerate(P.SK_INTEGRALS):
                 if idx in ps.sk_present[(int(zA), int(zB))]:
-                    vs[slot] = splev(r, (knots, cs[slot], 3))
-                    vh[slot] = splev(r, (knots, ch[slot], 3))
+                    vs[slot] = splev(r, (knots, cs[slot], 3), ext=1)
+                    vh[slot] = splev(r, (knots, ch[slot], 3), ext=1)
             eA, eB = ps.element(zA), ps.element(zB)
             for p1 in range(eA.n_orbs):
                 for p2 in range(eB.n_orbs):
