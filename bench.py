@@ -301,6 +301,25 @@ def run_reference(args):
             "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
+def run_products(args):
+    """Profiling helper: set up the workload and evaluate A.X for `--k` random trial vectors once
+    (used for ncu captures of the product kernels on the full-size system)."""
+    from tincr_gb300 import _lib, build
+    from tincr_gb300 import tda as T
+    build.build()
+    sy, g = workload()
+    ctx = _lib.Context(0)
+    es = T.ExcitedStateSystem.from_ground_state(ctx, sy, g)
+    es.prepare_tda()
+    x = np.random.default_rng(0).standard_normal((es.dim, args.k))
+    prec = {"fp64": _lib.PREC_FP64, "bf16x3": _lib.PREC_BF16X3}[args.precision]
+    for _ in range(max(1, args.steps)):
+        ax = es.compute_products(x, precision=prec)
+    ms, nl = ctx.last_timing()
+    print(json.dumps({"mode": "products", "k": args.k, "ms": ms, "launches": nl,
+                      "checksum": float(np.abs(ax).sum())}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -311,7 +330,12 @@ def main():
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
     ap.add_argument("--ref-products", type=int, default=420)
     ap.add_argument("--ref-iters", type=int, default=20)
+    ap.add_argument("--mode", default="solve", choices=["solve", "products"])
+    ap.add_argument("--k", type=int, default=4)
     args = ap.parse_args()
+    if args.mode == "products":
+        run_products(args)
+        return
     out = run_reference(args) if args.impl == "reference" else run_gpu(args)
     if out is not None:
         print(json.dumps(out))

@@ -46,6 +46,11 @@ const char *tincr_last_error(const tincr_ctx *ctx);
  * number of kernels it launched. */
 int tincr_last_timing(const tincr_ctx *ctx, double *ms, long long *kernel_launches);
 
+/* Replaces `set_ci_eigenvalues` / `set_ci_coefficients` (src/properties/setter.rs): install
+ * excitation energies [n_roots] and CI vectors [n_occ*n_virt, n_roots] computed elsewhere (for
+ * example by a caller's own solver) as the roots the gradient of this context works on. */
+int tincr_tda_set_states(tincr_ctx *ctx, int n_roots, const double *energies, const double *coefficients);
+
 /* Statistics of the last tincr_tda_solve: A.X products evaluated (tincr's compute_products
  * columns), subspace collapses and the final largest residual norm. */
 int tincr_last_solve_stats(const tincr_ctx *ctx, long long *n_products, int *n_collapses, double *max_residual);

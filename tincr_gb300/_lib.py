@@ -28,6 +28,7 @@ SIGNATURES = {
     "tincr_ctx_destroy": (C.c_int, [C.c_void_p]),
     "tincr_last_error": (C.c_char_p, [C.c_void_p]),
     "tincr_last_timing": (C.c_int, [C.c_void_p, _dp, C.POINTER(C.c_longlong)]),
+    "tincr_tda_set_states": (C.c_int, [C.c_void_p, C.c_int, _dp, _dp]),
     "tincr_last_solve_stats": (C.c_int, [C.c_void_p, C.POINTER(C.c_longlong), _ip, _dp]),
     "tincr_set_profiling": (C.c_int, [C.c_void_p, C.c_int]),
     "tincr_kernel_stats": (C.c_int, [C.c_void_p, C.c_int, _dp, C.POINTER(C.c_longlong), _dp, _dp]),

@@ -63,6 +63,13 @@ int tincr_last_timing(const tincr_ctx *ctx, double *ms, long long *kernel_launch
     return TINCR_OK;
 }
 
+int tincr_tda_set_states(tincr_ctx *ctx, int n_roots, const double *energies, const double *coefficients) {
+    return guarded(ctx, [&](tincr::Ctx &c) {
+        c.set_states(n_roots, energies, coefficients);
+        return TINCR_OK;
+    });
+}
+
 int tincr_last_solve_stats(const tincr_ctx *ctx, long long *n_products, int *n_collapses, double *max_residual) {
     if (!ctx || !ctx->impl) return TINCR_BAD_ARG;
     if (n_products) *n_products = ctx->impl->last_products;

@@ -541,6 +541,20 @@ void Ctx::products(int k, const double *X, double *AX, int precision) {
     prof_resolve();
 }
 
+void Ctx::set_states(int n_roots, const double *energies, const double *coefficients) {
+    if (!ready) fail(TINCR_BAD_ARG, "tincr_tda_setup must be called first");
+    if (n_roots <= 0 || n_roots > ov || !energies || !coefficients) fail(TINCR_BAD_ARG, "set_states: bad arguments");
+    check_finite(energies, n_roots, "energies");
+    check_finite(coefficients, (size_t)ov * n_roots, "coefficients");
+    DevBuf<double> tmp((size_t)ov * n_roots);
+    dR.reserve((size_t)n_roots * ov);
+    TINCR_CUDA(cudaMemcpyAsync(tmp.p, coefficients, (size_t)ov * n_roots * sizeof(double), cudaMemcpyHostToDevice, stream));
+    launch_transpose((int)ov, n_roots, tmp.p, dR.p);     // [ov x n_roots] -> [n_roots x ov]
+    sync();
+    h_energies.assign(energies, energies + n_roots);
+    solved_roots = n_roots;
+}
+
 // ----------------------------------------------------------------------------------------------
 // Davidson (src/excited_states/solvers/davidson.rs:53-185)
 // ----------------------------------------------------------------------------------------------

@@ -110,6 +110,7 @@ struct Ctx {
     int zvector_cg(int variant, const double *R, double *Z, int max_iter, double conv, int *iters);
     int gradient(const int *atom_kind, double r_lr, const double *P, const double *h_coul_x, const double *dq,
                  int state, int variant, double *grad_gs, double *grad_exc, int *cg_iters);
+    void set_states(int n_roots, const double *energies, const double *coefficients);
     int solve(int n_roots, int max_iter, double tol, int precision, double *energies, double *coefficients,
               double *osc, double *tr_dip, double *q_trans, int *iterations);
 };

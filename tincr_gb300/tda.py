@@ -82,6 +82,15 @@ class ExcitedStateSystem:
         self.ctx.check(self.ctx.lib.tincr_tda_products(self.ctx.h, x.shape[1], dptr(x), dptr(out), int(precision)))
         return out
 
+    def set_states(self, energies, coefficients):
+        """Install roots computed elsewhere (`set_ci_eigenvalues` / `set_ci_coefficients`)."""
+        if not self.prepared:
+            self.prepare_tda()
+        e = f64(np.atleast_1d(energies))
+        x = f64(coefficients.reshape(self.dim, -1))
+        self.ctx.check(self.ctx.lib.tincr_tda_set_states(self.ctx.h, len(e), dptr(e), dptr(x)))
+        self.properties.update(ci_eigenvalues=e, ci_coefficients=x)
+
     def run_tda(self, n_roots, max_iter, tolerance, precision=_lib.PREC_FP64, raise_on_failure=True):
         """`System::run_tda(n_roots, max_iter, tolerance)`; results are stored in `properties`
         (ci_eigenvalues, ci_coefficients, q_trans, tr_dipoles, oscillator_strengths) and returned."""
