@@ -125,6 +125,13 @@ int tincr_tda_products(tincr_ctx *ctx, int k, const double *X, double *AX, int p
     });
 }
 
+int tincr_tda_products_noalloc(tincr_ctx *ctx, int k, const double *X_dev, double *AX_dev) {
+    return guarded(ctx, [&](tincr::Ctx &c) {
+        tincr::products_noalloc(c, k, X_dev, AX_dev);
+        return TINCR_OK;
+    });
+}
+
 int tincr_tda_solve(tincr_ctx *ctx, int n_roots, int max_iter, double tolerance, int precision, double *energies,
                     double *coefficients, double *osc, double *tr_dip, double *q_trans, int *iterations) {
     return guarded(ctx, [&](tincr::Ctx &c) {

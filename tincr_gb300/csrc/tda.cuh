@@ -115,4 +115,7 @@ struct Ctx {
               double *osc, double *tr_dip, double *q_trans, int *iterations);
 };
 
+// A.X product with caller-owned device buffers and fixed device scratch (noalloc.cu)
+void products_noalloc(Ctx &c, int k, const double *X, double *AX);
+
 }  // namespace tincr
