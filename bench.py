@@ -157,6 +157,7 @@ def run_gpu(args):
     # device-timed region: inputs resident (prepare_tda done), Davidson + moments per step
     ctx.set_profiling(True)
     dev_ms, launches, iters = [], 0, []
+    n_products_total = 0
     barrier_and_max(0.0, world)
     torch.cuda.synchronize()
     with ClockSampler(local) as clocks:
@@ -168,6 +169,7 @@ def run_gpu(args):
             dev_ms.append(ms)
             launches += nl
             iters.append(es.properties["davidson_iterations"])
+            n_products_total += es.properties["n_products"]
         torch.cuda.synchronize()
         wall = time.perf_counter() - t0
     stats = {f: ctx.kernel_stats(f) for f in range(4)}
@@ -203,10 +205,15 @@ def run_gpu(args):
             peak = peaks.get("bf16_tflops", 1900.0)
             peak_note = "measured bf16_tflops" if "bf16_tflops" in peaks else "fallback 1.9 PFLOP/s"
             bound, unit = "tensor", "TFLOP/s"
+        # DRAM bytes per launch of the exchange family: ncu bytes per product vector (full-size
+        # capture, profiles/) times the vectors per launch of this solve (2 launches per chunk)
         traffic = None
         tf = os.path.join(ROOT, "profiles", "ao_exchange_traffic.json")
-        if os.path.exists(tf):
-            traffic = json.load(open(tf)).get(args.precision)
+        if os.path.exists(tf) and ex["launches"] > 0:
+            rec = json.load(open(tf)).get(args.precision)
+            if rec:
+                vec_per_launch = 2.0 * n_products_total / ex["launches"]
+                traffic = rec["dram_bytes_per_vector"] * vec_per_launch / 2.0
         cpu = cpu_baseline(sy, g, sum(iters) / len(iters), es) if args.cpu_baseline else None
         out = {
             "metric": METRIC, "value": step_s, "unit": "s", "n_gpus": world, "steps": args.steps,
@@ -223,6 +230,8 @@ def run_gpu(args):
             "gpu_launches": int(launches),
             "roofline": {"bound": bound, "achieved": achieved, "peak": peak, "unit": unit,
                          "frac": (achieved / peak) if achieved else None, "traffic": traffic,
+                         "algorithmic_flops_per_launch": ex["flops"] / max(1, ex["launches"]),
+                         "algorithmic_bytes_per_launch": ex["bytes"] / max(1, ex["launches"]),
                          "kernel": "AO-exchange contractions (gemm_f64, A.X steps 2 and 4)",
                          "peak_source": peak_note,
                          "kernel_ms_per_step": ex["ms"] / args.steps,

@@ -158,3 +158,24 @@ def test_not_converged_and_bad_arguments(gpu_ctx):
         T.ExcitedStateSystem(gpu_ctx, [1, 1], c["orbs"], c["s"], c["orbe"], c["n_occ"], c["n_virt"], c["gamma"],
                              c["gamma_lr"], c["xyz"]).prepare_tda()
     assert e.value.status == _lib.BAD_ARG
+
+
+@pytest.mark.parametrize("name", ["uracil", "water27"])
+def test_mixed_products_close_to_fp64(gpu_ctx, name):
+    """Split-BF16 exchange contractions: A.X within 1e-5 of the FP64 product (relative to max |A.X|)."""
+    c = _case(name, True)
+    s = _solver(gpu_ctx, c)
+    x = np.random.default_rng(5).standard_normal((c["n_occ"] * c["n_virt"], 4))
+    ref = s.compute_products(x)
+    mix = s.compute_products(x, precision=_lib.PREC_BF16X3)
+    assert np.abs(mix - ref).max() < 1e-5 * np.abs(ref).max()
+
+
+@pytest.mark.parametrize("name", ["water27", "uracil"])
+def test_mixed_davidson_energies_within_bar(gpu_ctx, name):
+    """Mixed form: every root within 1e-6 Eh of the FP64 GPU roots (spec bar)."""
+    c = _case(name, True)
+    ref = _solver(gpu_ctx, c).run_tda(6, 300, 1e-6)
+    e_ref = ref["ci_eigenvalues"].copy()
+    mix = _solver(gpu_ctx, c).run_tda(6, 300, 1e-6, precision=_lib.PREC_BF16X3)
+    assert np.abs(mix["ci_eigenvalues"] - e_ref).max() < 1e-6

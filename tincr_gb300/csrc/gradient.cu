@@ -543,6 +543,7 @@ int Ctx::gradient(const int *atom_kind, double r_lr_, const double *P, const dou
     const int n = n_orb, o = n_occ, v = n_virt, N = n_atoms;
     const size_t nn = (size_t)n * n;
     g_launches = 0;
+    prec = TINCR_PREC_FP64;
     TINCR_CUDA(cudaEventRecord(ev0, stream));
     DevBuf<int> dkind(N);
     TINCR_CUDA(cudaMemcpyAsync(dkind.p, atom_kind, N * sizeof(int), cudaMemcpyHostToDevice, stream));

@@ -26,6 +26,7 @@
 #include "common.cuh"
 #include "gemm_f64.cuh"
 #include "ops.cuh"
+#include "subspace.cuh"
 #include "tda.cuh"
 
 namespace tincr {
@@ -434,6 +435,7 @@ void Ctx::ao_contract(int k, int R, int S, const double *V, int P, int Q, double
     const int n = n_orb;
     const int nr = bsz(R), ns = bsz(S), np = bsz(P), nq = bsz(Q);
     const bool exch = ax != 0.0 && lc;
+    const bool mixed = prec == TINCR_PREC_BF16X3;
     const int kc_max = product_chunk();
     const int wmax = std::max(n_occ, n_virt);
     wsH.reserve((size_t)kc_max * 2 * n * wmax);
@@ -450,8 +452,15 @@ void Ctx::ao_contract(int k, int R, int S, const double *V, int P, int Q, double
                             EpiStore{wsH.p, 2LL * n * ns, ns, 1.0, 0.0});
         if (exch) {
             // 2. F_b = ax gamma_lr o (H_b [C_S; SC_S]^T), diagonals captured for the Coulomb term
-            pgemm<false, true>(*this, TINCR_KF_AO_EXCHANGE, 2 * n, 2 * n, ns, wsH.p, ns, 2LL * n * ns, stk(S), ns, 0, kc,
-                               EpiLcHadamard{wsF.p, d_glr_ao.p, wsd3.p, wsd2.p, n, ax});
+            pgemm_prec<false, true>(*this, mixed, TINCR_KF_AO_EXCHANGE, 2 * n, 2 * n, ns, wsH.p, ns, 2LL * n * ns, stk(S),
+                                    ns, 0, kc, EpiLcHadamard{wsF.p, d_glr_ao.p, wsd3.p, wsd2.p, n, ax});
+            if (mixed && ac != 0.0) {
+                // Coulomb diagonals in FP64 (the mixed epilogue's captures are overwritten)
+                dim3 g(ceil_div(2LL * n * 32, 256), kc);
+                diag_dots_kernel<<<g, 256, 0, stream>>>(n, ns, wsH.p, stk(S), wsd3.p, wsd2.p);
+                count_launch(stream, "diag_dots");
+                check_launch("diag_dots");
+            }
         } else if (ac != 0.0) {
             dim3 g(ceil_div(2LL * n * 32, 256), kc);
             diag_dots_kernel<<<g, 256, 0, stream>>>(n, ns, wsH.p, stk(S), wsd3.p, wsd2.p);
@@ -468,8 +477,8 @@ void Ctx::ao_contract(int k, int R, int S, const double *V, int P, int Q, double
         }
         // 4. G_b = F_b [SC_Q; C_Q]
         if (exch) {
-            pgemm<false, false>(*this, TINCR_KF_AO_EXCHANGE, 2 * n, nq, 2 * n, wsF.p, 2 * n, 4LL * n * n, swp(Q), nq, 0, kc,
-                                EpiStore{wsG.p, 2LL * n * nq, nq, 1.0, 0.0});
+            pgemm_prec<false, false>(*this, mixed, TINCR_KF_AO_EXCHANGE, 2 * n, nq, 2 * n, wsF.p, 2 * n, 4LL * n * n,
+                                     swp(Q), nq, 0, kc, EpiStore{wsG.p, 2LL * n * nq, nq, 1.0, 0.0});
         } else if (ac != 0.0) {
             dim3 g(grid_for(2LL * n * nq, 256, n_sm), kc);
             scale_rows_kernel<<<g, 256, 0, stream>>>(n, nq, wsz.p, stk(Q), wsG.p);
@@ -522,7 +531,8 @@ void Ctx::qtrans_dev(int k, const double *X, double *y_out) {
 void Ctx::products(int k, const double *X, double *AX, int precision) {
     if (!ready) fail(TINCR_BAD_ARG, "tincr_tda_setup must be called first");
     if (k <= 0 || !X || !AX) fail(TINCR_BAD_ARG, "products: bad arguments");
-    if (precision != TINCR_PREC_FP64) fail(TINCR_BAD_ARG, "products: precision not available in this build");
+    if (precision != TINCR_PREC_FP64 && precision != TINCR_PREC_BF16X3) fail(TINCR_BAD_ARG, "products: unknown precision");
+    prec = precision;
     check_finite(X, (size_t)ov * k, "X");
     g_launches = 0;
     DevBuf<double> dXin((size_t)ov * k), dX((size_t)ov * k), dAX((size_t)ov * k);
@@ -564,7 +574,8 @@ int Ctx::solve(int n_roots, int max_iter, double tol, int precision, double *ene
     if (!ready) fail(TINCR_BAD_ARG, "tincr_tda_setup must be called first");
     if (n_roots <= 0 || n_roots > ov || max_iter <= 0 || !(tol > 0.0)) fail(TINCR_BAD_ARG, "solve: bad arguments");
     if (!energies || !coefficients) fail(TINCR_BAD_ARG, "solve: null outputs");
-    if (precision != TINCR_PREC_FP64) fail(TINCR_BAD_ARG, "solve: precision not available in this build");
+    if (precision != TINCR_PREC_FP64 && precision != TINCR_PREC_BF16X3) fail(TINCR_BAD_ARG, "solve: unknown precision");
+    prec = precision;
     g_launches = 0;
     last_products = 0;
     last_collapses = 0;
@@ -619,9 +630,15 @@ int Ctx::solve(int n_roots, int max_iter, double tol, int precision, double *ene
             for (int j = 0; j < mold; ++j) aproj[(size_t)i * m + j] = old[(size_t)i * mold + j];
         if (knew > 0) {
             TINCR_CUDA(cudaMemsetAsync(dP.p, 0, (size_t)m * knew * sizeof(double), stream));
-            int sk = pick_splitk(m, knew, (int)ov, 1, n_sm);
-            pgemm<false, true>(*this, TINCR_KF_SUBSPACE, m, knew, (int)ov, dV.p, (int)ov, 0, dAV.p + (long long)mold * ov,
-                               (int)ov, 0, 1, EpiAtomicAdd{dP.p, 0, knew, 1.0}, sk);
+            if (knew <= 32) {
+                int slot = prof_begin(TINCR_KF_SUBSPACE);
+                skinny_dots(stream, n_sm, m, knew, ov, dV.p, ov, dAV.p + (long long)mold * ov, ov, dP.p, knew);
+                prof_end(slot, 2.0 * m * (double)knew * ov, 8.0 * (double)(m + knew) * ov);
+            } else {
+                int sk = pick_splitk(m, knew, (int)ov, 1, n_sm);
+                pgemm<false, true>(*this, TINCR_KF_SUBSPACE, m, knew, (int)ov, dV.p, (int)ov, 0,
+                                   dAV.p + (long long)mold * ov, (int)ov, 0, 1, EpiAtomicAdd{dP.p, 0, knew, 1.0}, sk);
+            }
             hP.resize((size_t)m * knew);
             TINCR_CUDA(cudaMemcpyAsync(hP.data(), dP.p, hP.size() * sizeof(double), cudaMemcpyDeviceToHost, stream));
             sync();
@@ -641,10 +658,17 @@ int Ctx::solve(int n_roots, int max_iter, double tol, int precision, double *ene
         TINCR_CUDA(cudaMemcpyAsync(dYt.p, yt.data(), yt.size() * sizeof(double), cudaMemcpyHostToDevice, stream));
         TINCR_CUDA(cudaMemcpyAsync(du.p, u.data(), n_roots * sizeof(double), cudaMemcpyHostToDevice, stream));
         // 3.1 Ritz vectors R = Y^T V ; 3.2 residuals Rk = Y^T AV - u o R
-        pgemm<false, false>(*this, TINCR_KF_SUBSPACE, n_roots, (int)ov, m, dYt.p, m, 0, dV.p, (int)ov, 0, 1,
-                            EpiStore{dR.p, 0, (int)ov, 1.0, 0.0});
-        pgemm<false, false>(*this, TINCR_KF_SUBSPACE, n_roots, (int)ov, m, dYt.p, m, 0, dAV.p, (int)ov, 0, 1,
-                            EpiResidual{dRk.p, dR.p, du.p, ov});
+        if (n_roots <= 32) {
+            int slot = prof_begin(TINCR_KF_SUBSPACE);
+            skinny_comb(stream, n_roots, m, ov, dYt.p, m, 1, dV.p, ov, CombStore{dR.p, ov, 1.0, 0.0});
+            skinny_comb(stream, n_roots, m, ov, dYt.p, m, 1, dAV.p, ov, CombResidual{dRk.p, dR.p, du.p, ov});
+            prof_end(slot, 4.0 * n_roots * (double)m * ov, 8.0 * (2.0 * m + 3.0 * n_roots) * ov);
+        } else {
+            pgemm<false, false>(*this, TINCR_KF_SUBSPACE, n_roots, (int)ov, m, dYt.p, m, 0, dV.p, (int)ov, 0, 1,
+                                EpiStore{dR.p, 0, (int)ov, 1.0, 0.0});
+            pgemm<false, false>(*this, TINCR_KF_SUBSPACE, n_roots, (int)ov, m, dYt.p, m, 0, dAV.p, (int)ov, 0, 1,
+                                EpiResidual{dRk.p, dR.p, du.p, ov});
+        }
         row_norms_kernel<<<n_roots, 256, 0, stream>>>(ov, dRk.p, dnorm.p);
         count_launch(stream, "row_norms");
         check_launch("row_norms");
@@ -679,11 +703,19 @@ int Ctx::solve(int n_roots, int max_iter, double tol, int precision, double *ene
                 check_launch("precondition");
                 // orthogonalise against the current basis in one block: T -= (T V^T) V
                 TINCR_CUDA(cudaMemsetAsync(dc.p, 0, (size_t)kadd * m * sizeof(double), stream));
-                int sk = pick_splitk(kadd, m, (int)ov, 1, n_sm);
-                pgemm<false, true>(*this, TINCR_KF_SUBSPACE, kadd, m, (int)ov, dT.p, (int)ov, 0, dV.p, (int)ov, 0, 1,
-                                   EpiAtomicAdd{dc.p, 0, m, 1.0}, sk);
-                pgemm<false, false>(*this, TINCR_KF_SUBSPACE, kadd, (int)ov, m, dc.p, m, 0, dV.p, (int)ov, 0, 1,
-                                    EpiStore{dT.p, 0, (int)ov, -1.0, 1.0});
+                if (kadd <= 32) {
+                    // c = V T^T  [m x kadd];  T -= c^T V
+                    int slot = prof_begin(TINCR_KF_SUBSPACE);
+                    skinny_dots(stream, n_sm, m, kadd, ov, dV.p, ov, dT.p, ov, dc.p, kadd);
+                    skinny_comb(stream, kadd, m, ov, dc.p, 1, kadd, dV.p, ov, CombStore{dT.p, ov, -1.0, 1.0});
+                    prof_end(slot, 4.0 * kadd * (double)m * ov, 8.0 * (2.0 * m + 3.0 * kadd) * ov);
+                } else {
+                    int sk = pick_splitk(kadd, m, (int)ov, 1, n_sm);
+                    pgemm<false, true>(*this, TINCR_KF_SUBSPACE, kadd, m, (int)ov, dT.p, (int)ov, 0, dV.p, (int)ov, 0, 1,
+                                       EpiAtomicAdd{dc.p, 0, m, 1.0}, sk);
+                    pgemm<false, false>(*this, TINCR_KF_SUBSPACE, kadd, (int)ov, m, dc.p, m, 0, dV.p, (int)ov, 0, 1,
+                                        EpiStore{dT.p, 0, (int)ov, -1.0, 1.0});
+                }
                 // then sequentially against the vectors accepted in this step (davidson.rs:162-168)
                 int m0 = m;
                 for (int j = 0; j < kadd; ++j) {
@@ -691,11 +723,12 @@ int Ctx::solve(int n_roots, int max_iter, double tol, int precision, double *ene
                     int acc = m - m0;
                     if (acc > 0) {
                         TINCR_CUDA(cudaMemsetAsync(dc.p, 0, acc * sizeof(double), stream));
-                        int sk2 = pick_splitk(1, acc, (int)ov, 1, n_sm);
-                        pgemm<false, true>(*this, TINCR_KF_SUBSPACE, 1, acc, (int)ov, t, (int)ov, 0,
-                                           dV.p + (long long)m0 * ov, (int)ov, 0, 1, EpiAtomicAdd{dc.p, 0, acc, 1.0}, sk2);
-                        pgemm<false, false>(*this, TINCR_KF_SUBSPACE, 1, (int)ov, acc, dc.p, acc, 0,
-                                            dV.p + (long long)m0 * ov, (int)ov, 0, 1, EpiStore{t, 0, (int)ov, -1.0, 1.0});
+                        // c = Q t  [acc x 1] over the vectors accepted in this step;  t -= c^T Q
+                        int slot = prof_begin(TINCR_KF_SUBSPACE);
+                        skinny_dots(stream, n_sm, acc, 1, ov, dV.p + (long long)m0 * ov, ov, t, ov, dc.p, 1);
+                        skinny_comb(stream, 1, acc, ov, dc.p, acc, 1, dV.p + (long long)m0 * ov, ov,
+                                    CombStore{t, ov, -1.0, 1.0});
+                        prof_end(slot, 4.0 * acc * (double)ov, 8.0 * (acc + 2.0) * ov);
                     }
                     row_norms_kernel<<<1, 256, 0, stream>>>(ov, t, dnorm.p);
                     count_launch(stream, "row_norms");

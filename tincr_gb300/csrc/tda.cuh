@@ -76,6 +76,8 @@ struct Ctx {
     DevBuf<double> gw, gv, gcg;            // gradient workspaces
     int last_cg_status = TINCR_OK;
 
+    int prec = TINCR_PREC_FP64;           // arithmetic of the exchange contractions in ao_contract
+
     // product workspace
     DevBuf<double> wsH, wsF, wsG, wsd3, wsd2, wsz;
     // Davidson state
