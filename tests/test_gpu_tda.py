@@ -94,6 +94,23 @@ def test_davidson_matches_oracle(gpu_ctx, name, lc):
     assert gpu["davidson_iterations"] == ref["iterations"]
 
 
+@pytest.mark.parametrize("name,lc", [("uracil", True), ("water8", True), ("polyene8", False)])
+def test_davidson_history_matches_oracle(gpu_ctx, name, lc):
+    """Iteration by iteration, the FP64 solve has the oracle's subspace size and number of
+    unconverged roots, and its largest residual agrees to 1e-8."""
+    c = _case(name, lc)
+    o = oracle_inputs(c)
+    hist = []
+    OT.run_tda(o["omega"], o["q_ov"], o["gamma"], c["xyz"], 4, 200, 1e-7, o["q_oo"], o["q_vv"], o["gamma_lr"],
+               o["n_occ"], o["n_virt"], history=hist)
+    _solver(gpu_ctx, c).run_tda(4, 200, 1e-7)
+    gh = gpu_ctx.davidson_history()
+    assert [h["n_sub"] for h in gh] == [h["n_sub"] for h in hist]
+    assert [h["roots_left"] for h in gh] == [h["roots_left"] for h in hist]
+    assert all(h["precision"] == _lib.PREC_FP64 for h in gh)
+    assert max(abs(a["max_residual"] - b["max_res"]) for a, b in zip(gh, hist)) < 1e-8
+
+
 def test_polyene_ten_roots_plain_fp64(gpu_ctx):
     """C20H22 all-trans polyene, non-LC DFTB, lowest 10 roots with residual < 1e-6."""
     c = synthetic_case("polyene", lc=False)
@@ -160,9 +177,27 @@ def test_not_converged_and_bad_arguments(gpu_ctx):
     assert e.value.status == _lib.BAD_ARG
 
 
+@pytest.mark.parametrize("plane", ["tc", "mma"])
+@pytest.mark.parametrize("name,lc", [("h2o", True), ("uracil", True), ("uracil", False), ("polyene8", True)])
+def test_mixed_plane_gemms_match_fp64(monkeypatch, name, lc, plane):
+    """Both plane GEMMs (tcgen05 + TMA, warp MMA) give the same split-BF16 A.X, within 1e-5 of the
+    FP64 product relative to max |A.X|, with and without the long-range exchange."""
+    monkeypatch.setenv("TINCR_GB300_PLANE_GEMM", plane)
+    ctx = _lib.Context(0)
+    try:
+        c = _case(name, lc)
+        s = _solver(ctx, c)
+        x = np.random.default_rng(11).standard_normal((c["n_occ"] * c["n_virt"], 5))
+        ref = s.compute_products(x)
+        mix = s.compute_products(x, precision=_lib.PREC_BF16X3)
+        assert np.abs(mix - ref).max() < 1e-5 * np.abs(ref).max()
+    finally:
+        ctx.close()
+
+
 @pytest.mark.parametrize("name", ["uracil", "water27"])
 def test_mixed_products_close_to_fp64(gpu_ctx, name):
-    """Split-BF16 exchange contractions: A.X within 1e-5 of the FP64 product (relative to max |A.X|)."""
+    """Split-BF16 contractions: A.X within 1e-5 of the FP64 product (relative to max |A.X|)."""
     c = _case(name, True)
     s = _solver(gpu_ctx, c)
     x = np.random.default_rng(5).standard_normal((c["n_occ"] * c["n_virt"], 4))
@@ -171,11 +206,31 @@ def test_mixed_products_close_to_fp64(gpu_ctx, name):
     assert np.abs(mix - ref).max() < 1e-5 * np.abs(ref).max()
 
 
+@pytest.mark.parametrize("plane", ["tc", "mma"])
 @pytest.mark.parametrize("name", ["water27", "uracil"])
-def test_mixed_davidson_energies_within_bar(gpu_ctx, name):
-    """Mixed form: every root within 1e-6 Eh of the FP64 GPU roots (spec bar)."""
-    c = _case(name, True)
-    ref = _solver(gpu_ctx, c).run_tda(6, 300, 1e-6)
-    e_ref = ref["ci_eigenvalues"].copy()
-    mix = _solver(gpu_ctx, c).run_tda(6, 300, 1e-6, precision=_lib.PREC_BF16X3)
-    assert np.abs(mix["ci_eigenvalues"] - e_ref).max() < 1e-6
+def test_mixed_davidson_energies_within_bar(monkeypatch, name, plane):
+    """Mixed form: every root within 1e-6 Eh of the FP64 GPU roots (spec bar), with either
+    plane GEMM."""
+    monkeypatch.setenv("TINCR_GB300_PLANE_GEMM", plane)
+    ctx = _lib.Context(0)
+    try:
+        c = _case(name, True)
+        ref = _solver(ctx, c).run_tda(6, 300, 1e-6)
+        e_ref = ref["ci_eigenvalues"].copy()
+        s = _solver(ctx, c)
+        mix = s.run_tda(6, 300, 1e-6, precision=_lib.PREC_BF16X3)
+        err = np.abs(mix["ci_eigenvalues"] - e_ref)
+        print("%s %s per-root |dE| (Eh):" % (name, plane), " ".join("%.2e" % e for e in err))
+        hist = ctx.davidson_history()
+        if err.max() >= 1e-6:
+            print("mixed energies", mix["ci_eigenvalues"])
+            for h in hist:
+                print(h)
+            x = np.random.default_rng(3).standard_normal((c["n_occ"] * c["n_virt"], 6))
+            p64 = s.compute_products(x)
+            pmx = s.compute_products(x, precision=_lib.PREC_BF16X3)
+            print("product check: max |mixed - fp64| / max |fp64| =", np.abs(pmx - p64).max() / np.abs(p64).max())
+        assert err.max() < 1e-6
+        assert hist[-1]["precision"] == _lib.PREC_FP64 and hist[0]["precision"] == _lib.PREC_BF16X3
+    finally:
+        ctx.close()

@@ -30,6 +30,7 @@ SIGNATURES = {
     "tincr_last_timing": (C.c_int, [C.c_void_p, _dp, C.POINTER(C.c_longlong)]),
     "tincr_tda_set_states": (C.c_int, [C.c_void_p, C.c_int, _dp, _dp]),
     "tincr_last_solve_stats": (C.c_int, [C.c_void_p, C.POINTER(C.c_longlong), _ip, _dp]),
+    "tincr_davidson_history": (C.c_int, [C.c_void_p, C.c_int, _ip, _ip, _ip, _dp, _ip, _ip]),
     "tincr_set_profiling": (C.c_int, [C.c_void_p, C.c_int]),
     "tincr_kernel_stats": (C.c_int, [C.c_void_p, C.c_int, _dp, C.POINTER(C.c_longlong), _dp, _dp]),
     "tincr_trans_charges": (C.c_int, [C.c_void_p, C.c_int, _ip, C.c_int, _dp, _dp, C.c_int, C.c_int, C.c_int,
@@ -131,6 +132,18 @@ class Context:
         r = C.c_double()
         self.check(self.lib.tincr_last_solve_stats(self.h, C.byref(n), C.byref(k), C.byref(r)))
         return dict(n_products=n.value, n_collapses=k.value, max_residual=r.value)
+
+    def davidson_history(self):
+        """Records of the last solve: list of dict(iter, n_sub, max_residual, roots_left, precision)."""
+        n = C.c_int()
+        self.check(self.lib.tincr_davidson_history(self.h, 0, C.byref(n), None, None, None, None, None))
+        k = n.value
+        it, ns, rl, pr = (np.zeros(k, np.int32) for _ in range(4))
+        mr = np.zeros(k)
+        self.check(self.lib.tincr_davidson_history(self.h, k, C.byref(n), iptr(it), iptr(ns), dptr(mr), iptr(rl),
+                                                   iptr(pr)))
+        return [dict(iter=int(it[i]), n_sub=int(ns[i]), max_residual=float(mr[i]), roots_left=int(rl[i]),
+                     precision=int(pr[i])) for i in range(k)]
 
     def last_timing(self):
         ms = C.c_double()

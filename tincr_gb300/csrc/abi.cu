@@ -78,6 +78,21 @@ int tincr_last_solve_stats(const tincr_ctx *ctx, long long *n_products, int *n_c
     return TINCR_OK;
 }
 
+int tincr_davidson_history(const tincr_ctx *ctx, int capacity, int *n_steps, int *iter, int *n_sub,
+                           double *max_residual, int *roots_left, int *precision) {
+    if (!ctx || !ctx->impl || capacity < 0) return TINCR_BAD_ARG;
+    const auto &h = ctx->impl->last_history;
+    if (n_steps) *n_steps = (int)h.size();
+    for (int i = 0; i < capacity && i < (int)h.size(); ++i) {
+        if (iter) iter[i] = h[i].iter;
+        if (n_sub) n_sub[i] = h[i].n_sub;
+        if (max_residual) max_residual[i] = h[i].max_residual;
+        if (roots_left) roots_left[i] = h[i].roots_left;
+        if (precision) precision[i] = h[i].prec;
+    }
+    return TINCR_OK;
+}
+
 int tincr_set_profiling(tincr_ctx *ctx, int enable) {
     return guarded(ctx, [&](tincr::Ctx &c) {
         c.sync();

@@ -1,0 +1,306 @@
+// Plane GEMM on the 5th-generation tensor cores: tcgen05.mma with TMEM accumulators, TMA loads.
+//
+// C[M x N] = A[M x K] B[N x K]^T with A = A_hi + A_lo, B = B_hi + B_lo split-BF16 planes
+// (planes.cuh), accumulated as A_hi B_hi + A_hi B_lo + A_lo B_hi.
+//
+// CTA = 192 threads, one 128 x 128 output tile, K consumed in 64-element (128-byte) blocks:
+//   * warp 4 / lane 0: TMA producer, four boxes (A_hi, A_lo, B_hi, B_lo; 128 rows x 64 bf16, 128-byte
+//     swizzle) per stage into a 3-stage ring, completion on the stage's "full" mbarrier;
+//   * warp 5 / lane 0: MMA issuer, 4 K=16 steps x 3 products per block (tcgen05.mma.cta_group::1
+//     .kind::f16, M = N = 128) into one of two TMEM accumulators (ping-pong), tcgen05.commit to the
+//     stage's "empty" and the accumulator's "full" mbarrier;
+//   * warps 0-3: fold each K block's accumulator into FP32 running sums held in registers (warp w
+//     owns TMEM lanes 32w..32w+31 = tile rows, one row per thread), then the epilogue functor.
+// The tensor core accumulates a block of only 12 MMAs before the CUDA cores add it with
+// round-to-nearest, which keeps long K (up to 2 n_orb) from building up a one-sided accumulation
+// error; the fold overlaps the next block's MMAs.
+// Every mbarrier wait is bounded (2 s); on expiry the thread records an error code and leaves its
+// loop, the MMA issuer waits (bounded) for its MMAs in flight, the producer for its loads, and the
+// CTA frees its TMEM and returns.
+#pragma once
+
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
+#include "planes.cuh"
+
+namespace tincr {
+
+constexpr int TC_M = 128, TC_N = 128, TC_K = 64, TC_STAGES = 3, TC_T = 192;
+constexpr int TC_TILE = TC_M * TC_K * 2;                  // 16 KB (128 rows x 128 bytes)
+constexpr int TC_STAGE = 4 * TC_TILE;                     // A_hi, A_lo, B_hi, B_lo
+constexpr int TC_SMEM = TC_STAGES * TC_STAGE + 1024 + 256;
+constexpr int TC_COLS = 2 * TC_N;                         // two accumulators
+constexpr unsigned long long TC_WAIT_NS = 2000000000ull;  // a wait gives up after 2 s
+
+// instruction descriptor, kind::f16: D = F32 (bits 4-5 = 1), A = B = BF16 (bits 7-9, 10-12 = 1),
+// both K-major (bits 15, 16 = 0), N >> 3 at bits 17-22, M >> 4 at bits 24-28
+constexpr uint32_t TC_IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(TC_N >> 3) << 17) |
+                              ((uint32_t)(TC_M >> 4) << 24);
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row groups 1024 bytes apart
+__device__ __forceinline__ uint64_t tc_desc(uint32_t saddr) {
+    uint64_t d = (uint64_t)((saddr >> 4) & 0x3FFF);
+    d |= (uint64_t)1 << 16;                 // leading byte offset (unused for swizzled K-major), 16 B
+    d |= (uint64_t)(1024 >> 4) << 32;       // stride byte offset: 1024 B between 8-row groups
+    d |= (uint64_t)1 << 46;                 // descriptor version for tcgen05
+    d |= (uint64_t)2 << 61;                 // swizzle: 128 B
+    return d;
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(count));
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;\n" : "=l"(t));
+    return t;
+}
+// bounded wait for the completion of the phase with the given parity; false on timeout
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, unsigned parity) {
+    uint32_t a = smem_u32(bar);
+    const unsigned long long t0 = global_ns();
+    for (unsigned it = 0;; ++it) {
+        uint32_t done;
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(done)
+            : "r"(a), "r"(parity)
+            : "memory");
+        if (done) return true;
+        if ((it & 63) == 63 && global_ns() - t0 > TC_WAIT_NS) return false;
+    }
+}
+
+__device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *map, int x, int y, int z, uint64_t *bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+        "[%5];\n" ::"r"(smem_u32(dst)),
+        "l"((uint64_t)map), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
+        : "memory");
+}
+
+__device__ __forceinline__ void tc_mma(uint32_t tmem, uint64_t adesc, uint64_t bdesc, uint32_t accumulate) {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+        " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+        "l"(adesc), "l"(bdesc), "r"(TC_IDESC), "r"(accumulate));
+}
+
+__device__ __forceinline__ void tc_commit(uint64_t *bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(smem_u32(bar))
+                 : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(smem_u32(bar)) : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+        "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];\n"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+          "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+          "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+        : "r"(taddr));
+}
+
+template <class Epi>
+__global__ void __launch_bounds__(TC_T, 1)
+gemm_planes_tc_kernel(const __grid_constant__ CUtensorMap ma_hi, const __grid_constant__ CUtensorMap ma_lo,
+                      const __grid_constant__ CUtensorMap mb_hi, const __grid_constant__ CUtensorMap mb_lo, int M,
+                      int N, int Kpad, int a_batched, int b_batched, Epi epi, int *err) {
+    extern __shared__ unsigned char tc_raw[];
+    unsigned char *smem = (unsigned char *)(((uintptr_t)tc_raw + 1023) & ~(uintptr_t)1023);
+    uint64_t *full = reinterpret_cast<uint64_t *>(smem + TC_STAGES * TC_STAGE);
+    uint64_t *empty = full + TC_STAGES;
+    uint64_t *accf = empty + TC_STAGES;      // accumulator a holds a finished K block
+    uint64_t *acce = accf + 2;               // accumulator a has been folded
+    uint64_t *done = acce + 2;               // every MMA issued has completed
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(done + 1);
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int b = blockIdx.z;
+    const int m0 = blockIdx.y * TC_M, n0 = blockIdx.x * TC_N;
+    const int nk = Kpad / TC_K;
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < TC_STAGES; ++s) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], 1);
+        }
+        for (int a = 0; a < 2; ++a) {
+            mbar_init(&accf[a], 1);
+            mbar_init(&acce[a], 4);          // one arrival per folding warp
+        }
+        mbar_init(done, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_u32(tmem_slot)),
+                     "r"(TC_COLS));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    const uint32_t tmem = *tmem_slot;
+
+    if (warp == 4) {
+        if (lane == 0) {
+            int issued = 0;
+            bool ok = true;
+            for (int kb = 0; kb < nk; ++kb) {
+                const int s = kb % TC_STAGES;
+                if (kb >= TC_STAGES && !mbar_wait(&empty[s], ((kb / TC_STAGES) & 1) ^ 1)) {
+                    atomicExch(err, 1);
+                    ok = false;
+                    break;
+                }
+                unsigned char *st = smem + s * TC_STAGE;
+                mbar_expect_tx(&full[s], TC_STAGE);
+                tma_load_3d(st + 0 * TC_TILE, &ma_hi, kb * TC_K, m0, a_batched ? b : 0, &full[s]);
+                tma_load_3d(st + 1 * TC_TILE, &ma_lo, kb * TC_K, m0, a_batched ? b : 0, &full[s]);
+                tma_load_3d(st + 2 * TC_TILE, &mb_hi, kb * TC_K, n0, b_batched ? b : 0, &full[s]);
+                tma_load_3d(st + 3 * TC_TILE, &mb_lo, kb * TC_K, n0, b_batched ? b : 0, &full[s]);
+                issued = kb + 1;
+            }
+            if (!ok)   // loads still in flight land before the CTA exits
+                for (int kb = (issued > TC_STAGES ? issued - TC_STAGES : 0); kb < issued; ++kb)
+                    mbar_wait(&full[kb % TC_STAGES], (kb / TC_STAGES) & 1);
+        }
+    } else if (warp == 5) {
+        if (lane == 0) {
+            for (int kb = 0; kb < nk; ++kb) {
+                const int s = kb % TC_STAGES, a = kb & 1;
+                if (!mbar_wait(&full[s], (kb / TC_STAGES) & 1)) {
+                    atomicExch(err, 2);
+                    break;
+                }
+                if (kb >= 2 && !mbar_wait(&acce[a], ((kb >> 1) - 1) & 1)) {
+                    atomicExch(err, 3);
+                    break;
+                }
+                asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+                const uint32_t base = smem_u32(smem + s * TC_STAGE);
+                const uint32_t d = tmem + (uint32_t)(a * TC_N);
+#pragma unroll
+                for (int kk = 0; kk < TC_K / 16; ++kk) {
+                    const uint32_t off = kk * 32;   // 16 bf16 = 32 bytes along K
+                    const uint64_t ah = tc_desc(base + 0 * TC_TILE + off), al = tc_desc(base + 1 * TC_TILE + off);
+                    const uint64_t bh = tc_desc(base + 2 * TC_TILE + off), bl = tc_desc(base + 3 * TC_TILE + off);
+                    tc_mma(d, ah, bh, kk > 0 ? 1u : 0u);
+                    tc_mma(d, ah, bl, 1u);
+                    tc_mma(d, al, bh, 1u);
+                }
+                tc_commit(&empty[s]);
+                tc_commit(&accf[a]);
+            }
+            tc_commit(done);
+            mbar_wait(done, 0);   // no MMA is in flight once the issuer leaves (also after a failure)
+        }
+    } else {
+        // folding warps 0-3: row m0 + 32 warp + lane, columns n0 .. n0 + 127
+        float sum[TC_N];
+#pragma unroll
+        for (int j = 0; j < TC_N; ++j) sum[j] = 0.f;
+        bool ok = true;
+        for (int kb = 0; kb < nk; ++kb) {
+            const int a = kb & 1;
+            ok = __all_sync(0xffffffffu, mbar_wait(&accf[a], (kb >> 1) & 1));
+            if (!ok) {
+                if (lane == 0) atomicExch(err, 4);
+                break;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+            const uint32_t t0 = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(a * TC_N);
+#pragma unroll
+            for (int c0 = 0; c0 < TC_N; c0 += 32) {
+                uint32_t r[32];
+                tmem_ld32(t0 + (uint32_t)c0, r);
+                asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+#pragma unroll
+                for (int j = 0; j < 32; ++j) sum[c0 + j] += __uint_as_float(r[j]);
+            }
+            asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&acce[a]);
+        }
+        const int row = m0 + warp * 32 + lane;
+        if (ok && row < M) {
+#pragma unroll
+            for (int c0 = 0; c0 < TC_N; c0 += 8) {
+                F8 v;
+#pragma unroll
+                for (int j = 0; j < 8; ++j) v.x[j] = sum[c0 + j];
+                epi.run8(b, row, n0 + c0, N, v);
+            }
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    if (warp == 0) {
+        asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(TC_COLS));
+    }
+}
+
+// ---------------------------------------------------------------------------------------------
+// host: tensor maps and launch
+// ---------------------------------------------------------------------------------------------
+
+inline PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    if (!fn) {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        TINCR_CUDA(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q));
+        if (!p || q != cudaDriverEntryPointSuccess) fail(TINCR_CUDA_ERR, "cuTensorMapEncodeTiled not available");
+        fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    }
+    return fn;
+}
+
+// 3-D map over bf16 planes [batch][rows][ld] with logical extent [batch][rows][Kpad], box 64 x 128
+inline CUtensorMap plane_map(const bf16 *base, int rows, long long Kpad, long long ld, long long sb, int batch) {
+    if (((uintptr_t)base & 15) || (ld * 2) % 16 || (sb * 2) % 16 || Kpad % TC_K)
+        fail(TINCR_BAD_ARG, "plane_map: alignment");
+    CUtensorMap m;
+    cuuint64_t dims[3] = {(cuuint64_t)Kpad, (cuuint64_t)rows, (cuuint64_t)(sb ? batch : 1)};
+    cuuint64_t strides[2] = {(cuuint64_t)(ld * 2), (cuuint64_t)((sb ? sb : ld * rows) * 2)};
+    cuuint32_t box[3] = {TC_K, TC_M, 1};
+    cuuint32_t estr[3] = {1, 1, 1};
+    CUresult r = tensor_map_encoder()(&m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<bf16 *>(base), dims, strides,
+                                      box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                                      CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) fail(TINCR_CUDA_ERR, "cuTensorMapEncodeTiled failed: " + std::to_string((int)r));
+    return m;
+}
+
+template <class Epi>
+void gemm_planes_tc(cudaStream_t st, int M, int N, int Kpad, PlaneOperand A, PlaneOperand B, int batch, Epi epi,
+                    int *d_err) {
+    if (M <= 0 || N <= 0 || batch <= 0) return;
+    if (Kpad <= 0 || Kpad % TC_K) fail(TINCR_BAD_ARG, "gemm_planes_tc: K not padded to 64");
+    CUtensorMap ah = plane_map(A.hi, M, Kpad, A.ld, A.sb, batch), al = plane_map(A.lo, M, Kpad, A.ld, A.sb, batch);
+    CUtensorMap bh = plane_map(B.hi, N, Kpad, B.ld, B.sb, batch), bl = plane_map(B.lo, N, Kpad, B.ld, B.sb, batch);
+    static bool attr = false;
+    if (!attr) {
+        TINCR_CUDA(cudaFuncSetAttribute(gemm_planes_tc_kernel<Epi>, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM));
+        attr = true;
+    }
+    dim3 grid(ceil_div(N, TC_N), ceil_div(M, TC_M), batch);
+    gemm_planes_tc_kernel<Epi><<<grid, TC_T, TC_SMEM, st>>>(ah, al, bh, bl, M, N, Kpad, A.sb ? 1 : 0, B.sb ? 1 : 0, epi,
+                                                           d_err);
+    count_launch(st, "gemm_planes_tc");
+    check_launch("gemm_planes_tc");
+}
+
+}  // namespace tincr

@@ -1,7 +1,6 @@
 // GEMM epilogues of the linear-response path and the timed GEMM launcher.
 #pragma once
 
-#include "gemm_bf16x3.cuh"
 #include "gemm_f64.cuh"
 #include "tda.cuh"
 
@@ -55,21 +54,6 @@ static void pgemm(Ctx &c, int family, int M, int N, int K, const double *A, int 
                   int ldb, long long sB, int batch, Epi epi, int splitk = 1) {
     int slot = c.prof_begin(family);
     gemm_f64<TA, TB>(c.stream, M, N, K, A, lda, sA, B, ldb, sB, batch, epi, splitk);
-    double nb = (double)batch;
-    double bytes = 8.0 * ((double)M * K * (sA ? nb : 1.0) + (double)K * N * (sB ? nb : 1.0) + (double)M * N * nb);
-    c.prof_end(slot, 2.0 * M * (double)N * K * nb, bytes);
-}
-
-// Same as pgemm, on the split-BF16 tensor-core GEMM when `mixed` is set.
-template <bool TA, bool TB, class Epi>
-static void pgemm_prec(Ctx &c, bool mixed, int family, int M, int N, int K, const double *A, int lda, long long sA,
-                       const double *B, int ldb, long long sB, int batch, Epi epi) {
-    if (!mixed) {
-        pgemm<TA, TB>(c, family, M, N, K, A, lda, sA, B, ldb, sB, batch, epi);
-        return;
-    }
-    int slot = c.prof_begin(family);
-    gemm_bf16x3<TA, TB>(c.stream, M, N, K, A, lda, sA, B, ldb, sB, batch, epi);
     double nb = (double)batch;
     double bytes = 8.0 * ((double)M * K * (sA ? nb : 1.0) + (double)K * N * (sB ? nb : 1.0) + (double)M * N * nb);
     c.prof_end(slot, 2.0 * M * (double)N * K * nb, bytes);

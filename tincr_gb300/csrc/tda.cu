@@ -17,6 +17,7 @@
 // sum_jb (ij|ab)_lr X_jb).  Cost per vector 8 n o v + 16 n^2 v instead of 2 N o v (o + v).
 // Without long-range correction F is diagonal-only and the two n^2 v products drop out.
 #include <algorithm>
+#include <cstdlib>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -293,6 +294,9 @@ Ctx::Ctx(int dev) : device(dev) {
     TINCR_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
     TINCR_CUDA(cudaEventCreate(&ev0));
     TINCR_CUDA(cudaEventCreate(&ev1));
+    // plane GEMM of the mixed-precision contraction: tcgen05 (default) or warp MMA
+    const char *pg = std::getenv("TINCR_GB300_PLANE_GEMM");
+    if (pg && std::string(pg) == "mma") use_tc = false;
 }
 
 Ctx::~Ctx() {
@@ -383,6 +387,8 @@ void Ctx::tda_setup(int n_atoms_, const int *opa, int n, const double *C, const 
     ov = (long long)no * nv;
     lc = gamma_lr != nullptr;
     upload_mo(n, C, S);
+    planes_ready = false;
+    mx_key = -1;
     h_xyz.assign(xyz, xyz + 3 * (size_t)n_atoms);
     upload(stream, d_xyz, xyz, 3 * (size_t)n_atoms);
     h_gamma.assign(gamma, gamma + (size_t)n_atoms * n_atoms);
@@ -432,10 +438,13 @@ int Ctx::product_chunk() const {
 // Implemented as  [SC_P; C_P]^T (ax gamma_lr o M + ac D(z)) [SC_Q; C_Q],  M = [C_R; SC_R] V [C_S; SC_S]^T.
 void Ctx::ao_contract(int k, int R, int S, const double *V, int P, int Q, double ax, double ac, double *out,
                       double alpha, double beta, const double *Xomega) {
+    if (prec == TINCR_PREC_BF16X3) {
+        ao_contract_mixed(k, R, S, V, P, Q, ax, ac, out, alpha, beta, Xomega);
+        return;
+    }
     const int n = n_orb;
     const int nr = bsz(R), ns = bsz(S), np = bsz(P), nq = bsz(Q);
     const bool exch = ax != 0.0 && lc;
-    const bool mixed = prec == TINCR_PREC_BF16X3;
     const int kc_max = product_chunk();
     const int wmax = std::max(n_occ, n_virt);
     wsH.reserve((size_t)kc_max * 2 * n * wmax);
@@ -452,15 +461,8 @@ void Ctx::ao_contract(int k, int R, int S, const double *V, int P, int Q, double
                             EpiStore{wsH.p, 2LL * n * ns, ns, 1.0, 0.0});
         if (exch) {
             // 2. F_b = ax gamma_lr o (H_b [C_S; SC_S]^T), diagonals captured for the Coulomb term
-            pgemm_prec<false, true>(*this, mixed, TINCR_KF_AO_EXCHANGE, 2 * n, 2 * n, ns, wsH.p, ns, 2LL * n * ns, stk(S),
-                                    ns, 0, kc, EpiLcHadamard{wsF.p, d_glr_ao.p, wsd3.p, wsd2.p, n, ax});
-            if (mixed && ac != 0.0) {
-                // Coulomb diagonals in FP64 (the mixed epilogue's captures are overwritten)
-                dim3 g(ceil_div(2LL * n * 32, 256), kc);
-                diag_dots_kernel<<<g, 256, 0, stream>>>(n, ns, wsH.p, stk(S), wsd3.p, wsd2.p);
-                count_launch(stream, "diag_dots");
-                check_launch("diag_dots");
-            }
+            pgemm<false, true>(*this, TINCR_KF_AO_EXCHANGE, 2 * n, 2 * n, ns, wsH.p, ns, 2LL * n * ns, stk(S), ns, 0, kc,
+                               EpiLcHadamard{wsF.p, d_glr_ao.p, wsd3.p, wsd2.p, n, ax});
         } else if (ac != 0.0) {
             dim3 g(ceil_div(2LL * n * 32, 256), kc);
             diag_dots_kernel<<<g, 256, 0, stream>>>(n, ns, wsH.p, stk(S), wsd3.p, wsd2.p);
@@ -477,8 +479,8 @@ void Ctx::ao_contract(int k, int R, int S, const double *V, int P, int Q, double
         }
         // 4. G_b = F_b [SC_Q; C_Q]
         if (exch) {
-            pgemm_prec<false, false>(*this, mixed, TINCR_KF_AO_EXCHANGE, 2 * n, nq, 2 * n, wsF.p, 2 * n, 4LL * n * n,
-                                     swp(Q), nq, 0, kc, EpiStore{wsG.p, 2LL * n * nq, nq, 1.0, 0.0});
+            pgemm<false, false>(*this, TINCR_KF_AO_EXCHANGE, 2 * n, nq, 2 * n, wsF.p, 2 * n, 4LL * n * n, swp(Q), nq, 0,
+                                kc, EpiStore{wsG.p, 2LL * n * nq, nq, 1.0, 0.0});
         } else if (ac != 0.0) {
             dim3 g(grid_for(2LL * n * nq, 256, n_sm), kc);
             scale_rows_kernel<<<g, 256, 0, stream>>>(n, nq, wsz.p, stk(Q), wsG.p);
@@ -569,16 +571,10 @@ void Ctx::set_states(int n_roots, const double *energies, const double *coeffici
 // Davidson (src/excited_states/solvers/davidson.rs:53-185)
 // ----------------------------------------------------------------------------------------------
 
-int Ctx::solve(int n_roots, int max_iter, double tol, int precision, double *energies, double *coefficients,
-               double *osc, double *tr_dip, double *q_trans, int *iterations) {
-    if (!ready) fail(TINCR_BAD_ARG, "tincr_tda_setup must be called first");
-    if (n_roots <= 0 || n_roots > ov || max_iter <= 0 || !(tol > 0.0)) fail(TINCR_BAD_ARG, "solve: bad arguments");
-    if (!energies || !coefficients) fail(TINCR_BAD_ARG, "solve: null outputs");
-    if (precision != TINCR_PREC_FP64 && precision != TINCR_PREC_BF16X3) fail(TINCR_BAD_ARG, "solve: unknown precision");
-    prec = precision;
-    g_launches = 0;
-    last_products = 0;
-    last_collapses = 0;
+// Block Davidson on the current operator (precision `prec`).  Initial subspace: unit vectors on the
+// n_roots smallest omega (tincr's guess), or the rows of dR (Ritz vectors of an earlier run), in which
+// case the run may stop at its first iteration.  Leaves Ritz values in u and Ritz vectors in dR.
+int Ctx::davidson(int n_roots, int max_iter, double tol, bool from_ritz, std::vector<double> &u, int *it_out) {
     const int max_space = 15 * n_roots;                        // davidson.rs:74
     const int mmax = std::max(max_space, n_roots);
     dV.reserve((size_t)mmax * ov);
@@ -589,13 +585,24 @@ int Ctx::solve(int n_roots, int max_iter, double tol, int precision, double *ene
     DevBuf<double> dP((size_t)mmax * n_roots + 64), dYt((size_t)n_roots * mmax), du(n_roots), dnorm(n_roots),
         dw(n_roots), dc((size_t)mmax * n_roots + 64);
     DevBuf<int> didx(n_roots);
-    TINCR_CUDA(cudaEventRecord(ev0, stream));
-
-    // initial subspace: unit vectors on the n_roots smallest omega (solvers/utils.rs:17-26, stable ties)
-    std::vector<int> order(ov);
-    std::iota(order.begin(), order.end(), 0);
-    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return h_omega[a] < h_omega[b]; });
-    {
+    u.assign(n_roots, 0.0);
+    if (from_ritz) {
+        TINCR_CUDA(cudaMemcpyAsync(dV.p, dR.p, (size_t)n_roots * ov * sizeof(double), cudaMemcpyDeviceToDevice, stream));
+        // the Ritz vectors of an orthonormal basis are unit vectors; anything else is a broken run
+        row_norms_kernel<<<n_roots, 256, 0, stream>>>(ov, dV.p, dnorm.p);
+        count_launch(stream, "row_norms");
+        check_launch("row_norms");
+        std::vector<double> nr(n_roots);
+        TINCR_CUDA(cudaMemcpyAsync(nr.data(), dnorm.p, n_roots * sizeof(double), cudaMemcpyDeviceToHost, stream));
+        sync();
+        for (int r = 0; r < n_roots; ++r)
+            if (!(std::fabs(nr[r] - 1.0) < 1e-6))
+                fail(TINCR_NONFINITE, "Ritz vector " + std::to_string(r) + " has norm " + std::to_string(nr[r]));
+    } else {
+        // unit vectors on the n_roots smallest omega (solvers/utils.rs:17-26, stable ties)
+        std::vector<int> order(ov);
+        std::iota(order.begin(), order.end(), 0);
+        std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return h_omega[a] < h_omega[b]; });
         std::vector<int> pos(order.begin(), order.begin() + n_roots);
         DevBuf<int> dpos(n_roots);
         TINCR_CUDA(cudaMemcpyAsync(dpos.p, pos.data(), n_roots * sizeof(int), cudaMemcpyHostToDevice, stream));
@@ -610,7 +617,7 @@ int Ctx::solve(int n_roots, int max_iter, double tol, int precision, double *ene
     int dim_sub = n_roots;      // tincr's dim_sub bookkeeping
     const int dim_sub_origin = n_roots;
     std::vector<double> aproj;  // m x m upper triangle used
-    std::vector<double> hP, u(n_roots), w(mmax), z;
+    std::vector<double> hP, w(mmax), z;
     std::vector<double> errs(n_roots);
     int status = TINCR_NOT_CONVERGED;
     int it_done = 0;
@@ -681,8 +688,8 @@ int Ctx::solve(int n_roots, int max_iter, double tol, int precision, double *ene
         }
         int roots_lft = n_roots - roots_cvd;
         last_max_residual = *std::max_element(errs.begin(), errs.end());
-        last_history.push_back({it, m, last_max_residual, roots_lft});
-        if (roots_lft == 0 && it > 0) {                        // davidson.rs:121
+        last_history.push_back({it, m, last_max_residual, roots_lft, prec});
+        if (roots_lft == 0 && (it > 0 || from_ritz)) {         // davidson.rs:121
             status = TINCR_OK;
             break;
         }
@@ -754,6 +761,34 @@ int Ctx::solve(int n_roots, int max_iter, double tol, int precision, double *ene
             m_done = 0;
             aproj.clear();
         }
+    }
+    *it_out = it_done;
+    return status;
+}
+
+int Ctx::solve(int n_roots, int max_iter, double tol, int precision, double *energies, double *coefficients,
+               double *osc, double *tr_dip, double *q_trans, int *iterations) {
+    if (!ready) fail(TINCR_BAD_ARG, "tincr_tda_setup must be called first");
+    if (n_roots <= 0 || n_roots > ov || max_iter <= 0 || !(tol > 0.0)) fail(TINCR_BAD_ARG, "solve: bad arguments");
+    if (!energies || !coefficients) fail(TINCR_BAD_ARG, "solve: null outputs");
+    if (precision != TINCR_PREC_FP64 && precision != TINCR_PREC_BF16X3) fail(TINCR_BAD_ARG, "solve: unknown precision");
+    g_launches = 0;
+    last_products = 0;
+    last_collapses = 0;
+    last_history.clear();
+    TINCR_CUDA(cudaEventRecord(ev0, stream));
+    std::vector<double> u;
+    int it_done = 0;
+    prec = precision;
+    int status = davidson(n_roots, max_iter, tol, false, u, &it_done);
+    if (precision == TINCR_PREC_BF16X3) {
+        // FP64 polish: Davidson on the exact operator from the mixed Ritz vectors, which may stop at
+        // its first Rayleigh-Ritz step.  Energies then come from an FP64 projection (second order in
+        // the mixed vectors' error) and every residual norm is that of the FP64 operator.
+        prec = TINCR_PREC_FP64;
+        int it2 = 0;
+        status = davidson(n_roots, std::max(1, max_iter - it_done), tol, true, u, &it2);
+        it_done += it2;
     }
     // results: energies, coefficients [ov x n_roots], transition charges, dipoles, oscillator strengths
     TINCR_CUDA(cudaEventRecord(ev1, stream));

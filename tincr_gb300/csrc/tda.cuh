@@ -1,6 +1,8 @@
 // Device context of one molecular system (see tda.cu).
 #pragma once
 
+#include <cuda_bf16.h>
+
 #include <vector>
 
 #include "common.cuh"
@@ -12,6 +14,7 @@ struct DavidsonStep {
     int n_sub;
     double max_residual;
     int roots_left;
+    int prec;
 };
 
 // Per-kernel-family device timing (CUDA events on the library stream), enabled on request.
@@ -76,7 +79,15 @@ struct Ctx {
     DevBuf<double> gw, gv, gcg;            // gradient workspaces
     int last_cg_status = TINCR_OK;
 
-    int prec = TINCR_PREC_FP64;           // arithmetic of the exchange contractions in ao_contract
+    int prec = TINCR_PREC_FP64;           // arithmetic of the contractions in ao_contract
+
+    // split-BF16 planes of the mixed-precision contraction (mixed.cu)
+    bool planes_ready = false;
+    bool use_tc = true;                   // tcgen05 plane GEMM; false: warp-MMA plane GEMM
+    DevBuf<__nv_bfloat16> cst_hi[2], cst_lo[2], cswT_hi[2], cswT_lo[2], mx_bf16;
+    DevBuf<double> mx_f64;
+    long long mx_key = -1;
+    DevBuf<int> d_tc_err;                 // error word of the tensor-core kernels' bounded waits
 
     // product workspace
     DevBuf<double> wsH, wsF, wsG, wsd3, wsd2, wsz;
@@ -100,6 +111,9 @@ struct Ctx {
     int bsz(int b) const { return b == BLK_OCC ? n_occ : n_virt; }
     void ao_contract(int k, int R, int S, const double *V, int P, int Q, double ax, double ac, double *out,
                      double alpha, double beta, const double *Xomega);
+    void prepare_planes();
+    void ao_contract_mixed(int k, int R, int S, const double *V, int P, int Q, double ax, double ac, double *out,
+                           double alpha, double beta, const double *Xomega);
     void products_dev(int k, const double *X, double *AX, double *y_out);
     void qtrans_dev(int k, const double *X, double *y_out);
     void products(int k, const double *X, double *AX, int precision);
@@ -115,6 +129,7 @@ struct Ctx {
     void set_states(int n_roots, const double *energies, const double *coefficients);
     int solve(int n_roots, int max_iter, double tol, int precision, double *energies, double *coefficients,
               double *osc, double *tr_dip, double *q_trans, int *iterations);
+    int davidson(int n_roots, int max_iter, double tol, bool from_ritz, std::vector<double> &u, int *it_out);
 };
 
 // A.X product with caller-owned device buffers and fixed device scratch (noalloc.cu)
