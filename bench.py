@@ -2,15 +2,19 @@
 
 Workload (one "step"): LC-TDA of the (H2O)128 water cluster (768 orbitals, 512 occupied x 256
 virtual, omega = 0.3 bohr^-1 i.e. R_lr = 3.3333 bohr), lowest 20 roots with tincr's `sp` job
-settings (max_iter 450, residual tolerance 1e-4; src/main.rs:124): transition charges / AO setup,
-block Davidson, oscillator strengths.  Geometry: seeded synthetic cluster (tincr_gb300.geometry);
-the ground state (C, S, orbital energies, gamma matrices) is prepared once on the host and is not
-part of a step.
+settings (max_iter 450, residual tolerance 1e-4; src/main.rs:124), then the analytic gradient of
+S1 (ground-state + excitation gradient, tincr's formulas: Z-vector, derivative contractions).
+Geometry: seeded synthetic cluster (tincr_gb300.geometry); the ground state (C, S, P, orbital
+energies, gamma matrices) is prepared once on the host and is not part of a step.
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--precision fp64|bf16x3] [--impl reference]
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--precision bf16x3|fp64] [--impl reference]
 
+The default precision is the mixed form (split-BF16 tensor-core products, FP64 convergence); the
+run also times the plain FP64 form of the same step and reports it under "fp64_gpu" with the
+largest energy and gradient differences between the two.
 `value` is device time per step (CUDA events on the library stream, inputs resident in HBM);
-`e2e` is the same step through the C ABI with host buffers (setup upload + solve + result copy).
+`e2e` is the same step through the C ABI with host buffers (setup upload, solve, parameter upload,
+gradient, result copies).
 `--impl reference` times the CPU restatement of tincr's algorithm (the oracle, numpy + the host
 BLAS with all host threads) on a bounded sample of the same workload and scales it to one step.
 Under torchrun (N > 1) every rank runs an independent replica (the path does not shard one
@@ -33,6 +37,7 @@ sys.path.insert(0, ROOT)
 
 METRIC = "LC-TDA roots+S1 grad wall s (mixed vs FP64 GPU, <=1e-6 Eh); FMO monomers/s"
 N_ROOTS, MAX_ITER, TOL = 20, 450, 1e-4
+PRECISIONS = {"fp64": 0, "bf16x3": 1}   # tincr_precision values
 R_LR = 1.0 / 0.3
 
 
@@ -133,9 +138,10 @@ def run_gpu(args):
         dist.init_process_group("gloo")
     torch.cuda.set_device(local)
     from tincr_gb300 import _lib, build
+    from tincr_gb300 import gradients as GR
     from tincr_gb300 import tda as T
     build.build()
-    prec = {"fp64": _lib.PREC_FP64, "bf16x3": _lib.PREC_BF16X3}[args.precision]
+    prec = PRECISIONS[args.precision]
     sy, g = workload()
     ctx = _lib.Context(local)
     es = T.ExcitedStateSystem.from_ground_state(ctx, sy, g)
@@ -143,38 +149,51 @@ def run_gpu(args):
     # pinned host copies of the step inputs for the end-to-end leg
     host_in = [es.orbs, es.s, es.orbe, es.gamma, es.gamma_lr, es.xyz]
     h2d_bytes = sum(a.nbytes for a in host_in) + es.opa.nbytes
-    d2h_bytes = 8 * (N_ROOTS * (1 + es.dim + 1 + 3 + es.n_atoms))
-
-    def step():
-        es.run_tda(N_ROOTS, MAX_ITER, TOL, precision=prec)
-        return ctx.last_timing()
-
     es.prepare_tda()
-    for _ in range(args.warmup):
-        l2_flush(flush)
-        torch.cuda.synchronize()
-        step()
-    # device-timed region: inputs resident (prepare_tda done), Davidson + moments per step
-    ctx.set_profiling(True)
-    dev_ms, launches, iters = [], 0, []
-    n_products_total = 0
-    barrier_and_max(0.0, world)
-    torch.cuda.synchronize()
-    with ClockSampler(local) as clocks:
-        t0 = time.perf_counter()
-        for _ in range(args.steps):
+    gr = GR.GradientSystem(es, sy, g)
+    h2d_bytes += gr.p.nbytes + gr.h.nbytes + gr.dq.nbytes + gr.atom_kind.nbytes
+    h2d_bytes += sum(np.asarray(v).nbytes for v in gr.tables.values() if isinstance(v, np.ndarray))
+    d2h_bytes = 8 * (N_ROOTS * (1 + es.dim + 1 + 3 + es.n_atoms)) + 2 * 8 * 3 * sy.n_atoms
+
+    def step(p):
+        """One step: lowest N_ROOTS roots, then the S1 (ground + excitation) gradient."""
+        r = es.run_tda(N_ROOTS, MAX_ITER, TOL, precision=p)
+        ms1, nl1 = ctx.last_timing()
+        ggs, gex = gr.both(0, "reference")
+        ms2, nl2 = ctx.last_timing()
+        return ms1 + ms2, nl1 + nl2, r, ggs + gex
+
+    def timed(p, warm, steps, profile):
+        for _ in range(warm):
             l2_flush(flush)
             torch.cuda.synchronize()
-            ms, nl = step()
+            step(p)
+        if profile:
+            ctx.set_profiling(True)
+        dev_ms, launches, iters, prods = [], 0, [], 0
+        barrier_and_max(0.0, world)
+        torch.cuda.synchronize()
+        for _ in range(steps):
+            l2_flush(flush)
+            torch.cuda.synchronize()
+            ms, nl, r, grad = step(p)
             dev_ms.append(ms)
             launches += nl
-            iters.append(es.properties["davidson_iterations"])
-            n_products_total += es.properties["n_products"]
+            iters.append(r["davidson_iterations"])
+            prods += es.properties["n_products"]
         torch.cuda.synchronize()
+        stats = {f: ctx.kernel_stats(f) for f in range(_lib.KF_COUNT)} if profile else None
+        if profile:
+            ctx.set_profiling(False)
+        return dict(dev_ms=dev_ms, launches=launches, iters=iters, products=prods, stats=stats,
+                    energies=r["ci_eigenvalues"].copy(), grad=grad.copy(), cg=gr.last_cg_iterations)
+
+    with ClockSampler(local) as clocks:
+        t0 = time.perf_counter()
+        main = timed(prec, args.warmup, args.steps, True)
         wall = time.perf_counter() - t0
-    stats = {f: ctx.kernel_stats(f) for f in range(4)}
-    ctx.set_profiling(False)
-    # end-to-end leg: the public call sequence with host buffers (setup upload + solve + download)
+    # end-to-end leg: the public call sequence with host buffers (setup upload, solve, parameter
+    # upload, gradient, result copies) for a system handed over from the host
     e2e = []
     for _ in range(args.steps):
         l2_flush(flush)
@@ -184,72 +203,93 @@ def run_gpu(args):
                                    es.gamma_lr, es.xyz)
         es2.prepare_tda()
         es2.run_tda(N_ROOTS, MAX_ITER, TOL, precision=prec)
+        gr2 = GR.GradientSystem(es2, sy, g)
+        gr2.both(0, "reference")
         e2e.append(time.perf_counter() - t0)
-    step_s = barrier_and_max(float(np.mean(dev_ms)) / 1e3, world)
+    # the plain FP64 form of the same step, for the mixed-vs-FP64 comparison
+    ref64 = None
+    if prec != _lib.PREC_FP64 and args.compare_fp64:
+        es.prepare_tda()
+        gr = GR.GradientSystem(es, sy, g)
+        ref64 = timed(_lib.PREC_FP64, 1, max(1, min(args.steps, 2)), False)
+    step_s = barrier_and_max(float(np.mean(main["dev_ms"])) / 1e3, world)
     e2e_s = barrier_and_max(float(np.mean(e2e)), world)
-    energies = es.properties["ci_eigenvalues"]
-    out = None
-    if rank == 0:
-        peaks = {}
-        pk = os.path.join(ROOT, "MEASURED_PEAKS.json")
-        if os.path.exists(pk):
-            peaks = json.load(open(pk))
-        ex = stats[_lib.KF_AO_EXCHANGE]
-        if prec == _lib.PREC_FP64:
-            # FP64 runs on the DFMA pipe; no measured FP64 peak exists, use the nominal GB300 rate
-            achieved = ex["flops"] / (ex["ms"] / 1e3) / 1e12 if ex["ms"] > 0 else None
-            peak, peak_note = 1.25, "nominal FP64 1.25 TFLOP/s (no measured FP64 peak)"
-            bound, unit = "fp64", "TFLOP/s"
-        else:
-            achieved = ex["flops"] / (ex["ms"] / 1e3) / 1e12 if ex["ms"] > 0 else None
-            peak = peaks.get("bf16_tflops", 1900.0)
-            peak_note = "measured bf16_tflops" if "bf16_tflops" in peaks else "fallback 1.9 PFLOP/s"
-            bound, unit = "tensor", "TFLOP/s"
-        # DRAM bytes per launch of the exchange family: ncu bytes per product vector (full-size
-        # capture, profiles/) times the vectors per launch of this solve (2 launches per chunk)
-        traffic = None
-        tf = os.path.join(ROOT, "profiles", "ao_exchange_traffic.json")
-        if os.path.exists(tf) and ex["launches"] > 0:
-            rec = json.load(open(tf)).get(args.precision)
-            if rec:
-                vec_per_launch = 2.0 * n_products_total / ex["launches"]
-                traffic = rec["dram_bytes_per_vector"] * vec_per_launch / 2.0
-        cpu = cpu_baseline(sy, g, sum(iters) / len(iters), es) if args.cpu_baseline else None
-        out = {
-            "metric": METRIC, "value": step_s, "unit": "s", "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": step_s * 1e3, "higher_is_better": False,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64" if prec == _lib.PREC_FP64 else "bf16x3+f64",
-            "data": "synthetic (seeded (H2O)128 cluster, host SCC ground state)",
-            "config": {"workload": "water128-lctda-20roots", "n_orb": int(sy.n_orbs), "n_occ": int(sy.n_occ),
-                       "n_virt": int(sy.n_virt), "n_roots": N_ROOTS, "tol": TOL, "max_iter": MAX_ITER,
-                       "r_lr_bohr": R_LR, "precision": args.precision, "l2": "flushed (256 MB write) between steps",
-                       "parallelism": "replicas" if world > 1 else "single-gpu",
-                       "davidson_iterations": iters[-1]},
-            "e2e": {"value": e2e_s, "unit": "s", "h2d_bytes_per_step": int(h2d_bytes),
-                    "d2h_bytes_per_step": int(d2h_bytes)},
-            "gpu_launches": int(launches),
-            "roofline": {"bound": bound, "achieved": achieved, "peak": peak, "unit": unit,
-                         "frac": (achieved / peak) if achieved else None, "traffic": traffic,
-                         "algorithmic_flops_per_launch": ex["flops"] / max(1, ex["launches"]),
-                         "algorithmic_bytes_per_launch": ex["bytes"] / max(1, ex["launches"]),
-                         "kernel": "AO-exchange contractions (gemm_f64, A.X steps 2 and 4)",
-                         "peak_source": peak_note,
-                         "kernel_ms_per_step": ex["ms"] / args.steps,
-                         "kernel_share_of_step": ex["ms"] / max(1e-9, sum(dev_ms))},
-            "kernel_families_ms_per_step": {n: stats[f]["ms"] / args.steps for f, n in
-                                            enumerate(["ao_exchange", "ao_transform", "subspace", "other"])},
-            "cpu_baseline": cpu,
-            "clocks": clocks.summary(),
-            "lowest_energies_eh": [float(e) for e in energies[:3]],
-            "wall_s": wall,
-        }
+    if rank != 0:
+        return None
+    stats = main["stats"]
+    peaks = {}
+    pk = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(pk):
+        peaks = json.load(open(pk))
+    ex = stats[_lib.KF_AO_EXCHANGE]
+    achieved = ex["flops"] / (ex["ms"] / 1e3) / 1e12 if ex["ms"] > 0 else None
+    if prec == _lib.PREC_FP64:
+        # FP64 runs on the DFMA pipe; no measured FP64 peak exists, use the nominal GB300 rate
+        peak, peak_note = 1.25, "nominal FP64 1.25 TFLOP/s (no measured FP64 peak)"
+        bound, kernel = "fp64", "AO-exchange contractions (gemm_f64, A.X steps 2 and 4)"
+    else:
+        peak = peaks.get("bf16_tflops", 1900.0)
+        peak_note = ("measured bf16_tflops" if "bf16_tflops" in peaks else "fallback 1.9 PFLOP/s") + \
+            "; achieved counts the algorithmic 2MNK once, the tensor pipe executes 3 split products"
+        bound, kernel = "tensor", "AO-exchange contractions (gemm_planes_tc, tcgen05 split-BF16, A.X steps 2 and 4)"
+    # DRAM bytes per launch of the exchange family: ncu bytes per product vector (capture in
+    # profiles/) times the vectors per launch of this step (2 launches per chunk)
+    traffic = None
+    tf = os.path.join(ROOT, "profiles", "ao_exchange_traffic.json")
+    if os.path.exists(tf) and ex["launches"] > 0:
+        rec = json.load(open(tf)).get(args.precision)
+        if rec:
+            vec_per_launch = 2.0 * main["products"] / ex["launches"]
+            traffic = rec["dram_bytes_per_vector"] * vec_per_launch / 2.0
+    cpu = cpu_baseline(sy, g, float(np.mean(main["iters"])), main["products"] / args.steps, main["cg"]) \
+        if args.cpu_baseline else None
+    fams = ["ao_exchange", "ao_transform", "subspace", "gradient", "other"][:_lib.KF_COUNT]
+    out = {
+        "metric": METRIC, "value": step_s, "unit": "s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": step_s * 1e3, "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64" if prec == _lib.PREC_FP64 else "bf16x3+f64",
+        "data": "synthetic (seeded (H2O)128 cluster, host SCC ground state)",
+        "config": {"workload": "water128-lctda-20roots+S1grad", "n_orb": int(sy.n_orbs), "n_occ": int(sy.n_occ),
+                   "n_virt": int(sy.n_virt), "n_roots": N_ROOTS, "tol": TOL, "max_iter": MAX_ITER,
+                   "r_lr_bohr": R_LR, "precision": args.precision, "gradient": "S1, tincr formulas",
+                   "l2": "flushed (256 MB write) between steps",
+                   "parallelism": "replicas" if world > 1 else "single-gpu",
+                   "davidson_iterations": main["iters"][-1], "zvector_cg_iterations": main["cg"]},
+        "e2e": {"value": e2e_s, "unit": "s", "h2d_bytes_per_step": int(h2d_bytes),
+                "d2h_bytes_per_step": int(d2h_bytes)},
+        "gpu_launches": int(main["launches"]),
+        "roofline": {"bound": bound, "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                     "frac": (achieved / peak) if achieved else None, "traffic": traffic,
+                     "algorithmic_flops_per_launch": ex["flops"] / max(1, ex["launches"]),
+                     "algorithmic_bytes_per_launch": ex["bytes"] / max(1, ex["launches"]),
+                     "kernel": kernel, "peak_source": peak_note,
+                     "kernel_ms_per_step": ex["ms"] / args.steps,
+                     "kernel_share_of_step": ex["ms"] / max(1e-9, sum(main["dev_ms"]))},
+        "kernel_families_ms_per_step": {n: stats[f]["ms"] / args.steps for f, n in enumerate(fams)},
+        "cpu_baseline": cpu,
+        "clocks": clocks.summary(),
+        "lowest_energies_eh": [float(e) for e in main["energies"][:3]],
+        "wall_s": wall,
+    }
+    if ref64 is not None:
+        out["fp64_gpu"] = {"value": float(np.mean(ref64["dev_ms"])) / 1e3, "unit": "s",
+                           "speedup_of_mixed": float(np.mean(ref64["dev_ms"])) / max(1e-9, float(np.mean(main["dev_ms"]))),
+                           "max_abs_energy_err_eh": float(np.abs(main["energies"] - ref64["energies"]).max()),
+                           "max_abs_grad_err_eh_per_bohr": float(np.abs(main["grad"] - ref64["grad"]).max())}
     return out
 
 
-def cpu_sample(sy, g, n_products, n_iters, sample_vectors=2):
-    """Time tincr's reference-form algorithm (oracle, numpy + host BLAS) on a bounded sample:
-    transition charges + `sample_vectors` A.X products + one Davidson subspace step at full
-    size, scaled to the products and iterations of one full solve."""
+def cpu_sample(sy, g, n_products, n_iters, cg_iters, sample_vectors=2):
+    """Time tincr's reference-form algorithm (oracle, numpy + host BLAS) on a bounded sample of one
+    step and scale it to the whole step.
+
+    TDA: transition charges + `sample_vectors` A.X products + one Davidson subspace step at full
+    size, scaled to the products and iterations of one solve.  Gradient (tincr's dense formulas,
+    src/gradients/helpers.rs:47-188): the f_v and f_lr loop bodies for the 3 coordinates of one atom
+    at full size (dense dS / dgamma operands, which is how tincr multiplies them), scaled to 3N
+    coordinates and their two calls each, plus `cg_iters` Z-vector products and the [3N, n^2]
+    contractions.  The construction of the derivative tensors themselves is not counted."""
+    from oracle import gradients as OG
     from oracle import tda as OT
     t0 = time.perf_counter()
     occ, virt = sy.occ_indices, sy.virt_indices
@@ -260,7 +300,7 @@ def cpu_sample(sy, g, n_products, n_iters, sample_vectors=2):
     rng = np.random.default_rng(0)
     x = rng.standard_normal((len(om), sample_vectors))
     t0 = time.perf_counter()
-    ax = eng.apply(x)
+    eng.apply(x)
     t_prod = (time.perf_counter() - t0) / sample_vectors
     # one subspace step with a half-full subspace (projection, eigh, Ritz, residuals)
     m = min(15 * N_ROOTS, 150)
@@ -273,16 +313,36 @@ def cpu_sample(sy, g, n_products, n_iters, sample_vectors=2):
     rk = av @ y[:, :N_ROOTS] - ritz * w[:N_ROOTS]
     np.linalg.norm(rk, axis=0)
     t_sub = time.perf_counter() - t0
-    total = t_setup + n_products * t_prod + n_iters * t_sub
+    del qov, qoo, qvv, eng, v, av
+    # gradient sample: one atom's 3 coordinates of f_lr and f_v, and of the [3N, n^2] contractions
+    n, N = g.s.shape[0], sy.n_atoms
+    ds = rng.standard_normal((3, n, n))
+    dg = rng.standard_normal((3, n, n))
+    vm = rng.standard_normal((n, n))
+    glr_ao = g.gamma_lr[np.ix_(sy.ao_atom, sy.ao_atom)]
+    g_ao = g.gamma[np.ix_(sy.ao_atom, sy.ao_atom)]
+    t0 = time.perf_counter()
+    OG.f_lr(vm, g.s, ds, glr_ao, dg, 1, n)
+    t_flr = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    OG.f_v(vm, g.s, ds, g_ao, dg, 1, n)
+    t_fv = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    ds.reshape(3, -1) @ vm.reshape(-1)
+    t_mv = time.perf_counter() - t0
+    t_grad = N * (2.0 * t_flr + 2.0 * t_fv + 6.0 * t_mv) + cg_iters * t_prod
+    total = t_setup + n_products * t_prod + n_iters * t_sub + t_grad
     threads = os.cpu_count()
-    sample = ("trans_charges + %d reference-form A.X products (%.2f s each) + one subspace step at m=%d, "
-              "scaled to %d products and %d Davidson iterations" % (sample_vectors, t_prod, m, n_products, n_iters))
+    sample = ("TDA: trans_charges + %d reference-form A.X products (%.2f s each) + one subspace step at m=%d, "
+              "scaled to %d products and %d Davidson iterations; S1 gradient: f_lr (%.2f s) and f_v (%.2f s) "
+              "on 3 of %d coordinates, scaled to all coordinates x 2 calls, + %d Z-vector products "
+              "(derivative-tensor construction not counted)"
+              % (sample_vectors, t_prod, m, n_products, n_iters, t_flr, t_fv, 3 * N, cg_iters))
     return total, threads, sample
 
 
-def cpu_baseline(sy, g, n_iters, es):
-    n_products = int(es.properties["n_products"])
-    total, threads, sample = cpu_sample(sy, g, n_products, int(n_iters))
+def cpu_baseline(sy, g, n_iters, n_products, cg_iters):
+    total, threads, sample = cpu_sample(sy, g, int(n_products), int(round(n_iters)), int(cg_iters))
     return {"value": total, "unit": "s", "cores": threads, "kind": "port", "sample": sample}
 
 
@@ -291,21 +351,22 @@ def run_reference(args):
     if rank != 0:
         return None
     sy, g = workload()
-    # product count of the GPU solve at these settings (same algorithm, same guesses)
-    n_products = args.ref_products
+    # products, Davidson iterations and CG iterations of the FP64 GPU step at these settings (same
+    # algorithm, same guesses)
     vals = []
     sample = ""
     threads = os.cpu_count()
     for _ in range(args.warmup):
-        cpu_sample(sy, g, n_products, args.ref_iters, sample_vectors=1)
+        cpu_sample(sy, g, args.ref_products, args.ref_iters, args.ref_cg, sample_vectors=1)
     for _ in range(args.steps):
-        total, threads, sample = cpu_sample(sy, g, n_products, args.ref_iters, sample_vectors=1)
+        total, threads, sample = cpu_sample(sy, g, args.ref_products, args.ref_iters, args.ref_cg, sample_vectors=1)
         vals.append(total)
     v = float(np.mean(vals))
     return {"impl": "reference", "metric": METRIC, "value": v, "unit": "s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": v * 1e3, "higher_is_better": False, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded (H2O)128 cluster, host SCC ground state)",
-            "config": {"workload": "water128-lctda-20roots", "n_roots": N_ROOTS, "tol": TOL, "max_iter": MAX_ITER},
+            "config": {"workload": "water128-lctda-20roots+S1grad", "n_roots": N_ROOTS, "tol": TOL,
+                       "max_iter": MAX_ITER},
             "cpu_baseline": {"value": v, "unit": "s", "cores": threads, "kind": "port", "sample": sample},
             "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
@@ -321,7 +382,7 @@ def run_products(args):
     es = T.ExcitedStateSystem.from_ground_state(ctx, sy, g)
     es.prepare_tda()
     x = np.random.default_rng(0).standard_normal((es.dim, args.k))
-    prec = {"fp64": _lib.PREC_FP64, "bf16x3": _lib.PREC_BF16X3}[args.precision]
+    prec = PRECISIONS[args.precision]
     for _ in range(max(1, args.steps)):
         ax = es.compute_products(x, precision=prec)
     ms, nl = ctx.last_timing()
@@ -334,11 +395,13 @@ def main():
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "bf16x3"])
+    ap.add_argument("--precision", default="bf16x3", choices=sorted(PRECISIONS))
+    ap.add_argument("--no-compare-fp64", dest="compare_fp64", action="store_false")
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
-    ap.add_argument("--ref-products", type=int, default=420)
-    ap.add_argument("--ref-iters", type=int, default=20)
+    ap.add_argument("--ref-products", type=int, default=369)
+    ap.add_argument("--ref-iters", type=int, default=40)
+    ap.add_argument("--ref-cg", type=int, default=14)
     ap.add_argument("--mode", default="solve", choices=["solve", "products"])
     ap.add_argument("--k", type=int, default=4)
     args = ap.parse_args()

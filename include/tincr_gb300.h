@@ -75,8 +75,9 @@ typedef enum {
     TINCR_KF_AO_EXCHANGE = 0,  /* the two n^2 v contractions of the LC exchange (A.X steps 2 and 4) */
     TINCR_KF_AO_TRANSFORM = 1, /* MO<->AO half transforms of A.X (steps 1 and 5)                    */
     TINCR_KF_SUBSPACE = 2,     /* Davidson projections, Ritz vectors, residuals, orthogonalisation  */
-    TINCR_KF_OTHER = 3,        /* Coulomb, packing, transition charges, small kernels              */
-    TINCR_KF_COUNT = 4
+    TINCR_KF_GRADIENT = 3,     /* gradient: pairwise-atom derivative kernel and adjoint GEMMs        */
+    TINCR_KF_OTHER = 4,        /* Coulomb, packing, transition charges, small kernels              */
+    TINCR_KF_COUNT = 5
 } tincr_kernel_family;
 
 /* Turn per-family kernel timing on (1) or off (0); turning it on clears the statistics. */

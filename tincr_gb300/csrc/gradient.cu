@@ -423,7 +423,7 @@ void Ctx::plr_adjoint(const double *v, const double *Y, double scale_p, double s
            *sYts = sYt + nn, *h1 = sYts + nn, *h2 = h1 + nn, *Q = h2 + nn;
     const double *s = dS_.p, *g = d_glr_ao.p;
     auto mm = [&](bool ta, bool tb, const double *A, const double *B, double *C, double alpha, double beta) {
-        int slot = prof_begin(TINCR_KF_OTHER);
+        int slot = prof_begin(TINCR_KF_GRADIENT);
         EpiStore e{C, 0, n, alpha, beta};
         if (!ta && !tb) gemm_f64<false, false>(stream, n, n, n, A, n, 0, B, n, 0, 1, e);
         else if (ta && !tb) gemm_f64<true, false>(stream, n, n, n, A, n, 0, B, n, 0, 1, e);
@@ -578,7 +578,7 @@ int Ctx::gradient(const int *atom_kind, double r_lr_, const double *P, const dou
         pa.rep_nt = (rep && rep_ntmax > 0) ? d_rep_nt.p : nullptr;
         pa.rep_ntmax = rep_ntmax; pa.rep_knots = d_rep_knots.p; pa.rep_coef = d_rep_coef.p; pa.rep_dmax = d_rep_dmax.p;
         pa.grad = dgrad.p;
-        int slot = prof_begin(TINCR_KF_OTHER);
+        int slot = prof_begin(TINCR_KF_GRADIENT);
         pair_gradient_kernel<<<N, 128, 0, stream>>>(pa);
         count_launch(stream, "pair_gradient");
         check_launch("pair_gradient");
@@ -589,7 +589,7 @@ int Ctx::gradient(const int *atom_kind, double r_lr_, const double *P, const dou
     auto mm = [&](bool ta, bool tb, int M, int Nn, int K, const double *A, int lda, const double *B, int ldb, double *C,
                   int ldc, double alpha, double beta) {
         EpiStore e{C, 0, ldc, alpha, beta};
-        int slot = prof_begin(TINCR_KF_OTHER);
+        int slot = prof_begin(TINCR_KF_GRADIENT);
         if (!ta && !tb) gemm_f64<false, false>(stream, M, Nn, K, A, lda, 0, B, ldb, 0, 1, e);
         else if (ta && !tb) gemm_f64<true, false>(stream, M, Nn, K, A, lda, 0, B, ldb, 0, 1, e);
         else if (!ta && tb) gemm_f64<false, true>(stream, M, Nn, K, A, lda, 0, B, ldb, 0, 1, e);
