@@ -129,6 +129,49 @@ int tincr_tda_solve(tincr_ctx *ctx, int n_roots, int max_iter, double tolerance,
                     double *energies, double *coefficients, double *osc, double *tr_dip,
                     double *q_trans, int *iterations);
 
+/* ---- batched LE / CT TDA (FMO) ------------------------------------------------------------ */
+
+/* One small TDA problem of a batch: an FMO monomer (tincr's Monomer::prepare_tda / run_tda,
+ * src/excited_states/tda/monomer.rs:8-53, tda/mod.rs:18-70) or one direction of a charge-transfer
+ * pair (PairChargeTransfer::prepare_ct_tda / run_ct_tda, src/excited_states/tda/ct_pair.rs:12-180).
+ * A CT pair direction is passed as the dimer: atoms of the hole monomer then of the electron
+ * monomer, the dimer overlap S, the dimer gamma / gamma_lr, and c = [C_occ | C_virt] where C_occ
+ * holds the hole monomer's occupied MOs (zero on the electron monomer's AOs) and C_virt the
+ * electron monomer's virtual MOs (zero on the hole monomer's AOs).  With that c, the Mulliken
+ * transition charges of the dimer equal tincr's pair charges (calculate_q_ov, :81-127, with q_oo
+ * of the hole and q_vv of the electron monomer), so the same A.X applies. */
+typedef struct {
+    int n_atoms, n_orb, n_occ, n_virt;
+    int n_roots;                 /* 1..6 */
+    const int *orbs_per_atom;    /* [n_atoms] */
+    const double *c;             /* [n_orb x (n_occ + n_virt)]: occupied MOs, then virtual MOs */
+    const double *s;             /* [n_orb x n_orb] */
+    const double *orbe;          /* [n_occ + n_virt]: occupied, then virtual orbital energies */
+    const double *gamma;         /* [n_atoms x n_atoms] */
+    const double *gamma_lr;      /* [n_atoms x n_atoms], NULL without long-range correction */
+    const double *xyz;           /* [n_atoms x 3] bohr, for the transition dipoles */
+} tincr_tda_instance;
+
+/* Results of one instance; any output pointer may be NULL. */
+typedef struct {
+    double *energies;            /* [n_roots] */
+    double *coefficients;        /* [n_occ*n_virt x n_roots] (tincr's ci_coefficients layout) */
+    double *osc;                 /* [n_roots] */
+    double *tr_dip;              /* [3 x n_roots] */
+    double *q_trans;             /* [n_atoms x n_roots] */
+    int iterations;              /* Davidson iterations of this instance */
+    int status;                  /* TINCR_OK, TINCR_NOT_CONVERGED or TINCR_NONFINITE */
+} tincr_tda_result;
+
+/* Replaces the per-monomer TDA loop of SuperSystem::create_exciton_hamiltonian_new
+ * (src/fmo/lcmo/basis.rs:462-465, rayon over monomers) and the CT pair TDAs of
+ * create_diab_basis_new (basis.rs:170-238): every instance runs tincr's block Davidson
+ * (davidson.rs:53-185, guesses of solvers/utils.rs:17-26) with its own convergence, all on the
+ * device in lockstep.  Returns TINCR_OK when every instance converged, otherwise the worst
+ * instance status (per-instance status in res[i].status); tincr unwraps a DavidsonError instead. */
+int tincr_tda_solve_batch(tincr_ctx *ctx, int n_inst, const tincr_tda_instance *inst, int max_iter,
+                          double tolerance, int precision, tincr_tda_result *res);
+
 /* A.X product that allocates no device memory.  No counterpart in tincr: it exists for callers
  * that own all device memory themselves (pool or arena allocators of an MD or FMO driver) or that
  * cannot accept the implicit device synchronisation of cudaMalloc/cudaFree between their kernels.

@@ -107,6 +107,61 @@ class TdaEngine:
         return len(self.omega)
 
 
+def ct_pair_q_ov(ao_off_h, ao_off_l, orbs_h, orbs_l, s_hl, n_occ_h, n_occ_l):
+    """Transition charges of a charge-transfer pair, hole on H and electron on L
+    (`PairChargeTransfer::calculate_q_ov`, `src/excited_states/tda/ct_pair.rs:81-127`).
+
+    s_hl is the overlap block between H's and L's AOs; returns q_ov [N_H + N_L, o_H * v_L]."""
+    occs = orbs_h[:, :n_occ_h]
+    virts = orbs_l[:, n_occ_l:]
+    s_c_l = s_hl @ virts                 # `:88`
+    s_c_h = s_hl.T @ occs                # `:90`
+    nh, nl = len(ao_off_h) - 1, len(ao_off_l) - 1
+    q = np.zeros((nh + nl, occs.shape[1], virts.shape[1]))
+    for a in range(nh):                  # `:104-113`
+        mu = slice(ao_off_h[a], ao_off_h[a + 1])
+        q[a] = occs[mu].T @ s_c_l[mu]
+    for b in range(nl):                  # `:115-124`
+        mu = slice(ao_off_l[b], ao_off_l[b + 1])
+        q[nh + b] = s_c_h[mu].T @ virts[mu]
+    return 0.5 * q.reshape(nh + nl, -1)
+
+
+class CtEngine(TdaEngine):
+    """`DavidsonEngine` for a `PairChargeTransfer` (`src/excited_states/solvers/mod.rs:166-276`):
+    the exchange couples q_oo of the hole monomer H with q_vv of the electron monomer L through
+    the H x L block of gamma_lr."""
+
+    def __init__(self, omega, q_ov, gamma, q_oo_h, q_vv_l, gamma_lr_hl, n_occ, n_virt):
+        super().__init__(omega, q_ov, gamma, q_oo_h, q_vv_l, gamma_lr_hl, n_occ, n_virt)
+
+    def apply(self, x):
+        fock = self.omega[:, None] * x                                        # `:198-199`
+        two_el = 2.0 * self.q_ov.T @ (self.gamma @ (self.q_ov @ x))           # `:202`
+        no, nv = self.n_occ, self.n_virt
+        nl = self.gamma_lr.shape[1]
+        gamma_oo = (self.gamma_lr.T @ self.q_oo).reshape(nl * no, no)        # `:219-222`
+        q_vv_r = self.q_vv.reshape(nl * nv, nv)
+        k_x = np.zeros_like(two_el)
+        for i in range(x.shape[1]):                                            # `:226-248`
+            xi = x[:, i].reshape(no, nv)
+            t = (xi @ q_vv_r.T).reshape(no, nl, nv).transpose(1, 0, 2).reshape(nl * no, nv)
+            k_x[:, i] = (gamma_oo.T @ t).reshape(-1)
+        self.n_products += x.shape[1]
+        return fock + two_el - k_x                                             # `:250`
+
+
+def run_tda_engine(eng, xyz, n_roots, max_iter, tolerance, history=None):
+    """`run_tda` / `run_ct_tda` around an existing engine: Davidson from `initial_subspace`,
+    transition charges, Mulliken dipoles, oscillator strengths (ct_pair.rs:129-180)."""
+    guess = initial_subspace(eng.omega, n_roots)
+    e, x, iters = davidson(eng, guess, n_roots, tolerance, max_iter, history=history)
+    q_trans = eng.q_ov @ x
+    mu = mulliken_dipoles(q_trans, xyz)
+    return dict(energies=e, coefficients=x, q_trans=q_trans, tr_dipoles=mu, f=oscillator_strength(e, mu),
+                iterations=iters, n_products=eng.n_products)
+
+
 class DavidsonError(RuntimeError):
     """`DavidsonError` (`solvers/davidson.rs:28-37`)."""
 

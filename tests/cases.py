@@ -72,3 +72,50 @@ def oracle_inputs(case):
     om = tda.orbe_differences(case["orbe"][occ], case["orbe"][virt])
     return dict(omega=om, q_ov=qov, q_oo=qoo, q_vv=qvv, gamma=case["gamma"], gamma_lr=case["gamma_lr"],
                 n_occ=no, n_virt=nv)
+
+
+_FMO = {}
+
+
+def fmo_case(nx=3, ny=1, nz=1, lc=True, n_le=4, n_ct=1, cutoff_angstrom=4.5, seed=20240064):
+    """Small seeded acene aggregate (the 4.5 A CT cutoff and ring counts of the FMO benchmark) with
+    its batched work list: every monomer, both directions of every close pair."""
+    from tincr_gb300 import fmo
+    key = (nx, ny, nz, lc, n_le, n_ct, cutoff_angstrom, seed)
+    if key in _FMO:
+        return _FMO[key]
+    z, x, mono = G.acene_lattice(nx, ny, nz, seed=seed)
+    mons = fmo.build_monomers(z, G.to_bohr(x), mono, lc=lc)
+    pairs = fmo.close_pairs(mons, cutoff_angstrom / gs.P.BOHR_TO_ANGS)
+    inst, labels = fmo.aggregate_instances(mons, pairs, n_le, n_ct)
+    case = dict(monomers=mons, pairs=pairs, instances=inst, labels=labels, lc=lc)
+    _FMO[key] = case
+    return case
+
+
+def fmo_oracle_engine(case, k):
+    """Oracle engine of instance k: TdaEngine of the monomer (LE) or CtEngine of the pair (CT)."""
+    from oracle import tda as OT
+    lab = case["labels"][k]
+    mons = {m.index: m for m in case["monomers"]}
+    if lab[0] == "LE":
+        m = mons[lab[1]]
+        sy, g = m.system, m.ground
+        qov, qoo, qvv = OT.trans_charges(sy.ao_offset, g.orbs, g.s, sy.occ_indices, sy.virt_indices)
+        om = OT.orbe_differences(g.orbe[sy.occ_indices], g.orbe[sy.virt_indices])
+        eng = OT.TdaEngine(om, qov, g.gamma, qoo, qvv, g.gamma_lr if case["lc"] else None, sy.n_occ, sy.n_virt)
+        return eng, sy.xyz
+    mh, ml = mons[lab[1]], mons[lab[2]]
+    from tincr_gb300 import fmo
+    d = fmo.Dimer(mh, ml)
+    nh = mh.system.n_orbs
+    sh, sl = mh.system, ml.system
+    qov = OT.ct_pair_q_ov(sh.ao_offset, sl.ao_offset, mh.ground.orbs, ml.ground.orbs, d.s[:nh, nh:], sh.n_occ,
+                          sl.n_occ)
+    _, qoo_h, _ = OT.trans_charges(sh.ao_offset, mh.ground.orbs, mh.ground.s, sh.occ_indices, sh.virt_indices)
+    _, _, qvv_l = OT.trans_charges(sl.ao_offset, ml.ground.orbs, ml.ground.s, sl.occ_indices, sl.virt_indices)
+    om = OT.orbe_differences(mh.ground.orbe[sh.occ_indices], ml.ground.orbe[sl.virt_indices])
+    na = sh.n_atoms
+    glr = d.gamma_lr[:na, na:] if case["lc"] else np.zeros((na, sl.n_atoms))
+    eng = OT.CtEngine(om, qov, d.gamma, qoo_h, qvv_l, glr, sh.n_occ, sl.n_virt)
+    return eng, d.system.xyz

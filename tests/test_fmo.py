@@ -1,0 +1,113 @@
+"""Batched LE / CT TDA (FMO monomers and charge-transfer pair directions).
+
+CPU: the dimer formulation that the GPU batch uses for a CT pair (Mulliken charges of the dimer
+with C = [C_H,occ | C_L,virt]) reproduces tincr's pair engine (`calculate_q_ov` + the H x L
+exchange of solvers/mod.rs:166-276) to rounding.
+GPU: `tincr_tda_solve_batch` against the oracle engines instance by instance: energies within
+1e-10 Eh, |overlap| of the eigenvectors 1 within 1e-7, oscillator strengths within 1e-8, the same
+Davidson iteration counts, with convergence masks (instances finishing at different iterations).
+"""
+
+import numpy as np
+import pytest
+
+from cases import fmo_case, fmo_oracle_engine
+from oracle import tda as OT
+from tincr_gb300 import _lib
+from tincr_gb300 import fmo
+
+
+def _dimer_engine(q):
+    """TdaEngine of the dimer formulation of an instance dict."""
+    ao = np.concatenate([[0], np.cumsum(q["opa"])])
+    no, nv = q["n_occ"], q["n_virt"]
+    qov, qoo, qvv = OT.trans_charges(ao, q["c"], q["s"], np.arange(no), np.arange(no, no + nv))
+    om = OT.orbe_differences(q["orbe"][:no], q["orbe"][no:])
+    return OT.TdaEngine(om, qov, q["gamma"], qoo, qvv, q["gamma_lr"], no, nv)
+
+
+def test_ct_dimer_formulation_equals_pair_engine():
+    case = fmo_case(2, 1, 1)
+    assert case["pairs"], "the two stacked acenes must form a CT pair"
+    for k, lab in enumerate(case["labels"]):
+        if lab[0] != "CT":
+            continue
+        q = case["instances"][k]
+        ref, _ = fmo_oracle_engine(case, k)
+        dim = _dimer_engine(q)
+        x = np.random.default_rng(k).standard_normal((q["n_occ"] * q["n_virt"], 3))
+        a, b = ref.apply(x), dim.apply(x)
+        assert np.abs(a - b).max() < 1e-12 * np.abs(a).max()
+        assert np.abs(ref.omega - dim.omega).max() == 0.0
+
+
+def test_aggregate_work_list():
+    case = fmo_case(3, 1, 1)
+    n_mon = len(case["monomers"])
+    assert [lab[0] for lab in case["labels"]].count("LE") == n_mon
+    assert len(case["instances"]) == n_mon + 2 * len(case["pairs"])
+    for q in case["instances"]:
+        assert q["c"].shape == (q["n_orb"], q["n_occ"] + q["n_virt"])
+        assert q["orbe"].shape == (q["n_occ"] + q["n_virt"],)
+
+
+def _oracle(case, k, tol, max_iter):
+    eng, xyz = fmo_oracle_engine(case, k)
+    q = case["instances"][k]
+    return OT.run_tda_engine(eng, xyz, q["n_roots"], max_iter, tol)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("tol", [1e-4, 1e-8])
+def test_batch_matches_oracle(gpu_ctx, tol):
+    case = fmo_case(3, 1, 1)
+    rc, res = fmo.solve_batch(gpu_ctx, case["instances"], max_iter=150, tol=tol)
+    assert rc == _lib.OK
+    iters = set()
+    for k, r in enumerate(res):
+        ref = _oracle(case, k, tol, 150)
+        assert r["status"] == _lib.OK
+        e_tol = 1e-10 if tol < 1e-6 else 1e-8
+        assert np.abs(r["energies"] - ref["energies"]).max() < e_tol, case["labels"][k]
+        if tol < 1e-6:
+            ov = np.abs(np.einsum("xr,xr->r", r["coefficients"], ref["coefficients"]))
+            assert np.abs(ov - 1.0).max() < 1e-7
+            assert np.abs(r["osc"] - ref["f"]).max() < 1e-8
+            sgn = np.sign(np.einsum("xr,xr->r", r["coefficients"], ref["coefficients"]))
+            assert np.abs(r["q_trans"] * sgn - ref["q_trans"]).max() < 1e-8
+        assert r["iterations"] == ref["iterations"], case["labels"][k]
+        iters.add(r["iterations"])
+    assert len(iters) > 1     # instances converged at different iterations: the masks were exercised
+
+
+@pytest.mark.gpu
+def test_batch_single_instance_equals_system_solver(gpu_ctx):
+    """A one-instance batch gives the single-system solver's roots."""
+    from tincr_gb300 import tda as T
+    case = fmo_case(2, 1, 1)
+    q = case["instances"][0]
+    rc, res = fmo.solve_batch(gpu_ctx, [q], max_iter=100, tol=1e-8)
+    m = case["monomers"][0]
+    es = T.ExcitedStateSystem.from_ground_state(gpu_ctx, m.system, m.ground)
+    ref = es.run_tda(q["n_roots"], 100, 1e-8)
+    assert np.abs(res[0]["energies"] - ref["ci_eigenvalues"]).max() < 1e-10
+    assert res[0]["iterations"] == ref["davidson_iterations"]
+
+
+@pytest.mark.gpu
+def test_batch_not_converged_and_bad_input(gpu_ctx):
+    case = fmo_case(2, 1, 1)
+    rc, res = fmo.solve_batch(gpu_ctx, case["instances"], max_iter=2, tol=1e-12)
+    assert rc == _lib.NOT_CONVERGED
+    assert all(r["status"] == _lib.NOT_CONVERGED and r["iterations"] == 2 for r in res)
+    bad = dict(case["instances"][0])
+    bad["n_roots"] = 7
+    with pytest.raises(_lib.TincrError) as e:
+        fmo.solve_batch(gpu_ctx, [bad])
+    assert e.value.status == _lib.BAD_ARG
+    bad = dict(case["instances"][0])
+    bad["s"] = bad["s"].copy()
+    bad["s"][0, 1] = np.nan
+    with pytest.raises(_lib.TincrError) as e:
+        fmo.solve_batch(gpu_ctx, [bad])
+    assert e.value.status == _lib.NONFINITE

@@ -156,6 +156,11 @@ int tincr_tda_solve(tincr_ctx *ctx, int n_roots, int max_iter, double tolerance,
     });
 }
 
+int tincr_tda_solve_batch(tincr_ctx *ctx, int n_inst, const tincr_tda_instance *inst, int max_iter, double tolerance,
+                          int precision, tincr_tda_result *res) {
+    return guarded(ctx, [&](tincr::Ctx &c) { return c.solve_batch(n_inst, inst, max_iter, tolerance, precision, res); });
+}
+
 int tincr_set_parameters(tincr_ctx *ctx, int n_kinds, const int *kind_z, const int *kind_norb, const int *kind_l,
                          const int *kind_m, const double *kind_hubbard, const double *kind_occ, int n_knots,
                          const double *sk_knots, const double *sk_coef, int rep_ntmax, const int *rep_nt,

@@ -28,6 +28,8 @@ void check_cuda(cudaError_t e, const char *what);
 extern thread_local long long g_launches;
 inline void count_launch(cudaStream_t, const char *) { ++g_launches; }
 void check_launch(const char *name);
+// Fails with TINCR_NONFINITE if any of the n host values is NaN or infinite.
+void check_finite(const double *p, size_t n, const char *what);
 
 // Owning device buffer of T.
 template <class T>

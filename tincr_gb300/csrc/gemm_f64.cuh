@@ -41,22 +41,15 @@ struct EpiAtomicAdd {
     }
 };
 
-template <bool TA, bool TB, class Epi>
-__global__ void __launch_bounds__(GB_T)
-gemm_f64_kernel(int M, int N, int K, int k_chunk, int splitk, const double *__restrict__ A, int lda,
-                long long sA, const double *__restrict__ B, int ldb, long long sB, Epi epi) {
-    __shared__ double As[GB_K][GB_M + 1];
-    __shared__ double Bs[GB_K][GB_N + 1];
+// One 64 x 64 output tile over k in [kbeg, kend): acc[i][j] holds C(m0 + ty + 16 i, n0 + tx + 16 j)
+// for thread (tx, ty) = (tid & 15, tid >> 4).  All 256 threads of the CTA take part.
+template <bool TA, bool TB>
+__device__ __forceinline__ void gemm_f64_tile(int M, int N, int kbeg, int kend, const double *__restrict__ A, int lda,
+                                              const double *__restrict__ B, int ldb, int m0, int n0,
+                                              double (&As)[GB_K][GB_M + 1], double (&Bs)[GB_K][GB_N + 1],
+                                              double (&acc)[4][4]) {
     const int tid = threadIdx.x;
     const int tx = tid & 15, ty = tid >> 4;
-    const int zb = blockIdx.z / splitk, zk = blockIdx.z % splitk;
-    const int m0 = blockIdx.y * GB_M, n0 = blockIdx.x * GB_N;
-    const int kbeg = zk * k_chunk;
-    const int kend = min(K, kbeg + k_chunk);
-    A += zb * sA;
-    B += zb * sB;
-
-    double acc[4][4];
 #pragma unroll
     for (int i = 0; i < 4; ++i)
 #pragma unroll
@@ -113,6 +106,21 @@ gemm_f64_kernel(int M, int N, int K, int k_chunk, int splitk, const double *__re
             }
         }
     }
+}
+
+template <bool TA, bool TB, class Epi>
+__global__ void __launch_bounds__(GB_T)
+gemm_f64_kernel(int M, int N, int K, int k_chunk, int splitk, const double *__restrict__ A, int lda,
+                long long sA, const double *__restrict__ B, int ldb, long long sB, Epi epi) {
+    __shared__ double As[GB_K][GB_M + 1];
+    __shared__ double Bs[GB_K][GB_N + 1];
+    const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+    const int zb = blockIdx.z / splitk, zk = blockIdx.z % splitk;
+    const int m0 = blockIdx.y * GB_M, n0 = blockIdx.x * GB_N;
+    const int kbeg = zk * k_chunk;
+    const int kend = min(K, kbeg + k_chunk);
+    double acc[4][4];
+    gemm_f64_tile<TA, TB>(M, N, kbeg, kend, A + zb * sA, lda, B + zb * sB, ldb, m0, n0, As, Bs, acc);
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
         int m = m0 + ty + 16 * i;

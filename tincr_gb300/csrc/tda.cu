@@ -301,6 +301,7 @@ Ctx::Ctx(int dev) : device(dev) {
 
 Ctx::~Ctx() {
     cudaSetDevice(device);
+    release_batch(batch);
     for (auto &p : pending) { cudaEventDestroy(p.a); cudaEventDestroy(p.b); }
     for (auto e : event_pool) cudaEventDestroy(e);
     if (ev0) cudaEventDestroy(ev0);
@@ -316,7 +317,7 @@ static void upload(cudaStream_t st, DevBuf<T> &d, const T *h, size_t n) {
     TINCR_CUDA(cudaMemcpyAsync(d.p, h, n * sizeof(T), cudaMemcpyHostToDevice, st));
 }
 
-static void check_finite(const double *p, size_t n, const char *what) {
+void check_finite(const double *p, size_t n, const char *what) {
     for (size_t i = 0; i < n; ++i)
         if (!std::isfinite(p[i])) fail(TINCR_NONFINITE, std::string("non-finite value in ") + what);
 }

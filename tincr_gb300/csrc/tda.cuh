@@ -27,6 +27,9 @@ struct KernelStats {
 
 enum Blk { BLK_OCC = 0, BLK_VIRT = 1 };
 
+struct BatchWork;                      // batched LE / CT TDA workspace (batch.cu)
+void release_batch(BatchWork *w);
+
 struct Ctx {
     int device = 0;
     int n_sm = 0;
@@ -93,6 +96,7 @@ struct Ctx {
     DevBuf<double> wsH, wsF, wsG, wsd3, wsd2, wsz;
     // Davidson state
     DevBuf<double> dV, dAV, dR, dRk, dT;
+    BatchWork *batch = nullptr;
 
     explicit Ctx(int dev);
     ~Ctx();
@@ -130,6 +134,8 @@ struct Ctx {
     int solve(int n_roots, int max_iter, double tol, int precision, double *energies, double *coefficients,
               double *osc, double *tr_dip, double *q_trans, int *iterations);
     int davidson(int n_roots, int max_iter, double tol, bool from_ritz, std::vector<double> &u, int *it_out);
+    int solve_batch(int n_inst, const tincr_tda_instance *inst, int max_iter, double tol, int precision,
+                    tincr_tda_result *res);
 };
 
 // A.X product with caller-owned device buffers and fixed device scratch (noalloc.cu)

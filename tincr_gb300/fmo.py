@@ -1,0 +1,152 @@
+"""Host-side mirror of tincr's FMO excited-state set-up for the batched GPU TDA.
+
+tincr (src/fmo/lcmo/basis.rs:449-533) runs one TDA per monomer (n_le locally excited roots,
+max_iter 50, tolerance 1e-4; `Monomer::run_tda`) and, for the diabatic basis, one TDA per direction
+of every monomer pair (n_ct roots, max_iter 150, tolerance 1e-4; `PairChargeTransfer::run_ct_tda`,
+src/excited_states/tda/ct_pair.rs).  Here every such problem becomes one `tincr_tda_instance` and
+the whole set is solved by `tincr_tda_solve_batch` in one call.
+
+A CT pair direction (hole on monomer H, electron on monomer L) is passed as the dimer with
+orbital block C = [C_H,occ (on H's AOs) | C_L,virt (on L's AOs)], the dimer overlap, gamma and
+gamma_lr.  The dimer's Mulliken transition charges for that C are exactly tincr's pair charges:
+q_ov from `calculate_q_ov` (ct_pair.rs:81-127, S_HL blocks), q_oo of H and q_vv of L (they vanish
+on the other monomer's atoms), so A.X needs no special case.
+
+The monomer ground states come from the host SCC of the isolated monomers (tincr's FMO SCC adds
+the electrostatic embedding of the other monomers, src/fmo/scc; that step precedes the TDA path).
+"""
+
+import numpy as np
+
+from . import _lib
+from . import groundstate as gs
+from ._lib import C as ct
+
+
+class Monomer:
+    """One fragment: its atoms in the aggregate, its System and its SCC ground state."""
+
+    def __init__(self, index, atoms, system, ground):
+        self.index = index
+        self.atoms = atoms
+        self.system = system
+        self.ground = ground
+
+
+def build_monomers(numbers, xyz_bohr, monomer_of_atom, lc=True, r_lr=gs.LONG_RANGE_RADIUS, scc_tol=1e-10):
+    """Monomers by construction (one per distinct `monomer_of_atom` value), each with a host SCC."""
+    mons = []
+    for k in np.unique(monomer_of_atom):
+        at = np.nonzero(monomer_of_atom == k)[0]
+        sy = gs.build_system(numbers[at], xyz_bohr[at], lc=lc, r_lr=r_lr)
+        mons.append(Monomer(int(k), at, sy, gs.run_scc(sy, tol=scc_tol)))
+    return mons
+
+
+def close_pairs(monomers, cutoff_bohr):
+    """Pairs (I, J), I < J, whose smallest interatomic distance is below the cutoff."""
+    out = []
+    for i, a in enumerate(monomers):
+        for j in range(i + 1, len(monomers)):
+            b = monomers[j]
+            d = np.linalg.norm(a.system.xyz[:, None, :] - b.system.xyz[None, :, :], axis=-1).min()
+            if d < cutoff_bohr:
+                out.append((i, j))
+    return out
+
+
+def monomer_instance(m, n_roots):
+    """Instance of `Monomer::prepare_tda` / `run_tda` (tda/monomer.rs:8-53)."""
+    sy, g = m.system, m.ground
+    no, nv = sy.n_occ, sy.n_virt
+    return dict(n_atoms=sy.n_atoms, n_orb=sy.n_orbs, n_occ=no, n_virt=nv, n_roots=n_roots,
+                opa=sy.orbs_per_atom.astype(np.int32), c=g.orbs[:, :no + nv], s=g.s, orbe=g.orbe[:no + nv],
+                gamma=g.gamma, gamma_lr=g.gamma_lr if sy.lc else None, xyz=sy.xyz)
+
+
+class Dimer:
+    """Overlap and gamma matrices of two monomers' atoms (H's atoms first)."""
+
+    def __init__(self, mh, ml):
+        sy = gs.build_system(np.concatenate([mh.system.numbers, ml.system.numbers]),
+                             np.concatenate([mh.system.xyz, ml.system.xyz]), lc=mh.system.lc, r_lr=mh.system.r_lr)
+        self.system = sy
+        self.s, _ = gs.h0_and_s(sy)
+        self.gamma = gs.gamma_atomwise(sy, 0.0)
+        self.gamma_lr = gs.gamma_atomwise(sy, sy.r_lr) if sy.lc else None
+
+
+def ct_instance(mh, ml, dimer, n_roots):
+    """Instance of `PairChargeTransfer::prepare_ct_tda` (ct_pair.rs:12-79): hole on mh, electron on ml."""
+    nh, nl = mh.system.n_orbs, ml.system.n_orbs
+    oh, ol = mh.system.n_occ, ml.system.n_occ
+    vl = ml.system.n_virt
+    c = np.zeros((nh + nl, oh + vl))
+    c[:nh, :oh] = mh.ground.orbs[:, :oh]
+    c[nh:, oh:] = ml.ground.orbs[:, ol:ol + vl]
+    orbe = np.concatenate([mh.ground.orbe[:oh], ml.ground.orbe[ol:ol + vl]])
+    sy = dimer.system
+    return dict(n_atoms=sy.n_atoms, n_orb=sy.n_orbs, n_occ=oh, n_virt=vl, n_roots=n_roots,
+                opa=sy.orbs_per_atom.astype(np.int32), c=c, s=dimer.s, orbe=orbe, gamma=dimer.gamma,
+                gamma_lr=dimer.gamma_lr, xyz=sy.xyz)
+
+
+def aggregate_instances(monomers, pairs, n_le, n_ct):
+    """tincr's FMO excited-state work list: every monomer (n_le roots), then both directions of
+    every pair (n_ct roots): (I -> J) and (J -> I) (basis.rs:170-238)."""
+    inst, labels = [], []
+    for m in monomers:
+        inst.append(monomer_instance(m, n_le))
+        labels.append(("LE", m.index))
+    for i, j in pairs:
+        inst.append(ct_instance(monomers[i], monomers[j], Dimer(monomers[i], monomers[j]), n_ct))
+        labels.append(("CT", monomers[i].index, monomers[j].index))
+        inst.append(ct_instance(monomers[j], monomers[i], Dimer(monomers[j], monomers[i]), n_ct))
+        labels.append(("CT", monomers[j].index, monomers[i].index))
+    return inst, labels
+
+
+class _Instance(ct.Structure):
+    _fields_ = [("n_atoms", ct.c_int), ("n_orb", ct.c_int), ("n_occ", ct.c_int), ("n_virt", ct.c_int),
+                ("n_roots", ct.c_int), ("orbs_per_atom", ct.POINTER(ct.c_int)), ("c", ct.POINTER(ct.c_double)),
+                ("s", ct.POINTER(ct.c_double)), ("orbe", ct.POINTER(ct.c_double)),
+                ("gamma", ct.POINTER(ct.c_double)), ("gamma_lr", ct.POINTER(ct.c_double)),
+                ("xyz", ct.POINTER(ct.c_double))]
+
+
+class _Result(ct.Structure):
+    _fields_ = [("energies", ct.POINTER(ct.c_double)), ("coefficients", ct.POINTER(ct.c_double)),
+                ("osc", ct.POINTER(ct.c_double)), ("tr_dip", ct.POINTER(ct.c_double)),
+                ("q_trans", ct.POINTER(ct.c_double)), ("iterations", ct.c_int), ("status", ct.c_int)]
+
+
+def solve_batch(ctx, instances, max_iter=50, tol=1e-4, precision=_lib.PREC_FP64):
+    """Run `tincr_tda_solve_batch`; returns (status, list of result dicts)."""
+    n = len(instances)
+    keep = []
+    arr = (_Instance * n)()
+    res = (_Result * n)()
+    outs = []
+    for k, q in enumerate(instances):
+        host = {}
+        for key in ("c", "s", "orbe", "gamma", "xyz"):
+            host[key] = np.ascontiguousarray(q[key], dtype=np.float64)
+        host["opa"] = np.ascontiguousarray(q["opa"], dtype=np.int32)
+        host["gamma_lr"] = None if q["gamma_lr"] is None else np.ascontiguousarray(q["gamma_lr"], dtype=np.float64)
+        keep.append(host)
+        arr[k] = _Instance(q["n_atoms"], q["n_orb"], q["n_occ"], q["n_virt"], q["n_roots"], _lib.iptr(host["opa"]),
+                           _lib.dptr(host["c"]), _lib.dptr(host["s"]), _lib.dptr(host["orbe"]),
+                           _lib.dptr(host["gamma"]), _lib.dptr(host["gamma_lr"]), _lib.dptr(host["xyz"]))
+        nr, ov = q["n_roots"], q["n_occ"] * q["n_virt"]
+        o = dict(energies=np.zeros(nr), coefficients=np.zeros((ov, nr)), osc=np.zeros(nr), tr_dip=np.zeros((3, nr)),
+                 q_trans=np.zeros((q["n_atoms"], nr)))
+        outs.append(o)
+        res[k] = _Result(_lib.dptr(o["energies"]), _lib.dptr(o["coefficients"]), _lib.dptr(o["osc"]),
+                         _lib.dptr(o["tr_dip"]), _lib.dptr(o["q_trans"]), 0, 0)
+    rc = ctx.lib.tincr_tda_solve_batch(ctx.h, n, ct.cast(arr, ct.c_void_p), int(max_iter), float(tol), int(precision),
+                                       ct.cast(res, ct.c_void_p))
+    ctx.check(rc, allow=(_lib.OK, _lib.NOT_CONVERGED))
+    for k in range(n):
+        outs[k]["iterations"] = res[k].iterations
+        outs[k]["status"] = res[k].status
+    return rc, outs
