@@ -31,16 +31,17 @@ typedef enum {
 
 /* Arithmetic of the two-electron contractions (Coulomb + long-range exchange) of A.X.
  * Subspace Rayleigh-Ritz, orthogonalisation, residual norms and CG scalars are always FP64.
- * TINCR_PREC_BF16X3: the four GEMMs of the AO-direct product run on split-BF16 planes
- * (x = hi + lo; hi*hi + hi*lo + lo*hi) on tcgen05 tensor cores with FP32 accumulation folded every
- * 64 elements of K; the Coulomb diagonals and omega o X stay FP64.  tincr_tda_solve then finishes
- * with FP64 Davidson iterations started from the mixed Ritz vectors (usually one Rayleigh-Ritz
- * step), so the convergence test and the returned energies are those of the FP64 operator.
+ * TINCR_PREC_BF16X3: the four GEMMs of the AO-direct product run on tensor cores with every operand
+ * split into three BF16 planes (x = hi + mid + lo holds x's FP32 value; six plane products per
+ * MMA step) and FP32 accumulation folded every 64 elements of K: products to about 1e-7 relative.
+ * The Coulomb diagonals and omega o X stay FP64.  For a residual tolerance below 1e-6 the solve
+ * ends with FP64 Davidson iterations started from the mixed Ritz vectors (usually one
+ * Rayleigh-Ritz step), so the convergence test and the energies are then those of FP64.
  * Setting the environment variable TINCR_GB300_PLANE_GEMM=mma before tincr_ctx_create selects
- * the warp-MMA implementation of the plane GEMM instead of tcgen05 (same numbers to rounding). */
+ * the warp-MMA implementation of the single-system plane GEMM instead of tcgen05. */
 typedef enum {
     TINCR_PREC_FP64 = 0,      /* plain FP64 drop-in                                             */
-    TINCR_PREC_BF16X3 = 1     /* split-BF16 tensor-core products, FP64 convergence               */
+    TINCR_PREC_BF16X3 = 1     /* three-plane split-BF16 tensor-core products, FP64 subspace       */
 } tincr_precision;
 
 /* ---- context --------------------------------------------------------------------------------- */
@@ -65,7 +66,7 @@ int tincr_last_solve_stats(const tincr_ctx *ctx, long long *n_products, int *n_c
 /* Per-iteration record of the last tincr_tda_solve (tincr logs the same quantities to stdout in
  * src/excited_states/solvers/davidson.rs:123-143): iteration index within its phase, subspace size,
  * largest residual norm, roots not yet converged and the precision of the phase (a TINCR_PREC_BF16X3
- * solve runs a mixed phase, then an FP64 phase).  Up to `capacity` records are written to each
+ * solve runs a mixed phase, then, for tolerances below 1e-6, an FP64 phase).  Up to `capacity` records are written to each
  * non-NULL array; *n_steps receives the total count. */
 int tincr_davidson_history(const tincr_ctx *ctx, int capacity, int *n_steps, int *iter, int *n_sub,
                            double *max_residual, int *roots_left, int *precision);

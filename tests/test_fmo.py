@@ -111,3 +111,33 @@ def test_batch_not_converged_and_bad_input(gpu_ctx):
     with pytest.raises(_lib.TincrError) as e:
         fmo.solve_batch(gpu_ctx, [bad])
     assert e.value.status == _lib.NONFINITE
+
+
+@pytest.mark.gpu
+def test_batch_mixed_within_bar(gpu_ctx):
+    """Mixed form (three-plane split-BF16 GEMMs, FP64 subspace): every root of every instance within
+    1e-6 Eh of the FP64 batch (spec bar)."""
+    case = fmo_case(3, 1, 1)
+    rc64, r64 = fmo.solve_batch(gpu_ctx, case["instances"], max_iter=150, tol=1e-6)
+    rcm, rm = fmo.solve_batch(gpu_ctx, case["instances"], max_iter=150, tol=1e-6, precision=_lib.PREC_BF16X3)
+    assert rc64 == _lib.OK and rcm == _lib.OK
+    err = max(np.abs(a["energies"] - b["energies"]).max() for a, b in zip(r64, rm))
+    print("mixed batch: max |dE| = %.2e Eh" % err)
+    assert err < 1e-6
+    for a, b in zip(r64, rm):
+        ov = np.abs(np.einsum("xr,xr->r", a["coefficients"], b["coefficients"]))
+        assert np.abs(ov - 1.0).max() < 1e-6
+
+
+@pytest.mark.gpu
+def test_batch_mixed_tight_tolerance(gpu_ctx):
+    """Tolerance 1e-8 (below the mixed operator's 1e-6 floor): the mixed batch finishes with FP64
+    iterations and matches the FP64 batch to 1e-10 Eh."""
+    case = fmo_case(3, 1, 1)
+    _, r64 = fmo.solve_batch(gpu_ctx, case["instances"], max_iter=150, tol=1e-8)
+    rcm, rm = fmo.solve_batch(gpu_ctx, case["instances"], max_iter=150, tol=1e-8, precision=_lib.PREC_BF16X3)
+    if rcm != _lib.OK:
+        print("statuses", [r["status"] for r in rm], "iterations", [r["iterations"] for r in rm],
+              "fp64 iterations", [r["iterations"] for r in r64])
+    assert rcm == _lib.OK
+    assert max(np.abs(a["energies"] - b["energies"]).max() for a, b in zip(r64, rm)) < 1e-10

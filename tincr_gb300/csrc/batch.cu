@@ -18,11 +18,13 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <functional>
 #include <numeric>
 #include <vector>
 
 #include "batch.cuh"
 #include "gemm_f64.cuh"
+#include "planes.cuh"
 #include "tda.cuh"
 
 namespace tincr {
@@ -34,10 +36,14 @@ struct BtArrays {
     const BtInst *inst;
     BtState *state;
     double *C, *SC, *S, *blk, *glr, *gam, *omega, *V, *AV, *R, *Rk, *T, *sub, *H, *F, *D, *u, *err, *Y;
+    bf16 *P;           // split-BF16 planes (mixed form): plane q of element k at P[k + q * ps]
+    long long ps;
     const int *ao_off, *ao_atom;
     int *active;
     double tol;
 };
+
+enum BtMode { BT_FP64 = 0, BT_FINAL = 1, BT_MIXED = 2 };
 
 // ----------------------------------------------------------------------------------------------
 // grouped FP64 GEMM over static tiles {instance, vector, tile row, tile column}
@@ -249,12 +255,12 @@ __global__ void bt_guess_kernel(BtArrays a, const int *__restrict__ pos) {
 
 // Coulomb diagonals d3_mu = M[mu][n+mu], d2_mu = M[n+mu][mu] of M = H [C_v;SC_v]^T, one warp per row
 // (non-LC instances in the products, every instance in the final pass)
-__global__ void bt_diag_kernel(BtArrays a, int final_pass) {
+__global__ void bt_diag_kernel(BtArrays a, int mode) {
     const int I = blockIdx.y, b = blockIdx.x;
     const BtInst in = a.inst[I];
     const double *X;
-    if (!bt_vector(a, in, I, b, final_pass != 0, &X)) return;
-    if (!final_pass && in.lc) return;
+    if (!bt_vector(a, in, I, b, mode == BT_FINAL, &X)) return;
+    if (mode == BT_FP64 && in.lc) return;   // the exchange GEMM's epilogue captures them
     const int n = in.n, v = in.v;
     const double *H = a.H + in.off_h + (long long)b * 2 * n * v;
     const double *rv = a.blk + in.off_blk + 2LL * n * in.o;
@@ -272,13 +278,15 @@ __global__ void bt_diag_kernel(BtArrays a, int final_pass) {
 }
 
 // y_A = 1/2 sum_{mu in A}(d3 + d2) (= q_ov X per atom), z = gamma y; z onto F's off-diagonal-block
-// diagonals (LC) or kept per AO (non-LC); in the final pass y is the transition charge of the root.
-__global__ void bt_coulomb_kernel(BtArrays a, int final_pass) {
+// diagonals (FP64 form, LC) or kept per AO (non-LC, and the mixed form); in the final pass y is the
+// transition charge of the root.
+__global__ void bt_coulomb_kernel(BtArrays a, int mode) {
     extern __shared__ double ysh[];
     const int I = blockIdx.y, b = blockIdx.x;
     const BtInst in = a.inst[I];
     const double *X;
-    if (!bt_vector(a, in, I, b, final_pass != 0, &X)) return;
+    const bool final_pass = mode == BT_FINAL;
+    if (!bt_vector(a, in, I, b, final_pass, &X)) return;
     const int n = in.n, N = in.N;
     const int *ao_off = a.ao_off + in.off_ao;
     const double *d3 = a.D + in.off_d + (long long)b * n, *d2 = a.D + in.off_d + (long long)(in.nr + b) * n;
@@ -296,7 +304,7 @@ __global__ void bt_coulomb_kernel(BtArrays a, int final_pass) {
         double z = 0.0;
         for (int B = 0; B < N; ++B) z += gam[(long long)A * N + B] * ysh[B];
         for (int mu = ao_off[A]; mu < ao_off[A + 1]; ++mu) {
-            if (in.lc) {
+            if (in.lc && mode == BT_FP64) {
                 double *f = a.F + in.off_f + (long long)b * n2 * n2;
                 f[(long long)mu * n2 + n + mu] += z;
                 f[(long long)(n + mu) * n2 + mu] += z;
@@ -320,6 +328,292 @@ __global__ void bt_scale_rows_kernel(BtArrays a) {
     for (long long t = threadIdx.x; t < 2LL * n * v; t += blockDim.x) {
         const int r = int(t / v);
         G[t] = z[r < n ? r : r - n] * rv[t];
+    }
+}
+
+// ----------------------------------------------------------------------------------------------
+// mixed form: grouped three-plane split-BF16 GEMM (64 x 64 tiles, warp MMA, six plane products,
+// FP32 folded every 32 of K)
+// ----------------------------------------------------------------------------------------------
+
+inline int pad32(int k) { return (k + 31) / 32 * 32; }
+
+struct BtPlaneOp {
+    int M, N, Kpad, lda, ldb;
+    const bf16 *A, *B;   // plane 0 (plane q at + q * ps)
+    const BtInst *in;
+    int I, b;
+    const double *X;
+};
+
+constexpr int BP_T = 128, BP_K = 32, BP_LD = BP_K + 8, BP_TILE = 64 * BP_LD;
+constexpr int BP_SMEM = 2 * 2 * N_PLANES * BP_TILE * 2;   // 2 stages x {A, B} x planes x bytes
+
+template <class Step>
+__global__ void __launch_bounds__(BP_T) bt_plane_kernel(const int4 *__restrict__ tiles, Step step) {
+    extern __shared__ __align__(16) unsigned char bp_raw[];
+    bf16 *sm = reinterpret_cast<bf16 *>(bp_raw);
+    const int4 t = tiles[blockIdx.x];
+    BtPlaneOp op;
+    if (!step.setup(t.x, t.y, op)) return;   // uniform over the CTA
+    const long long ps = step.a.ps;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int wm = warp >> 1, wn = warp & 1, g = lane >> 2, tg = lane & 3;
+    const int m0 = t.z * 64, n0 = t.w * 64;
+    auto tile = [&](int s, int which) { return sm + (s * 2 * N_PLANES + which) * BP_TILE; };
+    auto load_stage = [&](int s, int k0) {
+#pragma unroll
+        for (int q = 0; q < 12; ++q) {
+            const int idx = tid + q * BP_T;         // 0 .. 1535: 6 tiles x 64 rows x 4 chunks
+            const int which = idx >> 8, within = idx & 255;
+            const int r = within >> 2, c = (within & 3) * 8;
+            const bf16 *base;
+            int ld, row0, lim;
+            if (which < N_PLANES) { base = op.A + which * ps; ld = op.lda; row0 = m0; lim = op.M; }
+            else                  { base = op.B + (which - N_PLANES) * ps; ld = op.ldb; row0 = n0; lim = op.N; }
+            const int gr = row0 + r;
+            cp_async16(tile(s, which) + r * BP_LD + c, base + (long long)(gr < lim ? gr : 0) * ld + k0 + c,
+                       gr < lim ? 16 : 0);
+        }
+        cp_async_commit();
+    };
+    // acc: FP32 running sums; pm: the hi x hi product of one 32-deep K slice, px: the five smaller
+    // plane products (kept apart so that the tensor core's accumulation of the small terms cannot
+    // shift the dominant one); both folded into acc with round-to-nearest adds every slice
+    float acc[2][4][4], pm[2][4][4], px[2][4][4];
+#pragma unroll
+    for (int i = 0; i < 2; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+#pragma unroll
+            for (int e = 0; e < 4; ++e) acc[i][j][e] = pm[i][j][e] = px[i][j][e] = 0.f;
+    const int nk = op.Kpad / BP_K;
+    load_stage(0, 0);
+    for (int kb = 0; kb < nk; ++kb) {
+        const int s = kb & 1;
+        cp_async_wait_all();
+        __syncthreads();
+        if (kb + 1 < nk) load_stage(s ^ 1, (kb + 1) * BP_K);
+#pragma unroll
+        for (int kk = 0; kk < BP_K; kk += 16) {
+            unsigned af[2][N_PLANES][4];
+#pragma unroll
+            for (int i = 0; i < 2; ++i)
+#pragma unroll
+                for (int q = 0; q < N_PLANES; ++q) {
+                    const bf16 *pa = tile(s, q) + (wm * 32 + i * 16 + g) * BP_LD + kk + tg * 2;
+                    af[i][q][0] = *(const unsigned *)(pa);
+                    af[i][q][1] = *(const unsigned *)(pa + 8 * BP_LD);
+                    af[i][q][2] = *(const unsigned *)(pa + 8);
+                    af[i][q][3] = *(const unsigned *)(pa + 8 * BP_LD + 8);
+                }
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                unsigned bf[N_PLANES][2];
+#pragma unroll
+                for (int q = 0; q < N_PLANES; ++q) {
+                    const bf16 *pb = tile(s, N_PLANES + q) + (wn * 32 + j * 8 + g) * BP_LD + kk + tg * 2;
+                    bf[q][0] = *(const unsigned *)(pb);
+                    bf[q][1] = *(const unsigned *)(pb + 8);
+                }
+#pragma unroll
+                for (int i = 0; i < 2; ++i) {
+                    mma_bf16(pm[i][j], af[i][0], bf[0]);
+                    mma_bf16(px[i][j], af[i][0], bf[1]);
+                    mma_bf16(px[i][j], af[i][1], bf[0]);
+                    mma_bf16(px[i][j], af[i][0], bf[2]);
+                    mma_bf16(px[i][j], af[i][2], bf[0]);
+                    mma_bf16(px[i][j], af[i][1], bf[1]);
+                }
+            }
+        }
+#pragma unroll
+        for (int i = 0; i < 2; ++i)
+#pragma unroll
+            for (int j = 0; j < 4; ++j)
+#pragma unroll
+                for (int e = 0; e < 4; ++e) {
+                    acc[i][j][e] += pm[i][j][e] + px[i][j][e];
+                    pm[i][j][e] = px[i][j][e] = 0.f;
+                }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int i = 0; i < 2; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+                const int m = m0 + wm * 32 + i * 16 + g + (e >= 2 ? 8 : 0);
+                const int n = n0 + wn * 32 + j * 8 + tg * 2 + (e & 1);
+                if (m < op.M && n < op.N) step.epi(op, m, n, acc[i][j][e]);
+            }
+}
+
+__device__ __forceinline__ void bt_split_store(const BtArrays &a, long long k, float x) { store3(a.P, a.ps, k, x); }
+
+// plane pointers of an instance
+__device__ __forceinline__ long long bt_pc_rv(const BtInst &in) { return in.off_pc + 2LL * in.n * in.ko; }
+__device__ __forceinline__ long long bt_pc_rswt(const BtInst &in) { return bt_pc_rv(in) + 2LL * in.n * in.kv; }
+__device__ __forceinline__ long long bt_pc_lswt(const BtInst &in) { return bt_pc_rswt(in) + (long long)in.v * in.k2; }
+__device__ __forceinline__ long long bt_pv_slot(const BtInst &in, int b) {
+    return in.off_pv + (long long)b * ((long long)in.v * in.ko + 2LL * in.n * in.kv + 2LL * in.n * in.k2 +
+                                       (long long)in.v * in.k2);
+}
+__device__ __forceinline__ long long bt_pv_h(const BtInst &in, int b) { return bt_pv_slot(in, b) + (long long)in.v * in.ko; }
+__device__ __forceinline__ long long bt_pv_f(const BtInst &in, int b) { return bt_pv_h(in, b) + 2LL * in.n * in.kv; }
+__device__ __forceinline__ long long bt_pv_gt(const BtInst &in, int b) { return bt_pv_f(in, b) + 2LL * in.n * in.k2; }
+
+// constant planes of every instance (set-up of the mixed form)
+__global__ void bt_const_planes_kernel(BtArrays a) {
+    const BtInst in = a.inst[blockIdx.x];
+    const int n = in.n, o = in.o, v = in.v, n2 = 2 * n;
+    const double *lst = a.blk + in.off_blk, *rv = lst + 2LL * n * o, *lsw = rv + 2LL * n * v, *rsw = lsw + 2LL * n * o;
+    for (long long t = threadIdx.x; t < (long long)n2 * o; t += blockDim.x) {
+        const int r = int(t / o), c = int(t % o);
+        bt_split_store(a, in.off_pc + (long long)r * in.ko + c, (float)lst[t]);
+        bt_split_store(a, bt_pc_lswt(in) + (long long)c * in.k2 + r, (float)lsw[t]);
+    }
+    for (long long t = threadIdx.x; t < (long long)n2 * v; t += blockDim.x) {
+        const int r = int(t / v), c = int(t % v);
+        bt_split_store(a, bt_pc_rv(in) + (long long)r * in.kv + c, (float)rv[t]);
+        bt_split_store(a, bt_pc_rswt(in) + (long long)c * in.k2 + r, (float)rsw[t]);
+    }
+}
+
+// X^T planes of the new trial vectors
+__global__ void bt_split_x_kernel(BtArrays a) {
+    const int I = blockIdx.y, b = blockIdx.x;
+    const BtInst in = a.inst[I];
+    const double *X;
+    if (!bt_vector(a, in, I, b, false, &X)) return;
+    const long long base = bt_pv_slot(in, b);
+    for (long long t = threadIdx.x; t < in.ov; t += blockDim.x) {
+        const int i = int(t / in.v), x = int(t % in.v);
+        bt_split_store(a, base + (long long)x * in.ko + i, (float)X[t]);
+    }
+}
+
+// 1. H = [C_o;SC_o] X: FP64 copy (Coulomb diagonals) and planes
+struct BtP1 {
+    BtArrays a;
+    __device__ bool setup(int I, int b, BtPlaneOp &op) const {
+        const BtInst &in = a.inst[I];
+        const double *X;
+        if (!bt_vector(a, in, I, b, false, &X)) return false;
+        op.in = &a.inst[I]; op.I = I; op.b = b;
+        op.M = 2 * in.n; op.N = in.v; op.Kpad = in.ko;
+        op.A = a.P + in.off_pc; op.lda = in.ko;
+        op.B = a.P + bt_pv_slot(in, b); op.ldb = in.ko;
+        return true;
+    }
+    __device__ void epi(const BtPlaneOp &op, int m, int n, float acc) const {
+        const BtInst &in = *op.in;
+        a.H[in.off_h + (long long)op.b * 2 * in.n * in.v + (long long)m * in.v + n] = (double)acc;
+        bt_split_store(a, bt_pv_h(in, op.b) + (long long)m * in.kv + n, acc);
+    }
+};
+
+// 2. F = -1/4 gamma_lr o (H [C_v;SC_v]^T) as planes (LC instances)
+struct BtP2 {
+    BtArrays a;
+    __device__ bool setup(int I, int b, BtPlaneOp &op) const {
+        const BtInst &in = a.inst[I];
+        const double *X;
+        if (!in.lc || !bt_vector(a, in, I, b, false, &X)) return false;
+        op.in = &a.inst[I]; op.I = I; op.b = b;
+        op.M = 2 * in.n; op.N = 2 * in.n; op.Kpad = in.kv;
+        op.A = a.P + bt_pv_h(in, b); op.lda = in.kv;
+        op.B = a.P + bt_pc_rv(in); op.ldb = in.kv;
+        return true;
+    }
+    __device__ void epi(const BtPlaneOp &op, int r, int c, float acc) const {
+        const BtInst &in = *op.in;
+        const int n = in.n;
+        const int rr = r < n ? r : r - n, cc = c < n ? c : c - n;
+        const float f = -0.25f * (float)a.glr[in.off_glr + (long long)rr * n + cc] * acc;
+        bt_split_store(a, bt_pv_f(in, op.b) + (long long)r * in.k2 + c, f);
+    }
+};
+
+// 4. G = F [SC_v;C_v] + diag(z, z) [C_v;SC_v], written transposed as planes (LC instances)
+struct BtP4 {
+    BtArrays a;
+    __device__ bool setup(int I, int b, BtPlaneOp &op) const {
+        const BtInst &in = a.inst[I];
+        const double *X;
+        if (!in.lc || !bt_vector(a, in, I, b, false, &X)) return false;
+        op.in = &a.inst[I]; op.I = I; op.b = b;
+        op.M = 2 * in.n; op.N = in.v; op.Kpad = in.k2;
+        op.A = a.P + bt_pv_f(in, b); op.lda = in.k2;
+        op.B = a.P + bt_pc_rswt(in); op.ldb = in.k2;
+        return true;
+    }
+    __device__ void epi(const BtPlaneOp &op, int r, int x, float acc) const {
+        const BtInst &in = *op.in;
+        const int n = in.n;
+        const double z = a.D[in.off_d + (long long)(2 * in.nr + op.b) * n + (r < n ? r : r - n)];
+        const double rv = a.blk[in.off_blk + 2LL * n * in.o + (long long)r * in.v + x];
+        bt_split_store(a, bt_pv_gt(in, op.b) + (long long)x * in.k2 + r, acc + (float)(z * rv));
+    }
+};
+
+// non-LC: G = diag(z, z) [C_v;SC_v] as transposed planes
+__global__ void bt_gt_nolc_kernel(BtArrays a) {
+    const int I = blockIdx.y, b = blockIdx.x;
+    const BtInst in = a.inst[I];
+    const double *X;
+    if (in.lc || !bt_vector(a, in, I, b, false, &X)) return;
+    const int n = in.n, v = in.v;
+    const double *z = a.D + in.off_d + (long long)(2 * in.nr + b) * n;
+    const double *rv = a.blk + in.off_blk + 2LL * n * in.o;
+    for (long long t = threadIdx.x; t < 2LL * n * v; t += blockDim.x) {
+        const int r = int(t / v), x = int(t % v);
+        bt_split_store(a, bt_pv_gt(in, b) + (long long)x * in.k2 + r, (float)(z[r < n ? r : r - n] * rv[t]));
+    }
+}
+
+// 5. AX = [SC_o;C_o]^T G + omega o X
+struct BtP5 {
+    BtArrays a;
+    __device__ bool setup(int I, int b, BtPlaneOp &op) const {
+        const BtInst &in = a.inst[I];
+        const double *X;
+        if (!bt_vector(a, in, I, b, false, &X)) return false;
+        op.in = &a.inst[I]; op.I = I; op.b = b; op.X = X;
+        op.M = in.o; op.N = in.v; op.Kpad = in.k2;
+        op.A = a.P + bt_pc_lswt(in); op.lda = in.k2;
+        op.B = a.P + bt_pv_gt(in, b); op.ldb = in.k2;
+        return true;
+    }
+    __device__ void epi(const BtPlaneOp &op, int m, int n, float acc) const {
+        const BtInst &in = *op.in;
+        const long long k = (long long)m * in.v + n;
+        const BtState &s = a.state[op.I];
+        a.AV[in.off_v + (long long)(s.m_done + op.b) * in.ov + k] = (double)acc + a.omega[in.off_omega + k] * op.X[k];
+    }
+};
+
+// restart every instance from its Ritz vectors (FP64 polish after the mixed phase)
+__global__ void bt_restart_kernel(BtArrays a) {
+    const int I = blockIdx.x;
+    const BtInst in = a.inst[I];
+    const BtState old = a.state[I];
+    if (old.status == BT_NONFINITE) return;
+    double *V = a.V + in.off_v;
+    const double *R = a.R + in.off_r;
+    for (long long t = threadIdx.x; t < (long long)in.nr * in.ov; t += blockDim.x) V[t] = R[t];
+    if (threadIdx.x == 0) {
+        BtState s{};
+        s.m = in.nr;
+        s.m_done = 0;
+        s.dim_sub = in.nr;
+        s.iter = old.iter;
+        s.status = BT_RUNNING;
+        s.products = old.products;
+        s.collapses = old.collapses;
+        s.first_stop = 1;
+        a.state[I] = s;
     }
 }
 
@@ -348,83 +642,211 @@ __device__ __forceinline__ void bt_block_sum(double (&v)[NV], double *red) {
     __syncthreads();
 }
 
-__device__ __forceinline__ int bt_rr(int pos, int step, int mm) {
-    return pos == 0 ? 0 : 1 + (pos - 1 + step) % (mm - 1);
+// number of eigenvalues of the symmetric tridiagonal (d, e) below x (Sturm count of T - x I)
+__device__ __forceinline__ int bt_sturm(const double *d, const double *e, int m, double x, double pivmin) {
+    int c = 0;
+    double q = d[0] - x;
+    if (fabs(q) < pivmin) q = -pivmin;
+    if (q < 0.0) ++c;
+    for (int i = 1; i < m; ++i) {
+        q = d[i] - x - e[i - 1] * e[i - 1] / q;
+        if (fabs(q) < pivmin) q = -pivmin;
+        if (q < 0.0) ++c;
+    }
+    return c;
 }
 
-// Cyclic Jacobi with the round-robin parallel ordering: A (m x m, symmetric) is diagonalised in
-// place, Z receives the eigenvectors as columns.  Stops when the off-diagonal Frobenius norm is
-// below 1e-14 of the total.
-__device__ void bt_jacobi(int m, double *A, double *Z, double *cs, int *pq, double *red) {
-    const int tid = threadIdx.x;
-    for (int e = tid; e < m * m; e += BT_T) Z[e] = (e / m == e % m) ? 1.0 : 0.0;
-    __syncthreads();
-    if (m == 1) return;
-    const int mm = (m + 1) & ~1, np = mm / 2;
-    for (int sweep = 0; sweep < 40; ++sweep) {
-        double s2[2] = {0.0, 0.0};
-        for (int e = tid; e < m * m; e += BT_T) {
-            const double x2 = A[e] * A[e];
-            if (e / m == e % m) s2[1] += x2;
-            else s2[0] += x2;
+// Lowest nr eigenpairs of the symmetric m x m matrix A (shared memory, overwritten), all in FP64:
+// Householder reduction to tridiagonal form T = Q^T A Q (Householder vectors kept in A's lower
+// triangle), the nr smallest eigenvalues of T by warp multisection on Sturm counts (one warp per
+// root, 33 points per step), their eigenvectors by inverse iteration on T (LU with partial
+// pivoting), Gram-Schmidt among them, and the back-transformation y = Q z.
+// Out: w[r] ascending; Y[r * m + i] orthonormal eigenvectors.  W: scratch of 4 m + 5 nr m doubles.
+__device__ void bt_eig_lowest(int m, int nr, double *A, double *W, double *w, double *red) {
+    double *d = W, *e = d + m, *beta = e + m, *p = beta + m, *Y = p + m, *F = Y + (size_t)nr * m;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    // 1. tridiagonalisation (one reflection per column k, acting on rows/columns k+1..m-1)
+    for (int k = 0; k + 2 < m; ++k) {
+        const int n1 = m - k - 1;
+        double s2[1] = {0.0};
+        for (int i = 1 + tid; i < n1; i += BT_T) {
+            const double x = A[(k + 1 + i) * m + k];
+            s2[0] += x * x;
         }
-        bt_block_sum<2>(s2, red);
-        if (s2[0] <= 1e-28 * (s2[0] + s2[1])) break;
-        for (int step = 0; step < mm - 1; ++step) {
-            for (int k = tid; k < np; k += BT_T) {
-                int p = bt_rr(k, step, mm), q = bt_rr(mm - 1 - k, step, mm);
-                if (p > q) { const int t = p; p = q; q = t; }
-                double c = 1.0, s = 0.0;
-                if (q < m) {
-                    const double apq = A[p * m + q];
-                    if (apq != 0.0) {
-                        const double theta = (A[q * m + q] - A[p * m + p]) / (2.0 * apq);
-                        const double t = (theta >= 0.0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1.0));
-                        c = 1.0 / sqrt(t * t + 1.0);
-                        s = t * c;
-                    }
+        bt_block_sum<1>(s2, red);
+        const double x0 = A[(k + 1) * m + k];
+        if (s2[0] == 0.0) {
+            if (tid == 0) { beta[k] = 0.0; e[k] = x0; d[k] = A[k * m + k]; }
+            __syncthreads();
+            continue;
+        }
+        const double nx = sqrt(x0 * x0 + s2[0]);
+        const double alpha = x0 > 0.0 ? -nx : nx;
+        const double bet = 1.0 / (alpha * (alpha - x0));   // H = I - bet u u^T, u = x - alpha e_1
+        __syncthreads();
+        if (tid == 0) {
+            A[(k + 1) * m + k] = x0 - alpha;
+            beta[k] = bet;
+            e[k] = alpha;
+            d[k] = A[k * m + k];
+        }
+        __syncthreads();
+        for (int i = tid; i < n1; i += BT_T) {              // p = bet A' u
+            const double *row = A + (size_t)(k + 1 + i) * m + (k + 1);
+            double acc = 0.0;
+            for (int j = 0; j < n1; ++j) acc += row[j] * A[(k + 1 + j) * m + k];
+            p[i] = bet * acc;
+        }
+        __syncthreads();
+        double up[1] = {0.0};
+        for (int i = tid; i < n1; i += BT_T) up[0] += A[(k + 1 + i) * m + k] * p[i];
+        bt_block_sum<1>(up, red);
+        const double K = 0.5 * bet * up[0];
+        for (int i = tid; i < n1; i += BT_T) p[i] -= K * A[(k + 1 + i) * m + k];   // q = p - K u
+        __syncthreads();
+        for (int t = tid; t < n1 * n1; t += BT_T) {          // A' -= u q^T + q u^T
+            const int i = t / n1, j = t % n1;
+            A[(k + 1 + i) * m + (k + 1 + j)] -= A[(k + 1 + i) * m + k] * p[j] + p[i] * A[(k + 1 + j) * m + k];
+        }
+        __syncthreads();
+    }
+    if (tid == 0) {
+        if (m >= 2) {
+            d[m - 2] = A[(m - 2) * m + m - 2];
+            e[m - 2] = A[(m - 1) * m + m - 2];
+        }
+        d[m - 1] = A[(m - 1) * m + m - 1];
+        e[m - 1] = 0.0;
+    }
+    __syncthreads();
+    // 2. eigenvalues: Gershgorin interval, then multisection per root
+    double lo = 1e300, hi = -1e300, emax2 = 0.0;
+    for (int i = 0; i < m; ++i) {
+        const double r = fabs(e[i]) + (i > 0 ? fabs(e[i - 1]) : 0.0);
+        lo = fmin(lo, d[i] - r);
+        hi = fmax(hi, d[i] + r);
+        emax2 = fmax(emax2, e[i] * e[i]);
+    }
+    const double eps = 2.220446049250313e-16;
+    const double tnorm = fmax(fabs(lo), fabs(hi));
+    const double pivmin = 2.2250738585072014e-308 * fmax(1.0, emax2);
+    lo -= 2.0 * eps * tnorm + 2.0 * pivmin;
+    hi += 2.0 * eps * tnorm + 2.0 * pivmin;
+    if (warp < nr) {
+        const int r = warp;
+        double a = lo, b = hi;
+        for (int it = 0; it < 64; ++it) {
+            if (b - a <= 2.0 * eps * fmax(fabs(a), fabs(b)) + 4.0 * pivmin) break;
+            const double h = (b - a) / 33.0;
+            const double x = a + h * (lane + 1);
+            const unsigned ball = __ballot_sync(0xffffffffu, bt_sturm(d, e, m, x, pivmin) > r);
+            if (ball == 0u) {
+                a = __shfl_sync(0xffffffffu, x, 31);
+            } else {
+                const int f = __ffs(ball) - 1;
+                const double xf = __shfl_sync(0xffffffffu, x, f);
+                const double xp = __shfl_sync(0xffffffffu, x, f > 0 ? f - 1 : 0);
+                if (f > 0) a = xp;
+                b = xf;
+            }
+        }
+        if (lane == 0) w[r] = 0.5 * (a + b);
+    }
+    __syncthreads();
+    // 3. inverse iteration for each root (lane 0 of warp r), on T - w_r I
+    if (warp < nr && lane == 0) {
+        const int r = warp;
+        const double lam = w[r];
+        double *z = Y + (size_t)r * m;
+        double *dl = F + (size_t)r * 4 * m, *dd = dl + m, *du = dd + m, *du2 = du + m;
+        const double tiny = eps * fmax(tnorm, 1e-300);
+        for (int i = 0; i < m; ++i) {
+            dd[i] = d[i] - lam;
+            dl[i] = e[i];
+            du[i] = e[i];
+            du2[i] = 0.0;
+        }
+        unsigned long long swp = 0, swp2 = 0;   // row interchanges (bit i)
+        for (int i = 0; i + 1 < m; ++i) {
+            if (fabs(dd[i]) >= fabs(dl[i])) {
+                if (fabs(dd[i]) < tiny) dd[i] = dd[i] < 0.0 ? -tiny : tiny;
+                const double l = dl[i] / dd[i];
+                dl[i] = l;
+                dd[i + 1] -= l * du[i];
+            } else {
+                const double l = dd[i] / dl[i];
+                dd[i] = dl[i];
+                dl[i] = l;
+                const double t = du[i];
+                du[i] = dd[i + 1];
+                dd[i + 1] = t - l * dd[i + 1];
+                if (i + 2 < m) {
+                    du2[i] = du[i + 1];
+                    du[i + 1] = -l * du[i + 1];
                 }
-                cs[2 * k] = c;
-                cs[2 * k + 1] = s;
-                pq[2 * k] = p;
-                pq[2 * k + 1] = q;
+                if (i < 64) swp |= 1ull << i; else swp2 |= 1ull << (i - 64);
             }
-            __syncthreads();
-            for (int e = tid; e < np * m; e += BT_T) {   // A <- A J, Z <- Z J (columns p, q)
-                const int k = e / m, r = e % m, p = pq[2 * k], q = pq[2 * k + 1];
-                if (q >= m) continue;
-                const double c = cs[2 * k], s = cs[2 * k + 1];
-                const double ap = A[r * m + p], aq = A[r * m + q];
-                A[r * m + p] = c * ap - s * aq;
-                A[r * m + q] = s * ap + c * aq;
-                const double zp = Z[r * m + p], zq = Z[r * m + q];
-                Z[r * m + p] = c * zp - s * zq;
-                Z[r * m + q] = s * zp + c * zq;
+        }
+        if (fabs(dd[m - 1]) < tiny) dd[m - 1] = dd[m - 1] < 0.0 ? -tiny : tiny;
+        for (int i = 0; i < m; ++i) z[i] = 1.0 + 0.5 * (double)((i * (r + 1) * 7919 + 13 * r) % 97) / 97.0;
+        for (int it = 0; it < 3; ++it) {
+            for (int i = 0; i + 1 < m; ++i) {            // L^-1 with the interchanges
+                const bool sw = i < 64 ? ((swp >> i) & 1ull) : ((swp2 >> (i - 64)) & 1ull);
+                if (sw) { const double t = z[i]; z[i] = z[i + 1]; z[i + 1] = t; }
+                z[i + 1] -= dl[i] * z[i];
             }
-            __syncthreads();
-            for (int e = tid; e < np * m; e += BT_T) {   // A <- J^T A (rows p, q)
-                const int k = e / m, r = e % m, p = pq[2 * k], q = pq[2 * k + 1];
-                if (q >= m) continue;
-                const double c = cs[2 * k], s = cs[2 * k + 1];
-                const double ap = A[p * m + r], aq = A[q * m + r];
-                A[p * m + r] = c * ap - s * aq;
-                A[q * m + r] = s * ap + c * aq;
+            for (int i = m - 1; i >= 0; --i) {           // U^-1
+                double s = z[i];
+                if (i + 1 < m) s -= du[i] * z[i + 1];
+                if (i + 2 < m) s -= du2[i] * z[i + 2];
+                z[i] = s / dd[i];
             }
-            __syncthreads();
-            for (int k = tid; k < np; k += BT_T) {
-                const int p = pq[2 * k], q = pq[2 * k + 1];
-                if (q < m) A[p * m + q] = A[q * m + p] = 0.0;
-            }
-            __syncthreads();
+            double nrm = 0.0;
+            for (int i = 0; i < m; ++i) nrm += z[i] * z[i];
+            nrm = 1.0 / sqrt(nrm);
+            for (int i = 0; i < m; ++i) z[i] *= nrm;
         }
     }
+    __syncthreads();
+    // Gram-Schmidt of the roots in ascending order (separates vectors of (near-)degenerate roots)
+    if (tid == 0) {
+        for (int r = 1; r < nr; ++r) {
+            double *z = Y + (size_t)r * m;
+            for (int pass = 0; pass < 2; ++pass)
+                for (int q = 0; q < r; ++q) {
+                    const double *y = Y + (size_t)q * m;
+                    double s = 0.0;
+                    for (int i = 0; i < m; ++i) s += y[i] * z[i];
+                    for (int i = 0; i < m; ++i) z[i] -= s * y[i];
+                }
+            double nrm = 0.0;
+            for (int i = 0; i < m; ++i) nrm += z[i] * z[i];
+            nrm = 1.0 / sqrt(nrm);
+            for (int i = 0; i < m; ++i) z[i] *= nrm;
+        }
+    }
+    __syncthreads();
+    // 4. back-transformation y = H_0 H_1 ... H_{m-3} z (warp r, reflections in reverse order)
+    if (warp < nr) {
+        double *z = Y + (size_t)warp * m;
+        for (int k = m - 3; k >= 0; --k) {
+            const double bet = beta[k];
+            if (bet == 0.0) continue;
+            const int n1 = m - k - 1;
+            double s = 0.0;
+            for (int i = lane; i < n1; i += 32) s += A[(k + 1 + i) * m + k] * z[k + 1 + i];
+            for (int off = 16; off; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
+            for (int i = lane; i < n1; i += 32) z[k + 1 + i] -= bet * s * A[(k + 1 + i) * m + k];
+            __syncwarp();
+        }
+    }
+    __syncthreads();
 }
 
-// shared memory of the subspace kernel (doubles) for subspaces up to mmax
+// shared memory of the subspace kernel for subspaces up to mmax: the projected matrix, eigensolver
+// scratch (4 m + 5 nr m <= mmax^2 doubles since mmax = 15 nr), reductions and Gram-Schmidt dots
 inline size_t bt_subspace_smem(int mmax) {
-    const size_t mm = (size_t)mmax + 1;
-    return (2 * (size_t)mmax * mmax + 8 * BT_MAXR * (BT_T / 32) + 2 * mm + mmax + BT_MAXR + 16) * sizeof(double) +
-           (2 * mm + BT_MAXR + 8) * sizeof(int);
+    return (2 * (size_t)mmax * mmax + 8 * BT_MAXR * (BT_T / 32) + mmax + BT_MAXR + 16 + BT_MAXR) * sizeof(double);
 }
 
 __global__ void __launch_bounds__(BT_T) bt_subspace_kernel(BtArrays a) {
@@ -448,9 +870,8 @@ __global__ void __launch_bounds__(BT_T) bt_subspace_kernel(BtArrays a) {
     extern __shared__ double smem[];
     double *A = smem, *Z = A + (size_t)mmax * mmax;
     double *red = Z + (size_t)mmax * mmax;
-    double *cs = red + 8 * BT_MAXR * (BT_T / 32);
-    double *cdot = cs + 2 * (mmax + 1);
-    int *pq = reinterpret_cast<int *>(cdot + mmax + BT_MAXR + 16);
+    double *cdot = red + 8 * BT_MAXR * (BT_T / 32);
+    double *wev = cdot + mmax + BT_MAXR + 16;
 
     // 1. new columns of the projected matrix: P[i][j] = V_i . AV_j, j in [m_done, m)
     {
@@ -472,22 +893,9 @@ __global__ void __launch_bounds__(BT_T) bt_subspace_kernel(BtArrays a) {
         A[e] = i <= j ? P[(long long)i * mmax + j] : P[(long long)j * mmax + i];
     }
     __syncthreads();
-    bt_jacobi(m, A, Z, cs, pq, red);
-    if (tid == 0) {
-        // the nr smallest eigenvalues in ascending order (ties: lower index first)
-        unsigned long long used = 0, used2 = 0;
-        for (int r = 0; r < nr; ++r) {
-            int best = -1;
-            for (int i = 0; i < m; ++i) {
-                const bool u = i < 64 ? ((used >> i) & 1ull) : ((used2 >> (i - 64)) & 1ull);
-                if (u) continue;
-                if (best < 0 || A[i * m + i] < A[best * m + best]) best = i;
-            }
-            if (best < 64) used |= 1ull << best; else used2 |= 1ull << (best - 64);
-            s_sel[r] = best;
-            s_u[r] = A[best * m + best];
-        }
-    }
+    bt_eig_lowest(m, nr, A, Z, wev, red);
+    const double *Yev = Z + 4 * m;   // eigenvector r at Yev[r * m + i]
+    if (tid < nr) s_u[tid] = wev[tid];
     __syncthreads();
     // 3. Ritz vectors R_r = sum_i y_ir V_i and residuals Rk_r = sum_i y_ir AV_i - u_r R_r (:101-107)
     double sq[BT_MAXR];
@@ -502,7 +910,7 @@ __global__ void __launch_bounds__(BT_T) bt_subspace_kernel(BtArrays a) {
 #pragma unroll
             for (int r = 0; r < BT_MAXR; ++r)
                 if (r < nr) {
-                    const double y = Z[i * m + s_sel[r]];
+                    const double y = Yev[r * m + i];
                     rv[r] += y * vi;
                     av[r] += y * ai;
                 }
@@ -539,7 +947,7 @@ __global__ void __launch_bounds__(BT_T) bt_subspace_kernel(BtArrays a) {
         s_action = 0;
         if (!finite) {
             st.status = BT_NONFINITE;
-        } else if (lft == 0 && it > 0) {
+        } else if (lft == 0 && (it > 0 || st.first_stop)) {
             st.status = BT_CONVERGED;
         } else if (it == in.max_iter - 1) {
             st.status = BT_MAXITER;
@@ -640,7 +1048,8 @@ struct BatchWork {
     DevBuf<double> C, SC, S, blk, glr, glr_atoms, gam, omega, V, AV, R, Rk, T, sub, H, F, D, u, err, Y;
     DevBuf<int> ao_off, ao_atom, pos, active;
     DevBuf<long long> off_glr_atoms;
-    DevBuf<int4> t_sc, t1, t2, t4, t5;
+    DevBuf<int4> t_sc, t1, t2, t4, t5, p1, p2, p4, p5;
+    DevBuf<bf16> Pl;
     cudaGraphExec_t graph = nullptr;
     ~BatchWork() {
         if (graph) cudaGraphExecDestroy(graph);
@@ -668,10 +1077,26 @@ static void bt_launch(Ctx &c, const DevBuf<int4> &tiles, size_t n_tiles, const S
     c.prof_end(slot, flops, 0.0);
 }
 
+template <class Step>
+static void bt_plane_launch(Ctx &c, const DevBuf<int4> &tiles, size_t n_tiles, const Step &step, int family) {
+    if (n_tiles == 0) return;
+    int slot = c.prof_begin(family);
+    static bool attr = false;
+    if (!attr) {
+        TINCR_CUDA(cudaFuncSetAttribute(bt_plane_kernel<Step>, cudaFuncAttributeMaxDynamicSharedMemorySize, BP_SMEM));
+        attr = true;
+    }
+    bt_plane_kernel<Step><<<(unsigned)n_tiles, BP_T, BP_SMEM, c.stream>>>(tiles.p, step);
+    count_launch(c.stream, "bt_plane");
+    check_launch("bt_plane");
+    c.prof_end(slot, 0.0, 0.0);
+}
+
 int Ctx::solve_batch(int n_inst, const tincr_tda_instance *hin, int max_iter, double tol, int precision,
                      tincr_tda_result *res) {
     if (n_inst <= 0 || !hin || !res || max_iter <= 0 || !(tol > 0.0)) fail(TINCR_BAD_ARG, "solve_batch: bad arguments");
-    if (precision != TINCR_PREC_FP64) fail(TINCR_BAD_ARG, "solve_batch: only TINCR_PREC_FP64 is implemented");
+    if (precision != TINCR_PREC_FP64 && precision != TINCR_PREC_BF16X3) fail(TINCR_BAD_ARG, "solve_batch: unknown precision");
+    const bool mixed = precision == TINCR_PREC_BF16X3;
     g_launches = 0;
     if (!batch) batch = new BatchWork();
     BatchWork &w = *batch;
@@ -681,6 +1106,7 @@ int Ctx::solve_batch(int n_inst, const tincr_tda_instance *hin, int max_iter, do
     std::vector<long long> hGlrOff(n_inst, 0);
     long long o_c = 0, o_s = 0, o_blk = 0, o_glr = 0, o_gam = 0, o_om = 0, o_v = 0, o_r = 0, o_sub = 0, o_h = 0, o_f = 0,
               o_d = 0, o_u = 0, o_y = 0;
+    long long o_pc = 0, o_pv = 0;
     int o_ao = 0, o_aoatom = 0, mmax_all = 1, nr_max = 1, nmax_atoms = 1;
     for (int I = 0; I < n_inst; ++I) {
         const tincr_tda_instance &q = hin[I];
@@ -713,6 +1139,10 @@ int Ctx::solve_batch(int n_inst, const tincr_tda_instance *hin, int max_iter, do
         b.off_d = o_d; o_d += 3LL * b.nr * n;
         b.off_u = o_u; o_u += b.nr;
         b.off_y = o_y; o_y += (long long)b.nr * N;
+        b.ko = pad32(b.o); b.kv = pad32(b.v); b.k2 = pad32(2 * n);
+        b.off_pc = o_pc; o_pc += 2LL * n * b.ko + 2LL * n * b.kv + (long long)b.v * b.k2 + (long long)b.o * b.k2;
+        b.off_pv = o_pv;
+        o_pv += (long long)b.nr * ((long long)b.v * b.ko + 2LL * n * b.kv + 2LL * n * b.k2 + (long long)b.v * b.k2);
         b.off_ao = o_ao; o_ao += N + 1;
         b.off_aoatom = o_aoatom; o_aoatom += n;
         mmax_all = std::max(mmax_all, b.mmax);
@@ -802,6 +1232,34 @@ int Ctx::solve_batch(int n_inst, const tincr_tda_instance *hin, int max_iter, do
     upload_any(stream, w.t2, t2);
     upload_any(stream, w.t4, t4);
     upload_any(stream, w.t5, t5);
+    // plane GEMM tiles of the mixed form (64 x 64)
+    std::vector<int4> p1, p2, p4, p5;
+    if (mixed) {
+        for (int I = 0; I < n_inst; ++I) {
+            const BtInst &b = w.h[I];
+            const int n2 = 2 * b.n;
+            for (int s = 0; s < b.nr; ++s) {
+                for (int tm = 0; tm < ceil_div(n2, 64); ++tm)
+                    for (int tn = 0; tn < ceil_div(b.v, 64); ++tn) {
+                        p1.push_back(make_int4(I, s, tm, tn));
+                        if (b.lc) p4.push_back(make_int4(I, s, tm, tn));
+                    }
+                if (b.lc)
+                    for (int tm = 0; tm < ceil_div(n2, 64); ++tm)
+                        for (int tn = 0; tn < ceil_div(n2, 64); ++tn) p2.push_back(make_int4(I, s, tm, tn));
+                for (int tm = 0; tm < ceil_div(b.o, 64); ++tm)
+                    for (int tn = 0; tn < ceil_div(b.v, 64); ++tn) p5.push_back(make_int4(I, s, tm, tn));
+            }
+        }
+        upload_any(stream, w.p1, p1);
+        upload_any(stream, w.p2, p2);
+        upload_any(stream, w.p4, p4);
+        upload_any(stream, w.p5, p5);
+        w.Pl.reserve(N_PLANES * (o_pc + o_pv));
+        TINCR_CUDA(cudaMemsetAsync(w.Pl.p, 0, N_PLANES * (o_pc + o_pv) * sizeof(bf16), stream));   // K padding stays zero
+        for (auto &b : w.h) b.off_pv += o_pc;
+        upload_any(stream, w.inst, w.h);
+    }
 
     BtArrays a{};
     a.inst = w.inst.p; a.state = w.state.p;
@@ -809,6 +1267,8 @@ int Ctx::solve_batch(int n_inst, const tincr_tda_instance *hin, int max_iter, do
     a.V = w.V.p; a.AV = w.AV.p; a.R = w.R.p; a.Rk = w.Rk.p; a.T = w.T.p; a.sub = w.sub.p; a.H = w.H.p; a.F = w.F.p;
     a.D = w.D.p; a.u = w.u.p; a.err = w.err.p; a.Y = w.Y.p; a.ao_off = w.ao_off.p; a.ao_atom = w.ao_atom.p;
     a.active = w.active.p; a.tol = tol;
+    a.P = mixed ? w.Pl.p : nullptr;
+    a.ps = o_pc + o_pv;
 
     TINCR_CUDA(cudaEventRecord(ev0, stream));
     // set-up: SC, packed blocks, gamma_lr in the AO basis, guesses
@@ -820,6 +1280,11 @@ int Ctx::solve_batch(int n_inst, const tincr_tda_instance *hin, int max_iter, do
         bt_expand_kernel<<<n_inst, BT_T, 0, stream>>>(a, w.glr_atoms.p, w.off_glr_atoms.p);
         count_launch(stream, "bt_expand");
         check_launch("bt_expand");
+    }
+    if (mixed) {
+        bt_const_planes_kernel<<<n_inst, BT_T, 0, stream>>>(a);
+        count_launch(stream, "bt_const_planes");
+        check_launch("bt_const_planes");
     }
     bt_guess_kernel<<<n_inst, BT_T, 0, stream>>>(a, w.pos.p);
     count_launch(stream, "bt_guess");
@@ -852,34 +1317,77 @@ int Ctx::solve_batch(int n_inst, const tincr_tda_instance *hin, int max_iter, do
         count_launch(stream, "bt_subspace");
         check_launch("bt_subspace");
     };
-    int iters = 0, active = n_inst;
-    const bool use_graph = !profiling;
-    cudaGraphExec_t exec = nullptr;
-    if (use_graph) {
-        cudaGraph_t g = nullptr;
-        TINCR_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
-        long long before = g_launches;
-        iteration();
-        const long long per_iter = g_launches - before;
-        g_launches = before;
-        TINCR_CUDA(cudaStreamEndCapture(stream, &g));
-        TINCR_CUDA(cudaGraphInstantiate(&exec, g, 0));
-        cudaGraphDestroy(g);
-        while (active > 0 && iters < max_iter) {
-            TINCR_CUDA(cudaGraphLaunch(exec, stream));
-            g_launches += per_iter;
-            ++iters;
-            TINCR_CUDA(cudaMemcpyAsync(&active, w.active.p, sizeof(int), cudaMemcpyDeviceToHost, stream));
-            sync();
+    // the mixed-form iteration: split-BF16 plane GEMMs, FP64 Coulomb diagonals and subspace step
+    auto iteration_mixed = [&]() {
+        bt_split_x_kernel<<<gv, BT_T, 0, stream>>>(a);
+        count_launch(stream, "bt_split_x");
+        check_launch("bt_split_x");
+        bt_plane_launch(*this, w.p1, p1.size(), BtP1{a}, TINCR_KF_AO_TRANSFORM);
+        bt_diag_kernel<<<gv, BT_T, 0, stream>>>(a, BT_MIXED);
+        count_launch(stream, "bt_diag");
+        check_launch("bt_diag");
+        bt_coulomb_kernel<<<gv, BT_T, coul_smem, stream>>>(a, BT_MIXED);
+        count_launch(stream, "bt_coulomb");
+        check_launch("bt_coulomb");
+        bt_plane_launch(*this, w.p2, p2.size(), BtP2{a}, TINCR_KF_AO_EXCHANGE);
+        bt_plane_launch(*this, w.p4, p4.size(), BtP4{a}, TINCR_KF_AO_EXCHANGE);
+        bt_gt_nolc_kernel<<<gv, BT_T, 0, stream>>>(a);
+        count_launch(stream, "bt_gt_nolc");
+        check_launch("bt_gt_nolc");
+        bt_plane_launch(*this, w.p5, p5.size(), BtP5{a}, TINCR_KF_AO_TRANSFORM);
+        TINCR_CUDA(cudaMemsetAsync(w.active.p, 0, sizeof(int), stream));
+        bt_subspace_kernel<<<n_inst, BT_T, sub_smem, stream>>>(a);
+        count_launch(stream, "bt_subspace");
+        check_launch("bt_subspace");
+    };
+    // run an iteration function (as a CUDA graph unless kernel timing is on) until no instance is
+    // running or `limit` iterations are done; returns the iterations run
+    auto run_loop = [&](const std::function<void()> &body, int limit) {
+        int its = 0, active = n_inst;
+        if (!profiling) {
+            cudaGraph_t g = nullptr;
+            cudaGraphExec_t exec = nullptr;
+            TINCR_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+            const long long before = g_launches;
+            body();
+            const long long per_iter = g_launches - before;
+            g_launches = before;
+            TINCR_CUDA(cudaStreamEndCapture(stream, &g));
+            TINCR_CUDA(cudaGraphInstantiate(&exec, g, 0));
+            cudaGraphDestroy(g);
+            while (active > 0 && its < limit) {
+                TINCR_CUDA(cudaGraphLaunch(exec, stream));
+                g_launches += per_iter;
+                ++its;
+                TINCR_CUDA(cudaMemcpyAsync(&active, w.active.p, sizeof(int), cudaMemcpyDeviceToHost, stream));
+                sync();
+            }
+            cudaGraphExecDestroy(exec);
+        } else {
+            while (active > 0 && its < limit) {
+                body();
+                ++its;
+                TINCR_CUDA(cudaMemcpyAsync(&active, w.active.p, sizeof(int), cudaMemcpyDeviceToHost, stream));
+                sync();
+            }
         }
-        cudaGraphExecDestroy(exec);
+        return its;
+    };
+    if (mixed && tol >= MIXED_TOL_FLOOR) {
+        run_loop(iteration_mixed, max_iter);
+    } else if (mixed) {
+        // the mixed operator resolves residuals down to MIXED_TOL_FLOOR: the mixed phase stops there
+        a.tol = MIXED_TOL_FLOOR;
+        const int its = run_loop(iteration_mixed, max_iter);
+        a.tol = tol;
+        // FP64 polish: every instance restarts from its mixed Ritz vectors on the FP64 operator and
+        // may stop at its first Rayleigh-Ritz step; convergence and energies are those of FP64
+        bt_restart_kernel<<<n_inst, BT_T, 0, stream>>>(a);
+        count_launch(stream, "bt_restart");
+        check_launch("bt_restart");
+        run_loop(iteration, std::max(1, max_iter - its));
     } else {
-        while (active > 0 && iters < max_iter) {
-            iteration();
-            ++iters;
-            TINCR_CUDA(cudaMemcpyAsync(&active, w.active.p, sizeof(int), cudaMemcpyDeviceToHost, stream));
-            sync();
-        }
+        run_loop(iteration, max_iter);
     }
     // final pass: transition charges of the Ritz vectors
     bt_launch<false, false>(*this, w.t1, t1.size(), BtStep1{a, true}, TINCR_KF_OTHER, 0.0);

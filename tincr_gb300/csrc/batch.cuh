@@ -39,6 +39,11 @@ struct BtInst {
     long long off_y;         // transition charges of the roots [nr x N]
     int off_ao;              // ao_off [N + 1]
     int off_aoatom;          // AO -> atom [n]
+    // split-BF16 planes of the mixed form (K padded to 32 elements: ko = pad(o), kv = pad(v),
+    // k2 = pad(2n)); hi and lo planes share the offsets
+    int ko, kv, k2;
+    long long off_pc;        // [C_o;SC_o] 2n x ko | [C_v;SC_v] 2n x kv | [SC_v;C_v]^T v x k2 | [SC_o;C_o]^T o x k2
+    long long off_pv;        // per slot: X^T v x ko | H 2n x kv | F 2n x k2 | G^T v x k2
 };
 
 // Dynamic Davidson state of one instance (davidson.rs:53-185 bookkeeping).
@@ -50,7 +55,7 @@ struct BtState {
     int status;       // BtStatus
     int products;     // A.X products evaluated
     int collapses;
-    int pad;
+    int first_stop;   // may stop at iteration 0 (FP64 polish started from Ritz vectors)
     double max_res;   // largest residual of the last iteration
 };
 

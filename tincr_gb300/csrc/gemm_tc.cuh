@@ -1,19 +1,20 @@
 // Plane GEMM on the 5th-generation tensor cores: tcgen05.mma with TMEM accumulators, TMA loads.
 //
-// C[M x N] = A[M x K] B[N x K]^T with A = A_hi + A_lo, B = B_hi + B_lo split-BF16 planes
-// (planes.cuh), accumulated as A_hi B_hi + A_hi B_lo + A_lo B_hi.
+// C[M x N] = A[M x K] B[N x K]^T with A and B in three split-BF16 planes each (planes.cuh),
+// accumulated as the six plane products A0B0 + A0B1 + A1B0 + A0B2 + A2B0 + A1B1.
 //
 // CTA = 192 threads, one 128 x 128 output tile, K consumed in 64-element (128-byte) blocks:
-//   * warp 4 / lane 0: TMA producer, four boxes (A_hi, A_lo, B_hi, B_lo; 128 rows x 64 bf16, 128-byte
-//     swizzle) per stage into a 3-stage ring, completion on the stage's "full" mbarrier;
-//   * warp 5 / lane 0: MMA issuer, 4 K=16 steps x 3 products per block (tcgen05.mma.cta_group::1
-//     .kind::f16, M = N = 128) into one of two TMEM accumulators (ping-pong), tcgen05.commit to the
-//     stage's "empty" and the accumulator's "full" mbarrier;
-//   * warps 0-3: fold each K block's accumulator into FP32 running sums held in registers (warp w
-//     owns TMEM lanes 32w..32w+31 = tile rows, one row per thread), then the epilogue functor.
-// The tensor core accumulates a block of only 12 MMAs before the CUDA cores add it with
-// round-to-nearest, which keeps long K (up to 2 n_orb) from building up a one-sided accumulation
-// error; the fold overlaps the next block's MMAs.
+//   * warp 4 / lane 0: TMA producer, six boxes (A0, A1, A2, B0, B1, B2; 128 rows x 64 bf16, 128-byte
+//     swizzle) per stage into a 2-stage ring, completion on the stage's "full" mbarrier;
+//   * warp 5 / lane 0: MMA issuer, 4 K=16 steps x 6 products per block (tcgen05.mma.cta_group::1
+//     .kind::f16, M = N = 128) into one of two TMEM accumulator pairs (ping-pong): the hi x hi product
+//     in one accumulator, the five smaller products in the other; tcgen05.commit to the stage's
+//     "empty" and the pair's "full" mbarrier;
+//   * warps 0-3: fold each K block's pair into FP32 running sums held in registers (warp w owns
+//     TMEM lanes 32w..32w+31 = tile rows, one row per thread), then the epilogue functor.
+// The dominant accumulator takes only 4 MMAs per block before the CUDA cores add it with
+// round-to-nearest, and the small products accumulate apart from it, which keeps long K (up to
+// 2 n_orb) from building up a one-sided accumulation error; the fold overlaps the next block's MMAs.
 // Every mbarrier wait is bounded (2 s); on expiry the thread records an error code and leaves its
 // loop, the MMA issuer waits (bounded) for its MMAs in flight, the producer for its loads, and the
 // CTA frees its TMEM and returns.
@@ -26,11 +27,11 @@
 
 namespace tincr {
 
-constexpr int TC_M = 128, TC_N = 128, TC_K = 64, TC_STAGES = 3, TC_T = 192;
+constexpr int TC_M = 128, TC_N = 128, TC_K = 64, TC_STAGES = 2, TC_T = 192;
 constexpr int TC_TILE = TC_M * TC_K * 2;                  // 16 KB (128 rows x 128 bytes)
-constexpr int TC_STAGE = 4 * TC_TILE;                     // A_hi, A_lo, B_hi, B_lo
+constexpr int TC_STAGE = 2 * N_PLANES * TC_TILE;          // A0, A1, A2, B0, B1, B2
 constexpr int TC_SMEM = TC_STAGES * TC_STAGE + 1024 + 256;
-constexpr int TC_COLS = 2 * TC_N;                         // two accumulators
+constexpr int TC_COLS = 4 * TC_N;                         // two ping-pong pairs {hi x hi, other products}
 constexpr unsigned long long TC_WAIT_NS = 2000000000ull;  // a wait gives up after 2 s
 
 // instruction descriptor, kind::f16: D = F32 (bits 4-5 = 1), A = B = BF16 (bits 7-9, 10-12 = 1),
@@ -101,6 +102,14 @@ __device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(smem_u32(bar)) : "memory");
 }
 
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&r)[16]) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+}
+
 __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
     asm volatile(
         "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
@@ -112,11 +121,15 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
         : "r"(taddr));
 }
 
+// tensor maps of the three A planes, then the three B planes
+struct TcMaps {
+    CUtensorMap m[2 * N_PLANES];
+};
+
 template <class Epi>
 __global__ void __launch_bounds__(TC_T, 1)
-gemm_planes_tc_kernel(const __grid_constant__ CUtensorMap ma_hi, const __grid_constant__ CUtensorMap ma_lo,
-                      const __grid_constant__ CUtensorMap mb_hi, const __grid_constant__ CUtensorMap mb_lo, int M,
-                      int N, int Kpad, int a_batched, int b_batched, Epi epi, int *err) {
+gemm_planes_tc_kernel(const __grid_constant__ TcMaps maps, int M, int N, int Kpad, int a_batched, int b_batched,
+                      Epi epi, int *err) {
     extern __shared__ unsigned char tc_raw[];
     unsigned char *smem = (unsigned char *)(((uintptr_t)tc_raw + 1023) & ~(uintptr_t)1023);
     uint64_t *full = reinterpret_cast<uint64_t *>(smem + TC_STAGES * TC_STAGE);
@@ -166,10 +179,12 @@ gemm_planes_tc_kernel(const __grid_constant__ CUtensorMap ma_hi, const __grid_co
                 }
                 unsigned char *st = smem + s * TC_STAGE;
                 mbar_expect_tx(&full[s], TC_STAGE);
-                tma_load_3d(st + 0 * TC_TILE, &ma_hi, kb * TC_K, m0, a_batched ? b : 0, &full[s]);
-                tma_load_3d(st + 1 * TC_TILE, &ma_lo, kb * TC_K, m0, a_batched ? b : 0, &full[s]);
-                tma_load_3d(st + 2 * TC_TILE, &mb_hi, kb * TC_K, n0, b_batched ? b : 0, &full[s]);
-                tma_load_3d(st + 3 * TC_TILE, &mb_lo, kb * TC_K, n0, b_batched ? b : 0, &full[s]);
+#pragma unroll
+                for (int q = 0; q < N_PLANES; ++q) {
+                    tma_load_3d(st + q * TC_TILE, &maps.m[q], kb * TC_K, m0, a_batched ? b : 0, &full[s]);
+                    tma_load_3d(st + (N_PLANES + q) * TC_TILE, &maps.m[N_PLANES + q], kb * TC_K, n0,
+                                b_batched ? b : 0, &full[s]);
+                }
                 issued = kb + 1;
             }
             if (!ok)   // loads still in flight land before the CTA exits
@@ -190,15 +205,20 @@ gemm_planes_tc_kernel(const __grid_constant__ CUtensorMap ma_hi, const __grid_co
                 }
                 asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
                 const uint32_t base = smem_u32(smem + s * TC_STAGE);
-                const uint32_t d = tmem + (uint32_t)(a * TC_N);
+                const uint32_t dm = tmem + (uint32_t)(a * 2 * TC_N), dx = dm + (uint32_t)TC_N;
 #pragma unroll
                 for (int kk = 0; kk < TC_K / 16; ++kk) {
                     const uint32_t off = kk * 32;   // 16 bf16 = 32 bytes along K
-                    const uint64_t ah = tc_desc(base + 0 * TC_TILE + off), al = tc_desc(base + 1 * TC_TILE + off);
-                    const uint64_t bh = tc_desc(base + 2 * TC_TILE + off), bl = tc_desc(base + 3 * TC_TILE + off);
-                    tc_mma(d, ah, bh, kk > 0 ? 1u : 0u);
-                    tc_mma(d, ah, bl, 1u);
-                    tc_mma(d, al, bh, 1u);
+                    const uint64_t a0 = tc_desc(base + 0 * TC_TILE + off), a1 = tc_desc(base + 1 * TC_TILE + off),
+                                   a2 = tc_desc(base + 2 * TC_TILE + off);
+                    const uint64_t b0 = tc_desc(base + 3 * TC_TILE + off), b1 = tc_desc(base + 4 * TC_TILE + off),
+                                   b2 = tc_desc(base + 5 * TC_TILE + off);
+                    tc_mma(dm, a0, b0, kk > 0 ? 1u : 0u);
+                    tc_mma(dx, a0, b1, kk > 0 ? 1u : 0u);
+                    tc_mma(dx, a1, b0, 1u);
+                    tc_mma(dx, a0, b2, 1u);
+                    tc_mma(dx, a2, b0, 1u);
+                    tc_mma(dx, a1, b1, 1u);
                 }
                 tc_commit(&empty[s]);
                 tc_commit(&accf[a]);
@@ -220,14 +240,15 @@ gemm_planes_tc_kernel(const __grid_constant__ CUtensorMap ma_hi, const __grid_co
                 break;
             }
             asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-            const uint32_t t0 = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(a * TC_N);
+            const uint32_t t0 = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(a * 2 * TC_N);
 #pragma unroll
-            for (int c0 = 0; c0 < TC_N; c0 += 32) {
-                uint32_t r[32];
-                tmem_ld32(t0 + (uint32_t)c0, r);
+            for (int c0 = 0; c0 < TC_N; c0 += 16) {
+                uint32_t rm[16], rx[16];
+                tmem_ld16(t0 + (uint32_t)c0, rm);
+                tmem_ld16(t0 + (uint32_t)(TC_N + c0), rx);
                 asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
 #pragma unroll
-                for (int j = 0; j < 32; ++j) sum[c0 + j] += __uint_as_float(r[j]);
+                for (int j = 0; j < 16; ++j) sum[c0 + j] += __uint_as_float(rm[j]) + __uint_as_float(rx[j]);
             }
             asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
             __syncwarp();
@@ -289,16 +310,18 @@ void gemm_planes_tc(cudaStream_t st, int M, int N, int Kpad, PlaneOperand A, Pla
                     int *d_err) {
     if (M <= 0 || N <= 0 || batch <= 0) return;
     if (Kpad <= 0 || Kpad % TC_K) fail(TINCR_BAD_ARG, "gemm_planes_tc: K not padded to 64");
-    CUtensorMap ah = plane_map(A.hi, M, Kpad, A.ld, A.sb, batch), al = plane_map(A.lo, M, Kpad, A.ld, A.sb, batch);
-    CUtensorMap bh = plane_map(B.hi, N, Kpad, B.ld, B.sb, batch), bl = plane_map(B.lo, N, Kpad, B.ld, B.sb, batch);
+    TcMaps maps;
+    for (int q = 0; q < N_PLANES; ++q) {
+        maps.m[q] = plane_map(A.p + q * A.ps, M, Kpad, A.ld, A.sb, batch);
+        maps.m[N_PLANES + q] = plane_map(B.p + q * B.ps, N, Kpad, B.ld, B.sb, batch);
+    }
     static bool attr = false;
     if (!attr) {
         TINCR_CUDA(cudaFuncSetAttribute(gemm_planes_tc_kernel<Epi>, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM));
         attr = true;
     }
     dim3 grid(ceil_div(N, TC_N), ceil_div(M, TC_M), batch);
-    gemm_planes_tc_kernel<Epi><<<grid, TC_T, TC_SMEM, st>>>(ah, al, bh, bl, M, N, Kpad, A.sb ? 1 : 0, B.sb ? 1 : 0, epi,
-                                                           d_err);
+    gemm_planes_tc_kernel<Epi><<<grid, TC_T, TC_SMEM, st>>>(maps, M, N, Kpad, A.sb ? 1 : 0, B.sb ? 1 : 0, epi, d_err);
     count_launch(st, "gemm_planes_tc");
     check_launch("gemm_planes_tc");
 }

@@ -1,19 +1,21 @@
 // Split-BF16 operand planes and the plane GEMM of the mixed-precision A.X product.
 //
-// A value x is carried as two BF16 numbers, hi = bf16(x) and lo = bf16(x - hi) (16 significant
-// bits together; the dropped lo*lo product is ~2^-16 relative).  The GEMM
-//     C[M x N] = A[M x K] B[N x K]^T,   A = A_hi + A_lo, B = B_hi + B_lo,
-// is accumulated as A_hi B_hi + A_hi B_lo + A_lo B_hi in FP32 on the tensor cores.  Operands are
-// K-contiguous planes with a padded leading dimension (multiple of 64 elements, padding zero), so
-// every GEMM of the chain reads only BF16 and no FP64 instruction sits in the inner loop (GB300's
-// FP64 pipe is ~1/1000 of its BF16 tensor rate).  The producing epilogues write the next GEMM's
-// planes directly.
+// A value x (FP32) is carried as three BF16 numbers: hi = bf16(x), mid = bf16(x - hi),
+// lo = bf16(x - hi - mid).  The two differences are exact in FP32 and the three planes hold x's 24
+// significant bits.  The GEMM
+//     C[M x N] = A[M x K] B[N x K]^T,   A = A0 + A1 + A2, B = B0 + B1 + B2 (plane 0 = hi),
+// is accumulated as A0B0 + A0B1 + A1B0 + A0B2 + A2B0 + A1B1 in FP32 on the tensor cores (the
+// dropped products are below 2^-24 relative), which gives FP32-level products from BF16 tensor
+// cores.  The tensor-core sum of every 64 elements of K is folded into FP32 running sums with
+// round-to-nearest adds on the CUDA cores.  Operands are K-contiguous planes with a padded
+// leading dimension (padding zero): the three planes of an operand lie `ps` elements apart in one
+// buffer, so every GEMM of the chain reads only BF16 and no FP64 instruction sits in the inner
+// loop (GB300's FP64 pipe is ~1/1000 of its BF16 tensor rate).  The producing epilogues write the
+// next GEMM's planes directly.
 //
 // This file holds the split kernel, the epilogue functors and a warp-level MMA implementation of
 // the plane GEMM (128 x 128 CTA tile, 8 warps of 64 x 32, 32-deep K slices double-buffered with
-// cp.async).  gemm_tc.cuh implements the same GEMM with tcgen05 + TMA.  Both fold the tensor-core
-// sum into FP32 running sums every 64 elements of K: the tensor core's own accumulation is
-// one-sided over long chains, the CUDA-core adds round to nearest.
+// cp.async).  gemm_tc.cuh implements the same GEMM with tcgen05 + TMA.
 #pragma once
 
 #include <cuda_bf16.h>
@@ -24,16 +26,30 @@ namespace tincr {
 
 typedef __nv_bfloat16 bf16;
 
+constexpr int N_PLANES = 3;
+
 inline long long pad64(long long k) { return (k + 63) / 64 * 64; }
 
-__device__ __forceinline__ void split_f32(float x, bf16 &hi, bf16 &lo) {
-    hi = __float2bfloat16_rn(x);
-    lo = __float2bfloat16_rn(x - __bfloat162float(hi));
+__device__ __forceinline__ void split3(float x, bf16 &h, bf16 &m, bf16 &l) {
+    h = __float2bfloat16_rn(x);
+    const float r1 = x - __bfloat162float(h);
+    m = __float2bfloat16_rn(r1);
+    l = __float2bfloat16_rn(r1 - __bfloat162float(m));
+}
+
+// x split into the three planes at p[k], p[k + ps], p[k + 2 ps]
+__device__ __forceinline__ void store3(bf16 *p, long long ps, long long k, float x) {
+    bf16 h, m, l;
+    split3(x, h, m, l);
+    p[k] = h;
+    p[k + ps] = m;
+    p[k + 2 * ps] = l;
 }
 
 // planes[b][r][c] (ld ldp, padding zeroed) from src[b][r][c] (or src[b][c][r] when trans) in FP64
-__global__ void split_planes_kernel(int batch, int rows, int cols, const double *__restrict__ src, long long lds,
-                                    long long sbs, int trans, bf16 *hi, bf16 *lo, long long ldp, long long sbp) {
+static __global__ void split_planes_kernel(int batch, int rows, int cols, const double *__restrict__ src, long long lds,
+                                           long long sbs, int trans, bf16 *dst, long long ps, long long ldp,
+                                           long long sbp) {
     long long per = (long long)rows * ldp;
     long long total = per * batch;
     for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total; t += (long long)gridDim.x * blockDim.x) {
@@ -42,10 +58,7 @@ __global__ void split_planes_kernel(int batch, int rows, int cols, const double 
         int r = int(e / ldp), c = int(e % ldp);
         float x = 0.f;
         if (c < cols) x = (float)(trans ? src[b * sbs + (long long)c * lds + r] : src[b * sbs + (long long)r * lds + c]);
-        bf16 h, l;
-        split_f32(x, h, l);
-        hi[b * sbp + e] = h;
-        lo[b * sbp + e] = l;
+        store3(dst, ps, b * sbp + e, x);
     }
 }
 
@@ -58,34 +71,32 @@ struct F8 {
     float x[8];
 };
 
-// 8 consecutive split values as two 16-byte stores (plane rows are 64-element padded, so aligned)
-__device__ __forceinline__ void store_split8(bf16 *hi, bf16 *lo, const float (&v)[8]) {
-    __align__(16) bf16 h[8], l[8];
+// 8 consecutive values as three 16-byte stores (plane rows are 64-element padded, so aligned)
+__device__ __forceinline__ void store3_8(bf16 *p, long long ps, const float (&v)[8]) {
+    __align__(16) bf16 h[8], m[8], l[8];
 #pragma unroll
-    for (int j = 0; j < 8; ++j) split_f32(v[j], h[j], l[j]);
-    *reinterpret_cast<uint4 *>(hi) = *reinterpret_cast<const uint4 *>(h);
-    *reinterpret_cast<uint4 *>(lo) = *reinterpret_cast<const uint4 *>(l);
+    for (int j = 0; j < 8; ++j) split3(v[j], h[j], m[j], l[j]);
+    *reinterpret_cast<uint4 *>(p) = *reinterpret_cast<const uint4 *>(h);
+    *reinterpret_cast<uint4 *>(p + ps) = *reinterpret_cast<const uint4 *>(m);
+    *reinterpret_cast<uint4 *>(p + 2 * ps) = *reinterpret_cast<const uint4 *>(l);
 }
 
 // H = acc: FP64 copy (for the Coulomb diagonals) and planes for the next GEMM
 struct EpiPlaneH {
     double *H;           // [b][m][ldh]
     long long ldh, sbh;
-    bf16 *hi, *lo;       // [b][m][ldp]
-    long long ldp, sbp;
+    bf16 *p;             // planes [b][m][ldp], plane stride ps
+    long long ps, ldp, sbp;
     __device__ __forceinline__ void operator()(int b, int m, int n, float acc) const {
         H[b * sbh + (long long)m * ldh + n] = (double)acc;
-        bf16 h, l;
-        split_f32(acc, h, l);
-        hi[b * sbp + (long long)m * ldp + n] = h;
-        lo[b * sbp + (long long)m * ldp + n] = l;
+        store3(p, ps, b * sbp + (long long)m * ldp + n, acc);
     }
     __device__ __forceinline__ void run8(int b, int m, int n, int N, const F8 &v) const {
         if (n + 8 <= N) {
             double *h64 = H + b * sbh + (long long)m * ldh + n;
 #pragma unroll
             for (int j = 0; j < 8; ++j) h64[j] = (double)v.x[j];
-            store_split8(hi + b * sbp + (long long)m * ldp + n, lo + b * sbp + (long long)m * ldp + n, v.x);
+            store3_8(p + b * sbp + (long long)m * ldp + n, ps, v.x);
         } else {
 #pragma unroll
             for (int j = 0; j < 8; ++j)
@@ -99,15 +110,11 @@ struct EpiPlaneF {
     const double *G;     // n x n gamma_lr in the AO basis
     int n;
     float ax;
-    bf16 *hi, *lo;
-    long long ldp, sbp;
+    bf16 *p;
+    long long ps, ldp, sbp;
     __device__ __forceinline__ void operator()(int b, int m, int c, float acc) const {
         int rr = m < n ? m : m - n, cc = c < n ? c : c - n;
-        float v = ax * (float)G[(long long)rr * n + cc] * acc;
-        bf16 h, l;
-        split_f32(v, h, l);
-        hi[b * sbp + (long long)m * ldp + c] = h;
-        lo[b * sbp + (long long)m * ldp + c] = l;
+        store3(p, ps, b * sbp + (long long)m * ldp + c, ax * (float)G[(long long)rr * n + cc] * acc);
     }
     __device__ __forceinline__ void run8(int b, int m, int c, int N, const F8 &v) const {
         if (c + 8 <= N) {
@@ -118,7 +125,7 @@ struct EpiPlaneF {
                 const int cc = c + j < n ? c + j : c + j - n;
                 w[j] = ax * (float)G[(long long)rr * n + cc] * v.x[j];
             }
-            store_split8(hi + b * sbp + (long long)m * ldp + c, lo + b * sbp + (long long)m * ldp + c, w);
+            store3_8(p + b * sbp + (long long)m * ldp + c, ps, w);
         } else {
 #pragma unroll
             for (int j = 0; j < 8; ++j)
@@ -131,15 +138,12 @@ struct EpiPlaneF {
 struct EpiPlaneGT {
     const double *Gc;    // [b][m][ldg] or null
     long long ldg, sbg;
-    bf16 *hi, *lo;
-    long long ldp, sbp;
+    bf16 *p;
+    long long ps, ldp, sbp;
     __device__ __forceinline__ void operator()(int b, int m, int n, float acc) const {
         float g = acc;
         if (Gc) g += (float)Gc[b * sbg + (long long)m * ldg + n];
-        bf16 h, l;
-        split_f32(g, h, l);
-        hi[b * sbp + (long long)n * ldp + m] = h;
-        lo[b * sbp + (long long)n * ldp + m] = l;
+        store3(p, ps, b * sbp + (long long)n * ldp + m, g);
     }
     __device__ __forceinline__ void run8(int b, int m, int n, int N, const F8 &v) const {
 #pragma unroll
@@ -173,8 +177,8 @@ struct EpiPlaneOut {
 // ---------------------------------------------------------------------------------------------
 
 constexpr int PG_M = 128, PG_N = 128, PG_K = 32, PG_T = 256, PG_LD = PG_K + 8;
-constexpr int PG_TILE = PG_M * PG_LD;                 // bf16 per (rows x K-slice) tile incl. padding
-constexpr int PG_SMEM = 2 * 4 * PG_TILE * 2;          // 2 stages x {Ahi, Alo, Bhi, Blo} x bytes
+constexpr int PG_TILE = PG_M * PG_LD;                      // bf16 per (rows x K-slice) tile incl. padding
+constexpr int PG_SMEM = 2 * 2 * N_PLANES * PG_TILE * 2;   // 2 stages x {A, B} x planes x bytes
 
 __device__ __forceinline__ void cp_async16(void *smem, const void *gmem, int src_bytes) {
     unsigned s = (unsigned)__cvta_generic_to_shared(smem);
@@ -191,8 +195,20 @@ __device__ __forceinline__ void mma_bf16(float c[4], const unsigned a[4], const 
         : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
 }
 
+// the six plane products of one m16n8k16 step: (0,0) (0,1) (1,0) (0,2) (2,0) (1,1)
+__device__ __forceinline__ void mma_split6(float c[4], const unsigned (&a)[N_PLANES][4],
+                                           const unsigned (&b)[N_PLANES][2]) {
+    mma_bf16(c, a[0], b[0]);
+    mma_bf16(c, a[0], b[1]);
+    mma_bf16(c, a[1], b[0]);
+    mma_bf16(c, a[0], b[2]);
+    mma_bf16(c, a[2], b[0]);
+    mma_bf16(c, a[1], b[1]);
+}
+
 struct PlaneOperand {
-    const bf16 *hi, *lo;
+    const bf16 *p;       // plane 0; plane q at p + q * ps
+    long long ps;
     long long ld;        // elements, multiple of 8
     long long sb;        // batch stride (elements), 0 = shared
 };
@@ -207,22 +223,23 @@ gemm_planes_mma_kernel(int M, int N, int Kpad, PlaneOperand A, PlaneOperand B, E
     const int g = lane >> 2, tg = lane & 3;
     const int b = blockIdx.z;
     const int m0 = blockIdx.y * PG_M, n0 = blockIdx.x * PG_N;
-    const bf16 *Ah = A.hi + b * A.sb, *Al = A.lo + b * A.sb, *Bh = B.hi + b * B.sb, *Bl = B.lo + b * B.sb;
+    const bf16 *Ab = A.p + b * A.sb, *Bb = B.p + b * B.sb;
 
-    auto stage_ptr = [&](int s, int which) { return sm + (s * 4 + which) * PG_TILE; };
-    // one stage: 4 tiles of 128 rows x 32 bf16 = 4 x 512 chunks of 16 B; 256 threads x 8 chunks
+    // tile `which`: 0..2 = A planes, 3..5 = B planes
+    auto stage_ptr = [&](int s, int which) { return sm + (s * 2 * N_PLANES + which) * PG_TILE; };
+    // one stage: 6 tiles of 128 rows x 32 bf16 = 6 x 512 chunks of 16 B; 256 threads x 12 chunks
     auto load_stage = [&](int s, int k0) {
 #pragma unroll
-        for (int q = 0; q < 8; ++q) {
-            int idx = tid + q * PG_T;          // 0 .. 2047
-            int which = idx >> 9;              // 0 Ahi, 1 Alo, 2 Bhi, 3 Blo
+        for (int q = 0; q < 12; ++q) {
+            int idx = tid + q * PG_T;          // 0 .. 3071
+            int which = idx >> 9;
             int within = idx & 511;
             int r = within >> 2, c = (within & 3) * 8;
             const bf16 *base;
             long long ld;
             int row0, lim;
-            if (which < 2) { base = which == 0 ? Ah : Al; ld = A.ld; row0 = m0; lim = M; }
-            else           { base = which == 2 ? Bh : Bl; ld = B.ld; row0 = n0; lim = N; }
+            if (which < N_PLANES) { base = Ab + which * A.ps; ld = A.ld; row0 = m0; lim = M; }
+            else                  { base = Bb + (which - N_PLANES) * B.ps; ld = B.ld; row0 = n0; lim = N; }
             int gr = row0 + r;
             const bf16 *src = base + (long long)(gr < lim ? gr : 0) * ld + k0 + c;
             cp_async16(stage_ptr(s, which) + r * PG_LD + c, src, gr < lim ? 16 : 0);
@@ -246,42 +263,31 @@ gemm_planes_mma_kernel(int M, int N, int Kpad, PlaneOperand A, PlaneOperand B, E
         cp_async_wait_all();
         __syncthreads();
         if (kb + 1 < nk) load_stage(s ^ 1, (kb + 1) * PG_K);
-        const bf16 *sAh = stage_ptr(s, 0), *sAl = stage_ptr(s, 1), *sBh = stage_ptr(s, 2), *sBl = stage_ptr(s, 3);
 #pragma unroll
         for (int kk = 0; kk < PG_K; kk += 16) {
-            unsigned ah[4][4], al[4][4], bh[4][2], bl[4][2];
 #pragma unroll
             for (int i = 0; i < 4; ++i) {
-                int r = wm * 64 + i * 16 + g;
-                const bf16 *ph = sAh + r * PG_LD + kk + tg * 2;
-                const bf16 *pl = sAl + r * PG_LD + kk + tg * 2;
-                ah[i][0] = *(const unsigned *)(ph);
-                ah[i][1] = *(const unsigned *)(ph + 8 * PG_LD);
-                ah[i][2] = *(const unsigned *)(ph + 8);
-                ah[i][3] = *(const unsigned *)(ph + 8 * PG_LD + 8);
-                al[i][0] = *(const unsigned *)(pl);
-                al[i][1] = *(const unsigned *)(pl + 8 * PG_LD);
-                al[i][2] = *(const unsigned *)(pl + 8);
-                al[i][3] = *(const unsigned *)(pl + 8 * PG_LD + 8);
-            }
+                unsigned af[N_PLANES][4];
 #pragma unroll
-            for (int j = 0; j < 4; ++j) {
-                int c = wn * 32 + j * 8 + g;
-                const bf16 *ph = sBh + c * PG_LD + kk + tg * 2;
-                const bf16 *pl = sBl + c * PG_LD + kk + tg * 2;
-                bh[j][0] = *(const unsigned *)(ph);
-                bh[j][1] = *(const unsigned *)(ph + 8);
-                bl[j][0] = *(const unsigned *)(pl);
-                bl[j][1] = *(const unsigned *)(pl + 8);
-            }
-#pragma unroll
-            for (int i = 0; i < 4; ++i)
+                for (int q = 0; q < N_PLANES; ++q) {
+                    const bf16 *pa = stage_ptr(s, q) + (wm * 64 + i * 16 + g) * PG_LD + kk + tg * 2;
+                    af[q][0] = *(const unsigned *)(pa);
+                    af[q][1] = *(const unsigned *)(pa + 8 * PG_LD);
+                    af[q][2] = *(const unsigned *)(pa + 8);
+                    af[q][3] = *(const unsigned *)(pa + 8 * PG_LD + 8);
+                }
 #pragma unroll
                 for (int j = 0; j < 4; ++j) {
-                    mma_bf16(part[i][j], ah[i], bh[j]);
-                    mma_bf16(part[i][j], ah[i], bl[j]);
-                    mma_bf16(part[i][j], al[i], bh[j]);
+                    unsigned bf[N_PLANES][2];
+#pragma unroll
+                    for (int q = 0; q < N_PLANES; ++q) {
+                        const bf16 *pb = stage_ptr(s, N_PLANES + q) + (wn * 32 + j * 8 + g) * PG_LD + kk + tg * 2;
+                        bf[q][0] = *(const unsigned *)(pb);
+                        bf[q][1] = *(const unsigned *)(pb + 8);
+                    }
+                    mma_split6(part[i][j], af, bf);
                 }
+            }
         }
         if ((kb & 1) || kb + 1 == nk) {
 #pragma unroll

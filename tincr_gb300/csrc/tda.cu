@@ -781,11 +781,13 @@ int Ctx::solve(int n_roots, int max_iter, double tol, int precision, double *ene
     std::vector<double> u;
     int it_done = 0;
     prec = precision;
-    int status = davidson(n_roots, max_iter, tol, false, u, &it_done);
-    if (precision == TINCR_PREC_BF16X3) {
-        // FP64 polish: Davidson on the exact operator from the mixed Ritz vectors, which may stop at
-        // its first Rayleigh-Ritz step.  Energies then come from an FP64 projection (second order in
-        // the mixed vectors' error) and every residual norm is that of the FP64 operator.
+    // the mixed operator resolves residuals down to MIXED_TOL_FLOOR; below that the mixed phase
+    // stops there and FP64 iterations take over
+    const bool polish = precision == TINCR_PREC_BF16X3 && tol < MIXED_TOL_FLOOR;
+    int status = davidson(n_roots, max_iter, polish ? MIXED_TOL_FLOOR : tol, false, u, &it_done);
+    if (polish) {
+        // FP64 polish for tolerances below the mixed operator's resolution: Davidson on the FP64
+        // operator from the mixed Ritz vectors, which may stop at its first Rayleigh-Ritz step.
         prec = TINCR_PREC_FP64;
         int it2 = 0;
         status = davidson(n_roots, std::max(1, max_iter - it_done), tol, true, u, &it2);

@@ -27,6 +27,10 @@ struct KernelStats {
 
 enum Blk { BLK_OCC = 0, BLK_VIRT = 1 };
 
+// Residual tolerances at or above this are met by the mixed (three-plane split-BF16) operator alone;
+// tighter tolerances make a TINCR_PREC_BF16X3 solve finish with FP64 Davidson iterations.
+constexpr double MIXED_TOL_FLOOR = 1e-6;
+
 struct BatchWork;                      // batched LE / CT TDA workspace (batch.cu)
 void release_batch(BatchWork *w);
 
@@ -87,7 +91,7 @@ struct Ctx {
     // split-BF16 planes of the mixed-precision contraction (mixed.cu)
     bool planes_ready = false;
     bool use_tc = true;                   // tcgen05 plane GEMM; false: warp-MMA plane GEMM
-    DevBuf<__nv_bfloat16> cst_hi[2], cst_lo[2], cswT_hi[2], cswT_lo[2], mx_bf16;
+    DevBuf<__nv_bfloat16> cst[2], cswT[2], mx_bf16;   // three planes each (planes.cuh)
     DevBuf<double> mx_f64;
     long long mx_key = -1;
     DevBuf<int> d_tc_err;                 // error word of the tensor-core kernels' bounded waits
