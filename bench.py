@@ -38,6 +38,7 @@ sys.path.insert(0, ROOT)
 METRIC = "LC-TDA roots+S1 grad wall s (mixed vs FP64 GPU, <=1e-6 Eh); FMO monomers/s"
 N_ROOTS, MAX_ITER, TOL = 20, 450, 1e-4
 PRECISIONS = {"fp64": 0, "bf16x3": 1}   # tincr_precision values
+FMO_N_LE, FMO_N_CT, FMO_TOL, FMO_MAX_ITER = 4, 1, 1e-4, 150
 R_LR = 1.0 / 0.3
 
 
@@ -243,7 +244,7 @@ def run_gpu(args):
             traffic = rec["dram_bytes_per_vector"] * vec_per_launch / 2.0
     cpu = cpu_baseline(sy, g, float(np.mean(main["iters"])), main["products"] / args.steps, main["cg"]) \
         if args.cpu_baseline else None
-    fams = ["ao_exchange", "ao_transform", "subspace", "gradient", "other"][:_lib.KF_COUNT]
+    fams = ["ao_exchange", "ao_transform", "subspace", "gradient", "other", "host_subspace_eigensolver"][:_lib.KF_COUNT]
     out = {
         "metric": METRIC, "value": step_s, "unit": "s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": step_s * 1e3, "higher_is_better": False,
@@ -271,11 +272,92 @@ def run_gpu(args):
         "lowest_energies_eh": [float(e) for e in main["energies"][:3]],
         "wall_s": wall,
     }
+    if args.fmo:
+        out["fmo"] = run_fmo(args, ctx)
     if ref64 is not None:
         out["fp64_gpu"] = {"value": float(np.mean(ref64["dev_ms"])) / 1e3, "unit": "s",
                            "speedup_of_mixed": float(np.mean(ref64["dev_ms"])) / max(1e-9, float(np.mean(main["dev_ms"]))),
                            "max_abs_energy_err_eh": float(np.abs(main["energies"] - ref64["energies"]).max()),
                            "max_abs_grad_err_eh_per_bohr": float(np.abs(main["grad"] - ref64["grad"]).max())}
+    return out
+
+
+def fmo_workload():
+    """64-acene FMO aggregate: 4 x 4 x 4 lattice (3.6 / 5.0 / 14 A), ring counts drawn from {2..5},
+    +-15 deg in-plane rotation, +-0.1 A jitter (seeded); LC, monomer SCC on the host; CT pairs with a
+    smallest interatomic distance below 4.5 A; 4 LE roots per monomer, 1 CT root per pair direction."""
+    from tincr_gb300 import fmo
+    from tincr_gb300 import geometry as G
+    from tincr_gb300 import groundstate as gs
+    z, x, mono = G.acene_lattice(4, 4, 4)
+    mons = fmo.build_monomers(z, G.to_bohr(x), mono, lc=True)
+    pairs = fmo.close_pairs(mons, 4.5 / gs.P.BOHR_TO_ANGS)
+    inst, labels = fmo.aggregate_instances(mons, pairs, FMO_N_LE, FMO_N_CT)
+    return mons, pairs, inst, labels
+
+
+def fmo_cpu_sample(mons, inst, labels, n_le_sample=8, n_ct_sample=32):
+    """tincr's per-instance TDA (oracle engines, numpy + host BLAS) on a few LE and CT instances,
+    scaled to the whole work list by instance kind."""
+    from oracle import tda as OT
+    t_le, t_ct = [], []
+    le = [k for k, l in enumerate(labels) if l[0] == "LE"][:n_le_sample]
+    ct = [k for k, l in enumerate(labels) if l[0] == "CT"][:n_ct_sample]
+    for k in le + ct:
+        q = inst[k]
+        t0 = time.perf_counter()
+        no, nv = q["n_occ"], q["n_virt"]
+        ao = np.concatenate([[0], np.cumsum(q["opa"])])
+        qov, qoo, qvv = OT.trans_charges(ao, q["c"], q["s"], np.arange(no), np.arange(no, no + nv))
+        om = OT.orbe_differences(q["orbe"][:no], q["orbe"][no:])
+        eng = OT.TdaEngine(om, qov, q["gamma"], qoo, qvv, q["gamma_lr"], no, nv)
+        OT.run_tda_engine(eng, q["xyz"], q["n_roots"], FMO_MAX_ITER, FMO_TOL)
+        (t_le if labels[k][0] == "LE" else t_ct).append(time.perf_counter() - t0)
+    n_le = sum(1 for l in labels if l[0] == "LE")
+    n_ct = len(labels) - n_le
+    total = n_le * float(np.mean(t_le)) + n_ct * float(np.mean(t_ct))
+    sample = ("oracle TDA of %d LE and %d CT instances (%.3f s / %.3f s each), scaled to %d LE + %d CT instances"
+              % (len(t_le), len(t_ct), np.mean(t_le), np.mean(t_ct), n_le, n_ct))
+    return total, sample
+
+
+def run_fmo(args, ctx):
+    """Batched LE / CT TDA of the 64-acene aggregate, mixed and FP64 forms (monomers/s)."""
+    from tincr_gb300 import _lib
+    from tincr_gb300 import fmo
+    t0 = time.perf_counter()
+    mons, pairs, inst, labels = fmo_workload()
+    t_setup = time.perf_counter() - t0
+    out = {"workload": "acene64-fmo-le4-ct1", "monomers": len(mons), "ct_pairs": len(pairs),
+           "instances": len(inst), "tol": FMO_TOL, "max_iter": FMO_MAX_ITER,
+           "host_setup_s": t_setup}
+    res = {}
+    for name, prec in (("bf16x3", _lib.PREC_BF16X3), ("fp64", _lib.PREC_FP64)):
+        for _ in range(max(1, args.warmup)):
+            fmo.solve_batch(ctx, inst, FMO_MAX_ITER, FMO_TOL, prec)
+        dev, wall = [], []
+        for _ in range(args.steps):
+            t0 = time.perf_counter()
+            rc, r = fmo.solve_batch(ctx, inst, FMO_MAX_ITER, FMO_TOL, prec)
+            wall.append(time.perf_counter() - t0)
+            dev.append(ctx.last_timing()[0] / 1e3)
+        res[name] = (float(np.mean(dev)), float(np.mean(wall)), rc, r)
+    dm, wm, rcm, rm = res["bf16x3"]
+    d64, w64, rc64, r64 = res["fp64"]
+    out.update({
+        "value_monomers_per_s": len(mons) / dm, "unit": "monomers/s",
+        "step_ms": dm * 1e3, "instances_per_s": len(inst) / dm,
+        "e2e": {"value": len(mons) / wm, "unit": "monomers/s", "wall_ms": wm * 1e3},
+        "fp64_gpu": {"value": len(mons) / d64, "step_ms": d64 * 1e3, "e2e_wall_ms": w64 * 1e3},
+        "speedup_mixed_vs_fp64": d64 / dm,
+        "status_ok": bool(rcm == _lib.OK and rc64 == _lib.OK),
+        "max_abs_energy_err_eh": float(max(np.abs(a["energies"] - b["energies"]).max() for a, b in zip(rm, r64))),
+        "davidson_iterations_max": int(max(x["iterations"] for x in rm)),
+    })
+    if args.cpu_baseline:
+        total, sample = fmo_cpu_sample(mons, inst, labels)
+        out["cpu_baseline"] = {"value": len(mons) / total, "unit": "monomers/s", "step_s": total,
+                               "cores": os.cpu_count(), "kind": "port", "sample": sample}
     return out
 
 
@@ -362,7 +444,14 @@ def run_reference(args):
         total, threads, sample = cpu_sample(sy, g, args.ref_products, args.ref_iters, args.ref_cg, sample_vectors=1)
         vals.append(total)
     v = float(np.mean(vals))
-    return {"impl": "reference", "metric": METRIC, "value": v, "unit": "s", "n_gpus": world, "steps": args.steps,
+    fmo_ref = None
+    if args.fmo:
+        mons, pairs, inst, labels = fmo_workload()
+        total, fsample = fmo_cpu_sample(mons, inst, labels)
+        fmo_ref = {"workload": "acene64-fmo-le4-ct1", "value_monomers_per_s": len(mons) / total,
+                   "unit": "monomers/s", "step_s": total, "cores": os.cpu_count(), "kind": "port",
+                   "sample": fsample}
+    return {"impl": "reference", "metric": METRIC, "fmo": fmo_ref, "value": v, "unit": "s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": v * 1e3, "higher_is_better": False, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded (H2O)128 cluster, host SCC ground state)",
             "config": {"workload": "water128-lctda-20roots+S1grad", "n_roots": N_ROOTS, "tol": TOL,
@@ -397,6 +486,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--precision", default="bf16x3", choices=sorted(PRECISIONS))
     ap.add_argument("--no-compare-fp64", dest="compare_fp64", action="store_false")
+    ap.add_argument("--no-fmo", dest="fmo", action="store_false")
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
     ap.add_argument("--ref-products", type=int, default=369)

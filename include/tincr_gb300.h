@@ -78,7 +78,8 @@ typedef enum {
     TINCR_KF_SUBSPACE = 2,     /* Davidson projections, Ritz vectors, residuals, orthogonalisation  */
     TINCR_KF_GRADIENT = 3,     /* gradient: pairwise-atom derivative kernel and adjoint GEMMs        */
     TINCR_KF_OTHER = 4,        /* Coulomb, packing, transition charges, small kernels              */
-    TINCR_KF_COUNT = 5
+    TINCR_KF_HOST = 5,         /* host time of the Davidson subspace eigensolver (not a kernel)      */
+    TINCR_KF_COUNT = 6
 } tincr_kernel_family;
 
 /* Turn per-family kernel timing on (1) or off (0); turning it on clears the statistics. */

@@ -141,3 +141,38 @@ def test_batch_mixed_tight_tolerance(gpu_ctx):
               "fp64 iterations", [r["iterations"] for r in r64])
     assert rcm == _lib.OK
     assert max(np.abs(a["energies"] - b["energies"]).max() for a, b in zip(r64, rm)) < 1e-10
+
+
+@pytest.mark.gpu
+def test_le_gradients_concurrent_match_single_context(gpu_ctx):
+    """LE gradients on several concurrent contexts equal the single-context gradients (to 1e-12
+    Eh/bohr) and, for one monomer, the oracle's tincr-formula gradient (to 1e-8 Eh/bohr)."""
+    from oracle import gradients as OG
+    from tincr_gb300 import gradients as GR
+    from tincr_gb300 import groundstate as gs
+    from tincr_gb300 import tda as T
+    case = fmo_case(3, 1, 1)
+    n_mon = len(case["monomers"])
+    rc, res = fmo.solve_batch(gpu_ctx, case["instances"][:n_mon], max_iter=150, tol=1e-8)
+    states = [0] * n_mon
+    conc = fmo.le_gradients(case["monomers"], res, states, n_streams=3)
+    for k, m in enumerate(case["monomers"]):
+        es = T.ExcitedStateSystem.from_ground_state(gpu_ctx, m.system, m.ground)
+        es.set_states(res[k]["energies"], res[k]["coefficients"])
+        g1 = GR.GradientSystem(es, m.system, m.ground).tda_gradient(0)
+        assert np.abs(conc[k] - g1).max() < 1e-12
+    # oracle for the smallest monomer
+    k = int(np.argmin([m.system.n_orbs for m in case["monomers"]]))
+    m = case["monomers"][k]
+    sy, g = m.system, m.ground
+    from oracle import tda as OT
+    qov, qoo, qvv = OT.trans_charges(sy.ao_offset, g.orbs, g.s, sy.occ_indices, sy.virt_indices)
+    der = OG.derivative_tensors(sy.numbers, sy.xyz, sy.ao_offset, sy.ao_atom, sy.hubbard, sy.r_lr, sy.params)
+    inp = dict(p=g.p, p0=g.p0, h_coul_x=g.h_coul_x, gamma=g.gamma, dq=g.dq, s=g.s, ao_atom=sy.ao_atom,
+               numbers=sy.numbers, xyz=sy.xyz, params=sy.params, gamma_lr_ao=gs.atom_to_ao(sy, g.gamma_lr),
+               orbe=g.orbe, occ=sy.occ_indices, virt=sy.virt_indices, ci_eigenvalues=res[k]["energies"],
+               ci_coefficients=res[k]["coefficients"], q_ov=qov, q_oo=qoo, q_vv=qvv, gamma_lr=g.gamma_lr,
+               orbs=g.orbs, gamma_ao=gs.atom_to_ao(sy, g.gamma))
+    _, flr = OG.ground_state_gradient(inp, der, True)
+    ref = OG.tda_gradient(inp, der, 0, True, flr_dmd0=flr)
+    assert np.abs(conc[k] - ref).max() < 1e-8

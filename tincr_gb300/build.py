@@ -27,7 +27,7 @@ def _nvcc():
 
 
 def _flags(verbose_ptxas=False):
-    f = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-O3", "--expt-relaxed-constexpr",
+    f = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-O3,-fopenmp", "--expt-relaxed-constexpr",
          "-I", os.path.join(HERE, "..", "include")] + ARCH
     if verbose_ptxas:
         f += ["-Xptxas", "-v"]
@@ -60,7 +60,7 @@ def build(force=False, verbose_ptxas=False, jobs=None):
             if verbose_ptxas and log:
                 sys.stderr.write(log)
     tmp = LIB + ".tmp"
-    cmd = [nvcc, "-shared", "-o", tmp] + objs + ARCH + ["-lcudart"]
+    cmd = [nvcc, "-shared", "-o", tmp] + objs + ARCH + ["-lcudart", "-Xcompiler", "-fopenmp"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("link failed:\n%s\n%s" % (r.stdout, r.stderr))

@@ -160,4 +160,207 @@ bool eigh_upper(int n, const double *a, double *w, double *z) {
     return true;
 }
 
+// ----------------------------------------------------------------------------------------------
+// The k lowest eigenpairs only: Householder tridiagonalisation without accumulating Q (the
+// reflection vectors are kept), bisection on Sturm counts for the k smallest eigenvalues, inverse
+// iteration with partial-pivoting LU of T - w I for their eigenvectors, Gram-Schmidt among them
+// (separates (near-)degenerate roots) and back-transformation through the k vectors.  About
+// (4/3) n^3 flops against the full decomposition's ~9 n^3; Davidson needs n_roots << n pairs.
+// a: n x n row-major (upper triangle read); w: k eigenvalues ascending; y: y[r * n + i] = component
+// i of eigenvector r.  Returns false on non-finite input.
+// ----------------------------------------------------------------------------------------------
+
+namespace {
+
+int sturm_count(const std::vector<double> &d, const std::vector<double> &e, int n, double x, double pivmin) {
+    int c = 0;
+    double q = d[0] - x;
+    if (std::fabs(q) < pivmin) q = -pivmin;
+    if (q < 0.0) ++c;
+    for (int i = 1; i < n; ++i) {
+        q = d[i] - x - e[i - 1] * e[i - 1] / q;
+        if (std::fabs(q) < pivmin) q = -pivmin;
+        if (q < 0.0) ++c;
+    }
+    return c;
+}
+
+}  // namespace
+
+bool eigh_lowest_upper(int n, const double *a, int k, double *w, double *y) {
+    if (n <= 0 || k <= 0 || k > n) return false;
+    std::vector<double> A((size_t)n * n), d(n), e(n, 0.0), beta(n, 0.0), p(n);
+    for (int i = 0; i < n; ++i)
+        for (int j = 0; j < n; ++j) {
+            const double x = (i <= j) ? a[(size_t)i * n + j] : a[(size_t)j * n + i];
+            if (!std::isfinite(x)) return false;
+            A[(size_t)i * n + j] = x;
+        }
+    // 1. T = Q^T A Q; reflection k acts on rows/columns k+1..n-1, its vector u kept in column k
+    //    below the diagonal (stored transposed in row k to the right of the diagonal for contiguous
+    //    access)
+    // rows of the matrix-vector product and of the rank-2 update are spread over host threads for
+    // large subspaces; every row is computed by one thread in a fixed order (deterministic)
+    const bool par = n >= 256;
+    double bet_s = 0.0;
+    bool skip = false;
+#pragma omp parallel num_threads(8) if (par)
+    for (int c = 0; c + 2 < n; ++c) {
+        const int n1 = n - c - 1;
+        double *u = &A[(size_t)c * n + c + 1];            // row c, columns c+1.. (= column c by symmetry)
+#pragma omp single
+        {
+            const double x0 = u[0];
+            double s2 = 0.0;
+            for (int i = 1; i < n1; ++i) s2 += u[i] * u[i];
+            d[c] = A[(size_t)c * n + c];
+            skip = s2 == 0.0;
+            if (skip) {
+                beta[c] = 0.0;
+                e[c] = x0;
+            } else {
+                const double nx = std::sqrt(x0 * x0 + s2);
+                const double alpha = x0 > 0.0 ? -nx : nx;
+                bet_s = 1.0 / (alpha * (alpha - x0));
+                u[0] = x0 - alpha;
+                beta[c] = bet_s;
+                e[c] = alpha;
+            }
+        }
+        if (skip) continue;   // every thread sees the same flag after the single's barrier
+        const double bet = bet_s;
+        // p = bet A' u over the trailing block (symmetric, full storage kept up to date)
+#pragma omp for schedule(static)
+        for (int i = 0; i < n1; ++i) {
+            const double *row = &A[(size_t)(c + 1 + i) * n + c + 1];
+            double acc = 0.0;
+            for (int j = 0; j < n1; ++j) acc += row[j] * u[j];
+            p[i] = bet * acc;
+        }
+#pragma omp single
+        {
+            double up = 0.0;
+            for (int i = 0; i < n1; ++i) up += u[i] * p[i];
+            const double K = 0.5 * bet * up;
+            for (int i = 0; i < n1; ++i) p[i] -= K * u[i];
+        }
+#pragma omp for schedule(static)
+        for (int i = 0; i < n1; ++i) {
+            double *row = &A[(size_t)(c + 1 + i) * n + c + 1];
+            const double ui = u[i], pi = p[i];
+            for (int j = 0; j < n1; ++j) row[j] -= ui * p[j] + pi * u[j];
+        }
+    }
+    if (n >= 2) {
+        d[n - 2] = A[(size_t)(n - 2) * n + n - 2];
+        e[n - 2] = A[(size_t)(n - 2) * n + n - 1];
+    }
+    d[n - 1] = A[(size_t)(n - 1) * n + n - 1];
+    e[n - 1] = 0.0;
+    // 2. eigenvalues by bisection
+    double lo = 1e300, hi = -1e300, emax2 = 0.0;
+    for (int i = 0; i < n; ++i) {
+        const double r = std::fabs(e[i]) + (i > 0 ? std::fabs(e[i - 1]) : 0.0);
+        lo = std::min(lo, d[i] - r);
+        hi = std::max(hi, d[i] + r);
+        emax2 = std::max(emax2, e[i] * e[i]);
+    }
+    const double eps = 2.220446049250313e-16;
+    const double tnorm = std::max(std::fabs(lo), std::fabs(hi));
+    const double pivmin = 2.2250738585072014e-308 * std::max(1.0, emax2);
+    lo -= 2.0 * eps * tnorm + 2.0 * pivmin;
+    hi += 2.0 * eps * tnorm + 2.0 * pivmin;
+    double left = lo;   // eigenvalue r lies above the previous one
+    for (int r = 0; r < k; ++r) {
+        double x_lo = left, x_hi = hi;
+        for (int it = 0; it < 200; ++it) {
+            if (x_hi - x_lo <= 2.0 * eps * std::max(std::fabs(x_lo), std::fabs(x_hi)) + 4.0 * pivmin) break;
+            const double mid = 0.5 * (x_lo + x_hi);
+            if (sturm_count(d, e, n, mid, pivmin) > r) x_hi = mid;
+            else x_lo = mid;
+        }
+        w[r] = 0.5 * (x_lo + x_hi);
+        left = x_lo;
+    }
+    // 3. inverse iteration on T - w I (LU with partial pivoting)
+    std::vector<double> dl(n), dd(n), du(n), du2(n), z(n);
+    std::vector<char> swp(n);
+    const double tiny = eps * std::max(tnorm, 1e-300);
+    for (int r = 0; r < k; ++r) {
+        for (int i = 0; i < n; ++i) {
+            dd[i] = d[i] - w[r];
+            dl[i] = e[i];
+            du[i] = e[i];
+            du2[i] = 0.0;
+            swp[i] = 0;
+        }
+        for (int i = 0; i + 1 < n; ++i) {
+            if (std::fabs(dd[i]) >= std::fabs(dl[i])) {
+                if (std::fabs(dd[i]) < tiny) dd[i] = dd[i] < 0.0 ? -tiny : tiny;
+                const double l = dl[i] / dd[i];
+                dl[i] = l;
+                dd[i + 1] -= l * du[i];
+            } else {
+                const double l = dd[i] / dl[i];
+                dd[i] = dl[i];
+                dl[i] = l;
+                const double t = du[i];
+                du[i] = dd[i + 1];
+                dd[i + 1] = t - l * dd[i + 1];
+                if (i + 2 < n) {
+                    du2[i] = du[i + 1];
+                    du[i + 1] = -l * du[i + 1];
+                }
+                swp[i] = 1;
+            }
+        }
+        if (std::fabs(dd[n - 1]) < tiny) dd[n - 1] = dd[n - 1] < 0.0 ? -tiny : tiny;
+        for (int i = 0; i < n; ++i) z[i] = 1.0 + 0.5 * (double)((i * (r + 1) * 7919 + 13 * r) % 97) / 97.0;
+        for (int it = 0; it < 3; ++it) {
+            for (int i = 0; i + 1 < n; ++i) {
+                if (swp[i]) std::swap(z[i], z[i + 1]);
+                z[i + 1] -= dl[i] * z[i];
+            }
+            for (int i = n - 1; i >= 0; --i) {
+                double s = z[i];
+                if (i + 1 < n) s -= du[i] * z[i + 1];
+                if (i + 2 < n) s -= du2[i] * z[i + 2];
+                z[i] = s / dd[i];
+            }
+            double nrm = 0.0;
+            for (int i = 0; i < n; ++i) nrm += z[i] * z[i];
+            nrm = 1.0 / std::sqrt(nrm);
+            for (int i = 0; i < n; ++i) z[i] *= nrm;
+        }
+        // Gram-Schmidt against the lower roots (twice)
+        for (int pass = 0; pass < 2; ++pass)
+            for (int q = 0; q < r; ++q) {
+                const double *yq = y + (size_t)q * n;   // still in the tridiagonal basis
+                double s = 0.0;
+                for (int i = 0; i < n; ++i) s += yq[i] * z[i];
+                for (int i = 0; i < n; ++i) z[i] -= s * yq[i];
+            }
+        double nrm = 0.0;
+        for (int i = 0; i < n; ++i) nrm += z[i] * z[i];
+        nrm = 1.0 / std::sqrt(nrm);
+        for (int i = 0; i < n; ++i) y[(size_t)r * n + i] = z[i] * nrm;
+    }
+    // 4. back-transformation y = H_0 ... H_{n-3} z
+    for (int r = 0; r < k; ++r) {
+        double *yr = y + (size_t)r * n;
+        for (int c = n - 3; c >= 0; --c) {
+            if (beta[c] == 0.0) continue;
+            const int n1 = n - c - 1;
+            const double *u = &A[(size_t)c * n + c + 1];
+            double s = 0.0;
+            for (int i = 0; i < n1; ++i) s += u[i] * yr[c + 1 + i];
+            s *= beta[c];
+            for (int i = 0; i < n1; ++i) yr[c + 1 + i] -= s * u[i];
+        }
+    }
+    for (int r = 0; r < k; ++r)
+        if (!std::isfinite(w[r])) return false;
+    return true;
+}
+
 }  // namespace tincr

@@ -17,6 +17,7 @@
 // sum_jb (ij|ab)_lr X_jb).  Cost per vector 8 n o v + 16 n^2 v instead of 2 N o v (o + v).
 // Without long-range correction F is diagonal-only and the two n^2 v products drop out.
 #include <algorithm>
+#include <chrono>
 #include <cstdlib>
 #include <cmath>
 #include <cstdio>
@@ -46,6 +47,7 @@ void check_launch(const char *name) {
 }
 
 bool eigh_upper(int n, const double *a, double *w, double *z);
+bool eigh_lowest_upper(int n, const double *a, int k, double *w, double *y);
 
 // ----------------------------------------------------------------------------------------------
 // small kernels
@@ -618,7 +620,7 @@ int Ctx::davidson(int n_roots, int max_iter, double tol, bool from_ritz, std::ve
     int dim_sub = n_roots;      // tincr's dim_sub bookkeeping
     const int dim_sub_origin = n_roots;
     std::vector<double> aproj;  // m x m upper triangle used
-    std::vector<double> hP, w(mmax), z;
+    std::vector<double> hP, w(mmax);
     std::vector<double> errs(n_roots);
     int status = TINCR_NOT_CONVERGED;
     int it_done = 0;
@@ -655,14 +657,20 @@ int Ctx::davidson(int n_roots, int max_iter, double tol, bool from_ritz, std::ve
         }
         m_done = m;
         // 2. eigenproblem of the subspace matrix (upper triangle)
-        z.resize((size_t)m * m);
-        if (!eigh_upper(m, aproj.data(), w.data(), z.data())) fail(TINCR_NONFINITE, "subspace eigensolver failed");
+        //    (the n_roots lowest pairs only: eigh_lowest_upper, eigen_host.cpp)
+        const auto th0 = std::chrono::steady_clock::now();
+        std::vector<double> yt((size_t)n_roots * m);
+        if (!eigh_lowest_upper(m, aproj.data(), n_roots, w.data(), yt.data()))
+            fail(TINCR_NONFINITE, "subspace eigensolver failed");
+        if (profiling) {
+            KernelStats &hs = stats[TINCR_KF_HOST];
+            hs.ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - th0).count();
+            hs.launches += 1;
+            hs.flops += 4.0 / 3.0 * (double)m * m * m;
+        }
         for (int r = 0; r < n_roots; ++r) u[r] = w[r];
         for (int r = 0; r < n_roots; ++r)
             if (!std::isfinite(u[r])) fail(TINCR_NONFINITE, "non-finite Ritz value");
-        std::vector<double> yt((size_t)n_roots * m);
-        for (int r = 0; r < n_roots; ++r)
-            for (int i = 0; i < m; ++i) yt[(size_t)r * m + i] = z[(size_t)i * m + r];
         TINCR_CUDA(cudaMemcpyAsync(dYt.p, yt.data(), yt.size() * sizeof(double), cudaMemcpyHostToDevice, stream));
         TINCR_CUDA(cudaMemcpyAsync(du.p, u.data(), n_roots * sizeof(double), cudaMemcpyHostToDevice, stream));
         // 3.1 Ritz vectors R = Y^T V ; 3.2 residuals Rk = Y^T AV - u o R

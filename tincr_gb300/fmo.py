@@ -150,3 +150,40 @@ def solve_batch(ctx, instances, max_iter=50, tol=1e-4, precision=_lib.PREC_FP64)
         outs[k]["iterations"] = res[k].iterations
         outs[k]["status"] = res[k].status
     return rc, outs
+
+
+def le_gradients(monomers, results, states, n_streams=8, variant="reference", contexts=None):
+    """Excitation-energy gradients of locally excited states, the LE terms of tincr's FMO exciton
+    gradient (`SuperSystem::fmo_cis_gradient`, src/fmo/lcmo/cis_gradient.rs:118-126, which adds
+    c^2 * `Monomer::tda_gradient_lc(n)` per contributing LE state; src/fmo/gradients/excited_state.rs:
+    299-542).  For monomer k the gradient of root states[k] of results[k] (its batch TDA result) is
+    computed on the GPU; the monomers are spread over `n_streams` contexts, each driven by its own
+    host thread (tincr runs the monomers on rayon threads), so their kernels overlap on the device.
+
+    Returns a list of [3 N_k] arrays (Hartree/bohr, atom order of the monomer)."""
+    from concurrent.futures import ThreadPoolExecutor
+    from . import gradients as GR
+    from . import tda as T
+    own = contexts is None
+    ctxs = contexts if contexts is not None else [_lib.Context(0) for _ in range(n_streams)]
+    n_streams = len(ctxs)
+    out = [None] * len(monomers)
+
+    def work(lane):
+        ctx = ctxs[lane]
+        for k in range(lane, len(monomers), n_streams):
+            m = monomers[k]
+            es = T.ExcitedStateSystem.from_ground_state(ctx, m.system, m.ground)
+            es.prepare_tda()
+            es.set_states(results[k]["energies"], results[k]["coefficients"])
+            out[k] = GR.GradientSystem(es, m.system, m.ground).tda_gradient(int(states[k]), variant)
+
+    try:
+        with ThreadPoolExecutor(max_workers=n_streams) as ex:
+            for f in [ex.submit(work, lane) for lane in range(n_streams)]:
+                f.result()
+    finally:
+        if own:
+            for c in ctxs:
+                c.close()
+    return out
