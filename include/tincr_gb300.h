@@ -224,7 +224,11 @@ int tincr_set_parameters(tincr_ctx *ctx, int n_kinds, const int *kind_z, const i
  *   grad_gs [3*n_atoms] ground-state gradient or NULL; grad_exc [3*n_atoms] gradient of the
  *   excitation energy of `state` or NULL (total S_n gradient = grad_gs + grad_exc);
  *   cg_iterations: Z-vector CG iterations (or NULL).  Returns TINCR_CG_MAXITER when the CG did
- *   not reach r.r <= 1e-19 in 10000 iterations (gradient still written). */
+ *   not reach r.r <= 1e-19 in 10000 iterations (gradient still written).
+ * The two-electron contractions (Z-vector products included) use the precision the roots were
+ * solved with: TINCR_PREC_BF16X3 after a mixed tincr_tda_solve, FP64 after an FP64 solve or
+ * tincr_tda_set_states.  The CG's convergence test is FP64; a mixed CG that stalls after 200
+ * iterations continues in FP64 from its current Z. */
 int tincr_gradient(tincr_ctx *ctx, const int *atom_kind, double r_lr, const double *P,
                    const double *h_coul_x, const double *dq, int state, int variant,
                    double *grad_gs, double *grad_exc, int *cg_iterations);

@@ -141,3 +141,23 @@ def test_gradient_call_order_and_arguments(gpu_ctx):
     with pytest.raises(_lib.TincrError) as e:
         gr.tda_gradient(0)
     assert e.value.status == _lib.BAD_ARG
+
+
+@pytest.mark.parametrize("name,lc,variant", [("water8", True, "reference"), ("naphthalene", True, "exact"),
+                                             ("polyene8", False, "reference")])
+def test_mixed_gradient_within_bar(gpu_ctx, name, lc, variant):
+    """After a mixed solve the gradient's contractions and Z-vector run mixed: S1 gradient within
+    1e-5 Eh/bohr (spec bar) of the gradient after an FP64 solve of the same roots."""
+    z, x = _molecule(name)
+    sy = gs.build_system(z, x, lc=lc)
+    g = gs.run_scc(sy, tol=1e-11)
+    out = {}
+    for prec in (T._lib.PREC_FP64, T._lib.PREC_BF16X3):
+        es = T.ExcitedStateSystem.from_ground_state(gpu_ctx, sy, g)
+        es.run_tda(3, 300, 1e-6, precision=prec)
+        gr = GR.GradientSystem(es, sy, g)
+        out[prec] = gr.both(0, variant)
+    d_gs = np.abs(out[T._lib.PREC_FP64][0] - out[T._lib.PREC_BF16X3][0]).max()
+    d_ex = np.abs(out[T._lib.PREC_FP64][1] - out[T._lib.PREC_BF16X3][1]).max()
+    print("%s mixed gradient: |d grad_gs| %.2e |d grad_exc| %.2e Eh/bohr" % (name, d_gs, d_ex))
+    assert d_gs < 1e-5 and d_ex < 1e-5

@@ -38,6 +38,7 @@ struct BtArrays {
     double *C, *SC, *S, *blk, *glr, *gam, *omega, *V, *AV, *R, *Rk, *T, *sub, *H, *F, *D, *u, *err, *Y;
     bf16 *P;           // split-BF16 planes (mixed form): plane q of element k at P[k + q * ps]
     long long ps;
+    float *glr32, *blk32, *D32;   // FP32 copies of glr, blk and D (z slots) for the plane epilogues
     const int *ao_off, *ao_atom;
     int *active;
     double tol;
@@ -235,6 +236,16 @@ __global__ void bt_expand_kernel(BtArrays a, const double *__restrict__ glr_atom
     }
 }
 
+// FP32 copies of gamma_lr (AO) and the packed blocks for the mixed form's epilogues (set-up)
+__global__ void bt_f32_copies_kernel(BtArrays a) {
+    const BtInst in = a.inst[blockIdx.x];
+    const long long nb = 2LL * in.n * 2 * (in.o + in.v);
+    for (long long t = threadIdx.x; t < nb; t += blockDim.x) a.blk32[in.off_blk + t] = (float)a.blk[in.off_blk + t];
+    if (in.lc)
+        for (long long t = threadIdx.x; t < (long long)in.n * in.n; t += blockDim.x)
+            a.glr32[in.off_glr + t] = (float)a.glr[in.off_glr + t];
+}
+
 // unit vectors on the nr smallest omega (solvers/utils.rs:17-26), state reset
 __global__ void bt_guess_kernel(BtArrays a, const int *__restrict__ pos) {
     const int I = blockIdx.x;
@@ -260,7 +271,7 @@ __global__ void bt_diag_kernel(BtArrays a, int mode) {
     const BtInst in = a.inst[I];
     const double *X;
     if (!bt_vector(a, in, I, b, mode == BT_FINAL, &X)) return;
-    if (mode == BT_FP64 && in.lc) return;   // the exchange GEMM's epilogue captures them
+    if (mode != BT_FINAL && in.lc) return;   // the exchange GEMM's epilogue captures them
     const int n = in.n, v = in.v;
     const double *H = a.H + in.off_h + (long long)b * 2 * n * v;
     const double *rv = a.blk + in.off_blk + 2LL * n * in.o;
@@ -310,6 +321,7 @@ __global__ void bt_coulomb_kernel(BtArrays a, int mode) {
                 f[(long long)(n + mu) * n2 + mu] += z;
             } else {
                 a.D[in.off_d + (long long)(2 * in.nr + b) * n + mu] = z;
+                if (mode == BT_MIXED) a.D32[in.off_d + (long long)(2 * in.nr + b) * n + mu] = (float)z;
             }
         }
     }
@@ -509,7 +521,7 @@ struct BtP1 {
     }
     __device__ void epi(const BtPlaneOp &op, int m, int n, float acc) const {
         const BtInst &in = *op.in;
-        a.H[in.off_h + (long long)op.b * 2 * in.n * in.v + (long long)m * in.v + n] = (double)acc;
+        if (!in.lc) a.H[in.off_h + (long long)op.b * 2 * in.n * in.v + (long long)m * in.v + n] = (double)acc;
         bt_split_store(a, bt_pv_h(in, op.b) + (long long)m * in.kv + n, acc);
     }
 };
@@ -531,7 +543,10 @@ struct BtP2 {
         const BtInst &in = *op.in;
         const int n = in.n;
         const int rr = r < n ? r : r - n, cc = c < n ? c : c - n;
-        const float f = -0.25f * (float)a.glr[in.off_glr + (long long)rr * n + cc] * acc;
+        double *d = a.D + in.off_d;   // Coulomb diagonals of M from the same accumulator
+        if (r < n && c == r + n) d[(long long)op.b * n + r] = (double)acc;
+        if (r >= n && c == r - n) d[(long long)(in.nr + op.b) * n + c] = (double)acc;
+        const float f = -0.25f * a.glr32[in.off_glr + (long long)rr * n + cc] * acc;
         bt_split_store(a, bt_pv_f(in, op.b) + (long long)r * in.k2 + c, f);
     }
 };
@@ -552,9 +567,9 @@ struct BtP4 {
     __device__ void epi(const BtPlaneOp &op, int r, int x, float acc) const {
         const BtInst &in = *op.in;
         const int n = in.n;
-        const double z = a.D[in.off_d + (long long)(2 * in.nr + op.b) * n + (r < n ? r : r - n)];
-        const double rv = a.blk[in.off_blk + 2LL * n * in.o + (long long)r * in.v + x];
-        bt_split_store(a, bt_pv_gt(in, op.b) + (long long)x * in.k2 + r, acc + (float)(z * rv));
+        const float z = a.D32[in.off_d + (long long)(2 * in.nr + op.b) * n + (r < n ? r : r - n)];
+        const float rv = a.blk32[in.off_blk + 2LL * n * in.o + (long long)r * in.v + x];
+        bt_split_store(a, bt_pv_gt(in, op.b) + (long long)x * in.k2 + r, acc + z * rv);
     }
 };
 
@@ -1050,6 +1065,7 @@ struct BatchWork {
     DevBuf<long long> off_glr_atoms;
     DevBuf<int4> t_sc, t1, t2, t4, t5, p1, p2, p4, p5;
     DevBuf<bf16> Pl;
+    DevBuf<float> glr32, blk32, D32;
     cudaGraphExec_t graph = nullptr;
     ~BatchWork() {
         if (graph) cudaGraphExecDestroy(graph);
@@ -1269,6 +1285,14 @@ int Ctx::solve_batch(int n_inst, const tincr_tda_instance *hin, int max_iter, do
     a.active = w.active.p; a.tol = tol;
     a.P = mixed ? w.Pl.p : nullptr;
     a.ps = o_pc + o_pv;
+    if (mixed) {
+        w.glr32.reserve(std::max<long long>(1, o_glr));
+        w.blk32.reserve(std::max<long long>(1, o_blk));
+        w.D32.reserve(o_d);
+    }
+    a.glr32 = mixed ? w.glr32.p : nullptr;
+    a.blk32 = mixed ? w.blk32.p : nullptr;
+    a.D32 = mixed ? w.D32.p : nullptr;
 
     TINCR_CUDA(cudaEventRecord(ev0, stream));
     // set-up: SC, packed blocks, gamma_lr in the AO basis, guesses
@@ -1285,6 +1309,9 @@ int Ctx::solve_batch(int n_inst, const tincr_tda_instance *hin, int max_iter, do
         bt_const_planes_kernel<<<n_inst, BT_T, 0, stream>>>(a);
         count_launch(stream, "bt_const_planes");
         check_launch("bt_const_planes");
+        bt_f32_copies_kernel<<<n_inst, BT_T, 0, stream>>>(a);
+        count_launch(stream, "bt_f32_copies");
+        check_launch("bt_f32_copies");
     }
     bt_guess_kernel<<<n_inst, BT_T, 0, stream>>>(a, w.pos.p);
     count_launch(stream, "bt_guess");
@@ -1323,13 +1350,13 @@ int Ctx::solve_batch(int n_inst, const tincr_tda_instance *hin, int max_iter, do
         count_launch(stream, "bt_split_x");
         check_launch("bt_split_x");
         bt_plane_launch(*this, w.p1, p1.size(), BtP1{a}, TINCR_KF_AO_TRANSFORM);
-        bt_diag_kernel<<<gv, BT_T, 0, stream>>>(a, BT_MIXED);
+        bt_plane_launch(*this, w.p2, p2.size(), BtP2{a}, TINCR_KF_AO_EXCHANGE);   // + LC Coulomb diagonals
+        bt_diag_kernel<<<gv, BT_T, 0, stream>>>(a, BT_MIXED);                  // non-LC Coulomb diagonals
         count_launch(stream, "bt_diag");
         check_launch("bt_diag");
         bt_coulomb_kernel<<<gv, BT_T, coul_smem, stream>>>(a, BT_MIXED);
         count_launch(stream, "bt_coulomb");
         check_launch("bt_coulomb");
-        bt_plane_launch(*this, w.p2, p2.size(), BtP2{a}, TINCR_KF_AO_EXCHANGE);
         bt_plane_launch(*this, w.p4, p4.size(), BtP4{a}, TINCR_KF_AO_EXCHANGE);
         bt_gt_nolc_kernel<<<gv, BT_T, 0, stream>>>(a);
         count_launch(stream, "bt_gt_nolc");

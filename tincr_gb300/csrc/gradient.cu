@@ -502,26 +502,45 @@ int Ctx::zvector_cg(int variant, const double *R, double *Z, int max_iter, doubl
         return h;
     };
     EW(zguess_kernel, len, len, R, d_omega.p, Z);          // bs = R / omega
-    op(Z, Ap);
-    EW(axpby3_kernel, len, len, 1.0, R, -1.0, Ap, 0.0, nullptr, r);   // r = R - A bs
-    TINCR_CUDA(cudaMemcpyAsync(p, r, len * sizeof(double), cudaMemcpyDeviceToDevice, stream));
-    double rr = dot(r, r);
-    int it = 0;
-    int status = TINCR_CG_MAXITER;
-    for (it = 0; it < max_iter; ++it) {
-        op(p, Ap);
-        double pAp = dot(p, Ap);
-        double alpha = rr / pAp;
-        if (!std::isfinite(alpha)) fail(TINCR_NONFINITE, "Z-vector CG: non-finite step");
-        EW(cg_update_kernel, len, len, alpha, p, Ap, Z, r);
-        double rr_new = dot(r, r);
-        if (rr_new <= conv) {
-            status = TINCR_OK;
-            ++it;
-            break;
+    // CG from the current Z (tincr: helpers.rs:1146-1223); the convergence test is FP64
+    auto run = [&](int limit, int *done) {
+        op(Z, Ap);
+        EW(axpby3_kernel, len, len, 1.0, R, -1.0, Ap, 0.0, nullptr, r);   // r = R - A Z
+        TINCR_CUDA(cudaMemcpyAsync(p, r, len * sizeof(double), cudaMemcpyDeviceToDevice, stream));
+        double rr = dot(r, r);
+        int st = TINCR_CG_MAXITER;
+        int k = 0;
+        for (k = 0; k < limit; ++k) {
+            op(p, Ap);
+            double pAp = dot(p, Ap);
+            double alpha = rr / pAp;
+            if (!std::isfinite(alpha)) fail(TINCR_NONFINITE, "Z-vector CG: non-finite step");
+            EW(cg_update_kernel, len, len, alpha, p, Ap, Z, r);
+            double rr_new = dot(r, r);
+            if (rr_new <= conv) {
+                st = TINCR_OK;
+                ++k;
+                break;
+            }
+            EW(cg_dir_kernel, len, len, rr_new / rr, p, r);
+            rr = rr_new;
         }
-        EW(cg_dir_kernel, len, len, rr_new / rr, p, r);
-        rr = rr_new;
+        *done = k;
+        return st;
+    };
+    int it = 0, status;
+    if (prec == TINCR_PREC_BF16X3) {
+        // mixed products; if the recursion stalls on the mixed operator, FP64 CG continues from Z
+        status = run(std::min(max_iter, 200), &it);
+        if (status != TINCR_OK) {
+            prec = TINCR_PREC_FP64;
+            int it2 = 0;
+            status = run(std::max(1, max_iter - it), &it2);
+            it += it2;
+            prec = TINCR_PREC_BF16X3;
+        }
+    } else {
+        status = run(max_iter, &it);
     }
     if (iters) *iters = it;
     return status;
@@ -543,7 +562,7 @@ int Ctx::gradient(const int *atom_kind, double r_lr_, const double *P, const dou
     const int n = n_orb, o = n_occ, v = n_virt, N = n_atoms;
     const size_t nn = (size_t)n * n;
     g_launches = 0;
-    prec = TINCR_PREC_FP64;
+    prec = solve_prec;   // the contractions follow the precision the roots were solved with
     TINCR_CUDA(cudaEventRecord(ev0, stream));
     DevBuf<int> dkind(N);
     TINCR_CUDA(cudaMemcpyAsync(dkind.p, atom_kind, N * sizeof(int), cudaMemcpyHostToDevice, stream));

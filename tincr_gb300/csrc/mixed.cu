@@ -1,14 +1,17 @@
 // Mixed-precision AO-direct contraction (TINCR_PREC_BF16X3): the four GEMMs of Ctx::ao_contract
-// on three-plane split-BF16 operands with FP32 tensor-core accumulation (planes.cuh).  The Coulomb
-// diagonals (y = q_ov X per atom) are taken in FP64 from the FP64 copy of H, and omega o X is added
-// in FP64.
+// on three-plane split-BF16 operands with FP32 tensor-core accumulation (planes.cuh); omega o X is
+// added in FP64.
 //
 //   VT  = split(V^T)                                  [|S| x |R|]   planes
-//   H   = [C_R;SC_R] V                                [2n x |S|]    FP64 + planes      (step 1)
-//   z   = ac gamma y,  Gc = diag(z, z) [C_Q;SC_Q]      FP64 (Coulomb part of G)
+//   H   = [C_R;SC_R] V                                [2n x |S|]    planes             (step 1)
 //   F   = ax gamma_lr o (H [C_S;SC_S]^T)              [2n x 2n]     planes             (step 2)
-//   GT  = (F [SC_Q;C_Q] + Gc)^T                       [|Q| x 2n]    planes             (step 4)
+//         with the Coulomb diagonals y of M captured from the same accumulator
+//   z   = ac gamma y                                  FP64, then an FP32 copy
+//   GT  = (F [SC_Q;C_Q] + diag(z, z) [C_Q;SC_Q])^T    [|Q| x 2n]    planes             (step 4)
 //   out = [SC_P;C_P]^T G  (+ omega o X)               [|P| x |Q|]   FP64               (step 5)
+// The epilogues run in FP32 on FP32 copies of gamma_lr and [C;SC] (GB300's FP64 pipe is too narrow
+// for per-element conversions).  Without exchange, H is also kept in FP64 for the Coulomb
+// diagonals and the Coulomb part of G is split like an operand.
 #include <algorithm>
 
 #include "gemm_tc.cuh"
@@ -22,6 +25,17 @@ namespace tincr {
 static int grid_of(long long work, int n_sm) {
     long long b = (work + 255) / 256;
     return int(std::max<long long>(1, std::min<long long>(b, 32LL * n_sm)));
+}
+
+static __global__ void to_float_kernel(long long len, const double *__restrict__ x, float *y) {
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < len; t += (long long)gridDim.x * blockDim.x)
+        y[t] = (float)x[t];
+}
+
+static void to_float(Ctx &c, long long len, const double *x, float *y) {
+    to_float_kernel<<<grid_of(len, c.n_sm), 256, 0, c.stream>>>(len, x, y);
+    count_launch(c.stream, "to_float");
+    check_launch("to_float");
 }
 
 // constant planes of a system: [C_o;SC_o], [C_v;SC_v] (K = block) and [SC_o;C_o]^T, [SC_v;C_v]^T (K = 2n)
@@ -43,6 +57,12 @@ void Ctx::prepare_planes() {
                                                                     0);
         count_launch(stream, "split_planes");
         check_launch("split_planes");
+        stk32[blk].alloc((size_t)2 * n * w);
+        to_float(*this, 2LL * n * w, stk(blk), stk32[blk].p);
+    }
+    if (lc) {
+        glr32.alloc((size_t)n * n);
+        to_float(*this, (long long)n * n, d_glr_ao.p, glr32.p);
     }
     planes_ready = true;
 }
@@ -86,6 +106,8 @@ void Ctx::ao_contract_mixed(int k, int R, int S, const double *V, int P, int Q, 
         mx_key = key;
     }
     mx_f64.reserve(per_f64 * kc_max);
+    mx_f32.reserve((size_t)kc_max * n);
+    float *z32 = mx_f32.p;
     // plane 0 of each operand; plane q lies q * plane elements further
     bf16 *VT = mx_bf16.p;
     bf16 *Hp = VT + (size_t)kc_max * ns * kr;
@@ -104,36 +126,48 @@ void Ctx::ao_contract_mixed(int k, int R, int S, const double *V, int P, int Q, 
             kc, ns, nr, Vc, ns, (long long)nr * ns, 1, VT, ps, kr, (long long)ns * kr);
         count_launch(stream, "split_planes");
         check_launch("split_planes");
-        // step 1: H = [C_R;SC_R] V
-        plane_gemm(*this, TINCR_KF_AO_TRANSFORM, 2 * n, ns, kr, PlaneOperand{cst[R].p, ps_r, kr, 0},
-                   PlaneOperand{VT, ps, kr, (long long)ns * kr}, kc,
-                   EpiPlaneH{H64, ns, 2LL * n * ns, Hp, ps, ks, 2LL * n * ks}, nr);
-        // Coulomb in FP64
-        if (ac != 0.0) {
-            dim3 g(ceil_div(2LL * n * 32, 256), kc);
-            diag_dots_kernel<<<g, 256, 0, stream>>>(n, ns, H64, stk(S), d3, d2);
-            count_launch(stream, "diag_dots");
-            check_launch("diag_dots");
-            coulomb_kernel<<<kc, 256, n_atoms * sizeof(double), stream>>>(n, n_atoms, d_ao_off.p, d_gamma.p, d3, d2, z,
-                                                                           nullptr, nullptr, ac);
-            count_launch(stream, "coulomb");
-            check_launch("coulomb");
-            dim3 g2(grid_of(2LL * n * nq, n_sm), kc);
-            scale_rows_kernel<<<g2, 256, 0, stream>>>(n, nq, z, stk(Q), Gc);
-            count_launch(stream, "scale_rows");
-            check_launch("scale_rows");
-        }
         if (exch) {
-            // step 2: F = ax gamma_lr o (H [C_S;SC_S]^T)
+            // step 1: H = [C_R;SC_R] V (planes only)
+            plane_gemm(*this, TINCR_KF_AO_TRANSFORM, 2 * n, ns, kr, PlaneOperand{cst[R].p, ps_r, kr, 0},
+                       PlaneOperand{VT, ps, kr, (long long)ns * kr}, kc,
+                       EpiPlaneH{nullptr, 0, 0, Hp, ps, ks, 2LL * n * ks}, nr);
+            // step 2: F = ax gamma_lr o (H [C_S;SC_S]^T), Coulomb diagonals of M captured
             plane_gemm(*this, TINCR_KF_AO_EXCHANGE, 2 * n, 2 * n, ks, PlaneOperand{Hp, ps, ks, 2LL * n * ks},
                        PlaneOperand{cst[S].p, ps_s, ks, 0}, kc,
-                       EpiPlaneF{d_glr_ao.p, n, (float)ax, Fp, ps, k2, 2LL * n * k2}, ns);
-            // step 4: G^T = (F [SC_Q;C_Q] + Gc)^T
+                       EpiPlaneF{glr32.p, n, (float)ax, Fp, ps, k2, 2LL * n * k2, ac != 0.0 ? d3 : nullptr, d2}, ns);
+            if (ac != 0.0) {
+                // z = ac gamma y (FP64), then an FP32 copy for the step-4 epilogue
+                coulomb_kernel<<<kc, 256, n_atoms * sizeof(double), stream>>>(n, n_atoms, d_ao_off.p, d_gamma.p, d3, d2,
+                                                                               z, nullptr, nullptr, ac);
+                count_launch(stream, "coulomb");
+                check_launch("coulomb");
+                to_float(*this, (long long)kc * n, z, z32);
+            }
+            // step 4: G^T = (F [SC_Q;C_Q] + diag(z, z) [C_Q;SC_Q])^T
             plane_gemm(*this, TINCR_KF_AO_EXCHANGE, 2 * n, nq, k2, PlaneOperand{Fp, ps, k2, 2LL * n * k2},
                        PlaneOperand{cswT[Q].p, ps_t, k2, 0}, kc,
-                       EpiPlaneGT{ac != 0.0 ? Gc : nullptr, nq, 2LL * n * nq, GTp, ps, k2, (long long)nq * k2}, 2 * n);
+                       EpiPlaneGT{ac != 0.0 ? z32 : nullptr, stk32[Q].p, n, nq, GTp, ps, k2, (long long)nq * k2}, 2 * n);
         } else {
-            if (ac == 0.0) TINCR_CUDA(cudaMemsetAsync(Gc, 0, (size_t)kc * 2 * n * nq * sizeof(double), stream));
+            // step 1 with an FP64 copy of H for the Coulomb diagonals
+            plane_gemm(*this, TINCR_KF_AO_TRANSFORM, 2 * n, ns, kr, PlaneOperand{cst[R].p, ps_r, kr, 0},
+                       PlaneOperand{VT, ps, kr, (long long)ns * kr}, kc,
+                       EpiPlaneH{H64, ns, 2LL * n * ns, Hp, ps, ks, 2LL * n * ks}, nr);
+            if (ac != 0.0) {
+                dim3 g(ceil_div(2LL * n * 32, 256), kc);
+                diag_dots_kernel<<<g, 256, 0, stream>>>(n, ns, H64, stk(S), d3, d2);
+                count_launch(stream, "diag_dots");
+                check_launch("diag_dots");
+                coulomb_kernel<<<kc, 256, n_atoms * sizeof(double), stream>>>(n, n_atoms, d_ao_off.p, d_gamma.p, d3, d2,
+                                                                               z, nullptr, nullptr, ac);
+                count_launch(stream, "coulomb");
+                check_launch("coulomb");
+                dim3 g2(grid_of(2LL * n * nq, n_sm), kc);
+                scale_rows_kernel<<<g2, 256, 0, stream>>>(n, nq, z, stk(Q), Gc);
+                count_launch(stream, "scale_rows");
+                check_launch("scale_rows");
+            } else {
+                TINCR_CUDA(cudaMemsetAsync(Gc, 0, (size_t)kc * 2 * n * nq * sizeof(double), stream));
+            }
             split_planes_kernel<<<grid_of((long long)kc * nq * k2, n_sm), 256, 0, stream>>>(
                 kc, nq, 2 * n, Gc, nq, 2LL * n * nq, 1, GTp, ps, k2, (long long)nq * k2);
             count_launch(stream, "split_planes");

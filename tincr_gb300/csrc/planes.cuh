@@ -81,21 +81,24 @@ __device__ __forceinline__ void store3_8(bf16 *p, long long ps, const float (&v)
     *reinterpret_cast<uint4 *>(p + 2 * ps) = *reinterpret_cast<const uint4 *>(l);
 }
 
-// H = acc: FP64 copy (for the Coulomb diagonals) and planes for the next GEMM
+// H = acc: planes for the next GEMM and, when H is set, an FP64 copy (Coulomb diagonals of the
+// products without exchange)
 struct EpiPlaneH {
-    double *H;           // [b][m][ldh]
+    double *H;           // [b][m][ldh] or null
     long long ldh, sbh;
     bf16 *p;             // planes [b][m][ldp], plane stride ps
     long long ps, ldp, sbp;
     __device__ __forceinline__ void operator()(int b, int m, int n, float acc) const {
-        H[b * sbh + (long long)m * ldh + n] = (double)acc;
+        if (H) H[b * sbh + (long long)m * ldh + n] = (double)acc;
         store3(p, ps, b * sbp + (long long)m * ldp + n, acc);
     }
     __device__ __forceinline__ void run8(int b, int m, int n, int N, const F8 &v) const {
         if (n + 8 <= N) {
-            double *h64 = H + b * sbh + (long long)m * ldh + n;
+            if (H) {
+                double *h64 = H + b * sbh + (long long)m * ldh + n;
 #pragma unroll
-            for (int j = 0; j < 8; ++j) h64[j] = (double)v.x[j];
+                for (int j = 0; j < 8; ++j) h64[j] = (double)v.x[j];
+            }
             store3_8(p + b * sbp + (long long)m * ldp + n, ps, v.x);
         } else {
 #pragma unroll
@@ -105,25 +108,40 @@ struct EpiPlaneH {
     }
 };
 
-// F = ax * gamma_lr o M  as planes (row m, column n of the 2n x 2n block matrix)
+// F = ax * gamma_lr o M  as planes (row m, column c of the 2n x 2n block matrix), FP32 throughout;
+// the Coulomb diagonals M[mu][n+mu] -> d3 and M[n+mu][mu] -> d2 are captured when d3 is set
 struct EpiPlaneF {
-    const double *G;     // n x n gamma_lr in the AO basis
+    const float *G;      // n x n gamma_lr in the AO basis (FP32 copy)
     int n;
     float ax;
     bf16 *p;
     long long ps, ldp, sbp;
+    double *d3, *d2;     // [b][n] or null
+    __device__ __forceinline__ void diag(int b, int m, int c, float acc) const {
+        if (d3) {
+            if (m < n && c == m + n) d3[(long long)b * n + m] = (double)acc;
+            if (m >= n && c == m - n) d2[(long long)b * n + c] = (double)acc;
+        }
+    }
     __device__ __forceinline__ void operator()(int b, int m, int c, float acc) const {
         int rr = m < n ? m : m - n, cc = c < n ? c : c - n;
-        store3(p, ps, b * sbp + (long long)m * ldp + c, ax * (float)G[(long long)rr * n + cc] * acc);
+        diag(b, m, c, acc);
+        store3(p, ps, b * sbp + (long long)m * ldp + c, ax * G[(long long)rr * n + cc] * acc);
     }
     __device__ __forceinline__ void run8(int b, int m, int c, int N, const F8 &v) const {
         if (c + 8 <= N) {
             const int rr = m < n ? m : m - n;
+            const int dc = m < n ? m + n : m - n;   // column of the captured diagonal element
+            if (d3 && dc >= c && dc < c + 8) {
+#pragma unroll
+                for (int j = 0; j < 8; ++j)
+                    if (c + j == dc) diag(b, m, c + j, v.x[j]);
+            }
             float w[8];
 #pragma unroll
             for (int j = 0; j < 8; ++j) {
                 const int cc = c + j < n ? c + j : c + j - n;
-                w[j] = ax * (float)G[(long long)rr * n + cc] * v.x[j];
+                w[j] = ax * G[(long long)rr * n + cc] * v.x[j];
             }
             store3_8(p + b * sbp + (long long)m * ldp + c, ps, w);
         } else {
@@ -134,15 +152,16 @@ struct EpiPlaneF {
     }
 };
 
-// G = acc (+ Gc, the FP64 Coulomb part) written transposed as planes: GT[b][n][m]
+// G = acc + diag(z, z) [C_Q;SC_Q] (the Coulomb part, FP32), written transposed as planes: GT[b][n][m]
 struct EpiPlaneGT {
-    const double *Gc;    // [b][m][ldg] or null
-    long long ldg, sbg;
+    const float *z;      // [b][n_ao] Coulomb potential per AO, or null
+    const float *rv;     // [C_Q;SC_Q], 2 n_ao x ldr (FP32 copy)
+    int n_ao, ldr;
     bf16 *p;
     long long ps, ldp, sbp;
     __device__ __forceinline__ void operator()(int b, int m, int n, float acc) const {
         float g = acc;
-        if (Gc) g += (float)Gc[b * sbg + (long long)m * ldg + n];
+        if (z) g += z[(long long)b * n_ao + (m < n_ao ? m : m - n_ao)] * rv[(long long)m * ldr + n];
         store3(p, ps, b * sbp + (long long)n * ldp + m, g);
     }
     __device__ __forceinline__ void run8(int b, int m, int n, int N, const F8 &v) const {

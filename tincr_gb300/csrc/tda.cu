@@ -568,6 +568,7 @@ void Ctx::set_states(int n_roots, const double *energies, const double *coeffici
     sync();
     h_energies.assign(energies, energies + n_roots);
     solved_roots = n_roots;
+    solve_prec = TINCR_PREC_FP64;
 }
 
 // ----------------------------------------------------------------------------------------------
@@ -789,6 +790,7 @@ int Ctx::solve(int n_roots, int max_iter, double tol, int precision, double *ene
     std::vector<double> u;
     int it_done = 0;
     prec = precision;
+    solve_prec = precision;
     // the mixed operator resolves residuals down to MIXED_TOL_FLOOR; below that the mixed phase
     // stops there and FP64 iterations take over
     const bool polish = precision == TINCR_PREC_BF16X3 && tol < MIXED_TOL_FLOOR;

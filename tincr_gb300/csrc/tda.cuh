@@ -87,11 +87,13 @@ struct Ctx {
     int last_cg_status = TINCR_OK;
 
     int prec = TINCR_PREC_FP64;           // arithmetic of the contractions in ao_contract
+    int solve_prec = TINCR_PREC_FP64;     // precision the current roots were solved with (gradient follows)
 
     // split-BF16 planes of the mixed-precision contraction (mixed.cu)
     bool planes_ready = false;
     bool use_tc = true;                   // tcgen05 plane GEMM; false: warp-MMA plane GEMM
     DevBuf<__nv_bfloat16> cst[2], cswT[2], mx_bf16;   // three planes each (planes.cuh)
+    DevBuf<float> glr32, stk32[2], mx_f32;             // FP32 copies for the plane epilogues
     DevBuf<double> mx_f64;
     long long mx_key = -1;
     DevBuf<int> d_tc_err;                 // error word of the tensor-core kernels' bounded waits
