@@ -296,9 +296,34 @@ def fmo_workload():
     return mons, pairs, inst, labels
 
 
-def fmo_cpu_sample(mons, inst, labels, n_le_sample=8, n_ct_sample=32):
+def oracle_le_gradient_seconds(m, state=0):
+    """tincr's LE excitation gradient of one monomer (oracle: dense derivative tensors, Z-vector,
+    f_v / f_lr contractions), timed."""
+    from oracle import gradients as OG
+    from oracle import tda as OT
+    from tincr_gb300 import groundstate as gs
+    sy, g = m.system, m.ground
+    t0 = time.perf_counter()
+    qov, qoo, qvv = OT.trans_charges(sy.ao_offset, g.orbs, g.s, sy.occ_indices, sy.virt_indices)
+    om = OT.orbe_differences(g.orbe[sy.occ_indices], g.orbe[sy.virt_indices])
+    eng = OT.TdaEngine(om, qov, g.gamma, qoo, qvv, g.gamma_lr, sy.n_occ, sy.n_virt)
+    r = OT.run_tda_engine(eng, sy.xyz, FMO_N_LE, FMO_MAX_ITER, FMO_TOL)
+    t_tda = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    der = OG.derivative_tensors(sy.numbers, sy.xyz, sy.ao_offset, sy.ao_atom, sy.hubbard, sy.r_lr, sy.params)
+    inp = dict(p=g.p, p0=g.p0, h_coul_x=g.h_coul_x, gamma=g.gamma, dq=g.dq, s=g.s, ao_atom=sy.ao_atom,
+               numbers=sy.numbers, xyz=sy.xyz, params=sy.params, gamma_lr_ao=gs.atom_to_ao(sy, g.gamma_lr),
+               orbe=g.orbe, occ=sy.occ_indices, virt=sy.virt_indices, ci_eigenvalues=r["energies"],
+               ci_coefficients=r["coefficients"], q_ov=qov, q_oo=qoo, q_vv=qvv, gamma_lr=g.gamma_lr,
+               orbs=g.orbs, gamma_ao=gs.atom_to_ao(sy, g.gamma))
+    _, flr = OG.ground_state_gradient(inp, der, True)
+    OG.tda_gradient(inp, der, state, True, flr_dmd0=flr)
+    return time.perf_counter() - t0
+
+
+def fmo_cpu_sample(mons, inst, labels, n_le_sample=8, n_ct_sample=32, s1_monomer=None):
     """tincr's per-instance TDA (oracle engines, numpy + host BLAS) on a few LE and CT instances,
-    scaled to the whole work list by instance kind."""
+    scaled to the whole work list by instance kind, plus the LE gradient of the S1 monomer."""
     from oracle import tda as OT
     t_le, t_ct = [], []
     le = [k for k, l in enumerate(labels) if l[0] == "LE"][:n_le_sample]
@@ -318,11 +343,20 @@ def fmo_cpu_sample(mons, inst, labels, n_le_sample=8, n_ct_sample=32):
     total = n_le * float(np.mean(t_le)) + n_ct * float(np.mean(t_ct))
     sample = ("oracle TDA of %d LE and %d CT instances (%.3f s / %.3f s each), scaled to %d LE + %d CT instances"
               % (len(t_le), len(t_ct), np.mean(t_le), np.mean(t_ct), n_le, n_ct))
+    if s1_monomer is not None:
+        t_g = oracle_le_gradient_seconds(mons[s1_monomer])
+        total += t_g
+        sample += "; oracle LE gradient of the S1 monomer (%.2f s)" % t_g
     return total, sample
 
 
+def ctx_device(ctx):
+    return int(os.environ.get("LOCAL_RANK", "0"))
+
+
 def run_fmo(args, ctx):
-    """Batched LE / CT TDA of the 64-acene aggregate, mixed and FP64 forms (monomers/s)."""
+    """Batched LE / CT TDA of the 64-acene aggregate plus the S1 gradient, mixed and FP64 forms
+    (monomers/s)."""
     from tincr_gb300 import _lib
     from tincr_gb300 import fmo
     t0 = time.perf_counter()
@@ -332,30 +366,53 @@ def run_fmo(args, ctx):
            "instances": len(inst), "tol": FMO_TOL, "max_iter": FMO_MAX_ITER,
            "host_setup_s": t_setup}
     res = {}
+    gctx = _lib.Context(ctx_device(ctx))
+    n_mon = len(mons)
+
+    def fmo_step(prec):
+        """Batched LE / CT TDA, then the gradient of S1, the lowest LE root of the aggregate
+        (its LE gradient, c = 1; the exciton couplings that would mix LE and CT states are not part
+        of this path)."""
+        rc, r = fmo.solve_batch(ctx, inst, FMO_MAX_ITER, FMO_TOL, prec)
+        t_batch = ctx.last_timing()[0] / 1e3
+        k1 = int(np.argmin([r[k]["energies"][0] for k in range(n_mon)]))
+        states = [None] * n_mon
+        states[k1] = 0
+        g = fmo.le_gradients(mons, r[:n_mon], states, contexts=[gctx], precision=prec)
+        t_grad = gctx.last_timing()[0] / 1e3
+        return rc, r, g[k1], k1, t_batch, t_grad
+
     for name, prec in (("bf16x3", _lib.PREC_BF16X3), ("fp64", _lib.PREC_FP64)):
         for _ in range(max(1, args.warmup)):
-            fmo.solve_batch(ctx, inst, FMO_MAX_ITER, FMO_TOL, prec)
-        dev, wall = [], []
+            fmo_step(prec)
+        dev, wall, tb, tg = [], [], [], []
         for _ in range(args.steps):
             t0 = time.perf_counter()
-            rc, r = fmo.solve_batch(ctx, inst, FMO_MAX_ITER, FMO_TOL, prec)
+            rc, r, g1, k1, t_batch, t_grad = fmo_step(prec)
             wall.append(time.perf_counter() - t0)
-            dev.append(ctx.last_timing()[0] / 1e3)
-        res[name] = (float(np.mean(dev)), float(np.mean(wall)), rc, r)
-    dm, wm, rcm, rm = res["bf16x3"]
-    d64, w64, rc64, r64 = res["fp64"]
+            dev.append(t_batch + t_grad)
+            tb.append(t_batch)
+            tg.append(t_grad)
+        res[name] = (float(np.mean(dev)), float(np.mean(wall)), rc, r, g1, k1, float(np.mean(tb)), float(np.mean(tg)))
+    gctx.close()
+    dm, wm, rcm, rm, gm, km, tbm, tgm = res["bf16x3"]
+    d64, w64, rc64, r64, g64, k64, tb64, tg64 = res["fp64"]
     out.update({
         "value_monomers_per_s": len(mons) / dm, "unit": "monomers/s",
-        "step_ms": dm * 1e3, "instances_per_s": len(inst) / dm,
+        "step_ms": dm * 1e3, "batch_tda_ms": tbm * 1e3, "s1_gradient_ms": tgm * 1e3,
+        "instances_per_s": len(inst) / tbm,
         "e2e": {"value": len(mons) / wm, "unit": "monomers/s", "wall_ms": wm * 1e3},
-        "fp64_gpu": {"value": len(mons) / d64, "step_ms": d64 * 1e3, "e2e_wall_ms": w64 * 1e3},
+        "fp64_gpu": {"value": len(mons) / d64, "step_ms": d64 * 1e3, "batch_tda_ms": tb64 * 1e3,
+                     "s1_gradient_ms": tg64 * 1e3, "e2e_wall_ms": w64 * 1e3},
         "speedup_mixed_vs_fp64": d64 / dm,
         "status_ok": bool(rcm == _lib.OK and rc64 == _lib.OK),
         "max_abs_energy_err_eh": float(max(np.abs(a["energies"] - b["energies"]).max() for a, b in zip(rm, r64))),
+        "s1_monomer": km,
+        "max_abs_s1_grad_err_eh_per_bohr": float(np.abs(gm - g64).max()) if km == k64 else None,
         "davidson_iterations_max": int(max(x["iterations"] for x in rm)),
     })
     if args.cpu_baseline:
-        total, sample = fmo_cpu_sample(mons, inst, labels)
+        total, sample = fmo_cpu_sample(mons, inst, labels, s1_monomer=km)
         out["cpu_baseline"] = {"value": len(mons) / total, "unit": "monomers/s", "step_s": total,
                                "cores": os.cpu_count(), "kind": "port", "sample": sample}
     return out
@@ -428,6 +485,16 @@ def cpu_baseline(sy, g, n_iters, n_products, cg_iters):
     return {"value": total, "unit": "s", "cores": threads, "kind": "port", "sample": sample}
 
 
+def OT_lowest(mons, k):
+    """Lowest LE root of monomer k from the oracle's Davidson (picks the S1 monomer on the CPU)."""
+    from oracle import tda as OT
+    sy, g = mons[k].system, mons[k].ground
+    qov, qoo, qvv = OT.trans_charges(sy.ao_offset, g.orbs, g.s, sy.occ_indices, sy.virt_indices)
+    om = OT.orbe_differences(g.orbe[sy.occ_indices], g.orbe[sy.virt_indices])
+    eng = OT.TdaEngine(om, qov, g.gamma, qoo, qvv, g.gamma_lr, sy.n_occ, sy.n_virt)
+    return float(OT.run_tda_engine(eng, sy.xyz, 1, FMO_MAX_ITER, FMO_TOL)["energies"][0])
+
+
 def run_reference(args):
     rank, world, local = dist_env()
     if rank != 0:
@@ -447,7 +514,8 @@ def run_reference(args):
     fmo_ref = None
     if args.fmo:
         mons, pairs, inst, labels = fmo_workload()
-        total, fsample = fmo_cpu_sample(mons, inst, labels)
+        k1 = int(np.argmin([OT_lowest(mons, k) for k in range(len(mons))]))
+        total, fsample = fmo_cpu_sample(mons, inst, labels, s1_monomer=k1)
         fmo_ref = {"workload": "acene64-fmo-le4-ct1", "value_monomers_per_s": len(mons) / total,
                    "unit": "monomers/s", "step_s": total, "cores": os.cpu_count(), "kind": "port",
                    "sample": fsample}

@@ -59,6 +59,12 @@ int tincr_last_timing(const tincr_ctx *ctx, double *ms, long long *kernel_launch
  * example by a caller's own solver) as the roots the gradient of this context works on. */
 int tincr_tda_set_states(tincr_ctx *ctx, int n_roots, const double *energies, const double *coefficients);
 
+/* No counterpart in tincr: declare the precision that the installed roots were solved with, which
+ * the gradient's contractions then use (tincr_tda_set_states resets it to TINCR_PREC_FP64; a
+ * mixed tincr_tda_solve sets TINCR_PREC_BF16X3).  For roots taken from a mixed
+ * tincr_tda_solve_batch. */
+int tincr_set_precision(tincr_ctx *ctx, int precision);
+
 /* Statistics of the last tincr_tda_solve: A.X products evaluated (tincr's compute_products
  * columns), subspace collapses and the final largest residual norm. */
 int tincr_last_solve_stats(const tincr_ctx *ctx, long long *n_products, int *n_collapses, double *max_residual);

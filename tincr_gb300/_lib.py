@@ -31,6 +31,7 @@ SIGNATURES = {
     "tincr_last_timing": (C.c_int, [C.c_void_p, _dp, C.POINTER(C.c_longlong)]),
     "tincr_tda_set_states": (C.c_int, [C.c_void_p, C.c_int, _dp, _dp]),
     "tincr_last_solve_stats": (C.c_int, [C.c_void_p, C.POINTER(C.c_longlong), _ip, _dp]),
+    "tincr_set_precision": (C.c_int, [C.c_void_p, C.c_int]),
     "tincr_tda_solve_batch": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_double, C.c_int, C.c_void_p]),
     "tincr_davidson_history": (C.c_int, [C.c_void_p, C.c_int, _ip, _ip, _ip, _dp, _ip, _ip]),
     "tincr_set_profiling": (C.c_int, [C.c_void_p, C.c_int]),

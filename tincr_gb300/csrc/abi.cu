@@ -78,6 +78,15 @@ int tincr_last_solve_stats(const tincr_ctx *ctx, long long *n_products, int *n_c
     return TINCR_OK;
 }
 
+int tincr_set_precision(tincr_ctx *ctx, int precision) {
+    return guarded(ctx, [&](tincr::Ctx &c) {
+        if (precision != TINCR_PREC_FP64 && precision != TINCR_PREC_BF16X3)
+            tincr::fail(TINCR_BAD_ARG, "set_precision: unknown precision");
+        c.solve_prec = precision;
+        return TINCR_OK;
+    });
+}
+
 int tincr_davidson_history(const tincr_ctx *ctx, int capacity, int *n_steps, int *iter, int *n_sub,
                            double *max_residual, int *roots_left, int *precision) {
     if (!ctx || !ctx->impl || capacity < 0) return TINCR_BAD_ARG;

@@ -25,11 +25,15 @@
 #include <numeric>
 #include <vector>
 
+#include <cooperative_groups.h>
+
 #include "common.cuh"
 #include "gemm_f64.cuh"
 #include "ops.cuh"
 #include "subspace.cuh"
 #include "tda.cuh"
+
+namespace cg = cooperative_groups;
 
 namespace tincr {
 
@@ -181,20 +185,6 @@ __global__ void transpose_kernel(int rows, int cols, const double *__restrict__ 
 }
 
 // row norms: out[r] = ||A[r]||_2 (one CTA per row)
-__global__ void row_norms_kernel(long long len, const double *__restrict__ A, double *out) {
-    __shared__ double red[32];
-    const double *a = A + (long long)blockIdx.x * len;
-    double s = 0.0;
-    for (long long x = threadIdx.x; x < len; x += blockDim.x) s += a[x] * a[x];
-    for (int off = 16; off; off >>= 1) s += __shfl_down_sync(0xffffffffu, s, off);
-    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
-    __syncthreads();
-    if (threadIdx.x < 32) {
-        s = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.0;
-        for (int off = 16; off; off >>= 1) s += __shfl_down_sync(0xffffffffu, s, off);
-        if (threadIdx.x == 0) out[blockIdx.x] = sqrt(s);
-    }
-}
 
 // T[j][x] = Rk[idx_j][x] / denom with denom = w_j - omega[x], |denom| < 1e-4 -> 1 (solvers/mod.rs:373-380)
 __global__ void precondition_kernel(long long ov, int k, const int *__restrict__ idx, const double *__restrict__ w,
@@ -207,6 +197,123 @@ __global__ void precondition_kernel(long long ov, int k, const int *__restrict__
         if (fabs(d) < 1.0e-4) d = 1.0;
         T[(long long)j * ov + x] = r[x] / d;
     }
+}
+
+// Deterministic multi-CTA row norms: partial[r][c] = sum of A[r][x]^2 over chunk c (pass 1),
+// out[r] = sqrt(sum_c partial[r][c]) in chunk order (pass 2).
+__global__ void row_sq_partial_kernel(long long len, int chunks, const double *__restrict__ A, long long lda,
+                                      double *partial) {
+    __shared__ double red[32];
+    const int r = blockIdx.y, c = blockIdx.x;
+    const long long per = (len + chunks - 1) / chunks;
+    const long long x0 = (long long)c * per, x1 = x0 + per < len ? x0 + per : len;
+    const double *a = A + (long long)r * lda;
+    double s = 0.0;
+    for (long long x = x0 + threadIdx.x; x < x1; x += blockDim.x) s += a[x] * a[x];
+    for (int off = 16; off; off >>= 1) s += __shfl_down_sync(0xffffffffu, s, off);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        s = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.0;
+        for (int off = 16; off; off >>= 1) s += __shfl_down_sync(0xffffffffu, s, off);
+        if (threadIdx.x == 0) partial[(long long)r * chunks + c] = s;
+    }
+}
+
+__global__ void row_sq_finish_kernel(int rows, int chunks, const double *__restrict__ partial, double *out) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= rows) return;
+    double s = 0.0;
+    for (int c = 0; c < chunks; ++c) s += partial[(long long)r * chunks + c];
+    out[r] = sqrt(s);
+}
+
+// Sequential classical Gram-Schmidt of kadd candidate vectors T (already orthogonal to the old
+// basis) against the vectors accepted in this step, V[m0 .. m), with tincr's 1e-8 drop rule
+// (davidson.rs:162-168); accepted vectors are normalised into V[m].  One cooperative launch: every
+// CTA takes the same accept / drop decisions from partial sums reduced in a fixed order (so the
+// result does not depend on timing).  state[0]: m out; state[1]: 1 if a norm was not finite.
+__global__ void __launch_bounds__(256) seq_gs_kernel(int kadd, long long ov, int m0, int mmax, double *V, double *T,
+                                                     double *part, int *state) {
+    cg::grid_group grid = cg::this_grid();
+    __shared__ double c[32];
+    __shared__ double red[8][9];
+    __shared__ double s_nrm;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    const long long x0 = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    int m = m0;
+    for (int j = 0; j < kadd; ++j) {
+        double *t = T + (long long)j * ov;
+        const int acc = m - m0;
+        // 1. partial dots c_i = V[m0 + i] . t, eight at a time
+        for (int i0 = 0; i0 < acc; i0 += 8) {
+            double s[8];
+#pragma unroll
+            for (int q = 0; q < 8; ++q) s[q] = 0.0;
+            for (long long x = x0; x < ov; x += stride) {
+                const double tx = t[x];
+#pragma unroll
+                for (int q = 0; q < 8; ++q)
+                    if (i0 + q < acc) s[q] += V[(long long)(m0 + i0 + q) * ov + x] * tx;
+            }
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+                for (int off = 16; off; off >>= 1) s[q] += __shfl_down_sync(0xffffffffu, s[q], off);
+                if (lane == 0) red[warp][q] = s[q];
+            }
+            __syncthreads();
+            if (threadIdx.x < 8) {
+                double v = 0.0;
+                for (int w = 0; w < 8; ++w) v += red[w][threadIdx.x];
+                part[(long long)blockIdx.x * 33 + i0 + threadIdx.x] = v;
+            }
+            __syncthreads();
+        }
+        grid.sync();
+        // 2. c_i in a fixed order, t -= sum_i c_i V[m0 + i], partial |t|^2
+        if (threadIdx.x < acc) {
+            double v = 0.0;
+            for (int b = 0; b < (int)gridDim.x; ++b) v += part[(long long)b * 33 + threadIdx.x];
+            c[threadIdx.x] = v;
+        }
+        __syncthreads();
+        double sq = 0.0;
+        for (long long x = x0; x < ov; x += stride) {
+            double v = t[x];
+            for (int i = 0; i < acc; ++i) v -= c[i] * V[(long long)(m0 + i) * ov + x];
+            t[x] = v;
+            sq += v * v;
+        }
+        for (int off = 16; off; off >>= 1) sq += __shfl_down_sync(0xffffffffu, sq, off);
+        if (lane == 0) red[warp][8] = sq;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double v = 0.0;
+            for (int w = 0; w < 8; ++w) v += red[w][8];
+            part[(long long)blockIdx.x * 33 + 32] = v;
+        }
+        grid.sync();
+        // 3. the norm (fixed order), accept or drop
+        if (threadIdx.x == 0) {
+            double v = 0.0;
+            for (int b = 0; b < (int)gridDim.x; ++b) v += part[(long long)b * 33 + 32];
+            s_nrm = sqrt(v);
+        }
+        __syncthreads();
+        const double nrm = s_nrm;
+        if (!isfinite(nrm)) {
+            if (blockIdx.x == 0 && threadIdx.x == 0) state[1] = 1;
+            break;   // every CTA sees the same norm
+        }
+        if (nrm > 1.0e-8 && m < mmax) {
+            const double inv = 1.0 / nrm;
+            for (long long x = x0; x < ov; x += stride) V[(long long)m * ov + x] = t[x] * inv;
+            ++m;
+        }
+        grid.sync();
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) state[0] = m;
 }
 
 // dst = src * s  (vector scaled copy)
@@ -296,6 +403,11 @@ Ctx::Ctx(int dev) : device(dev) {
     TINCR_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
     TINCR_CUDA(cudaEventCreate(&ev0));
     TINCR_CUDA(cudaEventCreate(&ev1));
+    // co-resident grid of the cooperative Gram-Schmidt kernel (0: cooperative launch unavailable)
+    int coop = 0, per_sm = 0;
+    TINCR_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
+    TINCR_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, seq_gs_kernel, 256, 0));
+    coop_grid = coop ? std::min(4, per_sm) * n_sm : 0;
     // plane GEMM of the mixed-precision contraction: tcgen05 (default) or warp MMA
     const char *pg = std::getenv("TINCR_GB300_PLANE_GEMM");
     if (pg && std::string(pg) == "mma") use_tc = false;
@@ -312,6 +424,18 @@ Ctx::~Ctx() {
 }
 
 void Ctx::sync() { TINCR_CUDA(cudaStreamSynchronize(stream)); }
+
+// norms of `rows` vectors of length len (stride lda) into out[rows], spread over the whole GPU
+void Ctx::row_norms(int rows, long long len, const double *A, long long lda, double *out) {
+    const int chunks = (int)std::max<long long>(1, std::min<long long>((4LL * n_sm + rows - 1) / rows, (len + 2047) / 2048));
+    norm_partial.reserve((size_t)rows * chunks);
+    row_sq_partial_kernel<<<dim3(chunks, rows), 256, 0, stream>>>(len, chunks, A, lda, norm_partial.p);
+    count_launch(stream, "row_sq_partial");
+    check_launch("row_sq_partial");
+    row_sq_finish_kernel<<<ceil_div(rows, 128), 128, 0, stream>>>(rows, chunks, norm_partial.p, out);
+    count_launch(stream, "row_sq_finish");
+    check_launch("row_sq_finish");
+}
 
 template <class T>
 static void upload(cudaStream_t st, DevBuf<T> &d, const T *h, size_t n) {
@@ -593,9 +717,7 @@ int Ctx::davidson(int n_roots, int max_iter, double tol, bool from_ritz, std::ve
     if (from_ritz) {
         TINCR_CUDA(cudaMemcpyAsync(dV.p, dR.p, (size_t)n_roots * ov * sizeof(double), cudaMemcpyDeviceToDevice, stream));
         // the Ritz vectors of an orthonormal basis are unit vectors; anything else is a broken run
-        row_norms_kernel<<<n_roots, 256, 0, stream>>>(ov, dV.p, dnorm.p);
-        count_launch(stream, "row_norms");
-        check_launch("row_norms");
+        row_norms(n_roots, ov, dV.p, ov, dnorm.p);
         std::vector<double> nr(n_roots);
         TINCR_CUDA(cudaMemcpyAsync(nr.data(), dnorm.p, n_roots * sizeof(double), cudaMemcpyDeviceToHost, stream));
         sync();
@@ -686,9 +808,7 @@ int Ctx::davidson(int n_roots, int max_iter, double tol, bool from_ritz, std::ve
             pgemm<false, false>(*this, TINCR_KF_SUBSPACE, n_roots, (int)ov, m, dYt.p, m, 0, dAV.p, (int)ov, 0, 1,
                                 EpiResidual{dRk.p, dR.p, du.p, ov});
         }
-        row_norms_kernel<<<n_roots, 256, 0, stream>>>(ov, dRk.p, dnorm.p);
-        count_launch(stream, "row_norms");
-        check_launch("row_norms");
+        row_norms(n_roots, ov, dRk.p, ov, dnorm.p);
         TINCR_CUDA(cudaMemcpyAsync(errs.data(), dnorm.p, n_roots * sizeof(double), cudaMemcpyDeviceToHost, stream));
         sync();
         int roots_cvd = 0;
@@ -734,32 +854,51 @@ int Ctx::davidson(int n_roots, int max_iter, double tol, bool from_ritz, std::ve
                                         EpiStore{dT.p, 0, (int)ov, -1.0, 1.0});
                 }
                 // then sequentially against the vectors accepted in this step (davidson.rs:162-168)
-                int m0 = m;
-                for (int j = 0; j < kadd; ++j) {
-                    double *t = dT.p + (long long)j * ov;
-                    int acc = m - m0;
-                    if (acc > 0) {
-                        TINCR_CUDA(cudaMemsetAsync(dc.p, 0, acc * sizeof(double), stream));
-                        // c = Q t  [acc x 1] over the vectors accepted in this step;  t -= c^T Q
-                        int slot = prof_begin(TINCR_KF_SUBSPACE);
-                        skinny_dots(stream, n_sm, acc, 1, ov, dV.p + (long long)m0 * ov, ov, t, ov, dc.p, 1);
-                        skinny_comb(stream, 1, acc, ov, dc.p, acc, 1, dV.p + (long long)m0 * ov, ov,
-                                    CombStore{t, ov, -1.0, 1.0});
-                        prof_end(slot, 4.0 * acc * (double)ov, 8.0 * (acc + 2.0) * ov);
-                    }
-                    row_norms_kernel<<<1, 256, 0, stream>>>(ov, t, dnorm.p);
-                    count_launch(stream, "row_norms");
-                    check_launch("row_norms");
-                    double nrm = 0.0;
-                    TINCR_CUDA(cudaMemcpyAsync(&nrm, dnorm.p, sizeof(double), cudaMemcpyDeviceToHost, stream));
+                if (kadd <= 32 && coop_grid > 0) {
+                    int slot = prof_begin(TINCR_KF_SUBSPACE);
+                    gs_part.reserve((size_t)coop_grid * 33);
+                    gs_state.reserve(2);
+                    int hstate[2] = {m, 0};
+                    TINCR_CUDA(cudaMemcpyAsync(gs_state.p, hstate, 2 * sizeof(int), cudaMemcpyHostToDevice, stream));
+                    int a_kadd = kadd, a_m0 = m, a_mmax = mmax;
+                    long long a_ov = ov;
+                    double *a_V = dV.p, *a_T = dT.p, *a_part = gs_part.p;
+                    int *a_state = gs_state.p;
+                    void *args[] = {&a_kadd, &a_ov, &a_m0, &a_mmax, &a_V, &a_T, &a_part, &a_state};
+                    TINCR_CUDA(cudaLaunchCooperativeKernel((const void *)seq_gs_kernel, dim3(coop_grid), dim3(256), args,
+                                                           0, stream));
+                    count_launch(stream, "seq_gs");
+                    prof_end(slot, 4.0 * kadd * (double)kadd * ov / 2.0, 8.0 * (kadd * (kadd + 3.0) / 2.0) * ov);
+                    TINCR_CUDA(cudaMemcpyAsync(hstate, gs_state.p, 2 * sizeof(int), cudaMemcpyDeviceToHost, stream));
                     sync();
-                    if (!std::isfinite(nrm)) fail(TINCR_NONFINITE, "non-finite correction vector");
-                    if (nrm > 1.0e-8 && m < mmax) {
-                        scale_copy_kernel<<<grid_for(ov, 256, n_sm), 256, 0, stream>>>(ov, t, 1.0 / nrm,
-                                                                                       dV.p + (long long)m * ov);
-                        count_launch(stream, "scale_copy");
-                        check_launch("scale_copy");
-                        ++m;
+                    if (hstate[1]) fail(TINCR_NONFINITE, "non-finite correction vector");
+                    m = hstate[0];
+                } else {
+                    int m0 = m;
+                    for (int j = 0; j < kadd; ++j) {
+                        double *t = dT.p + (long long)j * ov;
+                        int acc = m - m0;
+                        if (acc > 0) {
+                            TINCR_CUDA(cudaMemsetAsync(dc.p, 0, acc * sizeof(double), stream));
+                            // c = Q t  [acc x 1] over the vectors accepted in this step;  t -= c^T Q
+                            int slot = prof_begin(TINCR_KF_SUBSPACE);
+                            skinny_dots(stream, n_sm, acc, 1, ov, dV.p + (long long)m0 * ov, ov, t, ov, dc.p, 1);
+                            skinny_comb(stream, 1, acc, ov, dc.p, acc, 1, dV.p + (long long)m0 * ov, ov,
+                                        CombStore{t, ov, -1.0, 1.0});
+                            prof_end(slot, 4.0 * acc * (double)ov, 8.0 * (acc + 2.0) * ov);
+                        }
+                        row_norms(1, ov, t, ov, dnorm.p);
+                        double nrm = 0.0;
+                        TINCR_CUDA(cudaMemcpyAsync(&nrm, dnorm.p, sizeof(double), cudaMemcpyDeviceToHost, stream));
+                        sync();
+                        if (!std::isfinite(nrm)) fail(TINCR_NONFINITE, "non-finite correction vector");
+                        if (nrm > 1.0e-8 && m < mmax) {
+                            scale_copy_kernel<<<grid_for(ov, 256, n_sm), 256, 0, stream>>>(ov, t, 1.0 / nrm,
+                                                                                           dV.p + (long long)m * ov);
+                            count_launch(stream, "scale_copy");
+                            check_launch("scale_copy");
+                            ++m;
+                        }
                     }
                 }
             }

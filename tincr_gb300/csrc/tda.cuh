@@ -107,6 +107,10 @@ struct Ctx {
     explicit Ctx(int dev);
     ~Ctx();
     void sync();
+    DevBuf<double> norm_partial, gs_part;
+    DevBuf<int> gs_state;
+    int coop_grid = 0;                    // CTAs of the cooperative Gram-Schmidt launch
+    void row_norms(int rows, long long len, const double *A, long long lda, double *out);
     void launch_transpose(int rows, int cols, const double *in, double *out);
     void set_atoms(int n_atoms, const int *orbs_per_atom, int n_orb);
     void upload_mo(int n, const double *C, const double *S);

@@ -152,7 +152,8 @@ def solve_batch(ctx, instances, max_iter=50, tol=1e-4, precision=_lib.PREC_FP64)
     return rc, outs
 
 
-def le_gradients(monomers, results, states, n_streams=8, variant="reference", contexts=None):
+def le_gradients(monomers, results, states, n_streams=8, variant="reference", contexts=None,
+                 precision=_lib.PREC_FP64):
     """Excitation-energy gradients of locally excited states, the LE terms of tincr's FMO exciton
     gradient (`SuperSystem::fmo_cis_gradient`, src/fmo/lcmo/cis_gradient.rs:118-126, which adds
     c^2 * `Monomer::tda_gradient_lc(n)` per contributing LE state; src/fmo/gradients/excited_state.rs:
@@ -160,22 +161,27 @@ def le_gradients(monomers, results, states, n_streams=8, variant="reference", co
     computed on the GPU; the monomers are spread over `n_streams` contexts, each driven by its own
     host thread (tincr runs the monomers on rayon threads), so their kernels overlap on the device.
 
-    Returns a list of [3 N_k] arrays (Hartree/bohr, atom order of the monomer)."""
+    `precision` is the precision the results were solved with; the gradients' contractions follow it.
+    Entries of `states` that are None are skipped.  Returns a list of [3 N_k] arrays (Hartree/bohr,
+    atom order of the monomer) or None."""
     from concurrent.futures import ThreadPoolExecutor
     from . import gradients as GR
     from . import tda as T
     own = contexts is None
     ctxs = contexts if contexts is not None else [_lib.Context(0) for _ in range(n_streams)]
-    n_streams = len(ctxs)
+    n_streams = min(len(ctxs), max(1, sum(1 for x in states if x is not None)))
     out = [None] * len(monomers)
 
     def work(lane):
         ctx = ctxs[lane]
         for k in range(lane, len(monomers), n_streams):
+            if states[k] is None:
+                continue
             m = monomers[k]
             es = T.ExcitedStateSystem.from_ground_state(ctx, m.system, m.ground)
             es.prepare_tda()
             es.set_states(results[k]["energies"], results[k]["coefficients"])
+            es.set_precision(precision)
             out[k] = GR.GradientSystem(es, m.system, m.ground).tda_gradient(int(states[k]), variant)
 
     try:

@@ -91,6 +91,10 @@ class ExcitedStateSystem:
         self.ctx.check(self.ctx.lib.tincr_tda_set_states(self.ctx.h, len(e), dptr(e), dptr(x)))
         self.properties.update(ci_eigenvalues=e, ci_coefficients=x)
 
+    def set_precision(self, precision):
+        """Precision the installed roots were solved with; the gradient's contractions follow it."""
+        self.ctx.check(self.ctx.lib.tincr_set_precision(self.ctx.h, int(precision)))
+
     def run_tda(self, n_roots, max_iter, tolerance, precision=_lib.PREC_FP64, raise_on_failure=True):
         """`System::run_tda(n_roots, max_iter, tolerance)`; results are stored in `properties`
         (ci_eigenvalues, ci_coefficients, q_trans, tr_dipoles, oscillator_strengths) and returned."""
