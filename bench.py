@@ -528,6 +528,24 @@ def run_reference(args):
             "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
+def run_fmo_once(args):
+    """Profiling helper: the 64-acene FMO work list solved once by the batched TDA (`--steps`
+    repetitions after one warm-up), without kernel timing (so the CUDA-graph iteration runs)."""
+    from tincr_gb300 import _lib, build
+    from tincr_gb300 import fmo
+    build.build()
+    mons, pairs, inst, labels = fmo_workload()
+    ctx = _lib.Context(0)
+    prec = PRECISIONS[args.precision]
+    fmo.solve_batch(ctx, inst, FMO_MAX_ITER, FMO_TOL, prec)
+    for _ in range(max(1, args.steps)):
+        rc, r = fmo.solve_batch(ctx, inst, FMO_MAX_ITER, FMO_TOL, prec)
+    ms, nl = ctx.last_timing()
+    print(json.dumps({"mode": "fmo", "precision": args.precision, "instances": len(inst), "status": rc, "ms": ms,
+                      "launches": nl}))
+    ctx.close()
+
+
 def run_products(args):
     """Profiling helper: set up the workload and evaluate A.X for `--k` random trial vectors once
     (used for ncu captures of the product kernels on the full-size system)."""
@@ -560,11 +578,14 @@ def main():
     ap.add_argument("--ref-products", type=int, default=369)
     ap.add_argument("--ref-iters", type=int, default=40)
     ap.add_argument("--ref-cg", type=int, default=14)
-    ap.add_argument("--mode", default="solve", choices=["solve", "products"])
+    ap.add_argument("--mode", default="solve", choices=["solve", "products", "fmo"])
     ap.add_argument("--k", type=int, default=4)
     args = ap.parse_args()
     if args.mode == "products":
         run_products(args)
+        return
+    if args.mode == "fmo":
+        run_fmo_once(args)
         return
     out = run_reference(args) if args.impl == "reference" else run_gpu(args)
     if out is not None:

@@ -423,6 +423,10 @@ void Ctx::plr_adjoint(const double *v, const double *Y, double scale_p, double s
            *sYts = sYt + nn, *h1 = sYts + nn, *h2 = h1 + nn, *Q = h2 + nn;
     const double *s = dS_.p, *g = d_glr_ao.p;
     auto mm = [&](bool ta, bool tb, const double *A, const double *B, double *C, double alpha, double beta) {
+        if (prec == TINCR_PREC_BF16X3) {   // mixed form: the dense adjoint contractions on the tensor cores
+            gemm_mixed(ta, tb, n, n, n, A, n, B, n, C, n, alpha, beta);
+            return;
+        }
         int slot = prof_begin(TINCR_KF_GRADIENT);
         EpiStore e{C, 0, n, alpha, beta};
         if (!ta && !tb) gemm_f64<false, false>(stream, n, n, n, A, n, 0, B, n, 0, 1, e);
@@ -607,6 +611,10 @@ int Ctx::gradient(const int *atom_kind, double r_lr_, const double *P, const dou
     };
     auto mm = [&](bool ta, bool tb, int M, int Nn, int K, const double *A, int lda, const double *B, int ldb, double *C,
                   int ldc, double alpha, double beta) {
+        if (prec == TINCR_PREC_BF16X3) {
+            gemm_mixed(ta, tb, M, Nn, K, A, lda, B, ldb, C, ldc, alpha, beta);
+            return;
+        }
         EpiStore e{C, 0, ldc, alpha, beta};
         int slot = prof_begin(TINCR_KF_GRADIENT);
         if (!ta && !tb) gemm_f64<false, false>(stream, M, Nn, K, A, lda, 0, B, ldb, 0, 1, e);

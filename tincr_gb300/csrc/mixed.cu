@@ -191,4 +191,41 @@ void Ctx::ao_contract_mixed(int k, int R, int S, const double *V, int P, int Q, 
     }
 }
 
+// C = alpha op(A) op(B) + beta C (row-major FP64 in and out) on the three-plane tensor-core GEMM:
+// op(A) is M x K (A[m*lda + k], or A[k*lda + m] when ta), op(B) is K x N (B[k*ldb + n], or
+// B[n*ldb + k] when tb).  The operands are split into planes per call (K padded to 64).
+void Ctx::gemm_mixed(bool ta, bool tb, int M, int N, int K, const double *A, int lda, const double *B, int ldb,
+                     double *C, int ldc, double alpha, double beta) {
+    if (M <= 0 || N <= 0 || K <= 0) return;
+    if (use_tc && !d_tc_err.p) {
+        d_tc_err.alloc(1);
+        TINCR_CUDA(cudaMemsetAsync(d_tc_err.p, 0, sizeof(int), stream));
+    }
+    const long long kp = pad64(K);
+    const long long pa = (long long)M * kp, pb = (long long)N * kp;
+    if (mg_bf16.n < (size_t)N_PLANES * (pa + pb) || mg_key != kp) {
+        mg_bf16.reserve((size_t)N_PLANES * (pa + pb));
+        mg_key = kp;
+    }
+    bf16 *Ap = mg_bf16.p, *Bp = Ap + N_PLANES * pa;
+    // planes are written for every K column (padding included), so no memset is needed
+    split_planes_kernel<<<grid_of(pa, n_sm), 256, 0, stream>>>(1, M, K, A, lda, 0, ta ? 1 : 0, Ap, pa, kp, 0);
+    count_launch(stream, "split_planes");
+    check_launch("split_planes");
+    split_planes_kernel<<<grid_of(pb, n_sm), 256, 0, stream>>>(1, N, K, B, ldb, 0, tb ? 0 : 1, Bp, pb, kp, 0);
+    count_launch(stream, "split_planes");
+    check_launch("split_planes");
+    plane_gemm(*this, TINCR_KF_GRADIENT, M, N, kp, PlaneOperand{Ap, pa, kp, 0}, PlaneOperand{Bp, pb, kp, 0}, 1,
+               EpiPlaneOut{C, ldc, 0, nullptr, nullptr, alpha, beta}, K);
+    if (use_tc) {
+        int e = 0;
+        TINCR_CUDA(cudaMemcpyAsync(&e, d_tc_err.p, sizeof(int), cudaMemcpyDeviceToHost, stream));
+        sync();
+        if (e) {
+            TINCR_CUDA(cudaMemsetAsync(d_tc_err.p, 0, sizeof(int), stream));
+            fail(TINCR_CUDA_ERR, "tensor-core GEMM: a pipeline wait timed out (code " + std::to_string(e) + ")");
+        }
+    }
+}
+
 }  // namespace tincr

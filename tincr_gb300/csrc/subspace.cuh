@@ -127,8 +127,10 @@ inline void skinny_dots(cudaStream_t st, int n_sm, int M, int nb, long long L, c
     int l_chunk = (int)(((L + chunks - 1) / chunks + SK_COLS - 1) / SK_COLS * SK_COLS);
     int gx = (int)((L + l_chunk - 1) / l_chunk);
     dim3 grid(gx, my);
+    // the FP64 pipe is the bound: the instantiation closest above nb wastes the fewest FMAs
     if (nb <= 8) skinny_dots_guard_kernel<8><<<grid, SK_T, 0, st>>>(M, nb, (int)L, l_chunk, A, lda, B, ldb, C, ldc);
     else if (nb <= 16) skinny_dots_guard_kernel<16><<<grid, SK_T, 0, st>>>(M, nb, (int)L, l_chunk, A, lda, B, ldb, C, ldc);
+    else if (nb <= 24) skinny_dots_guard_kernel<24><<<grid, SK_T, 0, st>>>(M, nb, (int)L, l_chunk, A, lda, B, ldb, C, ldc);
     else if (nb <= 32) skinny_dots_guard_kernel<32><<<grid, SK_T, 0, st>>>(M, nb, (int)L, l_chunk, A, lda, B, ldb, C, ldc);
     else fail(TINCR_BAD_ARG, "skinny_dots: more than 32 short rows");
     count_launch(st, "skinny_dots");
@@ -140,10 +142,18 @@ inline void skinny_comb(cudaStream_t st, int rows, int m, long long L, const dou
                         const double *V, long long ldv, Epi epi) {
     if (rows <= 0 || L <= 0) return;
     dim3 grid((unsigned)((L + SK_T - 1) / SK_T));
-    if (rows <= 8) skinny_comb_kernel<8, Epi><<<grid, SK_T, 0, st>>>(m, L, Y, ysr, ysi, V, ldv, rows, epi);
-    else if (rows <= 16) skinny_comb_kernel<16, Epi><<<grid, SK_T, 0, st>>>(m, L, Y, ysr, ysi, V, ldv, rows, epi);
-    else if (rows <= 32) skinny_comb_kernel<32, Epi><<<grid, SK_T, 0, st>>>(m, L, Y, ysr, ysi, V, ldv, rows, epi);
+    // the FP64 pipe is the bound: rows are padded to the next multiple of 4 only
+#define TINCR_SKINNY_COMB(R) skinny_comb_kernel<R, Epi><<<grid, SK_T, 0, st>>>(m, L, Y, ysr, ysi, V, ldv, rows, epi)
+    if (rows <= 4) TINCR_SKINNY_COMB(4);
+    else if (rows <= 8) TINCR_SKINNY_COMB(8);
+    else if (rows <= 12) TINCR_SKINNY_COMB(12);
+    else if (rows <= 16) TINCR_SKINNY_COMB(16);
+    else if (rows <= 20) TINCR_SKINNY_COMB(20);
+    else if (rows <= 24) TINCR_SKINNY_COMB(24);
+    else if (rows <= 28) TINCR_SKINNY_COMB(28);
+    else if (rows <= 32) TINCR_SKINNY_COMB(32);
     else fail(TINCR_BAD_ARG, "skinny_comb: more than 32 output rows");
+#undef TINCR_SKINNY_COMB
     count_launch(st, "skinny_comb");
     check_launch("skinny_comb");
 }

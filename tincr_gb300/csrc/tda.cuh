@@ -94,6 +94,8 @@ struct Ctx {
     bool use_tc = true;                   // tcgen05 plane GEMM; false: warp-MMA plane GEMM
     DevBuf<__nv_bfloat16> cst[2], cswT[2], mx_bf16;   // three planes each (planes.cuh)
     DevBuf<float> glr32, stk32[2], mx_f32;             // FP32 copies for the plane epilogues
+    DevBuf<__nv_bfloat16> mg_bf16;                     // planes of gemm_mixed
+    long long mg_key = -1;
     DevBuf<double> mx_f64;
     long long mx_key = -1;
     DevBuf<int> d_tc_err;                 // error word of the tensor-core kernels' bounded waits
@@ -126,6 +128,8 @@ struct Ctx {
     void ao_contract(int k, int R, int S, const double *V, int P, int Q, double ax, double ac, double *out,
                      double alpha, double beta, const double *Xomega);
     void prepare_planes();
+    void gemm_mixed(bool ta, bool tb, int M, int N, int K, const double *A, int lda, const double *B, int ldb,
+                    double *C, int ldc, double alpha, double beta);
     void ao_contract_mixed(int k, int R, int S, const double *V, int P, int Q, double ax, double ac, double *out,
                            double alpha, double beta, const double *Xomega);
     void products_dev(int k, const double *X, double *AX, double *y_out);
