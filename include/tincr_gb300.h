@@ -77,6 +77,16 @@ int tincr_last_solve_stats(const tincr_ctx *ctx, long long *n_products, int *n_c
 int tincr_davidson_history(const tincr_ctx *ctx, int capacity, int *n_steps, int *iter, int *n_sub,
                            double *max_residual, int *roots_left, int *precision);
 
+/* The k lowest eigenpairs of a symmetric m x m matrix, as the Davidson loop computes them every iteration
+ * (the Rayleigh-Ritz step, `eigh(UPLO::Upper)` in src/excited_states/solvers/davidson.rs:93).  Only the
+ * upper triangle of `a` (row-major, host memory) is read.  The solver is the context's: the host
+ * (default; OpenMP threads) or, when the environment variable TINCR_GB300_SUBSPACE_EIG=cluster was set
+ * at context creation, one thread-block cluster of the device if the matrix fits its shared memory
+ * (m up to about 600 with 16 CTAs).  w [k] ascending; y [k*m], y[r*m + i] = component i of
+ * eigenvector r (unit length); *on_device (may be NULL) receives 1 when the cluster kernel ran.
+ * Non-finite input: TINCR_NONFINITE. */
+int tincr_subspace_eigh(tincr_ctx *ctx, int m, int k, const double *a, double *w, double *y, int *on_device);
+
 /* Kernel families timed with CUDA events when profiling is on. */
 typedef enum {
     TINCR_KF_AO_EXCHANGE = 0,  /* the two n^2 v contractions of the LC exchange (A.X steps 2 and 4) */
@@ -85,7 +95,8 @@ typedef enum {
     TINCR_KF_GRADIENT = 3,     /* gradient: pairwise-atom derivative kernel and adjoint GEMMs        */
     TINCR_KF_OTHER = 4,        /* Coulomb, packing, transition charges, small kernels              */
     TINCR_KF_HOST = 5,         /* host time of the Davidson subspace eigensolver (not a kernel)      */
-    TINCR_KF_COUNT = 6
+    TINCR_KF_EIGEN = 6,        /* the subspace eigensolver on one thread-block cluster               */
+    TINCR_KF_COUNT = 7
 } tincr_kernel_family;
 
 /* Turn per-family kernel timing on (1) or off (0); turning it on clears the statistics. */

@@ -16,8 +16,8 @@ OK, NOT_CONVERGED, NONFINITE, BAD_ARG, CUDA_ERR, NO_DEVICE, CG_MAXITER = range(7
 STATUS_NAMES = {0: "OK", 1: "NOT_CONVERGED", 2: "NONFINITE", 3: "BAD_ARG", 4: "CUDA_ERR", 5: "NO_DEVICE",
                 6: "CG_MAXITER"}
 PREC_FP64, PREC_BF16X3 = 0, 1
-KF_AO_EXCHANGE, KF_AO_TRANSFORM, KF_SUBSPACE, KF_GRADIENT, KF_OTHER, KF_HOST = range(6)
-KF_COUNT = 6
+KF_AO_EXCHANGE, KF_AO_TRANSFORM, KF_SUBSPACE, KF_GRADIENT, KF_OTHER, KF_HOST, KF_EIGEN = range(7)
+KF_COUNT = 7
 GRAD_REFERENCE, GRAD_EXACT = 0, 1
 
 _dp = C.POINTER(C.c_double)
@@ -34,6 +34,7 @@ SIGNATURES = {
     "tincr_set_precision": (C.c_int, [C.c_void_p, C.c_int]),
     "tincr_tda_solve_batch": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_double, C.c_int, C.c_void_p]),
     "tincr_davidson_history": (C.c_int, [C.c_void_p, C.c_int, _ip, _ip, _ip, _dp, _ip, _ip]),
+    "tincr_subspace_eigh": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _dp, _dp, _dp, _ip]),
     "tincr_set_profiling": (C.c_int, [C.c_void_p, C.c_int]),
     "tincr_kernel_stats": (C.c_int, [C.c_void_p, C.c_int, _dp, C.POINTER(C.c_longlong), _dp, _dp]),
     "tincr_trans_charges": (C.c_int, [C.c_void_p, C.c_int, _ip, C.c_int, _dp, _dp, C.c_int, C.c_int, C.c_int,
@@ -147,6 +148,16 @@ class Context:
                                                    iptr(pr)))
         return [dict(iter=int(it[i]), n_sub=int(ns[i]), max_residual=float(mr[i]), roots_left=int(rl[i]),
                      precision=int(pr[i])) for i in range(k)]
+
+    def subspace_eigh(self, a, k):
+        """k lowest eigenpairs of the symmetric matrix a (upper triangle read): (w [k], y [k, m], on_device)."""
+        a = f64(a)
+        m = a.shape[0]
+        w = np.zeros(k)
+        y = np.zeros((k, m))
+        dev = C.c_int()
+        self.check(self.lib.tincr_subspace_eigh(self.h, m, int(k), dptr(a), dptr(w), dptr(y), C.byref(dev)))
+        return w, y, bool(dev.value)
 
     def last_timing(self):
         ms = C.c_double()

@@ -16,7 +16,7 @@ SRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "lib")
 LIB = os.path.join(OUT, "libtincr_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["abi.cu", "tda.cu", "gradient.cu", "noalloc.cu", "mixed.cu", "batch.cu", "eigen_host.cpp"]
+SOURCES = ["abi.cu", "tda.cu", "gradient.cu", "noalloc.cu", "mixed.cu", "batch.cu", "eig_cluster.cu", "eigen_host.cpp"]
 
 
 def _nvcc():
@@ -60,7 +60,12 @@ def build(force=False, verbose_ptxas=False, jobs=None):
             if verbose_ptxas and log:
                 sys.stderr.write(log)
     tmp = LIB + ".tmp"
-    cmd = [nvcc, "-shared", "-o", tmp] + objs + ARCH + ["-lcudart", "-Xcompiler", "-fopenmp"]
+    # export the extern "C" entry points only
+    vscript = os.path.join(OUT, "exports.map")
+    with open(vscript, "w") as f:
+        f.write("{ global: tincr_*; local: *; };\n")
+    cmd = [nvcc, "-shared", "-o", tmp] + objs + ARCH + ["-lcudart", "-Xcompiler", "-fopenmp",
+                                                        "-Xlinker", "--version-script=" + vscript]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("link failed:\n%s\n%s" % (r.stdout, r.stderr))

@@ -87,6 +87,16 @@ int tincr_set_precision(tincr_ctx *ctx, int precision) {
     });
 }
 
+int tincr_subspace_eigh(tincr_ctx *ctx, int m, int k, const double *a, double *w, double *y, int *on_device) {
+    return guarded(ctx, [&](tincr::Ctx &c) {
+        if (m < 1 || k < 1 || k > m || !a || !w || !y) tincr::fail(TINCR_BAD_ARG, "subspace_eigh: bad arguments");
+        int used = 0;
+        if (!tincr::subspace_eigh(c, m, k, a, w, y, &used)) tincr::fail(TINCR_NONFINITE, "subspace_eigh: non-finite data");
+        if (on_device) *on_device = used;
+        return TINCR_OK;
+    });
+}
+
 int tincr_davidson_history(const tincr_ctx *ctx, int capacity, int *n_steps, int *iter, int *n_sub,
                            double *max_residual, int *roots_left, int *precision) {
     if (!ctx || !ctx->impl || capacity < 0) return TINCR_BAD_ARG;

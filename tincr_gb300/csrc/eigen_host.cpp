@@ -10,6 +10,10 @@
 #include <numeric>
 #include <vector>
 
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
 namespace tincr {
 
 // a: n x n row-major (upper triangle read); w: eigenvalues ascending; z: n x n row-major with the
@@ -163,92 +167,147 @@ bool eigh_upper(int n, const double *a, double *w, double *z) {
 // ----------------------------------------------------------------------------------------------
 // The k lowest eigenpairs only: Householder tridiagonalisation without accumulating Q (the
 // reflection vectors are kept), bisection on Sturm counts for the k smallest eigenvalues, inverse
-// iteration with partial-pivoting LU of T - w I for their eigenvectors, Gram-Schmidt among them
-// (separates (near-)degenerate roots) and back-transformation through the k vectors.  About
-// (4/3) n^3 flops against the full decomposition's ~9 n^3; Davidson needs n_roots << n pairs.
+// iteration with partial-pivoting LU of T - w I for their eigenvectors, Gram-Schmidt within clusters
+// of close roots and back-transformation through the k vectors.  About (4/3) n^3 flops against the
+// full decomposition's ~9 n^3; Davidson needs n_roots << n pairs.
 // a: n x n row-major (upper triangle read); w: k eigenvalues ascending; y: y[r * n + i] = component
 // i of eigenvector r.  Returns false on non-finite input.
+//
+// Threads: the tridiagonalisation splits rows cyclically over the team with two barriers per
+// reflection; bisection, inverse iteration and back-transformation run one root per task.  Every
+// value is computed by one thread in a fixed order, so results do not depend on the thread count.
 // ----------------------------------------------------------------------------------------------
 
 namespace {
 
-int sturm_count(const std::vector<double> &d, const std::vector<double> &e, int n, double x, double pivmin) {
-    int c = 0;
-    double q = d[0] - x;
-    if (std::fabs(q) < pivmin) q = -pivmin;
-    if (q < 0.0) ++c;
+// Number of eigenvalues of T (diagonal d, squared off-diagonal bsq) below x: the sign changes of the
+// leading principal minors N_i = (d_i - x) N_{i-1} - e_{i-1}^2 N_{i-2} (a division-free recurrence,
+// backward stable like the pivot form: each step's rounding is a relative perturbation of d_i - x
+// and of e_{i-1}^2).  An exact zero becomes a tiny value of the opposite sign; both terms are
+// rescaled by a power of two when the newest leaves [2^-400, 2^400].
+int sturm_count(const double *d, const double *bsq, int n, double x) {
+    double n0 = 1.0, n1 = d[0] - x;
+    if (n1 == 0.0) n1 = -0x1p-100;
+    int c = std::signbit(n1) ? 1 : 0;
     for (int i = 1; i < n; ++i) {
-        q = d[i] - x - e[i - 1] * e[i - 1] / q;
-        if (std::fabs(q) < pivmin) q = -pivmin;
-        if (q < 0.0) ++c;
+        double n2 = (d[i] - x) * n1 - bsq[i - 1] * n0;
+        if (n2 == 0.0) {
+            n2 = -0x1p-100 * n1;
+        } else {
+            const int ex = std::ilogb(n2);
+            if (ex > 400 || ex < -400) {
+                const double sc = std::ldexp(1.0, -ex);
+                n1 *= sc;
+                n2 *= sc;
+            }
+        }
+        c += std::signbit(n1) != std::signbit(n2) ? 1 : 0;
+        n0 = n1;
+        n1 = n2;
     }
     return c;
+}
+
+// threads for the tridiagonalisation: two barriers per reflection pay off from n ~ 128 (on a
+// 16-core Grace host: n = 300 in 1.9 ms with 16 threads, 5.7 ms with one)
+int tridiag_threads(int n) {
+#ifdef _OPENMP
+    return n >= 128 ? std::min(16, omp_get_max_threads()) : 1;
+#else
+    (void)n;
+    return 1;
+#endif
 }
 
 }  // namespace
 
 bool eigh_lowest_upper(int n, const double *a, int k, double *w, double *y) {
     if (n <= 0 || k <= 0 || k > n) return false;
-    std::vector<double> A((size_t)n * n), d(n), e(n, 0.0), beta(n, 0.0), p(n);
+    std::vector<double> A((size_t)n * n), d(n), e(n, 0.0), beta(n, 0.0), p(n), uv(2 * (size_t)n), bsq(n);
     for (int i = 0; i < n; ++i)
         for (int j = 0; j < n; ++j) {
             const double x = (i <= j) ? a[(size_t)i * n + j] : a[(size_t)j * n + i];
             if (!std::isfinite(x)) return false;
             A[(size_t)i * n + j] = x;
         }
-    // 1. T = Q^T A Q; reflection k acts on rows/columns k+1..n-1, its vector u kept in column k
-    //    below the diagonal (stored transposed in row k to the right of the diagonal for contiguous
-    //    access)
-    // rows of the matrix-vector product and of the rank-2 update are spread over host threads for
-    // large subspaces; every row is computed by one thread in a fixed order (deterministic)
-    const bool par = n >= 256;
-    double bet_s = 0.0;
-    bool skip = false;
-#pragma omp parallel num_threads(8) if (par)
-    for (int c = 0; c + 2 < n; ++c) {
+    // 1. T = Q^T A Q.  Reflection c acts on rows/columns c+1..n-1; its vector u (with u_0 = x0 - alpha)
+    //    replaces row c to the right of the diagonal (= column c below it), where the back-
+    //    transformation reads it.  The full symmetric trailing block is kept up to date.
+    //    Step c: (i) the owner of row c forms the reflection from row c (already updated) into uv (two
+    //    buffers by step parity);
+    //    barrier; (ii) p = beta A' u on the owned rows and partial u.p; barrier; (iii) K = beta u.p / 2,
+    //    q = p - K u, rows -= u q^T + q u^T; the owner of row c+1 updates that row first and forms the
+    //    next reflection before the barrier that closes the step.
+    const int T = tridiag_threads(n);
+    std::vector<double> part(64, 0.0);
+    std::vector<char> skip(n, 0);
+    auto reflect = [&](int c) {   // from row c, columns c+1..n-1
+        double *u = &A[(size_t)c * n + c + 1];
         const int n1 = n - c - 1;
-        double *u = &A[(size_t)c * n + c + 1];            // row c, columns c+1.. (= column c by symmetry)
-#pragma omp single
-        {
-            const double x0 = u[0];
-            double s2 = 0.0;
-            for (int i = 1; i < n1; ++i) s2 += u[i] * u[i];
-            d[c] = A[(size_t)c * n + c];
-            skip = s2 == 0.0;
-            if (skip) {
-                beta[c] = 0.0;
-                e[c] = x0;
-            } else {
-                const double nx = std::sqrt(x0 * x0 + s2);
-                const double alpha = x0 > 0.0 ? -nx : nx;
-                bet_s = 1.0 / (alpha * (alpha - x0));
-                u[0] = x0 - alpha;
-                beta[c] = bet_s;
-                e[c] = alpha;
+        const double x0 = u[0];
+        double s2 = 0.0;
+        for (int i = 1; i < n1; ++i) s2 += u[i] * u[i];
+        d[c] = A[(size_t)c * n + c];
+        if (s2 == 0.0) {
+            beta[c] = 0.0;
+            e[c] = x0;
+            skip[c] = 1;
+            return;
+        }
+        const double nx = std::sqrt(x0 * x0 + s2);
+        const double alpha = x0 > 0.0 ? -nx : nx;
+        beta[c] = 1.0 / (alpha * (alpha - x0));
+        e[c] = alpha;
+        u[0] = x0 - alpha;
+        double *ub = uv.data() + (size_t)(c & 1) * n;   // alternates: step c - 1 may still read the other
+        for (int i = 0; i < n1; ++i) ub[c + 1 + i] = u[i];
+    };
+    if (n >= 3) reflect(0);
+#pragma omp parallel num_threads(T) if (T > 1)
+    {
+#ifdef _OPENMP
+        const int nt = omp_get_num_threads(), me = omp_get_thread_num();
+#else
+        const int nt = 1, me = 0;
+#endif
+        std::vector<double> q(n);
+        for (int c = 0; c + 2 < n; ++c) {
+            if (skip[c]) {   // identical on every thread: written before the previous barrier
+                if ((c + 1) % nt == me && c + 3 < n) reflect(c + 1);
+#pragma omp barrier
+                continue;
             }
-        }
-        if (skip) continue;   // every thread sees the same flag after the single's barrier
-        const double bet = bet_s;
-        // p = bet A' u over the trailing block (symmetric, full storage kept up to date)
-#pragma omp for schedule(static)
-        for (int i = 0; i < n1; ++i) {
-            const double *row = &A[(size_t)(c + 1 + i) * n + c + 1];
-            double acc = 0.0;
-            for (int j = 0; j < n1; ++j) acc += row[j] * u[j];
-            p[i] = bet * acc;
-        }
-#pragma omp single
-        {
+            const double bet = beta[c];
+            const double *u = uv.data() + (size_t)(c & 1) * n;
             double up = 0.0;
-            for (int i = 0; i < n1; ++i) up += u[i] * p[i];
-            const double K = 0.5 * bet * up;
-            for (int i = 0; i < n1; ++i) p[i] -= K * u[i];
-        }
-#pragma omp for schedule(static)
-        for (int i = 0; i < n1; ++i) {
-            double *row = &A[(size_t)(c + 1 + i) * n + c + 1];
-            const double ui = u[i], pi = p[i];
-            for (int j = 0; j < n1; ++j) row[j] -= ui * p[j] + pi * u[j];
+            for (int i = c + 1; i < n; ++i) {
+                if (i % nt != me) continue;
+                const double *row = &A[(size_t)i * n];
+                double acc = 0.0;
+#pragma omp simd reduction(+ : acc)
+                for (int j = c + 1; j < n; ++j) acc += row[j] * u[j];
+                p[i] = bet * acc;
+                up += u[i] * p[i];
+            }
+            part[me] = up;
+#pragma omp barrier
+            double ut = 0.0;
+            for (int t = 0; t < nt; ++t) ut += part[t];
+            const double K = 0.5 * bet * ut;
+            for (int j = c + 1; j < n; ++j) q[j] = p[j] - K * u[j];
+            auto update = [&](int i) {
+                double *row = &A[(size_t)i * n];
+                const double ui = u[i], qi = q[i];
+#pragma omp simd
+                for (int j = c + 1; j < n; ++j) row[j] -= ui * q[j] + qi * u[j];
+            };
+            if ((c + 1) % nt == me) {
+                update(c + 1);
+                if (c + 3 < n) reflect(c + 1);
+            }
+            for (int i = c + 2; i < n; ++i)
+                if (i % nt == me) update(i);
+#pragma omp barrier
         }
     }
     if (n >= 2) {
@@ -257,36 +316,40 @@ bool eigh_lowest_upper(int n, const double *a, int k, double *w, double *y) {
     }
     d[n - 1] = A[(size_t)(n - 1) * n + n - 1];
     e[n - 1] = 0.0;
-    // 2. eigenvalues by bisection
+    // 2. eigenvalues by bisection, one root per task
     double lo = 1e300, hi = -1e300, emax2 = 0.0;
     for (int i = 0; i < n; ++i) {
         const double r = std::fabs(e[i]) + (i > 0 ? std::fabs(e[i - 1]) : 0.0);
         lo = std::min(lo, d[i] - r);
         hi = std::max(hi, d[i] + r);
         emax2 = std::max(emax2, e[i] * e[i]);
+        bsq[i] = e[i] * e[i];
     }
     const double eps = 2.220446049250313e-16;
     const double tnorm = std::max(std::fabs(lo), std::fabs(hi));
     const double pivmin = 2.2250738585072014e-308 * std::max(1.0, emax2);
     lo -= 2.0 * eps * tnorm + 2.0 * pivmin;
     hi += 2.0 * eps * tnorm + 2.0 * pivmin;
-    double left = lo;   // eigenvalue r lies above the previous one
+    const bool par_roots = k >= 4 && n >= 48;
+#pragma omp parallel for schedule(dynamic, 1) if (par_roots)
     for (int r = 0; r < k; ++r) {
-        double x_lo = left, x_hi = hi;
+        double x_lo = lo, x_hi = hi;
         for (int it = 0; it < 200; ++it) {
             if (x_hi - x_lo <= 2.0 * eps * std::max(std::fabs(x_lo), std::fabs(x_hi)) + 4.0 * pivmin) break;
             const double mid = 0.5 * (x_lo + x_hi);
-            if (sturm_count(d, e, n, mid, pivmin) > r) x_hi = mid;
+            if (sturm_count(d.data(), bsq.data(), n, mid) > r) x_hi = mid;
             else x_lo = mid;
         }
         w[r] = 0.5 * (x_lo + x_hi);
-        left = x_lo;
     }
-    // 3. inverse iteration on T - w I (LU with partial pivoting)
-    std::vector<double> dl(n), dd(n), du(n), du2(n), z(n);
-    std::vector<char> swp(n);
+    // 3. inverse iteration on T - w I (LU with partial pivoting), one root per task; y holds the
+    //    eigenvectors of T until the back-transformation
     const double tiny = eps * std::max(tnorm, 1e-300);
+#pragma omp parallel for schedule(dynamic, 1) if (par_roots)
     for (int r = 0; r < k; ++r) {
+        std::vector<double> dl(n), dd(n), du(n), du2(n);
+        std::vector<char> swp(n);
+        double *z = y + (size_t)r * n;
         for (int i = 0; i < n; ++i) {
             dd[i] = d[i] - w[r];
             dl[i] = e[i];
@@ -332,10 +395,19 @@ bool eigh_lowest_upper(int n, const double *a, int k, double *w, double *y) {
             nrm = 1.0 / std::sqrt(nrm);
             for (int i = 0; i < n; ++i) z[i] *= nrm;
         }
-        // Gram-Schmidt against the lower roots (twice)
+    }
+    // Gram-Schmidt (twice) against the lower roots of the same cluster: roots closer than 1e-3 |T|
+    // (the criterion of LAPACK's dstein); separated roots are orthogonal to rounding already
+    const double ortol = 1e-3 * tnorm;
+    for (int r = 1, r0 = 0; r < k; ++r) {
+        if (w[r] - w[r - 1] > ortol) {
+            r0 = r;
+            continue;
+        }
+        double *z = y + (size_t)r * n;
         for (int pass = 0; pass < 2; ++pass)
-            for (int q = 0; q < r; ++q) {
-                const double *yq = y + (size_t)q * n;   // still in the tridiagonal basis
+            for (int q = r0; q < r; ++q) {
+                const double *yq = y + (size_t)q * n;
                 double s = 0.0;
                 for (int i = 0; i < n; ++i) s += yq[i] * z[i];
                 for (int i = 0; i < n; ++i) z[i] -= s * yq[i];
@@ -343,9 +415,10 @@ bool eigh_lowest_upper(int n, const double *a, int k, double *w, double *y) {
         double nrm = 0.0;
         for (int i = 0; i < n; ++i) nrm += z[i] * z[i];
         nrm = 1.0 / std::sqrt(nrm);
-        for (int i = 0; i < n; ++i) y[(size_t)r * n + i] = z[i] * nrm;
+        for (int i = 0; i < n; ++i) z[i] *= nrm;
     }
-    // 4. back-transformation y = H_0 ... H_{n-3} z
+    // 4. back-transformation y = H_0 ... H_{n-3} z, one root per task
+#pragma omp parallel for schedule(dynamic, 1) if (par_roots)
     for (int r = 0; r < k; ++r) {
         double *yr = y + (size_t)r * n;
         for (int c = n - 3; c >= 0; --c) {
@@ -353,8 +426,10 @@ bool eigh_lowest_upper(int n, const double *a, int k, double *w, double *y) {
             const int n1 = n - c - 1;
             const double *u = &A[(size_t)c * n + c + 1];
             double s = 0.0;
+#pragma omp simd reduction(+ : s)
             for (int i = 0; i < n1; ++i) s += u[i] * yr[c + 1 + i];
             s *= beta[c];
+#pragma omp simd
             for (int i = 0; i < n1; ++i) yr[c + 1 + i] -= s * u[i];
         }
     }

@@ -51,7 +51,6 @@ void check_launch(const char *name) {
 }
 
 bool eigh_upper(int n, const double *a, double *w, double *z);
-bool eigh_lowest_upper(int n, const double *a, int k, double *w, double *y);
 
 // ----------------------------------------------------------------------------------------------
 // small kernels
@@ -411,6 +410,9 @@ Ctx::Ctx(int dev) : device(dev) {
     // plane GEMM of the mixed-precision contraction: tcgen05 (default) or warp MMA
     const char *pg = std::getenv("TINCR_GB300_PLANE_GEMM");
     if (pg && std::string(pg) == "mma") use_tc = false;
+    // Davidson subspace eigensolver: host (default) or the thread-block cluster kernel
+    const char *se = std::getenv("TINCR_GB300_SUBSPACE_EIG");
+    if (se && std::string(se) == "cluster") eig_cluster_on = true;
 }
 
 Ctx::~Ctx() {
@@ -710,9 +712,12 @@ int Ctx::davidson(int n_roots, int max_iter, double tol, bool from_ritz, std::ve
     dR.reserve((size_t)n_roots * ov);
     dRk.reserve((size_t)n_roots * ov);
     dT.reserve((size_t)n_roots * ov);
-    DevBuf<double> dP((size_t)mmax * n_roots + 64), dYt((size_t)n_roots * mmax), du(n_roots), dnorm(n_roots),
-        dw(n_roots), dc((size_t)mmax * n_roots + 64);
+    DevBuf<double> dYt((size_t)n_roots * mmax), du(n_roots), dnorm(n_roots), dw(n_roots),
+        dc((size_t)mmax * n_roots + 64);
     DevBuf<int> didx(n_roots);
+    dAp.reserve((size_t)mmax * mmax);
+    eig_err.reserve(1);
+    TINCR_CUDA(cudaMemsetAsync(eig_err.p, 0, sizeof(int), stream));
     u.assign(n_roots, 0.0);
     if (from_ritz) {
         TINCR_CUDA(cudaMemcpyAsync(dV.p, dR.p, (size_t)n_roots * ov * sizeof(double), cudaMemcpyDeviceToDevice, stream));
@@ -742,8 +747,8 @@ int Ctx::davidson(int n_roots, int max_iter, double tol, bool from_ritz, std::ve
     int m_done = 0;             // columns with products (product cache)
     int dim_sub = n_roots;      // tincr's dim_sub bookkeeping
     const int dim_sub_origin = n_roots;
-    std::vector<double> aproj;  // m x m upper triangle used
-    std::vector<double> hP, w(mmax);
+    std::vector<double> aproj;  // host copy of the projected matrix (host eigensolver only)
+    std::vector<double> w(mmax);
     std::vector<double> errs(n_roots);
     int status = TINCR_NOT_CONVERGED;
     int it_done = 0;
@@ -754,48 +759,48 @@ int Ctx::davidson(int n_roots, int max_iter, double tol, bool from_ritz, std::ve
             products_dev(m - m_done, dV.p + (long long)m_done * ov, dAV.p + (long long)m_done * ov, nullptr);
             last_products += m - m_done;
         }
-        // 1.1 projected matrix, new columns only: P = V[0:m] AV[m_done:m]^T  (m x knew)
+        // 1.1 projected matrix, new columns only: P[:, mold:m] = V[0:m] AV[mold:m]^T, kept on the device
+        //     (leading dimension mmax; the old columns stay valid until a collapse)
         int knew = m - m_done;
-        std::vector<double> old = aproj;
-        int mold = m_done;
-        aproj.assign((size_t)m * m, 0.0);
-        for (int i = 0; i < mold; ++i)
-            for (int j = 0; j < mold; ++j) aproj[(size_t)i * m + j] = old[(size_t)i * mold + j];
+        const int mold = m_done;
         if (knew > 0) {
-            TINCR_CUDA(cudaMemsetAsync(dP.p, 0, (size_t)m * knew * sizeof(double), stream));
+            TINCR_CUDA(cudaMemset2DAsync(dAp.p + mold, (size_t)mmax * sizeof(double), 0, (size_t)knew * sizeof(double),
+                                         m, stream));
             if (knew <= 32) {
                 int slot = prof_begin(TINCR_KF_SUBSPACE);
-                skinny_dots(stream, n_sm, m, knew, ov, dV.p, ov, dAV.p + (long long)mold * ov, ov, dP.p, knew);
+                skinny_dots(stream, n_sm, m, knew, ov, dV.p, ov, dAV.p + (long long)mold * ov, ov, dAp.p + mold, mmax);
                 prof_end(slot, 2.0 * m * (double)knew * ov, 8.0 * (double)(m + knew) * ov);
             } else {
                 int sk = pick_splitk(m, knew, (int)ov, 1, n_sm);
                 pgemm<false, true>(*this, TINCR_KF_SUBSPACE, m, knew, (int)ov, dV.p, (int)ov, 0,
-                                   dAV.p + (long long)mold * ov, (int)ov, 0, 1, EpiAtomicAdd{dP.p, 0, knew, 1.0}, sk);
+                                   dAV.p + (long long)mold * ov, (int)ov, 0, 1, EpiAtomicAdd{dAp.p + mold, 0, mmax, 1.0}, sk);
             }
-            hP.resize((size_t)m * knew);
-            TINCR_CUDA(cudaMemcpyAsync(hP.data(), dP.p, hP.size() * sizeof(double), cudaMemcpyDeviceToHost, stream));
-            sync();
-            for (int i = 0; i < m; ++i)
-                for (int j = 0; j < knew; ++j) aproj[(size_t)i * m + mold + j] = hP[(size_t)i * knew + j];
         }
         m_done = m;
-        // 2. eigenproblem of the subspace matrix (upper triangle)
-        //    (the n_roots lowest pairs only: eigh_lowest_upper, eigen_host.cpp)
-        const auto th0 = std::chrono::steady_clock::now();
-        std::vector<double> yt((size_t)n_roots * m);
-        if (!eigh_lowest_upper(m, aproj.data(), n_roots, w.data(), yt.data()))
-            fail(TINCR_NONFINITE, "subspace eigensolver failed");
-        if (profiling) {
-            KernelStats &hs = stats[TINCR_KF_HOST];
-            hs.ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - th0).count();
-            hs.launches += 1;
-            hs.flops += 4.0 / 3.0 * (double)m * m * m;
+        // 2. the n_roots lowest eigenpairs of the subspace matrix (upper triangle): on the host
+        //    (eigen_host.cpp), or on one thread-block cluster (eig_cluster.cu) when selected and it fits
+        bool on_device = eig_cluster_on && eig_cluster(*this, m, n_roots, dAp.p, mmax, du.p, dYt.p, eig_err.p);
+        if (!on_device) {
+            aproj.resize((size_t)m * m);
+            TINCR_CUDA(cudaMemcpy2DAsync(aproj.data(), (size_t)m * sizeof(double), dAp.p, (size_t)mmax * sizeof(double),
+                                         (size_t)m * sizeof(double), m, cudaMemcpyDeviceToHost, stream));
+            sync();
+            const auto th0 = std::chrono::steady_clock::now();
+            std::vector<double> yt((size_t)n_roots * m);
+            if (!eigh_lowest_upper(m, aproj.data(), n_roots, w.data(), yt.data()))
+                fail(TINCR_NONFINITE, "subspace eigensolver failed");
+            if (profiling) {
+                KernelStats &hs = stats[TINCR_KF_HOST];
+                hs.ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - th0).count();
+                hs.launches += 1;
+                hs.flops += 4.0 / 3.0 * (double)m * m * m;
+            }
+            for (int r = 0; r < n_roots; ++r) u[r] = w[r];
+            for (int r = 0; r < n_roots; ++r)
+                if (!std::isfinite(u[r])) fail(TINCR_NONFINITE, "non-finite Ritz value");
+            TINCR_CUDA(cudaMemcpyAsync(dYt.p, yt.data(), yt.size() * sizeof(double), cudaMemcpyHostToDevice, stream));
+            TINCR_CUDA(cudaMemcpyAsync(du.p, u.data(), n_roots * sizeof(double), cudaMemcpyHostToDevice, stream));
         }
-        for (int r = 0; r < n_roots; ++r) u[r] = w[r];
-        for (int r = 0; r < n_roots; ++r)
-            if (!std::isfinite(u[r])) fail(TINCR_NONFINITE, "non-finite Ritz value");
-        TINCR_CUDA(cudaMemcpyAsync(dYt.p, yt.data(), yt.size() * sizeof(double), cudaMemcpyHostToDevice, stream));
-        TINCR_CUDA(cudaMemcpyAsync(du.p, u.data(), n_roots * sizeof(double), cudaMemcpyHostToDevice, stream));
         // 3.1 Ritz vectors R = Y^T V ; 3.2 residuals Rk = Y^T AV - u o R
         if (n_roots <= 32) {
             int slot = prof_begin(TINCR_KF_SUBSPACE);
@@ -810,7 +815,13 @@ int Ctx::davidson(int n_roots, int max_iter, double tol, bool from_ritz, std::ve
         }
         row_norms(n_roots, ov, dRk.p, ov, dnorm.p);
         TINCR_CUDA(cudaMemcpyAsync(errs.data(), dnorm.p, n_roots * sizeof(double), cudaMemcpyDeviceToHost, stream));
+        int eig_bad = 0;
+        if (on_device) {
+            TINCR_CUDA(cudaMemcpyAsync(u.data(), du.p, n_roots * sizeof(double), cudaMemcpyDeviceToHost, stream));
+            TINCR_CUDA(cudaMemcpyAsync(&eig_bad, eig_err.p, sizeof(int), cudaMemcpyDeviceToHost, stream));
+        }
         sync();
+        if (eig_bad) fail(TINCR_NONFINITE, "subspace eigensolver: non-finite projected matrix or Ritz pairs");
         int roots_cvd = 0;
         for (int r = 0; r < n_roots; ++r) {
             if (!std::isfinite(errs[r])) fail(TINCR_NONFINITE, "non-finite residual");

@@ -104,6 +104,10 @@ struct Ctx {
     DevBuf<double> wsH, wsF, wsG, wsd3, wsd2, wsz;
     // Davidson state
     DevBuf<double> dV, dAV, dR, dRk, dT;
+    DevBuf<double> dAp;                   // projected matrix V AV^T (upper triangle, leading dimension = capacity)
+    DevBuf<double> eig_U, eig_Z;          // reflection vectors and tridiagonal eigenvectors (eig_cluster.cu)
+    DevBuf<int> eig_err;
+    bool eig_cluster_on = false;          // subspace eigensolver on a thread-block cluster instead of the host
     BatchWork *batch = nullptr;
 
     explicit Ctx(int dev);
@@ -151,6 +155,16 @@ struct Ctx {
     int solve_batch(int n_inst, const tincr_tda_instance *inst, int max_iter, double tol, int precision,
                     tincr_tda_result *res);
 };
+
+// Lowest k eigenpairs of the m x m matrix P (upper triangle, leading dimension ldp) on one thread-block
+// cluster (eig_cluster.cu): w[k] ascending, Y[r * m + i]; *err set on non-finite data.  Returns false
+// without launching when the subspace does not fit the cluster's shared memory.
+bool eig_cluster(Ctx &c, int m, int k, const double *P, int ldp, double *w, double *Y, int *err);
+// host solver (eigen_host.cpp)
+bool eigh_lowest_upper(int n, const double *a, int k, double *w, double *y);
+// subspace eigenpairs with the context's solver: the host (default) or the cluster kernel when it
+// is selected and the matrix fits (tincr_subspace_eigh)
+bool subspace_eigh(Ctx &c, int m, int k, const double *a_host, double *w, double *y, int *used_device);
 
 // A.X product with caller-owned device buffers and fixed device scratch (noalloc.cu)
 void products_noalloc(Ctx &c, int k, const double *X, double *AX);
