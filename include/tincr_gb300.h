@@ -87,6 +87,13 @@ int tincr_davidson_history(const tincr_ctx *ctx, int capacity, int *n_steps, int
  * Non-finite input: TINCR_NONFINITE. */
 int tincr_subspace_eigh(tincr_ctx *ctx, int m, int k, const double *a, double *w, double *y, int *on_device);
 
+/* C = A B^T (A [M*K], B [N*K], C [M*N], row-major host arrays, 1 <= N <= 32) on the tensor cores with
+ * FP64-class accuracy: every row is cut into eight exact 7-bit digits under its own power-of-two bound,
+ * the digit products run as bf16 MMAs with exact FP32 sums over 128-element chunks and exact int64
+ * sums beyond (the same GEMM as the subspace products of the mixed Davidson).  Non-finite input:
+ * TINCR_NONFINITE. */
+int tincr_gemm_fp64_tensor(tincr_ctx *ctx, int M, int N, int K, const double *A, const double *B, double *C);
+
 /* Kernel families timed with CUDA events when profiling is on. */
 typedef enum {
     TINCR_KF_AO_EXCHANGE = 0,  /* the two n^2 v contractions of the LC exchange (A.X steps 2 and 4) */

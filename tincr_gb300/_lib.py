@@ -35,6 +35,7 @@ SIGNATURES = {
     "tincr_tda_solve_batch": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_double, C.c_int, C.c_void_p]),
     "tincr_davidson_history": (C.c_int, [C.c_void_p, C.c_int, _ip, _ip, _ip, _dp, _ip, _ip]),
     "tincr_subspace_eigh": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _dp, _dp, _dp, _ip]),
+    "tincr_gemm_fp64_tensor": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, _dp, _dp, _dp]),
     "tincr_set_profiling": (C.c_int, [C.c_void_p, C.c_int]),
     "tincr_kernel_stats": (C.c_int, [C.c_void_p, C.c_int, _dp, C.POINTER(C.c_longlong), _dp, _dp]),
     "tincr_trans_charges": (C.c_int, [C.c_void_p, C.c_int, _ip, C.c_int, _dp, _dp, C.c_int, C.c_int, C.c_int,
@@ -158,6 +159,14 @@ class Context:
         dev = C.c_int()
         self.check(self.lib.tincr_subspace_eigh(self.h, m, int(k), dptr(a), dptr(w), dptr(y), C.byref(dev)))
         return w, y, bool(dev.value)
+
+    def gemm_fp64_tensor(self, a, b):
+        """a [M, K] @ b[N, K]^T with FP64-class accuracy on the tensor cores (N <= 32)."""
+        a, b = f64(a), f64(b)
+        c = np.zeros((a.shape[0], b.shape[0]))
+        self.check(self.lib.tincr_gemm_fp64_tensor(self.h, a.shape[0], b.shape[0], a.shape[1], dptr(a), dptr(b),
+                                                   dptr(c)))
+        return c
 
     def last_timing(self):
         ms = C.c_double()

@@ -97,6 +97,14 @@ int tincr_subspace_eigh(tincr_ctx *ctx, int m, int k, const double *a, double *w
     });
 }
 
+int tincr_gemm_fp64_tensor(tincr_ctx *ctx, int M, int N, int K, const double *A, const double *B, double *C) {
+    return guarded(ctx, [&](tincr::Ctx &c) {
+        if (!A || !B || !C) tincr::fail(TINCR_BAD_ARG, "gemm_fp64_tensor: null argument");
+        c.gemm_f64_digits(M, N, K, A, B, C);
+        return TINCR_OK;
+    });
+}
+
 int tincr_davidson_history(const tincr_ctx *ctx, int capacity, int *n_steps, int *iter, int *n_sub,
                            double *max_residual, int *roots_left, int *precision) {
     if (!ctx || !ctx->impl || capacity < 0) return TINCR_BAD_ARG;

@@ -331,7 +331,12 @@ bool eigh_lowest_upper(int n, const double *a, int k, double *w, double *y) {
     lo -= 2.0 * eps * tnorm + 2.0 * pivmin;
     hi += 2.0 * eps * tnorm + 2.0 * pivmin;
     const bool par_roots = k >= 4 && n >= 48;
-#pragma omp parallel for schedule(dynamic, 1) if (par_roots)
+    const double tiny = eps * std::max(tnorm, 1e-300);
+    const double ortol = 1e-3 * tnorm;
+    // one parallel region for the root phases (each region start wakes the team)
+#pragma omp parallel if (par_roots)
+    {
+#pragma omp for schedule(dynamic, 1)
     for (int r = 0; r < k; ++r) {
         double x_lo = lo, x_hi = hi;
         for (int it = 0; it < 200; ++it) {
@@ -344,8 +349,7 @@ bool eigh_lowest_upper(int n, const double *a, int k, double *w, double *y) {
     }
     // 3. inverse iteration on T - w I (LU with partial pivoting), one root per task; y holds the
     //    eigenvectors of T until the back-transformation
-    const double tiny = eps * std::max(tnorm, 1e-300);
-#pragma omp parallel for schedule(dynamic, 1) if (par_roots)
+#pragma omp for schedule(dynamic, 1)
     for (int r = 0; r < k; ++r) {
         std::vector<double> dl(n), dd(n), du(n), du2(n);
         std::vector<char> swp(n);
@@ -398,7 +402,7 @@ bool eigh_lowest_upper(int n, const double *a, int k, double *w, double *y) {
     }
     // Gram-Schmidt (twice) against the lower roots of the same cluster: roots closer than 1e-3 |T|
     // (the criterion of LAPACK's dstein); separated roots are orthogonal to rounding already
-    const double ortol = 1e-3 * tnorm;
+#pragma omp single
     for (int r = 1, r0 = 0; r < k; ++r) {
         if (w[r] - w[r - 1] > ortol) {
             r0 = r;
@@ -418,7 +422,7 @@ bool eigh_lowest_upper(int n, const double *a, int k, double *w, double *y) {
         for (int i = 0; i < n; ++i) z[i] *= nrm;
     }
     // 4. back-transformation y = H_0 ... H_{n-3} z, one root per task
-#pragma omp parallel for schedule(dynamic, 1) if (par_roots)
+#pragma omp for schedule(dynamic, 1)
     for (int r = 0; r < k; ++r) {
         double *yr = y + (size_t)r * n;
         for (int c = n - 3; c >= 0; --c) {
@@ -433,6 +437,7 @@ bool eigh_lowest_upper(int n, const double *a, int k, double *w, double *y) {
             for (int i = 0; i < n1; ++i) yr[c + 1 + i] -= s * u[i];
         }
     }
+    }   // omp parallel
     for (int r = 0; r < k; ++r)
         if (!std::isfinite(w[r])) return false;
     return true;

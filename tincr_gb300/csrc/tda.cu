@@ -227,25 +227,28 @@ __global__ void row_sq_finish_kernel(int rows, int chunks, const double *__restr
     out[r] = sqrt(s);
 }
 
-// Sequential classical Gram-Schmidt of kadd candidate vectors T (already orthogonal to the old
-// basis) against the vectors accepted in this step, V[m0 .. m), with tincr's 1e-8 drop rule
-// (davidson.rs:162-168); accepted vectors are normalised into V[m].  One cooperative launch: every
-// CTA takes the same accept / drop decisions from partial sums reduced in a fixed order (so the
-// result does not depend on timing).  state[0]: m out; state[1]: 1 if a norm was not finite.
+// Sequential Gram-Schmidt of the kadd correction vectors T against the vectors accepted in this step
+// (davidson.rs:162-168): t -= sum_i (q_i . t) q_i over the accepted q_i, then accept t / |t| when
+// |t| > 1e-8 (and the basis has room), else drop it.  One cooperative launch, two grid barriers per
+// vector: (1) partial dots, (2) t' = t - sum c_i q_i written to its destination row with partial
+// |t'|^2.  The normalisation is deferred: an accepted row is kept as t' with the factor 1/|t'|, which
+// the dots and updates of the next vectors apply, and every accepted row is scaled in place at the
+// end.  Every CTA takes the same accept / drop decisions from partial sums reduced in a fixed order.
+// state[0]: m out; state[1]: 1 if a norm was not finite.  part: [gridDim.x][34] doubles.
 __global__ void __launch_bounds__(256) seq_gs_kernel(int kadd, long long ov, int m0, int mmax, double *V, double *T,
                                                      double *part, int *state) {
     cg::grid_group grid = cg::this_grid();
-    __shared__ double c[32];
+    __shared__ double c[32], sc[32];
     __shared__ double red[8][9];
-    __shared__ double s_nrm;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const long long stride = (long long)gridDim.x * blockDim.x;
     const long long x0 = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     int m = m0;
-    for (int j = 0; j < kadd; ++j) {
-        double *t = T + (long long)j * ov;
+    bool finite = true;
+    for (int j = 0; j < kadd && finite; ++j) {
+        const double *t = T + (long long)j * ov;
         const int acc = m - m0;
-        // 1. partial dots c_i = V[m0 + i] . t, eight at a time
+        // 1. partial dots d_i = t'_i . t of the accepted (unscaled) rows, eight at a time
         for (int i0 = 0; i0 < acc; i0 += 8) {
             double s[8];
 #pragma unroll
@@ -265,52 +268,58 @@ __global__ void __launch_bounds__(256) seq_gs_kernel(int kadd, long long ov, int
             if (threadIdx.x < 8) {
                 double v = 0.0;
                 for (int w = 0; w < 8; ++w) v += red[w][threadIdx.x];
-                part[(long long)blockIdx.x * 33 + i0 + threadIdx.x] = v;
+                part[(long long)blockIdx.x * 34 + i0 + threadIdx.x] = v;
             }
             __syncthreads();
         }
-        grid.sync();
-        // 2. c_i in a fixed order, t -= sum_i c_i V[m0 + i], partial |t|^2
+        if (acc > 0) grid.sync();
+        // 2. c_i = d_i / |t'_i|^2 in a fixed order; t' = t - sum_i c_i t'_i into its destination row
+        //    (the next basis row, or back into T when the basis is full); partial |t'|^2
         if (threadIdx.x < acc) {
             double v = 0.0;
-            for (int b = 0; b < (int)gridDim.x; ++b) v += part[(long long)b * 33 + threadIdx.x];
-            c[threadIdx.x] = v;
+            for (int b = 0; b < (int)gridDim.x; ++b) v += part[(long long)b * 34 + threadIdx.x];
+            c[threadIdx.x] = v * sc[threadIdx.x] * sc[threadIdx.x];
         }
         __syncthreads();
+        double *dst = m < mmax ? V + (long long)m * ov : T + (long long)j * ov;
         double sq = 0.0;
         for (long long x = x0; x < ov; x += stride) {
             double v = t[x];
             for (int i = 0; i < acc; ++i) v -= c[i] * V[(long long)(m0 + i) * ov + x];
-            t[x] = v;
+            dst[x] = v;
             sq += v * v;
         }
         for (int off = 16; off; off >>= 1) sq += __shfl_down_sync(0xffffffffu, sq, off);
         if (lane == 0) red[warp][8] = sq;
         __syncthreads();
+        const int slot = 32 + (j & 1);   // alternates: a CTA may run ahead into the next vector
         if (threadIdx.x == 0) {
             double v = 0.0;
             for (int w = 0; w < 8; ++w) v += red[w][8];
-            part[(long long)blockIdx.x * 33 + 32] = v;
+            part[(long long)blockIdx.x * 34 + slot] = v;
         }
         grid.sync();
-        // 3. the norm (fixed order), accept or drop
-        if (threadIdx.x == 0) {
-            double v = 0.0;
-            for (int b = 0; b < (int)gridDim.x; ++b) v += part[(long long)b * 33 + 32];
-            s_nrm = sqrt(v);
-        }
-        __syncthreads();
-        const double nrm = s_nrm;
+        // 3. the norm (fixed order, the same in every CTA): accept or drop
+        double v = 0.0;
+        for (int b = 0; b < (int)gridDim.x; ++b) v += part[(long long)b * 34 + slot];
+        const double nrm = sqrt(v);
         if (!isfinite(nrm)) {
             if (blockIdx.x == 0 && threadIdx.x == 0) state[1] = 1;
-            break;   // every CTA sees the same norm
-        }
-        if (nrm > 1.0e-8 && m < mmax) {
-            const double inv = 1.0 / nrm;
-            for (long long x = x0; x < ov; x += stride) V[(long long)m * ov + x] = t[x] * inv;
+            finite = false;   // every CTA sees the same norm
+        } else if (nrm > 1.0e-8 && m < mmax) {
+            if (threadIdx.x == 0) sc[acc] = 1.0 / nrm;
             ++m;
         }
-        grid.sync();
+        __syncthreads();
+        // part[.][0..31] (dots) of the next vector are written after every CTA has passed the barrier
+        // above, i.e. after this vector's phase 2 read them; its norm goes to the other slot, read here
+        // before any CTA passes the next vector's second barrier
+    }
+    // scale the accepted rows
+    for (int i = 0; i < m - m0; ++i) {
+        double *q = V + (long long)(m0 + i) * ov;
+        const double f = sc[i];
+        for (long long x = x0; x < ov; x += stride) q[x] *= f;
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) state[0] = m;
 }
@@ -406,13 +415,16 @@ Ctx::Ctx(int dev) : device(dev) {
     int coop = 0, per_sm = 0;
     TINCR_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
     TINCR_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, seq_gs_kernel, 256, 0));
-    coop_grid = coop ? std::min(4, per_sm) * n_sm : 0;
+    coop_grid = coop ? std::min(1, per_sm) * n_sm : 0;
     // plane GEMM of the mixed-precision contraction: tcgen05 (default) or warp MMA
     const char *pg = std::getenv("TINCR_GB300_PLANE_GEMM");
     if (pg && std::string(pg) == "mma") use_tc = false;
     // Davidson subspace eigensolver: host (default) or the thread-block cluster kernel
     const char *se = std::getenv("TINCR_GB300_SUBSPACE_EIG");
     if (se && std::string(se) == "cluster") eig_cluster_on = true;
+    // subspace products of the mixed Davidson: digit GEMMs on the tensor cores (default) or FP64
+    const char *sg = std::getenv("TINCR_GB300_SUBSPACE_GEMM");
+    if (sg && std::string(sg) == "fp64") use_digits = false;
 }
 
 Ctx::~Ctx() {
@@ -717,6 +729,9 @@ int Ctx::davidson(int n_roots, int max_iter, double tol, bool from_ritz, std::ve
     DevBuf<int> didx(n_roots);
     dAp.reserve((size_t)mmax * mmax);
     eig_err.reserve(1);
+    // mixed form: subspace products as FP64-accurate digit GEMMs (digits.cu)
+    const bool dg = prec == TINCR_PREC_BF16X3 && use_digits && n_roots <= 32;
+    if (dg) dg_reserve(mmax);
     TINCR_CUDA(cudaMemsetAsync(eig_err.p, 0, sizeof(int), stream));
     u.assign(n_roots, 0.0);
     if (from_ritz) {
@@ -743,6 +758,7 @@ int Ctx::davidson(int n_roots, int max_iter, double tol, bool from_ritz, std::ve
         check_launch("unit_vectors");
         sync();
     }
+    if (dg) dg_add_rows(false, 0, n_roots, dV.p);
     int m = n_roots;            // columns of the guess
     int m_done = 0;             // columns with products (product cache)
     int dim_sub = n_roots;      // tincr's dim_sub bookkeeping
@@ -758,12 +774,15 @@ int Ctx::davidson(int n_roots, int max_iter, double tol, bool from_ritz, std::ve
         if (m > m_done) {
             products_dev(m - m_done, dV.p + (long long)m_done * ov, dAV.p + (long long)m_done * ov, nullptr);
             last_products += m - m_done;
+            if (dg) dg_add_rows(true, m_done, m - m_done, dAV.p + (long long)m_done * ov);
         }
         // 1.1 projected matrix, new columns only: P[:, mold:m] = V[0:m] AV[mold:m]^T, kept on the device
         //     (leading dimension mmax; the old columns stay valid until a collapse)
         int knew = m - m_done;
         const int mold = m_done;
-        if (knew > 0) {
+        if (knew > 0 && dg) {
+            dg_project(m, mold, knew, dAp.p, mmax);
+        } else if (knew > 0) {
             TINCR_CUDA(cudaMemset2DAsync(dAp.p + mold, (size_t)mmax * sizeof(double), 0, (size_t)knew * sizeof(double),
                                          m, stream));
             if (knew <= 32) {
@@ -802,7 +821,9 @@ int Ctx::davidson(int n_roots, int max_iter, double tol, bool from_ritz, std::ve
             TINCR_CUDA(cudaMemcpyAsync(du.p, u.data(), n_roots * sizeof(double), cudaMemcpyHostToDevice, stream));
         }
         // 3.1 Ritz vectors R = Y^T V ; 3.2 residuals Rk = Y^T AV - u o R
-        if (n_roots <= 32) {
+        if (dg) {
+            dg_ritz(n_roots, m, dYt.p, dR.p, dRk.p, du.p);
+        } else if (n_roots <= 32) {
             int slot = prof_begin(TINCR_KF_SUBSPACE);
             skinny_comb(stream, n_roots, m, ov, dYt.p, m, 1, dV.p, ov, CombStore{dR.p, ov, 1.0, 0.0});
             skinny_comb(stream, n_roots, m, ov, dYt.p, m, 1, dAV.p, ov, CombResidual{dRk.p, dR.p, du.p, ov});
@@ -815,13 +836,18 @@ int Ctx::davidson(int n_roots, int max_iter, double tol, bool from_ritz, std::ve
         }
         row_norms(n_roots, ov, dRk.p, ov, dnorm.p);
         TINCR_CUDA(cudaMemcpyAsync(errs.data(), dnorm.p, n_roots * sizeof(double), cudaMemcpyDeviceToHost, stream));
-        int eig_bad = 0;
+        int eig_bad = 0, dg_err[2] = {0, 0};
         if (on_device) {
             TINCR_CUDA(cudaMemcpyAsync(u.data(), du.p, n_roots * sizeof(double), cudaMemcpyDeviceToHost, stream));
             TINCR_CUDA(cudaMemcpyAsync(&eig_bad, eig_err.p, sizeof(int), cudaMemcpyDeviceToHost, stream));
         }
+        if (dg) {
+            TINCR_CUDA(cudaMemcpyAsync(&dg_err[0], d_tc_err.p, sizeof(int), cudaMemcpyDeviceToHost, stream));
+            TINCR_CUDA(cudaMemcpyAsync(&dg_err[1], dg_bad.p, sizeof(int), cudaMemcpyDeviceToHost, stream));
+        }
         sync();
         if (eig_bad) fail(TINCR_NONFINITE, "subspace eigensolver: non-finite projected matrix or Ritz pairs");
+        if (dg_err[0] || dg_err[1]) dg_check();
         int roots_cvd = 0;
         for (int r = 0; r < n_roots; ++r) {
             if (!std::isfinite(errs[r])) fail(TINCR_NONFINITE, "non-finite residual");
@@ -850,14 +876,17 @@ int Ctx::davidson(int n_roots, int max_iter, double tol, bool from_ritz, std::ve
                 count_launch(stream, "precondition");
                 check_launch("precondition");
                 // orthogonalise against the current basis in one block: T -= (T V^T) V
-                TINCR_CUDA(cudaMemsetAsync(dc.p, 0, (size_t)kadd * m * sizeof(double), stream));
-                if (kadd <= 32) {
+                if (dg) {
+                    dg_ortho(kadd, m, dT.p, dc.p);
+                } else if (kadd <= 32) {
+                    TINCR_CUDA(cudaMemsetAsync(dc.p, 0, (size_t)kadd * m * sizeof(double), stream));
                     // c = V T^T  [m x kadd];  T -= c^T V
                     int slot = prof_begin(TINCR_KF_SUBSPACE);
                     skinny_dots(stream, n_sm, m, kadd, ov, dV.p, ov, dT.p, ov, dc.p, kadd);
                     skinny_comb(stream, kadd, m, ov, dc.p, 1, kadd, dV.p, ov, CombStore{dT.p, ov, -1.0, 1.0});
                     prof_end(slot, 4.0 * kadd * (double)m * ov, 8.0 * (2.0 * m + 3.0 * kadd) * ov);
                 } else {
+                    TINCR_CUDA(cudaMemsetAsync(dc.p, 0, (size_t)kadd * m * sizeof(double), stream));
                     int sk = pick_splitk(kadd, m, (int)ov, 1, n_sm);
                     pgemm<false, true>(*this, TINCR_KF_SUBSPACE, kadd, m, (int)ov, dT.p, (int)ov, 0, dV.p, (int)ov, 0, 1,
                                        EpiAtomicAdd{dc.p, 0, m, 1.0}, sk);
@@ -867,7 +896,7 @@ int Ctx::davidson(int n_roots, int max_iter, double tol, bool from_ritz, std::ve
                 // then sequentially against the vectors accepted in this step (davidson.rs:162-168)
                 if (kadd <= 32 && coop_grid > 0) {
                     int slot = prof_begin(TINCR_KF_SUBSPACE);
-                    gs_part.reserve((size_t)coop_grid * 33);
+                    gs_part.reserve((size_t)coop_grid * 34);
                     gs_state.reserve(2);
                     int hstate[2] = {m, 0};
                     TINCR_CUDA(cudaMemcpyAsync(gs_state.p, hstate, 2 * sizeof(int), cudaMemcpyHostToDevice, stream));
@@ -883,9 +912,10 @@ int Ctx::davidson(int n_roots, int max_iter, double tol, bool from_ritz, std::ve
                     TINCR_CUDA(cudaMemcpyAsync(hstate, gs_state.p, 2 * sizeof(int), cudaMemcpyDeviceToHost, stream));
                     sync();
                     if (hstate[1]) fail(TINCR_NONFINITE, "non-finite correction vector");
+                    if (dg) dg_add_rows(false, m, hstate[0] - m, dV.p + (long long)m * ov);
                     m = hstate[0];
                 } else {
-                    int m0 = m;
+                    const int m0 = m;
                     for (int j = 0; j < kadd; ++j) {
                         double *t = dT.p + (long long)j * ov;
                         int acc = m - m0;
@@ -911,6 +941,7 @@ int Ctx::davidson(int n_roots, int max_iter, double tol, bool from_ritz, std::ve
                             ++m;
                         }
                     }
+                    if (dg) dg_add_rows(false, m0, m - m0, dV.p + (long long)m0 * ov);
                 }
             }
         } else {                                               // collapse, davidson.rs:172-176
@@ -918,6 +949,7 @@ int Ctx::davidson(int n_roots, int max_iter, double tol, bool from_ritz, std::ve
             ++last_collapses;
             TINCR_CUDA(cudaMemcpyAsync(dV.p, dR.p, (size_t)dim_sub * ov * sizeof(double), cudaMemcpyDeviceToDevice, stream));
             m = dim_sub;
+            if (dg) dg_add_rows(false, 0, dim_sub, dV.p);
             m_done = 0;
             aproj.clear();
         }

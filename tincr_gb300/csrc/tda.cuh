@@ -108,6 +108,21 @@ struct Ctx {
     DevBuf<double> eig_U, eig_Z;          // reflection vectors and tridiagonal eigenvectors (eig_cluster.cu)
     DevBuf<int> eig_err;
     bool eig_cluster_on = false;          // subspace eigensolver on a thread-block cluster instead of the host
+    // FP64-accurate digit GEMMs for the subspace products of the mixed Davidson (digits.cu)
+    bool use_digits = true;
+    DevBuf<__nv_bfloat16> dg_V, dg_VT, dg_AVT, dg_B, dg_C;   // basis digits (row, column layouts), operands
+    DevBuf<int> dg_eV, dg_eAV, dg_eB, dg_bad;
+    DevBuf<double> dg_scale;
+    DevBuf<unsigned long long> dg_acc, dg_mx;
+    int dg_mmax = 0;
+    long long dg_ovp = 0, dg_mpad = 0;
+    void dg_reserve(int mmax);
+    void dg_add_rows(bool av, int i0, int n, const double *rows);
+    void dg_project(int m, int mold, int knew, double *P, int ldp);
+    void dg_ritz(int k, int m, const double *Yt, double *R, double *Rk, const double *u);
+    void dg_ortho(int kadd, int m, double *T, double *cbuf);
+    int dg_check();
+    void gemm_f64_digits(int M, int N, int K, const double *A, const double *B, double *C);
     BatchWork *batch = nullptr;
 
     explicit Ctx(int dev);
