@@ -54,13 +54,12 @@ constexpr int DS_K = 64;   // k values per CTA of the split
 
 // Digits of rows r < nr of src (row maxima mx[r] from dg_row_max_kernel), k < K, DS_K values of k per
 // CTA: the bound exponents go to E[e0 + r] (CTA 0; *bad on inf/NaN); digits to
-//   row layout     dst[p * ps + (drow + r) * ld + k]     (when dst)
-//   column layout  dstT[p * psT + k * ldT + dcol + r]    (when dstT; staged through shared memory so
-//                  that consecutive threads write consecutive r)
+//   row layout     element (p, drow + r, k) of `rowop`   (when rowop.p)
+//   column layout  element (p, k, dcol + r) of `colop`   (when colop.p; staged through shared memory
+//                  so that consecutive threads write consecutive r)
 __global__ void __launch_bounds__(256) dg_split_kernel(int nr, long long K, const double *__restrict__ src, long long lds,
                                                       const unsigned long long *__restrict__ mx, int *E, int e0, int *bad,
-                                                      bf16 *dst, int drow, long long ld, long long ps, bf16 *dstT,
-                                                      int dcol, long long ldT, long long psT) {
+                                                      DgOperand rowop, int drow, DgOperand colop, int dcol) {
     __shared__ unsigned short sd[DG_PLANES][DS_K][33];
     __shared__ int sE[32];
     if (threadIdx.x < nr) {
@@ -73,8 +72,8 @@ __global__ void __launch_bounds__(256) dg_split_kernel(int nr, long long K, cons
         }
     }
     __syncthreads();
-    unsigned short *o = reinterpret_cast<unsigned short *>(dst);
-    unsigned short *oT = reinterpret_cast<unsigned short *>(dstT);
+    unsigned short *o = reinterpret_cast<unsigned short *>(rowop.p);
+    unsigned short *oT = reinterpret_cast<unsigned short *>(colop.p);
     const long long k0 = blockIdx.x * (long long)DS_K;
     for (int idx = threadIdx.x; idx < nr * DS_K; idx += 256) {
         const int r = idx / DS_K, kk = idx % DS_K;
@@ -88,7 +87,7 @@ __global__ void __launch_bounds__(256) dg_split_kernel(int nr, long long K, cons
         }
         if (o && k < K)
 #pragma unroll
-            for (int p = 0; p < DG_PLANES; ++p) o[p * ps + (long long)(drow + r) * ld + k] = d[p];
+            for (int p = 0; p < DG_PLANES; ++p) o[dg_off(rowop, p, drow + r, k)] = d[p];
 #pragma unroll
         for (int p = 0; p < DG_PLANES; ++p) sd[p][kk][r] = d[p];
     }
@@ -98,13 +97,13 @@ __global__ void __launch_bounds__(256) dg_split_kernel(int nr, long long K, cons
     for (int idx = threadIdx.x; idx < DG_PLANES * per; idx += 256) {
         const int p = idx / per, rem = idx % per, kk = rem / nr, r = rem % nr;
         const long long k = k0 + kk;
-        if (k < K) oT[p * psT + k * ldT + dcol + r] = sd[p][kk][r];
+        if (k < K) oT[dg_off(colop, p, k, dcol + r)] = sd[p][kk][r];
     }
 }
 
 // digits of nr <= 32 rows (length K, stride lds) with their bound exponents
-static void dg_split_rows(Ctx &c, int nr, long long K, const double *src, long long lds, int *E, int e0, bf16 *dst,
-                          int drow, long long ld, long long ps, bf16 *dstT, int dcol, long long ldT, long long psT) {
+static void dg_split_rows(Ctx &c, int nr, long long K, const double *src, long long lds, int *E, int e0,
+                          const DgOperand &rowop, int drow, const DgOperand &colop, int dcol) {
     if (nr <= 0) return;
     if (nr > 32) fail(TINCR_BAD_ARG, "dg_split_rows: more than 32 rows");
     TINCR_CUDA(cudaMemsetAsync(c.dg_mx.p, 0, 32 * sizeof(unsigned long long), c.stream));
@@ -112,18 +111,25 @@ static void dg_split_rows(Ctx &c, int nr, long long K, const double *src, long l
     dg_row_max_kernel<<<dim3(chunks, nr), 256, 0, c.stream>>>(K, src, lds, c.dg_mx.p);
     count_launch(c.stream, "dg_row_max");
     check_launch("dg_row_max");
-    dg_split_kernel<<<ceil_div(K, DS_K), 256, 0, c.stream>>>(nr, K, src, lds, c.dg_mx.p, E, e0, c.dg_bad.p, dst, drow, ld,
-                                                             ps, dstT, dcol, ldT, psT);
+    dg_split_kernel<<<ceil_div(K, DS_K), 256, 0, c.stream>>>(nr, K, src, lds, c.dg_mx.p, E, e0, c.dg_bad.p, rowop, drow,
+                                                             colop, dcol);
     count_launch(c.stream, "dg_split");
     check_launch("dg_split");
 }
 
+}  // namespace
+
+inline long long pad128(long long r) { return (r + 127) / 128 * 128; }
+static const DgOperand kNoOperand{nullptr, 0, 0, 0};
+
+namespace {
+
 // Coefficient digits of a combination: Y(r, i) = Y[r * ysr + i * ysi] 2^(Erow[i]) for r < k, i < m,
-// cut with one bound per r into out[p * ps + r * ld + i] (zero for i >= m and for rows k..31);
+// cut with one bound per r into the tiled operand out (zero for i >= m and for rows k..31);
 // scale[r] = 2^(Eb_r - 63).  One CTA per r < 32.
 __global__ void __launch_bounds__(256) dg_comb_b_kernel(int k, int m, const double *__restrict__ Y, long long ysr,
-                                                       long long ysi, const int *__restrict__ Erow, bf16 *out,
-                                                       long long ld, long long ps, double *scale) {
+                                                       long long ysi, const int *__restrict__ Erow, DgOperand out,
+                                                       double *scale) {
     __shared__ unsigned long long red[8];
     const int r = blockIdx.x;
     unsigned long long mx = 0;
@@ -134,13 +140,13 @@ __global__ void __launch_bounds__(256) dg_comb_b_kernel(int k, int m, const doub
         }
     mx = block_max_u64(mx, red);
     const int E = mx >= 0x7FF0000000000000ull ? 0 : dg_bound_exp(mx);
-    unsigned short *o = reinterpret_cast<unsigned short *>(out);
-    for (long long i = threadIdx.x; i < ld; i += 256) {
+    unsigned short *o = reinterpret_cast<unsigned short *>(out.p);
+    for (long long i = threadIdx.x; i < out.Kpad; i += 256) {
         const double v = (r < k && i < m) ? ldexp(Y[r * ysr + i * ysi], Erow[i]) : 0.0;
         unsigned short d[DG_PLANES];
         dg_digits(v, E, d);
 #pragma unroll
-        for (int p = 0; p < DG_PLANES; ++p) o[p * ps + (long long)r * ld + i] = d[p];
+        for (int p = 0; p < DG_PLANES; ++p) o[dg_off(out, p, r, i)] = d[p];
     }
     if (threadIdx.x == 0) scale[r] = ldexp(1.0, E - 63);
 }
@@ -163,9 +169,9 @@ void Ctx::dg_reserve(int mmax) {
     dg_mmax = mmax;
     dg_ovp = ovp;
     dg_mpad = mpad;
-    dg_V.alloc((size_t)DG_PLANES * mmax * ovp);
-    dg_VT.alloc((size_t)DG_PLANES * ovp * mpad);
-    dg_AVT.alloc((size_t)DG_PLANES * ovp * mpad);
+    dg_V.alloc((size_t)DG_PLANES * pad128(mmax) * ovp);
+    dg_VT.alloc((size_t)DG_PLANES * pad128(ov) * mpad);
+    dg_AVT.alloc((size_t)DG_PLANES * pad128(ov) * mpad);
     dg_B.alloc((size_t)DG_PLANES * DG_N * ovp);
     dg_C.alloc((size_t)DG_PLANES * DG_N * mpad);
     dg_eV.alloc(mmax);
@@ -188,18 +194,22 @@ void Ctx::dg_reserve(int mmax) {
     }
 }
 
+// the tiled digit operands of the basis
+static DgOperand opV(const Ctx &c) { return DgOperand{c.dg_V.p, pad128(c.dg_mmax), c.dg_ovp, 7}; }
+static DgOperand opVT(const Ctx &c, bool av) { return DgOperand{av ? c.dg_AVT.p : c.dg_VT.p, pad128(c.ov), c.dg_mpad, 7}; }
+static DgOperand opB(const Ctx &c) { return DgOperand{c.dg_B.p, DG_N, c.dg_ovp, 5}; }
+static DgOperand opC(const Ctx &c) { return DgOperand{c.dg_C.p, DG_N, c.dg_mpad, 5}; }
+
 // rows i0 .. i0+n-1 of V (av = false) or AV (av = true) join the basis: bound exponents and digits;
 // AV rows also go to the row-layout B operand (rows 0..n-1) of the next projection
 void Ctx::dg_add_rows(bool av, int i0, int n, const double *rows) {
     if (n <= 0) return;
     if (n > DG_N || i0 + n > dg_mmax) fail(TINCR_BAD_ARG, "dg_add_rows: too many rows");
     if (av) {
-        dg_split_rows(*this, n, ov, rows, ov, dg_eAV.p, i0, dg_B.p, 0, dg_ovp, (long long)DG_N * dg_ovp, dg_AVT.p, i0,
-                      dg_mpad, dg_ovp * dg_mpad);
+        dg_split_rows(*this, n, ov, rows, ov, dg_eAV.p, i0, opB(*this), 0, opVT(*this, true), i0);
         TINCR_CUDA(cudaMemcpyAsync(dg_eB.p, dg_eAV.p + i0, n * sizeof(int), cudaMemcpyDeviceToDevice, stream));
     } else {
-        dg_split_rows(*this, n, ov, rows, ov, dg_eV.p, i0, dg_V.p, i0, dg_ovp, (long long)dg_mmax * dg_ovp, dg_VT.p, i0,
-                      dg_mpad, dg_ovp * dg_mpad);
+        dg_split_rows(*this, n, ov, rows, ov, dg_eV.p, i0, opV(*this), i0, opVT(*this, false), i0);
     }
 }
 
@@ -209,8 +219,7 @@ static void dg_dots(Ctx &c, int m, int n, double *out, long long ldo) {
     const int nkb = (int)(c.dg_ovp / DG_K);
     const int n_mt = ceil_div(m, DG_M);
     const int slot = c.prof_begin(TINCR_KF_SUBSPACE);
-    gemm_digits(c.stream, c.n_sm, m, nkb, std::max(1, c.n_sm / n_mt), c.dg_V.p, c.dg_ovp, (long long)c.dg_mmax * c.dg_ovp,
-                c.dg_mmax, c.dg_B.p, c.dg_ovp, (long long)DG_N * c.dg_ovp, DG_N, 0, DgEpiAtomic{c.dg_acc.p, m, n, DG_N},
+    gemm_digits(c.stream, c.n_sm, m, nkb, std::max(1, c.n_sm / n_mt), opV(c), opB(c), 0, DgEpiAtomic{c.dg_acc.p, m, n, DG_N},
                 c.d_tc_err.p);
     dg_finalize_kernel<<<ceil_div((long long)m * n, 256), 256, 0, c.stream>>>(m, n, c.dg_acc.p, DG_N, c.dg_eV.p, c.dg_eB.p,
                                                                              out, ldo);
@@ -222,14 +231,12 @@ static void dg_dots(Ctx &c, int m, int n, double *out, long long ldo) {
 // combination out_r(x) (mode of DgEpiComb) = sum_{i < m} A_i(x) Y(r, i), r < k, A = V (or AV) columns
 static void dg_comb(Ctx &c, bool av, int k, int m, const double *Y, long long ysr, long long ysi, double *out, int mode,
                     const double *R, const double *u) {
-    dg_comb_b_kernel<<<DG_N, 256, 0, c.stream>>>(k, m, Y, ysr, ysi, av ? c.dg_eAV.p : c.dg_eV.p, c.dg_C.p, c.dg_mpad,
-                                                 (long long)DG_N * c.dg_mpad, c.dg_scale.p);
+    dg_comb_b_kernel<<<DG_N, 256, 0, c.stream>>>(k, m, Y, ysr, ysi, av ? c.dg_eAV.p : c.dg_eV.p, opC(c), c.dg_scale.p);
     count_launch(c.stream, "dg_comb_b");
     check_launch("dg_comb_b");
     const int slot = c.prof_begin(TINCR_KF_SUBSPACE);
     const int nkb = ceil_div(m, DG_K);
-    gemm_digits(c.stream, c.n_sm, (int)c.ov, nkb, 1, av ? c.dg_AVT.p : c.dg_VT.p, c.dg_mpad, c.dg_ovp * c.dg_mpad,
-                (int)c.dg_ovp, c.dg_C.p, c.dg_mpad, (long long)DG_N * c.dg_mpad, DG_N, 0,
+    gemm_digits(c.stream, c.n_sm, (int)c.ov, nkb, 1, opVT(c, av), opC(c), 0,
                 DgEpiComb{out, c.ov, c.dg_scale.p, (int)c.ov, k, mode, R, u}, c.d_tc_err.p);
     c.prof_end(slot, 2.0 * k * (double)m * c.ov, 2.0 * DG_PLANES * (double)m * c.ov + 8.0 * k * c.ov * (mode ? 2 : 1));
 }
@@ -243,7 +250,7 @@ void Ctx::dg_ritz(int k, int m, const double *Yt, double *R, double *Rk, const d
 
 void Ctx::dg_ortho(int kadd, int m, double *T, double *cbuf) {
     // T rows: bound exponents and row digits (the B operand of the dots)
-    dg_split_rows(*this, kadd, ov, T, ov, dg_eB.p, 0, dg_B.p, 0, dg_ovp, (long long)DG_N * dg_ovp, nullptr, 0, 0, 0);
+    dg_split_rows(*this, kadd, ov, T, ov, dg_eB.p, 0, opB(*this), 0, kNoOperand, 0);
     // c = V T^T [m x kadd];  T -= c^T V
     dg_dots(*this, m, kadd, cbuf, kadd);
     dg_comb(*this, false, kadd, m, cbuf, 1, kadd, T, 2, nullptr, nullptr);
@@ -272,7 +279,7 @@ void Ctx::gemm_f64_digits(int M, int N, int K, const double *A, const double *B,
     if (M <= 0 || N <= 0 || N > DG_N || K <= 0) fail(TINCR_BAD_ARG, "gemm_f64_digits: bad sizes");
     const long long Kp = pad64(K);
     DevBuf<double> dA((size_t)M * K), dB((size_t)N * K), dC((size_t)M * N);
-    DevBuf<bf16> pa((size_t)DG_PLANES * M * Kp), pb((size_t)DG_PLANES * DG_N * Kp);
+    DevBuf<bf16> pa((size_t)DG_PLANES * pad128(M) * Kp), pb((size_t)DG_PLANES * DG_N * Kp);
     DevBuf<int> ea(M), eb(DG_N);
     DevBuf<unsigned long long> acc((size_t)M * DG_N * 2);
     if (!d_tc_err.p) {
@@ -289,13 +296,12 @@ void Ctx::gemm_f64_digits(int M, int N, int K, const double *A, const double *B,
     TINCR_CUDA(cudaMemsetAsync(pa.p, 0, pa.n * sizeof(bf16), stream));
     TINCR_CUDA(cudaMemsetAsync(pb.p, 0, pb.n * sizeof(bf16), stream));
     TINCR_CUDA(cudaMemsetAsync(acc.p, 0, acc.n * sizeof(unsigned long long), stream));
+    const DgOperand oa{pa.p, pad128(M), Kp, 7}, ob{pb.p, DG_N, Kp, 5};
     for (int r0 = 0; r0 < M; r0 += DG_N)
-        dg_split_rows(*this, std::min(DG_N, M - r0), K, dA.p + (long long)r0 * K, K, ea.p, r0, pa.p, r0, Kp,
-                      (long long)M * Kp, nullptr, 0, 0, 0);
-    dg_split_rows(*this, N, K, dB.p, K, eb.p, 0, pb.p, 0, Kp, (long long)DG_N * Kp, nullptr, 0, 0, 0);
+        dg_split_rows(*this, std::min(DG_N, M - r0), K, dA.p + (long long)r0 * K, K, ea.p, r0, oa, r0, kNoOperand, 0);
+    dg_split_rows(*this, N, K, dB.p, K, eb.p, 0, ob, 0, kNoOperand, 0);
     const int nkb = (int)(Kp / DG_K), n_mt = ceil_div(M, DG_M);
-    gemm_digits(stream, n_sm, M, nkb, std::max(1, n_sm / n_mt), pa.p, Kp, (long long)M * Kp, M, pb.p, Kp,
-                (long long)DG_N * Kp, DG_N, 0, DgEpiAtomic{acc.p, M, N, DG_N}, d_tc_err.p);
+    gemm_digits(stream, n_sm, M, nkb, std::max(1, n_sm / n_mt), oa, ob, 0, DgEpiAtomic{acc.p, M, N, DG_N}, d_tc_err.p);
     dg_finalize_kernel<<<ceil_div((long long)M * N, 256), 256, 0, stream>>>(M, N, acc.p, DG_N, ea.p, eb.p, dC.p, N);
     check_launch("dg_finalize");
     dg_check();

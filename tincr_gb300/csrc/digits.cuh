@@ -5,7 +5,10 @@
 // sign of x_k (|D| <= 127, exact in bf16).  A dot product of two such rows is
 //     2^(Ea+Eb-112) sum_{s,t} 2^(7(14-s-t)) sum_k D^a_{k,s} D^b_{k,t},
 // and its 36 digit products with s + t <= 7 run as bf16 tcgen05 MMAs: the (g + 1) products of one
-// level g = s + t accumulate in one FP32 TMEM accumulator.  Over a chunk of 128 k a level sum is an
+// level g = s + t accumulate in one FP32 TMEM accumulator.  The eight 32-column level accumulators
+// are adjacent, and the B planes lie one after the other in shared memory, so one MMA of A plane s
+// against B planes 0 .. 7-s (N = 32 (8 - s)) with its accumulator address shifted by s levels adds
+// every product of A plane s to its level: eight MMAs per 16 k instead of 36.  Over a chunk of 128 k a level sum is an
 // integer below 8 * 128 * 127^2 < 2^24, so the accumulator holds it exactly whatever the order and
 // rounding of the hardware sums.  After each chunk the CUDA cores convert the eight level sums to
 // integers and add them into two int64 accumulators per output, H = sum_{g<=3} G_g 2^(7(3-g)) and
@@ -19,14 +22,15 @@
 // of matrix multiplication by using fast routines of matrix multiplication and its applications",
 // Numer. Algorithms 59, 2012) with 7-bit digits sized for exact FP32 tensor-core accumulation.
 //
-// Operands are eight digit planes, K-major, K padded to 64 with zeros: plane p of row r at
-// base[p * ps + r * ld + k].  CTA = 320 threads, one 128-row x 32-column output tile at a time
+// Operands are eight digit planes, K-major, in tiles of RT rows (128 for A, 32 for B) x 64 k, so
+// that every TMA box is one contiguous block per plane (DgOperand, dg_off); K padded to 64 and rows
+// to RT with zeros.  CTA = 320 threads, one 128-row x 32-column output tile at a time
 // (persistent over tiles), K consumed in 64-element blocks, each block in two half-stages
-// (A planes 0-3 with B planes 0-7, then A planes 4-7 with B planes 0-7) through a 2-buffer ring:
+// (A planes 0-3 with B planes 0-7, then A planes 4-7 with B planes 0-3) through a 2-buffer ring:
 //   * warp 8 / lane 0: TMA producer (A box 64 x 128 x 4 planes, B box 64 x 32 x 8 planes, 128-byte
 //     swizzle);
-//   * warp 9 / lane 0: MMA issuer (M = 128, N = 32, K = 16), the eight level accumulators of a
-//     128-K chunk in one of two TMEM sets (2 x 8 x 32 = 512 columns), ping-pong between chunks;
+//   * warp 9 / lane 0: MMA issuer (M = 128, N = 32 (8 - s), K = 16), the eight level accumulators of
+//     a 128-K chunk in one of two TMEM sets (2 x 8 x 32 = 512 columns), ping-pong between chunks;
 //   * warps 0-7: integer folds (warp w: TMEM lanes 32 (w % 4).., columns 16 (w / 4)..), then the
 //     epilogue functor on the tile's (H, L).
 // Every mbarrier wait is bounded (2 s); on expiry the thread records an error code and leaves its
@@ -44,14 +48,16 @@ constexpr int DG_BTILE = DG_N * DG_K * 2;                        // 4 KB: one B 
 constexpr int DG_BUF = 4 * DG_ATILE + DG_PLANES * DG_BTILE;      // 96 KB half-stage
 constexpr int DG_SMEM = 2 * DG_BUF + 1024 + 256;
 constexpr int DG_COLS = 2 * DG_LEVELS * DG_N;                    // 512 TMEM columns
-constexpr uint32_t DG_IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(DG_N >> 3) << 17) |
-                              ((uint32_t)(DG_M >> 4) << 24);
+// instruction descriptor, kind::f16, D = F32, A = B = BF16, both K-major, M = 128, N = n (16 <= n <= 256)
+__device__ __forceinline__ uint32_t dg_idesc(int n) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(DG_M >> 4) << 24);
+}
 
-__device__ __forceinline__ void dg_mma(uint32_t tmem, uint64_t adesc, uint64_t bdesc, uint32_t accumulate) {
+__device__ __forceinline__ void dg_mma(uint32_t tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc, uint32_t accumulate) {
     asm volatile(
         "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
         " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
-        "l"(adesc), "l"(bdesc), "r"(DG_IDESC), "r"(accumulate));
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate));
 }
 
 // Signed 7-bit digits of x for the row bound 2^E (|x| < 2^E): d[s] = sign(x) ((X >> 7(7-s)) & 127),
@@ -86,6 +92,29 @@ __device__ __forceinline__ int dg_bound_exp(unsigned long long maxbits) {
     return e;
 }
 
+// Eight digit planes in tiles: element (plane p, row r, k) at
+//   p * rows_pad * Kpad + (r / RT) * RT * Kpad + (k / 64) * RT * 64 + (r % RT) * 64 + k % 64,
+// RT = 2^rt_shift (128 for A operands, 32 for B operands), rows_pad a multiple of RT, Kpad of 64.
+struct DgOperand {
+    bf16 *p;
+    long long rows_pad, Kpad;
+    int rt_shift;
+};
+
+__host__ __device__ __forceinline__ long long dg_off(const DgOperand &o, int plane, long long r, long long k) {
+    const long long rt = 1LL << o.rt_shift;
+    return (long long)plane * o.rows_pad * o.Kpad + (r >> o.rt_shift) * rt * o.Kpad + (k >> 6) * rt * 64 +
+           (r & (rt - 1)) * 64 + (k & 63);
+}
+
+__device__ __forceinline__ void tma_load_5d(void *dst, const CUtensorMap *map, int c2, int c3, int c4, uint64_t *bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.5d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5, "
+        "%6}], [%7];\n" ::"r"(smem_u32(dst)),
+        "l"((uint64_t)map), "r"(0), "r"(0), "r"(c2), "r"(c3), "r"(c4), "r"(smem_u32(bar))
+        : "memory");
+}
+
 struct DgTiles {
     int n_mt;   // 128-row tiles of A
     int n_ks;   // K splits
@@ -101,8 +130,8 @@ struct DgTiles {
 
 template <class Epi>
 __global__ void __launch_bounds__(DG_T, 1)
-gemm_digits_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB, DgTiles tl,
-                   int nb0, Epi epi, int *err) {
+gemm_digits_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB,
+                   const __grid_constant__ CUtensorMap mapB4, DgTiles tl, int nbt, Epi epi, int *err) {
     extern __shared__ unsigned char dg_raw[];
     unsigned char *smem = (unsigned char *)(((uintptr_t)dg_raw + 1023) & ~(uintptr_t)1023);
     uint64_t *full = reinterpret_cast<uint64_t *>(smem + 2 * DG_BUF);
@@ -150,9 +179,10 @@ gemm_digits_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_consta
                             break;
                         }
                         unsigned char *st = smem + s * DG_BUF;
-                        mbar_expect_tx(&full[s], DG_BUF);
-                        tma_load_3d(st, &mapA, kb * DG_K, mt * DG_M, 4 * h, &full[s]);
-                        tma_load_3d(st + 4 * DG_ATILE, &mapB, kb * DG_K, nb0, 0, &full[s]);
+                        // the second half (A planes 4-7) pairs only with B planes 0-3
+                        mbar_expect_tx(&full[s], 4 * DG_ATILE + (h ? 4 : DG_PLANES) * DG_BTILE);
+                        tma_load_5d(st, &mapA, kb, mt, 4 * h, &full[s]);
+                        tma_load_5d(st + 4 * DG_ATILE, h ? &mapB4 : &mapB, kb, nbt, 0, &full[s]);
                     }
             }
             if (!ok)   // loads still in flight land before the CTA exits
@@ -187,18 +217,17 @@ gemm_digits_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_consta
                             const uint32_t base = smem_u32(smem + s * DG_BUF);
 #pragma unroll
                             for (int si = 0; si < 4; ++si) {
-                                const int sa = 4 * h + si;
-                                for (int tb = 0; sa + tb < DG_LEVELS; ++tb) {
-                                    const int lev = sa + tb;
-                                    const uint32_t d = tmem + (uint32_t)(a * DG_LEVELS * DG_N + lev * DG_N);
+                                const int sa = 4 * h + si;   // A plane; B planes 0 .. 7 - sa, levels sa .. 7
+                                const uint32_t d = tmem + (uint32_t)(a * DG_LEVELS * DG_N + sa * DG_N);
+                                const uint32_t idesc = dg_idesc(DG_N * (DG_LEVELS - sa));
 #pragma unroll
-                                    for (int kk = 0; kk < DG_K / 16; ++kk) {
-                                        const uint64_t ad = tc_desc(base + si * DG_ATILE + kk * 32);
-                                        const uint64_t bd = tc_desc(base + 4 * DG_ATILE + tb * DG_BTILE + kk * 32);
-                                        dg_mma(d, ad, bd, (((started >> lev) & 1u) | (kk > 0 ? 1u : 0u)));
-                                    }
-                                    started |= 1u << lev;
+                                for (int kk = 0; kk < DG_K / 16; ++kk) {
+                                    const uint64_t ad = tc_desc(base + si * DG_ATILE + kk * 32);
+                                    const uint64_t bd = tc_desc(base + 4 * DG_ATILE + kk * 32);
+                                    // the first MMA of a chunk (A plane 0, N = 256) initialises all eight levels
+                                    dg_mma(d, ad, bd, idesc, (started | (kk > 0 ? 1u : 0u)));
                                 }
+                                started = 1u;
                             }
                             tc_commit(&empty[s]);
                         }
@@ -316,31 +345,36 @@ struct DgEpiComb {
     }
 };
 
-// 3-D map over the eight digit planes [8][rows][ld] (K extent Kpad), box 64 x box_rows x box_planes
-inline CUtensorMap digit_map(const bf16 *base, int rows, long long Kpad, long long ld, long long ps, int box_rows,
-                             int box_planes) {
-    if (((uintptr_t)base & 15) || (ld * 2) % 16 || (ps * 2) % 16 || Kpad % DG_K || Kpad > ld)
-        fail(TINCR_BAD_ARG, "digit_map: alignment");
+// 5-D map over a tiled digit operand: (k % 64, r % RT, k / 64, r / RT, plane), box 64 x RT x 1 x 1 x planes
+inline CUtensorMap digit_map(const DgOperand &o, int box_planes) {
+    const long long rt = 1LL << o.rt_shift;
+    if (((uintptr_t)o.p & 15) || o.Kpad % DG_K || o.rows_pad % rt || o.Kpad <= 0 || o.rows_pad <= 0)
+        fail(TINCR_BAD_ARG, "digit_map: layout");
     CUtensorMap m;
-    cuuint64_t dims[3] = {(cuuint64_t)Kpad, (cuuint64_t)rows, (cuuint64_t)DG_PLANES};
-    cuuint64_t strides[2] = {(cuuint64_t)(ld * 2), (cuuint64_t)(ps * 2)};
-    cuuint32_t box[3] = {DG_K, (cuuint32_t)box_rows, (cuuint32_t)box_planes};
-    cuuint32_t estr[3] = {1, 1, 1};
-    CUresult r = tensor_map_encoder()(&m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<bf16 *>(base), dims, strides,
-                                      box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+    cuuint64_t dims[5] = {64, (cuuint64_t)rt, (cuuint64_t)(o.Kpad / 64), (cuuint64_t)(o.rows_pad / rt), DG_PLANES};
+    cuuint64_t strides[4] = {64 * 2, (cuuint64_t)(rt * 64 * 2), (cuuint64_t)(rt * o.Kpad * 2),
+                             (cuuint64_t)(o.rows_pad * o.Kpad * 2)};
+    cuuint32_t box[5] = {64, (cuuint32_t)rt, 1, 1, (cuuint32_t)box_planes};
+    cuuint32_t estr[5] = {1, 1, 1, 1, 1};
+    CUresult r = tensor_map_encoder()(&m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 5, o.p, dims, strides, box, estr,
+                                      CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
                                       CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) fail(TINCR_CUDA_ERR, "cuTensorMapEncodeTiled failed: " + std::to_string((int)r));
     return m;
 }
 
-// C tile loop over A rows [0, M) (digit planes, a_rows allocated rows) and B rows [nb0, nb0 + 32)
-// (b_rows allocated), K = 64 nkb, split into n_ks ranges; persistent grid of at most n_sm CTAs.
+// C tile loop over A rows [0, M) (128-row tiles) and the 32 B rows of row tile nbt, K = 64 nkb (at
+// most the operands' Kpad) split into n_ks ranges; persistent grid of at most n_sm CTAs.
 template <class Epi>
-void gemm_digits(cudaStream_t st, int n_sm, int M, int nkb, int n_ks, const bf16 *A, long long lda, long long psa,
-                 int a_rows, const bf16 *B, long long ldb, long long psb, int b_rows, int nb0, Epi epi, int *d_err) {
+void gemm_digits(cudaStream_t st, int n_sm, int M, int nkb, int n_ks, const DgOperand &A, const DgOperand &B, int nbt,
+                 Epi epi, int *d_err) {
     if (M <= 0 || nkb <= 0) return;
-    const CUtensorMap ma = digit_map(A, a_rows, (long long)nkb * DG_K, lda, psa, DG_M, 4);
-    const CUtensorMap mb = digit_map(B, b_rows, (long long)nkb * DG_K, ldb, psb, DG_N, DG_PLANES);
+    if (A.rt_shift != 7 || B.rt_shift != 5 || (long long)nkb * DG_K > A.Kpad || (long long)nkb * DG_K > B.Kpad ||
+        M > A.rows_pad || (nbt + 1) * 32LL > B.rows_pad)
+        fail(TINCR_BAD_ARG, "gemm_digits: operand layout");
+    const CUtensorMap ma = digit_map(A, 4);
+    const CUtensorMap mb = digit_map(B, DG_PLANES);
+    const CUtensorMap mb4 = digit_map(B, 4);
     static bool attr = false;
     if (!attr) {
         TINCR_CUDA(cudaFuncSetAttribute(gemm_digits_kernel<Epi>, cudaFuncAttributeMaxDynamicSharedMemorySize, DG_SMEM));
@@ -348,7 +382,7 @@ void gemm_digits(cudaStream_t st, int n_sm, int M, int nkb, int n_ks, const bf16
     }
     DgTiles tl{ceil_div(M, DG_M), std::max(1, std::min(n_ks, nkb)), nkb};
     const int ntiles = tl.n_mt * tl.n_ks;
-    gemm_digits_kernel<Epi><<<std::min(ntiles, n_sm), DG_T, DG_SMEM, st>>>(ma, mb, tl, nb0, epi, d_err);
+    gemm_digits_kernel<Epi><<<std::min(ntiles, n_sm), DG_T, DG_SMEM, st>>>(ma, mb, mb4, tl, nbt, epi, d_err);
     count_launch(st, "gemm_digits");
     check_launch("gemm_digits");
 }
