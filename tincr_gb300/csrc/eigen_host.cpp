@@ -173,7 +173,7 @@ bool eigh_upper(int n, const double *a, double *w, double *z) {
 // a: n x n row-major (upper triangle read); w: k eigenvalues ascending; y: y[r * n + i] = component
 // i of eigenvector r.  Returns false on non-finite input.
 //
-// Threads: the tridiagonalisation splits rows cyclically over the team with two barriers per
+// Threads: the tridiagonalisation deals rows to the team in blocks of eight, two barriers per
 // reflection; bisection, inverse iteration and back-transformation run one root per task.  Every
 // value is computed by one thread in a fixed order, so results do not depend on the thread count.
 // ----------------------------------------------------------------------------------------------
@@ -208,8 +208,8 @@ int sturm_count(const double *d, const double *bsq, int n, double x) {
     return c;
 }
 
-// threads for the tridiagonalisation: two barriers per reflection pay off from n ~ 128 (on a
-// 16-core Grace host: n = 300 in 1.9 ms with 16 threads, 5.7 ms with one)
+// threads for the tridiagonalisation: two barriers per reflection pay off from n ~ 128 (16-core
+// Grace host: n = 300 in 1.35 ms with 16 threads, 1.76 ms with 4)
 int tridiag_threads(int n) {
 #ifdef _OPENMP
     return n >= 128 ? std::min(16, omp_get_max_threads()) : 1;
@@ -217,6 +217,17 @@ int tridiag_threads(int n) {
     (void)n;
     return 1;
 #endif
+}
+
+// a . b with eight independent partial sums (vectorisable, fixed order)
+inline double dot8(const double *a, const double *b, int len) {
+    double s[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    int j = 0;
+    for (; j + 8 <= len; j += 8)
+        for (int t = 0; t < 8; ++t) s[t] += a[j + t] * b[j + t];
+    double r = ((s[0] + s[1]) + (s[2] + s[3])) + ((s[4] + s[5]) + (s[6] + s[7]));
+    for (; j < len; ++j) r += a[j] * b[j];
+    return r;
 }
 
 }  // namespace
@@ -233,7 +244,8 @@ bool eigh_lowest_upper(int n, const double *a, int k, double *w, double *y) {
     // 1. T = Q^T A Q.  Reflection c acts on rows/columns c+1..n-1; its vector u (with u_0 = x0 - alpha)
     //    replaces row c to the right of the diagonal (= column c below it), where the back-
     //    transformation reads it.  The full symmetric trailing block is kept up to date.
-    //    Step c: (i) the owner of row c forms the reflection from row c (already updated) into uv (two
+    //    Rows are dealt to threads in blocks of eight (one cache line of p per thread).
+//    Step c: (i) the owner of row c forms the reflection from row c (already updated) into uv (two
     //    buffers by step parity);
     //    barrier; (ii) p = beta A' u on the owned rows and partial u.p; barrier; (iii) K = beta u.p / 2,
     //    q = p - K u, rows -= u q^T + q u^T; the owner of row c+1 updates that row first and forms the
@@ -273,7 +285,7 @@ bool eigh_lowest_upper(int n, const double *a, int k, double *w, double *y) {
         std::vector<double> q(n);
         for (int c = 0; c + 2 < n; ++c) {
             if (skip[c]) {   // identical on every thread: written before the previous barrier
-                if ((c + 1) % nt == me && c + 3 < n) reflect(c + 1);
+                if (((c + 1) >> 3) % nt == me && c + 3 < n) reflect(c + 1);
 #pragma omp barrier
                 continue;
             }
@@ -281,11 +293,8 @@ bool eigh_lowest_upper(int n, const double *a, int k, double *w, double *y) {
             const double *u = uv.data() + (size_t)(c & 1) * n;
             double up = 0.0;
             for (int i = c + 1; i < n; ++i) {
-                if (i % nt != me) continue;
-                const double *row = &A[(size_t)i * n];
-                double acc = 0.0;
-#pragma omp simd reduction(+ : acc)
-                for (int j = c + 1; j < n; ++j) acc += row[j] * u[j];
+                if ((i >> 3) % nt != me) continue;
+                const double acc = dot8(&A[(size_t)i * n + c + 1], u + c + 1, n - c - 1);
                 p[i] = bet * acc;
                 up += u[i] * p[i];
             }
@@ -301,12 +310,12 @@ bool eigh_lowest_upper(int n, const double *a, int k, double *w, double *y) {
 #pragma omp simd
                 for (int j = c + 1; j < n; ++j) row[j] -= ui * q[j] + qi * u[j];
             };
-            if ((c + 1) % nt == me) {
+            if (((c + 1) >> 3) % nt == me) {
                 update(c + 1);
                 if (c + 3 < n) reflect(c + 1);
             }
             for (int i = c + 2; i < n; ++i)
-                if (i % nt == me) update(i);
+                if ((i >> 3) % nt == me) update(i);
 #pragma omp barrier
         }
     }
