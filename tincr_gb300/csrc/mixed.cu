@@ -137,10 +137,7 @@ void Ctx::ao_contract_mixed(int k, int R, int S, const double *V, int P, int Q, 
                        EpiPlaneF{glr32.p, n, (float)ax, Fp, ps, k2, 2LL * n * k2, ac != 0.0 ? d3 : nullptr, d2}, ns);
             if (ac != 0.0) {
                 // z = ac gamma y (FP64), then an FP32 copy for the step-4 epilogue
-                coulomb_kernel<<<kc, 256, n_atoms * sizeof(double), stream>>>(n, n_atoms, d_ao_off.p, d_gamma.p, d3, d2,
-                                                                               z, nullptr, nullptr, ac);
-                count_launch(stream, "coulomb");
-                check_launch("coulomb");
+                launch_coulomb(stream, kc, n, n_atoms, d_ao_off.p, d_gamma.p, d3, d2, z, nullptr, nullptr, ac);
                 to_float(*this, (long long)kc * n, z, z32);
             }
             // step 4: G^T = (F [SC_Q;C_Q] + diag(z, z) [C_Q;SC_Q])^T
@@ -154,13 +151,10 @@ void Ctx::ao_contract_mixed(int k, int R, int S, const double *V, int P, int Q, 
                        EpiPlaneH{H64, ns, 2LL * n * ns, Hp, ps, ks, 2LL * n * ks}, nr);
             if (ac != 0.0) {
                 dim3 g(ceil_div(2LL * n * 32, 256), kc);
-                diag_dots_kernel<<<g, 256, 0, stream>>>(n, ns, H64, stk(S), d3, d2);
+                diag_dots_kernel<<<g, 256, 0, stream>>>(n, ns, H64, ns, 2LL * n * ns, stk(S), d3, d2);
                 count_launch(stream, "diag_dots");
                 check_launch("diag_dots");
-                coulomb_kernel<<<kc, 256, n_atoms * sizeof(double), stream>>>(n, n_atoms, d_ao_off.p, d_gamma.p, d3, d2,
-                                                                               z, nullptr, nullptr, ac);
-                count_launch(stream, "coulomb");
-                check_launch("coulomb");
+                launch_coulomb(stream, kc, n, n_atoms, d_ao_off.p, d_gamma.p, d3, d2, z, nullptr, nullptr, ac);
                 dim3 g2(grid_of(2LL * n * nq, n_sm), kc);
                 scale_rows_kernel<<<g2, 256, 0, stream>>>(n, nq, z, stk(Q), Gc);
                 count_launch(stream, "scale_rows");
@@ -189,6 +183,39 @@ void Ctx::ao_contract_mixed(int k, int R, int S, const double *V, int P, int Q, 
             fail(TINCR_CUDA_ERR, "tensor-core GEMM: a pipeline wait timed out (code " + std::to_string(e) + ")");
         }
     }
+}
+
+// Transition charges of k vectors X (q_ov X per atom) in the mixed form: H = [C_o; SC_o] X_b for all
+// vectors as one three-plane split-BF16 GEMM (M = 2n, N = k v, K = o), then the AO-block diagonals
+// and the atomic sums in FP64 (diag_dots_kernel, launch_coulomb).
+void Ctx::qtrans_mixed(int k, const double *X, double *y_out) {
+    const int n = n_orb, o = n_occ, v = n_virt;
+    if (use_tc && !d_tc_err.p) {
+        d_tc_err.alloc(1);
+        TINCR_CUDA(cudaMemsetAsync(d_tc_err.p, 0, sizeof(int), stream));
+    }
+    const long long kp = pad64(o);
+    const long long pa = 2LL * n * kp, pb = (long long)k * v * kp;
+    mg_bf16.reserve((size_t)N_PLANES * (pa + pb));
+    bf16 *Ap = mg_bf16.p, *Bp = Ap + N_PLANES * pa;
+    split_planes_kernel<<<grid_of(pa, n_sm), 256, 0, stream>>>(1, 2 * n, o, dLst.p, o, 0, 0, Ap, pa, kp, 0);
+    count_launch(stream, "split_planes");
+    check_launch("split_planes");
+    // B rows (b, a) = X_b[:, a] (K = i): the transposed planes of each vector, one after the other
+    split_planes_kernel<<<grid_of(pb, n_sm), 256, 0, stream>>>(k, v, o, X, v, ov, 1, Bp, pb, kp, (long long)v * kp);
+    count_launch(stream, "split_planes");
+    check_launch("split_planes");
+    const long long nh = (long long)k * v;
+    wsH.reserve((size_t)2 * n * nh);
+    wsd3.reserve((size_t)k * n);
+    wsd2.reserve((size_t)k * n);
+    plane_gemm(*this, TINCR_KF_AO_TRANSFORM, 2 * n, (int)nh, kp, PlaneOperand{Ap, pa, kp, 0},
+               PlaneOperand{Bp, pb, kp, 0}, 1, EpiPlaneOut{wsH.p, nh, 0, nullptr, nullptr, 1.0, 0.0}, o);
+    dim3 g(ceil_div(2LL * n * 32, 256), k);
+    diag_dots_kernel<<<g, 256, 0, stream>>>(n, v, wsH.p, nh, v, dRv.p, wsd3.p, wsd2.p);
+    count_launch(stream, "diag_dots");
+    check_launch("diag_dots");
+    launch_coulomb(stream, k, n, n_atoms, d_ao_off.p, d_gamma.p, wsd3.p, wsd2.p, nullptr, nullptr, y_out, 1.0);
 }
 
 // C = alpha op(A) op(B) + beta C (row-major FP64 in and out) on the three-plane tensor-core GEMM:

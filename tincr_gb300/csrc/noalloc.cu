@@ -79,12 +79,11 @@ void products_noalloc(Ctx &c, int k, const double *X, double *AX) {
                                   EpiLcHadamard{F, c.d_glr_ao.p, d3, d2, n, -0.25});
         } else {
             dim3 g(ceil_div(2LL * n * 32, 256), 1);
-            diag_dots_kernel<<<g, 256, 0, st>>>(n, v, H, c.dRv.p, d3, d2);
+            diag_dots_kernel<<<g, 256, 0, st>>>(n, v, H, v, 2LL * n * v, c.dRv.p, d3, d2);
             check_launch("diag_dots");
         }
-        coulomb_kernel<<<1, 256, c.n_atoms * sizeof(double), st>>>(n, c.n_atoms, c.d_ao_off.p, c.d_gamma.p, d3, d2,
-                                                                   c.lc ? nullptr : z, c.lc ? F : nullptr, nullptr, 1.0);
-        check_launch("coulomb");
+        launch_coulomb(st, 1, n, c.n_atoms, c.d_ao_off.p, c.d_gamma.p, d3, d2, c.lc ? nullptr : z, c.lc ? F : nullptr,
+                       nullptr, 1.0);
         if (c.lc) {
             gemm_f64<false, false>(st, 2 * n, v, 2 * n, F, 2 * n, 0, c.dRsw.p, v, 0, 1, EpiStore{G, 0, v, 1.0, 0.0});
         } else {

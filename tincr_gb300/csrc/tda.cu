@@ -28,6 +28,7 @@
 #include <cooperative_groups.h>
 
 #include "common.cuh"
+#include "kernels.cuh"
 #include "gemm_f64.cuh"
 #include "ops.cuh"
 #include "subspace.cuh"
@@ -107,14 +108,15 @@ __global__ void trans_charges_kernel(int n, int n_atoms, const int *__restrict__
 }
 
 // Diagonals of the AO blocks without forming them: with H_b = [C_R; SC_R] V_b and St = [C_S; SC_S],
-// d3[b][mu] = sum_s H_b[mu][s] St[n+mu][s], d2[b][mu] = sum_s H_b[n+mu][s] St[mu][s]
-__global__ void diag_dots_kernel(int n, int v, const double *__restrict__ H, const double *__restrict__ Rv,
-                                 double *d3, double *d2) {
+// d3[b][mu] = sum_s H_b[mu][s] St[n+mu][s], d2[b][mu] = sum_s H_b[n+mu][s] St[mu][s];
+// row m of H_b at H + b * sbh + m * ldh
+__global__ void diag_dots_kernel(int n, int v, const double *__restrict__ H, long long ldh, long long sbh,
+                                 const double *__restrict__ Rv, double *d3, double *d2) {
     int b = blockIdx.y;
     int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if (warp >= 2 * n) return;
     int mu = warp < n ? warp : warp - n;
-    const double *h = H + (long long)b * 2 * n * v + (long long)warp * v;
+    const double *h = H + (long long)b * sbh + (long long)warp * ldh;
     const double *r = Rv + (long long)(warp < n ? n + mu : mu) * v;
     double s = 0.0;
     for (int a = lane; a < v; a += 32) s += h[a] * r[a];
@@ -122,37 +124,51 @@ __global__ void diag_dots_kernel(int n, int v, const double *__restrict__ H, con
     if (lane == 0) (warp < n ? d3 : d2)[(long long)b * n + mu] = s;
 }
 
-// Coulomb: y_A = 1/2 sum_{mu in A}(d3 + d2); z = gamma y; zao_mu = z_{A(mu)}.  One CTA per vector.
-// Optionally adds zao to F's off-diagonal-block diagonals (LC) and writes y (transition charges).
-__global__ void coulomb_kernel(int n, int n_atoms, const int *__restrict__ ao_off, const double *__restrict__ gamma,
-                               const double *__restrict__ d3, const double *__restrict__ d2, double *zao,
-                               double *F, double *y_out, double scale) {
+// Coulomb: y_A = 1/2 sum_{mu in A}(d3 + d2); z = gamma y; zao_mu = z_{A(mu)}.  Grid (atoms / 8,
+// vectors): every CTA forms y of its vector, each warp one z_A.  Optionally adds zao to F's
+// off-diagonal-block diagonals (LC) and writes y (transition charges).
+__global__ void __launch_bounds__(256)
+coulomb_kernel(int n, int n_atoms, const int *__restrict__ ao_off, const double *__restrict__ gamma,
+               const double *__restrict__ d3, const double *__restrict__ d2, double *zao, double *F, double *y_out,
+               double scale) {
     extern __shared__ double sh[];
     double *y = sh;            // [n_atoms]
-    int b = blockIdx.x;
+    const int b = blockIdx.y;
     const double *D3 = d3 + (long long)b * n, *D2 = d2 + (long long)b * n;
     for (int A = threadIdx.x; A < n_atoms; A += blockDim.x) {
         double s = 0.0;
         for (int mu = ao_off[A]; mu < ao_off[A + 1]; ++mu) s += D3[mu] + D2[mu];
         y[A] = 0.5 * s;
-        if (y_out) y_out[(long long)b * n_atoms + A] = 0.5 * s;
+        if (y_out && blockIdx.x == 0) y_out[(long long)b * n_atoms + A] = 0.5 * s;
     }
     __syncthreads();
-    int n2 = 2 * n;
-    for (int A = threadIdx.x; A < n_atoms; A += blockDim.x) {
-        const double *g = gamma + (long long)A * n_atoms;
-        double z = 0.0;
-        for (int B = 0; B < n_atoms; ++B) z += g[B] * y[B];
-        z *= scale;
-        for (int mu = ao_off[A]; mu < ao_off[A + 1]; ++mu) {
-            if (zao) zao[(long long)b * n + mu] = z;
-            if (F) {
-                double *f = F + (long long)b * n2 * n2;
-                f[(long long)mu * n2 + n + mu] += z;
-                f[(long long)(n + mu) * n2 + mu] += z;
-            }
+    // one warp per atom: z_A = scale sum_B gamma_AB y_B (coalesced gamma row)
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int A = blockIdx.x * COULOMB_ATOMS + warp;
+    if (A >= n_atoms) return;
+    const double *g = gamma + (long long)A * n_atoms;
+    double z = 0.0;
+    for (int B = lane; B < n_atoms; B += 32) z += g[B] * y[B];
+    for (int off = 16; off; off >>= 1) z += __shfl_xor_sync(0xffffffffu, z, off);
+    z *= scale;
+    const int n2 = 2 * n;
+    for (int mu = ao_off[A] + lane; mu < ao_off[A + 1]; mu += 32) {
+        if (zao) zao[(long long)b * n + mu] = z;
+        if (F) {
+            double *f = F + (long long)b * n2 * n2;
+            f[(long long)mu * n2 + n + mu] += z;
+            f[(long long)(n + mu) * n2 + mu] += z;
         }
     }
+}
+
+void launch_coulomb(cudaStream_t st, int kc, int n, int n_atoms, const int *ao_off, const double *gamma,
+                    const double *d3, const double *d2, double *zao, double *F, double *y_out, double scale) {
+    dim3 g(ceil_div(n_atoms, COULOMB_ATOMS), kc);
+    coulomb_kernel<<<g, 32 * COULOMB_ATOMS, n_atoms * sizeof(double), st>>>(n, n_atoms, ao_off, gamma, d3, d2, zao, F,
+                                                                            y_out, scale);
+    count_launch(st, "coulomb");
+    check_launch("coulomb");
 }
 
 // F diagonal-only (no exchange term): G_b = F_b [SC_Q; C_Q] = diag(z, z) [C_Q; SC_Q]
@@ -606,17 +622,14 @@ void Ctx::ao_contract(int k, int R, int S, const double *V, int P, int Q, double
                                EpiLcHadamard{wsF.p, d_glr_ao.p, wsd3.p, wsd2.p, n, ax});
         } else if (ac != 0.0) {
             dim3 g(ceil_div(2LL * n * 32, 256), kc);
-            diag_dots_kernel<<<g, 256, 0, stream>>>(n, ns, wsH.p, stk(S), wsd3.p, wsd2.p);
+            diag_dots_kernel<<<g, 256, 0, stream>>>(n, ns, wsH.p, ns, 2LL * n * ns, stk(S), wsd3.p, wsd2.p);
             count_launch(stream, "diag_dots");
             check_launch("diag_dots");
         }
         // 3. Coulomb: z = ac gamma y on the diagonals of F's off-diagonal blocks (or as a row scale)
         if (ac != 0.0) {
-            coulomb_kernel<<<kc, 256, n_atoms * sizeof(double), stream>>>(
-                n, n_atoms, d_ao_off.p, d_gamma.p, wsd3.p, wsd2.p, exch ? nullptr : wsz.p, exch ? wsF.p : nullptr,
-                nullptr, ac);
-            count_launch(stream, "coulomb");
-            check_launch("coulomb");
+            launch_coulomb(stream, kc, n, n_atoms, d_ao_off.p, d_gamma.p, wsd3.p, wsd2.p, exch ? nullptr : wsz.p,
+                           exch ? wsF.p : nullptr, nullptr, ac);
         }
         // 4. G_b = F_b [SC_Q; C_Q]
         if (exch) {
@@ -650,6 +663,10 @@ void Ctx::products_dev(int k, const double *X, double *AX, double *) {
 
 // q_ov X per atom only (transition charges of the vectors): steps 1 and the diagonal dots.
 void Ctx::qtrans_dev(int k, const double *X, double *y_out) {
+    if (solve_prec == TINCR_PREC_BF16X3) {   // mixed form: the half transform on the tensor cores
+        qtrans_mixed(k, X, y_out);
+        return;
+    }
     const int n = n_orb, o = n_occ, v = n_virt;
     const int kc_max = product_chunk();
     wsH.reserve((size_t)kc_max * 2 * n * v);
@@ -660,14 +677,11 @@ void Ctx::qtrans_dev(int k, const double *X, double *y_out) {
         gemm_f64<false, false>(stream, 2 * n, v, o, dLst.p, o, 0, X + (long long)c0 * ov, v, ov, kc,
                                EpiStore{wsH.p, 2LL * n * v, v, 1.0, 0.0});
         dim3 g(ceil_div(2LL * n * 32, 256), kc);
-        diag_dots_kernel<<<g, 256, 0, stream>>>(n, v, wsH.p, dRv.p, wsd3.p, wsd2.p);
+        diag_dots_kernel<<<g, 256, 0, stream>>>(n, v, wsH.p, v, 2LL * n * v, dRv.p, wsd3.p, wsd2.p);
         count_launch(stream, "diag_dots");
         check_launch("diag_dots");
-        coulomb_kernel<<<kc, 256, n_atoms * sizeof(double), stream>>>(n, n_atoms, d_ao_off.p, d_gamma.p, wsd3.p,
-                                                                      wsd2.p, nullptr, nullptr,
-                                                                      y_out + (long long)c0 * n_atoms, 1.0);
-        count_launch(stream, "coulomb");
-        check_launch("coulomb");
+        launch_coulomb(stream, kc, n, n_atoms, d_ao_off.p, d_gamma.p, wsd3.p, wsd2.p, nullptr, nullptr,
+                       y_out + (long long)c0 * n_atoms, 1.0);
     }
 }
 

@@ -153,6 +153,7 @@ struct Ctx {
                            double alpha, double beta, const double *Xomega);
     void products_dev(int k, const double *X, double *AX, double *y_out);
     void qtrans_dev(int k, const double *X, double *y_out);
+    void qtrans_mixed(int k, const double *X, double *y_out);
     void products(int k, const double *X, double *AX, int precision);
     void set_parameters(int n_kinds, const int *kind_z, const int *kind_norb, const int *kind_l, const int *kind_m,
                         const double *kind_hubbard, const double *kind_occ, int n_knots, const double *knots,
