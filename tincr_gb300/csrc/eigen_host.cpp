@@ -208,11 +208,12 @@ int sturm_count(const double *d, const double *bsq, int n, double x) {
     return c;
 }
 
-// threads for the tridiagonalisation: two barriers per reflection pay off from n ~ 128 (16-core
-// Grace host: n = 300 in 1.35 ms with 16 threads, 1.76 ms with 4)
+// threads for the tridiagonalisation: two barriers per reflection pay off from n ~ 128.  Eight
+// threads come within 10% of sixteen on a 16-core Grace host (n = 300: 1.45 ms vs 1.35 ms) and leave
+// cores to the CUDA driver and the caller, so a preempted thread does not stall every barrier.
 int tridiag_threads(int n) {
 #ifdef _OPENMP
-    return n >= 128 ? std::min(16, omp_get_max_threads()) : 1;
+    return n >= 128 ? std::min(8, omp_get_max_threads()) : 1;
 #else
     (void)n;
     return 1;
@@ -343,7 +344,12 @@ bool eigh_lowest_upper(int n, const double *a, int k, double *w, double *y) {
     const double tiny = eps * std::max(tnorm, 1e-300);
     const double ortol = 1e-3 * tnorm;
     // one parallel region for the root phases (each region start wakes the team)
-#pragma omp parallel if (par_roots)
+#ifdef _OPENMP
+    const int root_threads = std::min(12, omp_get_max_threads());
+#else
+    const int root_threads = 1;
+#endif
+#pragma omp parallel num_threads(root_threads) if (par_roots)
     {
 #pragma omp for schedule(dynamic, 1)
     for (int r = 0; r < k; ++r) {

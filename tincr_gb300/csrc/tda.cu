@@ -245,91 +245,91 @@ __global__ void row_sq_finish_kernel(int rows, int chunks, const double *__restr
 
 // Sequential Gram-Schmidt of the kadd correction vectors T against the vectors accepted in this step
 // (davidson.rs:162-168): t -= sum_i (q_i . t) q_i over the accepted q_i, then accept t / |t| when
-// |t| > 1e-8 (and the basis has room), else drop it.  One cooperative launch, two grid barriers per
-// vector: (1) partial dots, (2) t' = t - sum c_i q_i written to its destination row with partial
-// |t'|^2.  The normalisation is deferred: an accepted row is kept as t' with the factor 1/|t'|, which
-// the dots and updates of the next vectors apply, and every accepted row is scaled in place at the
-// end.  Every CTA takes the same accept / drop decisions from partial sums reduced in a fixed order.
-// state[0]: m out; state[1]: 1 if a norm was not finite.  part: [gridDim.x][34] doubles.
+// |t| > 1e-8 (and the basis has room), else drop it.  One cooperative launch, one grid barrier per
+// vector: the pass that forms t'_j = t_j - sum_i c_i q_i (into its destination row) and |t'_j|^2
+// also accumulates the dots of the next vector t_{j+1} with every accepted q_i and with t'_j, so the
+// accepted rows are read once per vector.  After the barrier every CTA reduces the partial sums in
+// the same fixed order and takes the same decision; when t'_j is accepted its dot with t_{j+1} joins
+// the next coefficients.  Normalisation is deferred: an accepted row is kept as t' with the factor
+// 1/|t'|, which the coefficients apply, and every accepted row is scaled in place at the end.
+// state[0]: m out; state[1]: 1 if a norm was not finite.  part: [2][gridDim.x][GS_SLOTS] doubles.
+constexpr int GS_MAX = 32, GS_SLOTS = GS_MAX + 2;
 __global__ void __launch_bounds__(256) seq_gs_kernel(int kadd, long long ov, int m0, int mmax, double *V, double *T,
                                                      double *part, int *state) {
     cg::grid_group grid = cg::this_grid();
-    __shared__ double c[32], sc[32];
-    __shared__ double red[8][9];
+    __shared__ double c[GS_MAX], sc[GS_MAX];
+    __shared__ double red[8][GS_SLOTS];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const long long stride = (long long)gridDim.x * blockDim.x;
     const long long x0 = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     int m = m0;
     bool finite = true;
+    int ncoef = 0;   // coefficients c[0 .. ncoef) of the current vector (its dots with the accepted rows)
     for (int j = 0; j < kadd && finite; ++j) {
-        const double *t = T + (long long)j * ov;
         const int acc = m - m0;
-        // 1. partial dots d_i = t'_i . t of the accepted (unscaled) rows, eight at a time
-        for (int i0 = 0; i0 < acc; i0 += 8) {
-            double s[8];
-#pragma unroll
-            for (int q = 0; q < 8; ++q) s[q] = 0.0;
-            for (long long x = x0; x < ov; x += stride) {
-                const double tx = t[x];
-#pragma unroll
-                for (int q = 0; q < 8; ++q)
-                    if (i0 + q < acc) s[q] += V[(long long)(m0 + i0 + q) * ov + x] * tx;
-            }
-#pragma unroll
-            for (int q = 0; q < 8; ++q) {
-                for (int off = 16; off; off >>= 1) s[q] += __shfl_down_sync(0xffffffffu, s[q], off);
-                if (lane == 0) red[warp][q] = s[q];
-            }
-            __syncthreads();
-            if (threadIdx.x < 8) {
-                double v = 0.0;
-                for (int w = 0; w < 8; ++w) v += red[w][threadIdx.x];
-                part[(long long)blockIdx.x * 34 + i0 + threadIdx.x] = v;
-            }
-            __syncthreads();
-        }
-        if (acc > 0) grid.sync();
-        // 2. c_i = d_i / |t'_i|^2 in a fixed order; t' = t - sum_i c_i t'_i into its destination row
-        //    (the next basis row, or back into T when the basis is full); partial |t'|^2
-        if (threadIdx.x < acc) {
-            double v = 0.0;
-            for (int b = 0; b < (int)gridDim.x; ++b) v += part[(long long)b * 34 + threadIdx.x];
-            c[threadIdx.x] = v * sc[threadIdx.x] * sc[threadIdx.x];
-        }
-        __syncthreads();
+        const double *t = T + (long long)j * ov;
+        const double *tn = j + 1 < kadd ? T + (long long)(j + 1) * ov : nullptr;
         double *dst = m < mmax ? V + (long long)m * ov : T + (long long)j * ov;
+        double d[GS_MAX + 1];
+#pragma unroll
+        for (int i = 0; i <= GS_MAX; ++i) d[i] = 0.0;
         double sq = 0.0;
         for (long long x = x0; x < ov; x += stride) {
             double v = t[x];
-            for (int i = 0; i < acc; ++i) v -= c[i] * V[(long long)(m0 + i) * ov + x];
+            const double tnx = tn ? tn[x] : 0.0;
+#pragma unroll
+            for (int i = 0; i < GS_MAX; ++i)
+                if (i < acc) {
+                    const double q = V[(long long)(m0 + i) * ov + x];
+                    if (i < ncoef) v -= c[i] * q;
+                    d[i] += q * tnx;
+                }
             dst[x] = v;
             sq += v * v;
+            d[GS_MAX] += v * tnx;
         }
-        for (int off = 16; off; off >>= 1) sq += __shfl_down_sync(0xffffffffu, sq, off);
-        if (lane == 0) red[warp][8] = sq;
+        // block partials: slots 0 .. acc-1 (dots with q_i), GS_MAX (dot with t'_j), GS_MAX + 1 (|t'_j|^2)
+        double *pb = part + ((long long)(j & 1) * gridDim.x + blockIdx.x) * GS_SLOTS;
+        for (int i = 0; i < GS_SLOTS; ++i) {
+            const bool used = i < acc || i >= GS_MAX;
+            if (!used) continue;   // uniform over the block
+            double v = i < GS_MAX ? d[i] : (i == GS_MAX ? d[GS_MAX] : sq);
+            for (int off = 16; off; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+            if (lane == 0) red[warp][i] = v;
+        }
         __syncthreads();
-        const int slot = 32 + (j & 1);   // alternates: a CTA may run ahead into the next vector
-        if (threadIdx.x == 0) {
+        if (threadIdx.x < GS_SLOTS && (threadIdx.x < acc || threadIdx.x >= GS_MAX)) {
             double v = 0.0;
-            for (int w = 0; w < 8; ++w) v += red[w][8];
-            part[(long long)blockIdx.x * 34 + slot] = v;
+            for (int w = 0; w < 8; ++w) v += red[w][threadIdx.x];
+            pb[threadIdx.x] = v;
         }
         grid.sync();
-        // 3. the norm (fixed order, the same in every CTA): accept or drop
-        double v = 0.0;
-        for (int b = 0; b < (int)gridDim.x; ++b) v += part[(long long)b * 34 + slot];
-        const double nrm = sqrt(v);
+        // every CTA: the norm of t'_j (fixed order), accept or drop, the next vector's coefficients
+        const double *pj = part + (long long)(j & 1) * gridDim.x * GS_SLOTS;
+        double nsq = 0.0;
+        for (int b = 0; b < (int)gridDim.x; ++b) nsq += pj[(long long)b * GS_SLOTS + GS_MAX + 1];
+        const double nrm = sqrt(nsq);
         if (!isfinite(nrm)) {
             if (blockIdx.x == 0 && threadIdx.x == 0) state[1] = 1;
             finite = false;   // every CTA sees the same norm
-        } else if (nrm > 1.0e-8 && m < mmax) {
-            if (threadIdx.x == 0) sc[acc] = 1.0 / nrm;
-            ++m;
+            break;
+        }
+        const bool accept = nrm > 1.0e-8 && m < mmax;
+        __syncthreads();   // c and sc of this vector are no longer read
+        if (threadIdx.x < acc || (accept && threadIdx.x == acc)) {
+            const int i = threadIdx.x;
+            double v = 0.0;
+            const int slot = i < acc ? i : GS_MAX;
+            for (int b = 0; b < (int)gridDim.x; ++b) v += pj[(long long)b * GS_SLOTS + slot];
+            const double f = i < acc ? sc[i] : 1.0 / nrm;
+            if (i == acc) sc[i] = f;
+            c[i] = v * f * f;   // (q_i . t_{j+1}) / |t'_i|^2 with the unscaled row t'_i
         }
         __syncthreads();
-        // part[.][0..31] (dots) of the next vector are written after every CTA has passed the barrier
-        // above, i.e. after this vector's phase 2 read them; its norm goes to the other slot, read here
-        // before any CTA passes the next vector's second barrier
+        if (accept) ++m;
+        ncoef = m - m0;
+        // part[(j + 1) & 1] is written next; every CTA has passed the barrier of vector j - 1, whose
+        // partials (same parity) it read before that barrier's successor
     }
     // scale the accepted rows
     for (int i = 0; i < m - m0; ++i) {
@@ -910,7 +910,7 @@ int Ctx::davidson(int n_roots, int max_iter, double tol, bool from_ritz, std::ve
                 // then sequentially against the vectors accepted in this step (davidson.rs:162-168)
                 if (kadd <= 32 && coop_grid > 0) {
                     int slot = prof_begin(TINCR_KF_SUBSPACE);
-                    gs_part.reserve((size_t)coop_grid * 34);
+                    gs_part.reserve((size_t)2 * coop_grid * GS_SLOTS);
                     gs_state.reserve(2);
                     int hstate[2] = {m, 0};
                     TINCR_CUDA(cudaMemcpyAsync(gs_state.p, hstate, 2 * sizeof(int), cudaMemcpyHostToDevice, stream));
