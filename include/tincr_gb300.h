@@ -103,7 +103,8 @@ typedef enum {
     TINCR_KF_OTHER = 4,        /* Coulomb, packing, transition charges, small kernels              */
     TINCR_KF_HOST = 5,         /* host time of the Davidson subspace eigensolver (not a kernel)      */
     TINCR_KF_EIGEN = 6,        /* the subspace eigensolver on one thread-block cluster               */
-    TINCR_KF_COUNT = 7
+    TINCR_KF_DIGITS = 7,       /* FP64-accurate digit GEMMs of the mixed Davidson subspace products  */
+    TINCR_KF_COUNT = 8
 } tincr_kernel_family;
 
 /* Turn per-family kernel timing on (1) or off (0); turning it on clears the statistics. */

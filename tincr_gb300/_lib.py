@@ -16,8 +16,8 @@ OK, NOT_CONVERGED, NONFINITE, BAD_ARG, CUDA_ERR, NO_DEVICE, CG_MAXITER = range(7
 STATUS_NAMES = {0: "OK", 1: "NOT_CONVERGED", 2: "NONFINITE", 3: "BAD_ARG", 4: "CUDA_ERR", 5: "NO_DEVICE",
                 6: "CG_MAXITER"}
 PREC_FP64, PREC_BF16X3 = 0, 1
-KF_AO_EXCHANGE, KF_AO_TRANSFORM, KF_SUBSPACE, KF_GRADIENT, KF_OTHER, KF_HOST, KF_EIGEN = range(7)
-KF_COUNT = 7
+KF_AO_EXCHANGE, KF_AO_TRANSFORM, KF_SUBSPACE, KF_GRADIENT, KF_OTHER, KF_HOST, KF_EIGEN, KF_DIGITS = range(8)
+KF_COUNT = 8
 GRAD_REFERENCE, GRAD_EXACT = 0, 1
 
 _dp = C.POINTER(C.c_double)

@@ -218,14 +218,15 @@ static void dg_dots(Ctx &c, int m, int n, double *out, long long ldo) {
     TINCR_CUDA(cudaMemsetAsync(c.dg_acc.p, 0, (size_t)m * DG_N * 2 * sizeof(unsigned long long), c.stream));
     const int nkb = (int)(c.dg_ovp / DG_K);
     const int n_mt = ceil_div(m, DG_M);
-    const int slot = c.prof_begin(TINCR_KF_SUBSPACE);
+    const int slot = c.prof_begin(TINCR_KF_DIGITS);
     gemm_digits(c.stream, c.n_sm, m, nkb, std::max(1, c.n_sm / n_mt), opV(c), opB(c), 0, DgEpiAtomic{c.dg_acc.p, m, n, DG_N},
                 c.d_tc_err.p);
     dg_finalize_kernel<<<ceil_div((long long)m * n, 256), 256, 0, c.stream>>>(m, n, c.dg_acc.p, DG_N, c.dg_eV.p, c.dg_eB.p,
                                                                              out, ldo);
     count_launch(c.stream, "dg_finalize");
     check_launch("dg_finalize");
-    c.prof_end(slot, 2.0 * m * (double)n * c.ov, 2.0 * DG_PLANES * (double)(m + n) * c.dg_ovp);
+    // algorithmic bytes: the digit planes of both operands read once and the int64 sums
+    c.prof_end(slot, 2.0 * m * (double)n * c.ov, 2.0 * DG_PLANES * (double)(m + DG_N) * c.dg_ovp + 16.0 * m * n);
 }
 
 // combination out_r(x) (mode of DgEpiComb) = sum_{i < m} A_i(x) Y(r, i), r < k, A = V (or AV) columns
@@ -234,11 +235,14 @@ static void dg_comb(Ctx &c, bool av, int k, int m, const double *Y, long long ys
     dg_comb_b_kernel<<<DG_N, 256, 0, c.stream>>>(k, m, Y, ysr, ysi, av ? c.dg_eAV.p : c.dg_eV.p, opC(c), c.dg_scale.p);
     count_launch(c.stream, "dg_comb_b");
     check_launch("dg_comb_b");
-    const int slot = c.prof_begin(TINCR_KF_SUBSPACE);
+    const int slot = c.prof_begin(TINCR_KF_DIGITS);
     const int nkb = ceil_div(m, DG_K);
     gemm_digits(c.stream, c.n_sm, (int)c.ov, nkb, 1, opVT(c, av), opC(c), 0,
                 DgEpiComb{out, c.ov, c.dg_scale.p, (int)c.ov, k, mode, R, u}, c.d_tc_err.p);
-    c.prof_end(slot, 2.0 * k * (double)m * c.ov, 2.0 * DG_PLANES * (double)m * c.ov + 8.0 * k * c.ov * (mode ? 2 : 1));
+    // algorithmic bytes: the digit planes of both operands (K padded to 64) read once and the FP64
+    // output written (read as well for the residual and the update)
+    c.prof_end(slot, 2.0 * k * (double)m * c.ov,
+               2.0 * DG_PLANES * 64.0 * nkb * ((double)c.ov + DG_N) + 8.0 * k * c.ov * (mode ? 2 : 1));
 }
 
 void Ctx::dg_project(int m, int mold, int knew, double *P, int ldp) { dg_dots(*this, m, knew, P + mold, ldp); }
