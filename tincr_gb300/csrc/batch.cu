@@ -636,7 +636,9 @@ __global__ void bt_restart_kernel(BtArrays a) {
 // subspace step: one CTA per instance
 // ----------------------------------------------------------------------------------------------
 
-// sum over the CTA of NV values per thread; every thread receives the totals
+// sum over the CTA of NV values per thread; every thread receives the totals.  The warp partials
+// are added by NV lanes of warp 0 only (GB300's FP64 unit takes ~64 cycles per warp instruction, so
+// the adds are not repeated in every warp).  red: (BT_T / 32 + 1) * NV doubles.
 template <int NV>
 __device__ __forceinline__ void bt_block_sum(double (&v)[NV], double *red) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -648,25 +650,81 @@ __device__ __forceinline__ void bt_block_sum(double (&v)[NV], double *red) {
 #pragma unroll
         for (int q = 0; q < NV; ++q) red[warp * NV + q] = v[q];
     __syncthreads();
-#pragma unroll
-    for (int q = 0; q < NV; ++q) {
+    double *tot = red + (BT_T / 32) * NV;
+    if (threadIdx.x < NV) {
         double s = 0.0;
-        for (int w = 0; w < BT_T / 32; ++w) s += red[w * NV + q];
-        v[q] = s;
+        for (int w = 0; w < BT_T / 32; ++w) s += red[w * NV + threadIdx.x];
+        tot[threadIdx.x] = s;
     }
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < NV; ++q) v[q] = tot[q];
     __syncthreads();
 }
 
-// number of eigenvalues of the symmetric tridiagonal (d, e) below x (Sturm count of T - x I)
-__device__ __forceinline__ int bt_sturm(const double *d, const double *e, int m, double x, double pivmin) {
-    int c = 0;
-    double q = d[0] - x;
-    if (fabs(q) < pivmin) q = -pivmin;
-    if (q < 0.0) ++c;
+// sum over the CTA of eight values per thread; every thread receives the totals.  Within a warp the
+// eight sums are reduced by halving exchanges (lanes 0-15 keep values 0-3 and receive them from lanes
+// 16-31, and so on): 9 shuffle-adds instead of 40.  red: (BT_T / 32 + 1) * 8 doubles.
+__device__ __forceinline__ void bt_block_sum8(double (&v)[8], double *red) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const bool h16 = lane & 16, h8 = lane & 8, h4 = lane & 4;
+    double a[4], b[2], c;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const double send = h16 ? v[q] : v[q + 4], keep = h16 ? v[q + 4] : v[q];
+        a[q] = keep + __shfl_xor_sync(0xffffffffu, send, 16);
+    }
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+        const double send = h8 ? a[q] : a[q + 2], keep = h8 ? a[q + 2] : a[q];
+        b[q] = keep + __shfl_xor_sync(0xffffffffu, send, 8);
+    }
+    {
+        const double send = h4 ? b[0] : b[1], keep = h4 ? b[1] : b[0];
+        c = keep + __shfl_xor_sync(0xffffffffu, send, 4);
+    }
+    c += __shfl_xor_sync(0xffffffffu, c, 2);
+    c += __shfl_xor_sync(0xffffffffu, c, 1);
+    // lane L now holds the warp total of value (L >> 2) & 7
+    __syncthreads();
+    if ((lane & 3) == 0) red[warp * 8 + ((lane >> 2) & 7)] = c;
+    __syncthreads();
+    double *tot = red + (BT_T / 32) * 8;
+    if (threadIdx.x < 8) {
+        double s = 0.0;
+        for (int w = 0; w < BT_T / 32; ++w) s += red[w * 8 + threadIdx.x];
+        tot[threadIdx.x] = s;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < 8; ++q) v[q] = tot[q];
+    __syncthreads();
+}
+
+// Number of eigenvalues of the symmetric tridiagonal (d, squared off-diagonal esq) below x: the
+// sign changes of the leading principal minors N_i = (d_i - x) N_{i-1} - e_{i-1}^2 N_{i-2}, a
+// division-free recurrence (3 FP64 operations per row instead of a division), rescaled by a power
+// of two when N_i leaves [2^-400, 2^400]; an exact zero becomes a tiny value of the other sign.
+__device__ __forceinline__ int bt_sturm(const double *d, const double *esq, int m, double x) {
+    double n0 = 1.0, n1 = d[0] - x;
+    if (n1 == 0.0) n1 = -0x1p-100;
+    int c = __double2hiint(n1) < 0;
     for (int i = 1; i < m; ++i) {
-        q = d[i] - x - e[i - 1] * e[i - 1] / q;
-        if (fabs(q) < pivmin) q = -pivmin;
-        if (q < 0.0) ++c;
+        double n2 = fma(d[i] - x, n1, -(esq[i - 1] * n0));
+        const long long bits = __double_as_longlong(n2);
+        if ((bits << 1) == 0) {
+            n2 = -0x1p-100 * n1;
+        } else {
+            const int ex = (int)((bits >> 52) & 0x7ff);
+            if ((ex > 1023 + 400 || ex < 1023 - 400) && ex < 2047) {
+                const double sc = __longlong_as_double((long long)(2046 - ex) << 52);   // 2^(1023 - ex)
+                n1 *= sc;
+                n2 *= sc;
+            }
+        }
+        c += (int)(((unsigned)__double2hiint(n1) ^ (unsigned)__double2hiint(n2)) >> 31);
+        n0 = n1;
+        n1 = n2;
     }
     return c;
 }
@@ -689,23 +747,22 @@ __device__ void bt_eig_lowest(int m, int nr, double *A, double *W, double *w, do
             s2[0] += x * x;
         }
         bt_block_sum<1>(s2, red);
-        const double x0 = A[(k + 1) * m + k];
-        if (s2[0] == 0.0) {
-            if (tid == 0) { beta[k] = 0.0; e[k] = x0; d[k] = A[k * m + k]; }
+        if (s2[0] == 0.0) {   // the same in every thread
+            if (tid == 0) { beta[k] = 0.0; e[k] = A[(k + 1) * m + k]; d[k] = A[k * m + k]; }
             __syncthreads();
             continue;
         }
-        const double nx = sqrt(x0 * x0 + s2[0]);
-        const double alpha = x0 > 0.0 ? -nx : nx;
-        const double bet = 1.0 / (alpha * (alpha - x0));   // H = I - bet u u^T, u = x - alpha e_1
-        __syncthreads();
-        if (tid == 0) {
+        if (tid == 0) {   // H = I - bet u u^T, u = x - alpha e_1 (one thread: FP64 chains are slow)
+            const double x0 = A[(k + 1) * m + k];
+            const double nx = sqrt(x0 * x0 + s2[0]);
+            const double alpha = x0 > 0.0 ? -nx : nx;
             A[(k + 1) * m + k] = x0 - alpha;
-            beta[k] = bet;
+            beta[k] = 1.0 / (alpha * (alpha - x0));
             e[k] = alpha;
             d[k] = A[k * m + k];
         }
         __syncthreads();
+        const double bet = beta[k];
         for (int i = tid; i < n1; i += BT_T) {              // p = bet A' u
             const double *row = A + (size_t)(k + 1 + i) * m + (k + 1);
             double acc = 0.0;
@@ -734,27 +791,41 @@ __device__ void bt_eig_lowest(int m, int nr, double *A, double *W, double *w, do
         e[m - 1] = 0.0;
     }
     __syncthreads();
-    // 2. eigenvalues: Gershgorin interval, then multisection per root
-    double lo = 1e300, hi = -1e300, emax2 = 0.0;
-    for (int i = 0; i < m; ++i) {
-        const double r = fabs(e[i]) + (i > 0 ? fabs(e[i - 1]) : 0.0);
-        lo = fmin(lo, d[i] - r);
-        hi = fmax(hi, d[i] + r);
-        emax2 = fmax(emax2, e[i] * e[i]);
+    // 2. eigenvalues: Gershgorin interval (warp 0), then multisection per root; p holds e^2
+    if (warp == 0) {
+        double glo = 1e300, ghi = -1e300, emax2 = 0.0;
+        for (int i = lane; i < m; i += 32) {
+            const double r = fabs(e[i]) + (i > 0 ? fabs(e[i - 1]) : 0.0);
+            glo = fmin(glo, d[i] - r);
+            ghi = fmax(ghi, d[i] + r);
+            p[i] = e[i] * e[i];
+            emax2 = fmax(emax2, p[i]);
+        }
+        for (int off = 16; off; off >>= 1) {
+            glo = fmin(glo, __shfl_xor_sync(0xffffffffu, glo, off));
+            ghi = fmax(ghi, __shfl_xor_sync(0xffffffffu, ghi, off));
+            emax2 = fmax(emax2, __shfl_xor_sync(0xffffffffu, emax2, off));
+        }
+        if (lane == 0) {
+            red[0] = glo;
+            red[1] = ghi;
+            red[2] = emax2;
+        }
     }
+    __syncthreads();
     const double eps = 2.220446049250313e-16;
-    const double tnorm = fmax(fabs(lo), fabs(hi));
-    const double pivmin = 2.2250738585072014e-308 * fmax(1.0, emax2);
-    lo -= 2.0 * eps * tnorm + 2.0 * pivmin;
-    hi += 2.0 * eps * tnorm + 2.0 * pivmin;
+    const double tnorm = fmax(fabs(red[0]), fabs(red[1]));
+    const double pivmin = 2.2250738585072014e-308 * fmax(1.0, red[2]);
+    const double lo = red[0] - (2.0 * eps * tnorm + 2.0 * pivmin);
+    const double hi = red[1] + (2.0 * eps * tnorm + 2.0 * pivmin);
     if (warp < nr) {
         const int r = warp;
         double a = lo, b = hi;
         for (int it = 0; it < 64; ++it) {
             if (b - a <= 2.0 * eps * fmax(fabs(a), fabs(b)) + 4.0 * pivmin) break;
-            const double h = (b - a) / 33.0;
+            const double h = (b - a) * (1.0 / 33.0);
             const double x = a + h * (lane + 1);
-            const unsigned ball = __ballot_sync(0xffffffffu, bt_sturm(d, e, m, x, pivmin) > r);
+            const unsigned ball = __ballot_sync(0xffffffffu, bt_sturm(d, p, m, x) > r);
             if (ball == 0u) {
                 a = __shfl_sync(0xffffffffu, x, 31);
             } else {
@@ -803,6 +874,7 @@ __device__ void bt_eig_lowest(int m, int nr, double *A, double *W, double *w, do
             }
         }
         if (fabs(dd[m - 1]) < tiny) dd[m - 1] = dd[m - 1] < 0.0 ? -tiny : tiny;
+        for (int i = 0; i < m; ++i) dd[i] = 1.0 / dd[i];   // reciprocal pivots: no division in the solves
         for (int i = 0; i < m; ++i) z[i] = 1.0 + 0.5 * (double)((i * (r + 1) * 7919 + 13 * r) % 97) / 97.0;
         for (int it = 0; it < 3; ++it) {
             for (int i = 0; i + 1 < m; ++i) {            // L^-1 with the interchanges
@@ -814,7 +886,7 @@ __device__ void bt_eig_lowest(int m, int nr, double *A, double *W, double *w, do
                 double s = z[i];
                 if (i + 1 < m) s -= du[i] * z[i + 1];
                 if (i + 2 < m) s -= du2[i] * z[i + 2];
-                z[i] = s / dd[i];
+                z[i] = s * dd[i];
             }
             double nrm = 0.0;
             for (int i = 0; i < m; ++i) nrm += z[i] * z[i];
@@ -823,21 +895,26 @@ __device__ void bt_eig_lowest(int m, int nr, double *A, double *W, double *w, do
         }
     }
     __syncthreads();
-    // Gram-Schmidt of the roots in ascending order (separates vectors of (near-)degenerate roots)
-    if (tid == 0) {
+    // Gram-Schmidt of the roots in ascending order (separates vectors of (near-)degenerate roots),
+    // warp 0 with lanes over the components
+    if (warp == 0) {
         for (int r = 1; r < nr; ++r) {
             double *z = Y + (size_t)r * m;
             for (int pass = 0; pass < 2; ++pass)
                 for (int q = 0; q < r; ++q) {
                     const double *y = Y + (size_t)q * m;
                     double s = 0.0;
-                    for (int i = 0; i < m; ++i) s += y[i] * z[i];
-                    for (int i = 0; i < m; ++i) z[i] -= s * y[i];
+                    for (int i = lane; i < m; i += 32) s += y[i] * z[i];
+                    for (int off = 16; off; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
+                    for (int i = lane; i < m; i += 32) z[i] -= s * y[i];
+                    __syncwarp();
                 }
             double nrm = 0.0;
-            for (int i = 0; i < m; ++i) nrm += z[i] * z[i];
+            for (int i = lane; i < m; i += 32) nrm += z[i] * z[i];
+            for (int off = 16; off; off >>= 1) nrm += __shfl_xor_sync(0xffffffffu, nrm, off);
             nrm = 1.0 / sqrt(nrm);
-            for (int i = 0; i < m; ++i) z[i] *= nrm;
+            for (int i = lane; i < m; i += 32) z[i] *= nrm;
+            __syncwarp();
         }
     }
     __syncthreads();
@@ -862,6 +939,33 @@ __device__ void bt_eig_lowest(int m, int nr, double *A, double *W, double *w, do
 // scratch (4 m + 5 nr m <= mmax^2 doubles since mmax = 15 nr), reductions and Gram-Schmidt dots
 inline size_t bt_subspace_smem(int mmax) {
     return (2 * (size_t)mmax * mmax + 8 * BT_MAXR * (BT_T / 32) + mmax + BT_MAXR + 16 + BT_MAXR) * sizeof(double);
+}
+
+// Ritz vectors and residuals of NR roots over this thread's components; sq[r] += |Rk_r|^2 partials
+template <int NR>
+__device__ __forceinline__ void bt_ritz(int m, long long ov, const double *V, const double *AV, const double *Yev,
+                                        const double *u, double *R, double *Rk, double (&sq)[BT_MAXR]) {
+    for (long long x = threadIdx.x; x < ov; x += BT_T) {
+        double rv[NR], av[NR];
+#pragma unroll
+        for (int r = 0; r < NR; ++r) rv[r] = av[r] = 0.0;
+        for (int i = 0; i < m; ++i) {
+            const double vi = V[(long long)i * ov + x], ai = AV[(long long)i * ov + x];
+#pragma unroll
+            for (int r = 0; r < NR; ++r) {
+                const double y = Yev[r * m + i];
+                rv[r] += y * vi;
+                av[r] += y * ai;
+            }
+        }
+#pragma unroll
+        for (int r = 0; r < NR; ++r) {
+            const double rk = av[r] - u[r] * rv[r];
+            R[(long long)r * ov + x] = rv[r];
+            Rk[(long long)r * ov + x] = rk;
+            sq[r] += rk * rk;
+        }
+    }
 }
 
 __global__ void __launch_bounds__(BT_T) bt_subspace_kernel(BtArrays a) {
@@ -912,32 +1016,18 @@ __global__ void __launch_bounds__(BT_T) bt_subspace_kernel(BtArrays a) {
     const double *Yev = Z + 4 * m;   // eigenvector r at Yev[r * m + i]
     if (tid < nr) s_u[tid] = wev[tid];
     __syncthreads();
-    // 3. Ritz vectors R_r = sum_i y_ir V_i and residuals Rk_r = sum_i y_ir AV_i - u_r R_r (:101-107)
+    // 3. Ritz vectors R_r = sum_i y_ir V_i and residuals Rk_r = sum_i y_ir AV_i - u_r R_r (:101-107),
+    //    with the loop over roots instantiated for this instance's count (no predicated FP64 work)
     double sq[BT_MAXR];
 #pragma unroll
     for (int r = 0; r < BT_MAXR; ++r) sq[r] = 0.0;
-    for (long long x = tid; x < ov; x += BT_T) {
-        double rv[BT_MAXR], av[BT_MAXR];
-#pragma unroll
-        for (int r = 0; r < BT_MAXR; ++r) rv[r] = av[r] = 0.0;
-        for (int i = 0; i < m; ++i) {
-            const double vi = V[(long long)i * ov + x], ai = AV[(long long)i * ov + x];
-#pragma unroll
-            for (int r = 0; r < BT_MAXR; ++r)
-                if (r < nr) {
-                    const double y = Yev[r * m + i];
-                    rv[r] += y * vi;
-                    av[r] += y * ai;
-                }
-        }
-#pragma unroll
-        for (int r = 0; r < BT_MAXR; ++r)
-            if (r < nr) {
-                const double rk = av[r] - s_u[r] * rv[r];
-                R[(long long)r * ov + x] = rv[r];
-                Rk[(long long)r * ov + x] = rk;
-                sq[r] += rk * rk;
-            }
+    switch (nr) {
+    case 1: bt_ritz<1>(m, ov, V, AV, Yev, s_u, R, Rk, sq); break;
+    case 2: bt_ritz<2>(m, ov, V, AV, Yev, s_u, R, Rk, sq); break;
+    case 3: bt_ritz<3>(m, ov, V, AV, Yev, s_u, R, Rk, sq); break;
+    case 4: bt_ritz<4>(m, ov, V, AV, Yev, s_u, R, Rk, sq); break;
+    case 5: bt_ritz<5>(m, ov, V, AV, Yev, s_u, R, Rk, sq); break;
+    default: bt_ritz<BT_MAXR>(m, ov, V, AV, Yev, s_u, R, Rk, sq); break;
     }
     bt_block_sum<BT_MAXR>(sq, red);
     // 4. convergence and the next action (:109-178)
@@ -1007,7 +1097,7 @@ __global__ void __launch_bounds__(BT_T) bt_subspace_kernel(BtArrays a) {
                     for (int q = 0; q < 8; ++q)
                         if (i0 + q < mc) c8[q] += V[(long long)(i0 + q) * ov + x] * tx;
                 }
-                bt_block_sum<8>(c8, red);
+                bt_block_sum8(c8, red);
 #pragma unroll
                 for (int q = 0; q < 8; ++q)
                     if (tid == q) cdot[i0 + q] = c8[q];
