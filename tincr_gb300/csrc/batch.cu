@@ -88,6 +88,61 @@ struct BtStepSC {
     }
 };
 
+// SC = S C for every instance in FP32 on the CUDA cores (mixed form): S and C rounded to FP32,
+// FP32 sums over n <= a few hundred terms, relative error ~1e-7, the accuracy the [C; SC] planes
+// of the mixed products carry anyway.  64 x 64 tile per CTA (tile table of BtStepSC), 4 x 4 per thread.
+__global__ void __launch_bounds__(GB_T) bt_sc32_kernel(const int4 *__restrict__ tiles, BtArrays a) {
+    __shared__ float As[GB_K][GB_M + 1];
+    __shared__ float Bs[GB_K][GB_N + 1];
+    const int4 t = tiles[blockIdx.x];
+    const BtInst &in = a.inst[t.x];
+    const int n = in.n, w = in.o + in.v;
+    const double *S = a.S + in.off_s, *C = a.C + in.off_c;
+    const int m0 = t.z * GB_M, n0 = t.w * GB_N;
+    const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+    float acc[4][4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[i][j] = 0.f;
+    for (int k0 = 0; k0 < n; k0 += GB_K) {
+        for (int e = threadIdx.x; e < GB_K * GB_M; e += GB_T) {
+            const int kk = e % GB_K, mm = e / GB_K;   // A[m][k] = S[m0 + mm][k0 + kk]
+            const int gm = m0 + mm, gk = k0 + kk;
+            As[kk][mm] = (gm < n && gk < n) ? (float)S[(long long)gm * n + gk] : 0.f;
+        }
+        for (int e = threadIdx.x; e < GB_K * GB_N; e += GB_T) {
+            const int nn = e % GB_N, kk = e / GB_N;   // B[k][n] = C[k0 + kk][n0 + nn]
+            const int gk = k0 + kk, gn = n0 + nn;
+            Bs[kk][nn] = (gk < n && gn < w) ? (float)C[(long long)gk * w + gn] : 0.f;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int kk = 0; kk < GB_K; ++kk) {
+            float av[4], bv[4];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) av[i] = As[kk][ty + 16 * i];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) bv[j] = Bs[kk][tx + 16 * j];
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+#pragma unroll
+                for (int j = 0; j < 4; ++j) acc[i][j] = fmaf(av[i], bv[j], acc[i][j]);
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        const int m = m0 + ty + 16 * i;
+        if (m >= n) continue;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const int c = n0 + tx + 16 * j;
+            if (c < w) a.SC[in.off_c + (long long)m * w + c] = (double)acc[i][j];
+        }
+    }
+}
+
 // 1. H_b = [C_o;SC_o] X_b   (2n x v)
 struct BtStep1 {
     BtArrays a;
@@ -1386,7 +1441,17 @@ int Ctx::solve_batch(int n_inst, const tincr_tda_instance *hin, int max_iter, do
 
     TINCR_CUDA(cudaEventRecord(ev0, stream));
     // set-up: SC, packed blocks, gamma_lr in the AO basis, guesses
-    bt_launch<false, false>(*this, w.t_sc, tsc.size(), BtStepSC{a}, TINCR_KF_OTHER, 0.0);
+    // FP32 S C serves the mixed operator; a solve that finishes with FP64 iterations (tolerance below
+    // the mixed floor) needs the FP64 product for them
+    if (mixed && tol >= MIXED_TOL_FLOOR) {
+        const int slot = prof_begin(TINCR_KF_OTHER);
+        bt_sc32_kernel<<<(unsigned)tsc.size(), GB_T, 0, stream>>>(w.t_sc.p, a);
+        count_launch(stream, "bt_sc32");
+        check_launch("bt_sc32");
+        prof_end(slot, 0.0, 0.0);
+    } else {
+        bt_launch<false, false>(*this, w.t_sc, tsc.size(), BtStepSC{a}, TINCR_KF_OTHER, 0.0);
+    }
     bt_pack_kernel<<<n_inst, BT_T, 0, stream>>>(a);
     count_launch(stream, "bt_pack");
     check_launch("bt_pack");
