@@ -188,10 +188,7 @@ void Ctx::dg_reserve(int mmax) {
     TINCR_CUDA(cudaMemsetAsync(dg_B.p, 0, dg_B.n * sizeof(bf16), stream));
     TINCR_CUDA(cudaMemsetAsync(dg_C.p, 0, dg_C.n * sizeof(bf16), stream));
     TINCR_CUDA(cudaMemsetAsync(dg_bad.p, 0, sizeof(int), stream));
-    if (!d_tc_err.p) {
-        d_tc_err.alloc(1);
-        TINCR_CUDA(cudaMemsetAsync(d_tc_err.p, 0, sizeof(int), stream));
-    }
+    tc_err_ensure();
 }
 
 // the tiled digit operands of the basis
@@ -286,10 +283,7 @@ void Ctx::gemm_f64_digits(int M, int N, int K, const double *A, const double *B,
     DevBuf<bf16> pa((size_t)DG_PLANES * pad128(M) * Kp), pb((size_t)DG_PLANES * DG_N * Kp);
     DevBuf<int> ea(M), eb(DG_N);
     DevBuf<unsigned long long> acc((size_t)M * DG_N * 2);
-    if (!d_tc_err.p) {
-        d_tc_err.alloc(1);
-        TINCR_CUDA(cudaMemsetAsync(d_tc_err.p, 0, sizeof(int), stream));
-    }
+    tc_err_ensure();
     if (!dg_bad.p) {
         dg_bad.alloc(1);
         TINCR_CUDA(cudaMemsetAsync(dg_bad.p, 0, sizeof(int), stream));

@@ -218,6 +218,16 @@ __global__ void cg_update_kernel(long long len, double alpha, const double *p, c
     }
 }
 
+// the same update with alpha = rr / pAp formed on the device (pAp left there by dot_kernel)
+__global__ void cg_update_dev_kernel(long long len, double rr, const double *pAp, const double *p, const double *Ap,
+                                     double *x, double *r) {
+    const double alpha = rr / *pAp;
+    GRID_STRIDE(t, len) {
+        x[t] += alpha * p[t];
+        r[t] -= alpha * Ap[t];
+    }
+}
+
 // p = beta p + r
 __global__ void cg_dir_kernel(long long len, double beta, double *p, const double *r) {
     GRID_STRIDE(t, len) p[t] = beta * p[t] + r[t];
@@ -486,6 +496,7 @@ int Ctx::zvector_cg(int variant, const double *R, double *Z, int max_iter, doubl
     const long long len = ov;
     gcg.reserve(5 * (size_t)len + 8);
     double *r = gcg.p, *p = r + len, *Ap = p + len, *tmp = Ap + len, *Xt = tmp + len, *dots = Xt + len;
+    double h_dots[2] = {0.0, 0.0};
     auto op = [&](const double *x, double *out) {
         // tincr: TDA matrix A for LC (mult_av_lc: 2 Coulomb - exchange), A+B without exchange otherwise
         // (mult_av_nolc: 4 Coulomb).  Exact variant with LC: (A+B) = 4 Coulomb - (ij|ab) - (ib|ja).
@@ -496,10 +507,13 @@ int Ctx::zvector_cg(int variant, const double *R, double *Z, int max_iter, doubl
             ao_contract(1, BLK_VIRT, BLK_OCC, Xt, BLK_OCC, BLK_VIRT, -0.25, 0.0, out, 1.0, 1.0, nullptr);
         }
     };
-    auto dot = [&](const double *a, const double *b) {
-        dot_kernel<<<1, 1024, 0, stream>>>(len, a, b, dots);
+    auto dot_dev = [&](const double *a, const double *b, double *out) {   // out on the device, no sync
+        dot_kernel<<<1, 1024, 0, stream>>>(len, a, b, out);
         count_launch(stream, "dot");
         check_launch("dot");
+    };
+    auto dot = [&](const double *a, const double *b) {
+        dot_dev(a, b, dots);
         double h = 0.0;
         TINCR_CUDA(cudaMemcpyAsync(&h, dots, sizeof(double), cudaMemcpyDeviceToHost, stream));
         sync();
@@ -514,13 +528,17 @@ int Ctx::zvector_cg(int variant, const double *R, double *Z, int max_iter, doubl
         double rr = dot(r, r);
         int st = TINCR_CG_MAXITER;
         int k = 0;
+        // one host synchronisation per iteration: alpha = rr / pAp is formed on the device (the same
+        // FP64 division), and pAp and the new r.r come back together
         for (k = 0; k < limit; ++k) {
             op(p, Ap);
-            double pAp = dot(p, Ap);
-            double alpha = rr / pAp;
+            dot_dev(p, Ap, dots + 1);
+            EW(cg_update_dev_kernel, len, len, rr, dots + 1, p, Ap, Z, r);
+            dot_dev(r, r, dots + 2);
+            TINCR_CUDA(cudaMemcpyAsync(h_dots, dots + 1, 2 * sizeof(double), cudaMemcpyDeviceToHost, stream));
+            sync();
+            const double alpha = rr / h_dots[0], rr_new = h_dots[1];
             if (!std::isfinite(alpha)) fail(TINCR_NONFINITE, "Z-vector CG: non-finite step");
-            EW(cg_update_kernel, len, len, alpha, p, Ap, Z, r);
-            double rr_new = dot(r, r);
             if (rr_new <= conv) {
                 st = TINCR_OK;
                 ++k;

@@ -84,10 +84,7 @@ static void plane_gemm(Ctx &c, int family, int M, int N, long long Kpad, PlaneOp
 void Ctx::ao_contract_mixed(int k, int R, int S, const double *V, int P, int Q, double ax, double ac, double *out,
                             double alpha, double beta, const double *Xomega) {
     prepare_planes();
-    if (use_tc && !d_tc_err.p) {
-        d_tc_err.alloc(1);
-        TINCR_CUDA(cudaMemsetAsync(d_tc_err.p, 0, sizeof(int), stream));
-    }
+    if (use_tc) tc_err_ensure();
     const int n = n_orb;
     const int nr = bsz(R), ns = bsz(S), np = bsz(P), nq = bsz(Q);
     const bool exch = ax != 0.0 && lc;
@@ -174,15 +171,7 @@ void Ctx::ao_contract_mixed(int k, int R, int S, const double *V, int P, int Q, 
                                Xomega ? Xomega + (long long)c0 * np * nq : nullptr, alpha, beta},
                    2 * n);
     }
-    if (use_tc) {
-        int e = 0;
-        TINCR_CUDA(cudaMemcpyAsync(&e, d_tc_err.p, sizeof(int), cudaMemcpyDeviceToHost, stream));
-        sync();
-        if (e) {
-            TINCR_CUDA(cudaMemsetAsync(d_tc_err.p, 0, sizeof(int), stream));
-            fail(TINCR_CUDA_ERR, "tensor-core GEMM: a pipeline wait timed out (code " + std::to_string(e) + ")");
-        }
-    }
+    if (use_tc) tc_err_watch();   // reported by the next sync()
 }
 
 // Transition charges of k vectors X (q_ov X per atom) in the mixed form: H = [C_o; SC_o] X_b for all
@@ -190,10 +179,7 @@ void Ctx::ao_contract_mixed(int k, int R, int S, const double *V, int P, int Q, 
 // and the atomic sums in FP64 (diag_dots_kernel, launch_coulomb).
 void Ctx::qtrans_mixed(int k, const double *X, double *y_out) {
     const int n = n_orb, o = n_occ, v = n_virt;
-    if (use_tc && !d_tc_err.p) {
-        d_tc_err.alloc(1);
-        TINCR_CUDA(cudaMemsetAsync(d_tc_err.p, 0, sizeof(int), stream));
-    }
+    if (use_tc) tc_err_ensure();
     const long long kp = pad64(o);
     const long long pa = 2LL * n * kp, pb = (long long)k * v * kp;
     mg_bf16.reserve((size_t)N_PLANES * (pa + pb));
@@ -216,6 +202,7 @@ void Ctx::qtrans_mixed(int k, const double *X, double *y_out) {
     count_launch(stream, "diag_dots");
     check_launch("diag_dots");
     launch_coulomb(stream, k, n, n_atoms, d_ao_off.p, d_gamma.p, wsd3.p, wsd2.p, nullptr, nullptr, y_out, 1.0);
+    if (use_tc) tc_err_watch();
 }
 
 // C = alpha op(A) op(B) + beta C (row-major FP64 in and out) on the three-plane tensor-core GEMM:
@@ -224,10 +211,7 @@ void Ctx::qtrans_mixed(int k, const double *X, double *y_out) {
 void Ctx::gemm_mixed(bool ta, bool tb, int M, int N, int K, const double *A, int lda, const double *B, int ldb,
                      double *C, int ldc, double alpha, double beta) {
     if (M <= 0 || N <= 0 || K <= 0) return;
-    if (use_tc && !d_tc_err.p) {
-        d_tc_err.alloc(1);
-        TINCR_CUDA(cudaMemsetAsync(d_tc_err.p, 0, sizeof(int), stream));
-    }
+    if (use_tc) tc_err_ensure();
     const long long kp = pad64(K);
     const long long pa = (long long)M * kp, pb = (long long)N * kp;
     if (mg_bf16.n < (size_t)N_PLANES * (pa + pb) || mg_key != kp) {
@@ -244,15 +228,7 @@ void Ctx::gemm_mixed(bool ta, bool tb, int M, int N, int K, const double *A, int
     check_launch("split_planes");
     plane_gemm(*this, TINCR_KF_GRADIENT, M, N, kp, PlaneOperand{Ap, pa, kp, 0}, PlaneOperand{Bp, pb, kp, 0}, 1,
                EpiPlaneOut{C, ldc, 0, nullptr, nullptr, alpha, beta}, K);
-    if (use_tc) {
-        int e = 0;
-        TINCR_CUDA(cudaMemcpyAsync(&e, d_tc_err.p, sizeof(int), cudaMemcpyDeviceToHost, stream));
-        sync();
-        if (e) {
-            TINCR_CUDA(cudaMemsetAsync(d_tc_err.p, 0, sizeof(int), stream));
-            fail(TINCR_CUDA_ERR, "tensor-core GEMM: a pipeline wait timed out (code " + std::to_string(e) + ")");
-        }
-    }
+    if (use_tc) tc_err_watch();   // reported by the next sync()
 }
 
 }  // namespace tincr

@@ -446,6 +446,7 @@ Ctx::Ctx(int dev) : device(dev) {
 Ctx::~Ctx() {
     cudaSetDevice(device);
     release_batch(batch);
+    if (h_tc_err) cudaFreeHost(h_tc_err);
     for (auto &p : pending) { cudaEventDestroy(p.a); cudaEventDestroy(p.b); }
     for (auto e : event_pool) cudaEventDestroy(e);
     if (ev0) cudaEventDestroy(ev0);
@@ -453,7 +454,33 @@ Ctx::~Ctx() {
     if (stream) cudaStreamDestroy(stream);
 }
 
-void Ctx::sync() { TINCR_CUDA(cudaStreamSynchronize(stream)); }
+// Every host synchronisation also reports a bounded-wait failure of the tensor-core kernels queued
+// before it (tc_err_watch), so those launches need no synchronisation of their own.
+void Ctx::sync() {
+    TINCR_CUDA(cudaStreamSynchronize(stream));
+    if (h_tc_err && *h_tc_err) {
+        const int e = *h_tc_err;
+        *h_tc_err = 0;
+        TINCR_CUDA(cudaMemsetAsync(d_tc_err.p, 0, sizeof(int), stream));
+        TINCR_CUDA(cudaStreamSynchronize(stream));
+        fail(TINCR_CUDA_ERR, "tensor-core GEMM: a pipeline wait timed out (code " + std::to_string(e) + ")");
+    }
+}
+
+void Ctx::tc_err_ensure() {
+    if (d_tc_err.p) return;
+    d_tc_err.alloc(1);
+    TINCR_CUDA(cudaMemsetAsync(d_tc_err.p, 0, sizeof(int), stream));
+    if (!h_tc_err) {
+        TINCR_CUDA(cudaMallocHost(&h_tc_err, sizeof(int)));
+        *h_tc_err = 0;
+    }
+}
+
+void Ctx::tc_err_watch() {
+    if (d_tc_err.p && h_tc_err)
+        TINCR_CUDA(cudaMemcpyAsync(h_tc_err, d_tc_err.p, sizeof(int), cudaMemcpyDeviceToHost, stream));
+}
 
 // norms of `rows` vectors of length len (stride lda) into out[rows], spread over the whole GPU
 void Ctx::row_norms(int rows, long long len, const double *A, long long lda, double *out) {

@@ -99,6 +99,9 @@ struct Ctx {
     DevBuf<double> mx_f64;
     long long mx_key = -1;
     DevBuf<int> d_tc_err;                 // error word of the tensor-core kernels' bounded waits
+    int *h_tc_err = nullptr;              // pinned copy, refreshed after tensor-core launches, read by sync()
+    void tc_err_ensure();                 // allocate and clear d_tc_err
+    void tc_err_watch();                  // queue the copy of d_tc_err to h_tc_err (checked at the next sync)
 
     // product workspace
     DevBuf<double> wsH, wsF, wsG, wsd3, wsd2, wsz;
