@@ -257,7 +257,7 @@ constexpr int GS_MAX = 32, GS_SLOTS = GS_MAX + 2;
 __global__ void __launch_bounds__(256) seq_gs_kernel(int kadd, long long ov, int m0, int mmax, double *V, double *T,
                                                      double *part, int *state) {
     cg::grid_group grid = cg::this_grid();
-    __shared__ double c[GS_MAX], sc[GS_MAX];
+    __shared__ double c[GS_MAX], sc[GS_MAX], tot[GS_SLOTS];
     __shared__ double red[8][GS_SLOTS];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const long long stride = (long long)gridDim.x * blockDim.x;
@@ -288,14 +288,43 @@ __global__ void __launch_bounds__(256) seq_gs_kernel(int kadd, long long ov, int
             sq += v * v;
             d[GS_MAX] += v * tnx;
         }
-        // block partials: slots 0 .. acc-1 (dots with q_i), GS_MAX (dot with t'_j), GS_MAX + 1 (|t'_j|^2)
+        // block partials: slots 0 .. acc-1 (dots with q_i), GS_MAX (dot with t'_j), GS_MAX + 1 (|t'_j|^2).
+        // The 32 dot slots are reduced over the warp by halving exchanges (lane L ends with slot L:
+        // 31 shuffle-adds instead of 160; GB300's FP64 unit takes ~64 cycles per warp instruction).
         double *pb = part + ((long long)(j & 1) * gridDim.x + blockIdx.x) * GS_SLOTS;
-        for (int i = 0; i < GS_SLOTS; ++i) {
-            const bool used = i < acc || i >= GS_MAX;
-            if (!used) continue;   // uniform over the block
-            double v = i < GS_MAX ? d[i] : (i == GS_MAX ? d[GS_MAX] : sq);
-            for (int off = 16; off; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
-            if (lane == 0) red[warp][i] = v;
+        {
+            double a16[16], a8[8], a4[4], a2[2];
+#pragma unroll
+            for (int q = 0; q < 16; ++q) {
+                const bool h = lane & 16;
+                a16[q] = (h ? d[q + 16] : d[q]) + __shfl_xor_sync(0xffffffffu, h ? d[q] : d[q + 16], 16);
+            }
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+                const bool h = lane & 8;
+                a8[q] = (h ? a16[q + 8] : a16[q]) + __shfl_xor_sync(0xffffffffu, h ? a16[q] : a16[q + 8], 8);
+            }
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const bool h = lane & 4;
+                a4[q] = (h ? a8[q + 4] : a8[q]) + __shfl_xor_sync(0xffffffffu, h ? a8[q] : a8[q + 4], 4);
+            }
+#pragma unroll
+            for (int q = 0; q < 2; ++q) {
+                const bool h = lane & 2;
+                a2[q] = (h ? a4[q + 2] : a4[q]) + __shfl_xor_sync(0xffffffffu, h ? a4[q] : a4[q + 2], 2);
+            }
+            const bool h = lane & 1;
+            red[warp][lane] = (h ? a2[1] : a2[0]) + __shfl_xor_sync(0xffffffffu, h ? a2[0] : a2[1], 1);
+            double vc = d[GS_MAX], vs = sq;
+            for (int off = 16; off; off >>= 1) {
+                vc += __shfl_xor_sync(0xffffffffu, vc, off);
+                vs += __shfl_xor_sync(0xffffffffu, vs, off);
+            }
+            if (lane == 0) {
+                red[warp][GS_MAX] = vc;
+                red[warp][GS_MAX + 1] = vs;
+            }
         }
         __syncthreads();
         if (threadIdx.x < GS_SLOTS && (threadIdx.x < acc || threadIdx.x >= GS_MAX)) {
@@ -304,11 +333,19 @@ __global__ void __launch_bounds__(256) seq_gs_kernel(int kadd, long long ov, int
             pb[threadIdx.x] = v;
         }
         grid.sync();
-        // every CTA: the norm of t'_j (fixed order), accept or drop, the next vector's coefficients
+        // every CTA: the sums over the CTAs of the used slots, in a fixed order (warp w takes slots
+        // w, w + 8, ...: lanes stride over the CTAs, then a shuffle tree), so every CTA holds the same
+        // totals; then the norm of t'_j, accept or drop, and the next vector's coefficients
         const double *pj = part + (long long)(j & 1) * gridDim.x * GS_SLOTS;
-        double nsq = 0.0;
-        for (int b = 0; b < (int)gridDim.x; ++b) nsq += pj[(long long)b * GS_SLOTS + GS_MAX + 1];
-        const double nrm = sqrt(nsq);
+        for (int i = warp; i < GS_SLOTS; i += 8) {
+            if (!(i < acc || i >= GS_MAX)) continue;   // uniform over the warp
+            double v = 0.0;
+            for (int b = lane; b < (int)gridDim.x; b += 32) v += pj[(long long)b * GS_SLOTS + i];
+            for (int off = 16; off; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+            if (lane == 0) tot[i] = v;
+        }
+        __syncthreads();
+        const double nrm = sqrt(tot[GS_MAX + 1]);
         if (!isfinite(nrm)) {
             if (blockIdx.x == 0 && threadIdx.x == 0) state[1] = 1;
             finite = false;   // every CTA sees the same norm
@@ -318,9 +355,7 @@ __global__ void __launch_bounds__(256) seq_gs_kernel(int kadd, long long ov, int
         __syncthreads();   // c and sc of this vector are no longer read
         if (threadIdx.x < acc || (accept && threadIdx.x == acc)) {
             const int i = threadIdx.x;
-            double v = 0.0;
-            const int slot = i < acc ? i : GS_MAX;
-            for (int b = 0; b < (int)gridDim.x; ++b) v += pj[(long long)b * GS_SLOTS + slot];
+            const double v = tot[i < acc ? i : GS_MAX];
             const double f = i < acc ? sc[i] : 1.0 / nrm;
             if (i == acc) sc[i] = f;
             c[i] = v * f * f;   // (q_i . t_{j+1}) / |t'_i|^2 with the unscaled row t'_i
