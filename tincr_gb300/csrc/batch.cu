@@ -22,6 +22,10 @@
 #include <numeric>
 #include <vector>
 
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
 #include "batch.cuh"
 #include "gemm_f64.cuh"
 #include "planes.cuh"
@@ -1201,8 +1205,26 @@ __global__ void __launch_bounds__(BT_T) bt_subspace_kernel(BtArrays a) {
 // host
 // ----------------------------------------------------------------------------------------------
 
+// page-locked host staging buffer (grow-only): uploads from it are plain DMA
+struct PinnedBuf {
+    double *p = nullptr;
+    size_t n = 0;
+    void reserve(size_t count) {
+        if (count <= n && p) return;
+        if (p) cudaFreeHost(p);
+        p = nullptr;
+        n = 0;
+        TINCR_CUDA(cudaMallocHost(&p, std::max<size_t>(1, count) * sizeof(double)));
+        n = std::max<size_t>(1, count);
+    }
+    ~PinnedBuf() {
+        if (p) cudaFreeHost(p);
+    }
+};
+
 struct BatchWork {
     std::vector<BtInst> h;
+    PinnedBuf pinC, pinS, pinG, pinGlr, pinOm;   // staging of the instance inputs
     DevBuf<BtInst> inst;
     DevBuf<BtState> state;
     DevBuf<double> C, SC, S, blk, glr, glr_atoms, gam, omega, V, AV, R, Rk, T, sub, H, F, D, u, err, Y;
@@ -1262,13 +1284,13 @@ int Ctx::solve_batch(int n_inst, const tincr_tda_instance *hin, int max_iter, do
     if (!batch) batch = new BatchWork();
     BatchWork &w = *batch;
     w.h.assign(n_inst, BtInst{});
-    std::vector<double> hC, hS, hG, hGlr, hOm;
     std::vector<int> hAo, hAoAtom, hPos;
-    std::vector<long long> hGlrOff(n_inst, 0);
+    std::vector<long long> hGlrOff(n_inst, 0), offPos(n_inst, 0);
     long long o_c = 0, o_s = 0, o_blk = 0, o_glr = 0, o_gam = 0, o_om = 0, o_v = 0, o_r = 0, o_sub = 0, o_h = 0, o_f = 0,
-              o_d = 0, o_u = 0, o_y = 0;
+              o_d = 0, o_u = 0, o_y = 0, o_glra = 0, o_pos = 0;
     long long o_pc = 0, o_pv = 0;
     int o_ao = 0, o_aoatom = 0, mmax_all = 1, nr_max = 1, nmax_atoms = 1;
+    // pass 1: validation and the packed offsets of every instance
     for (int I = 0; I < n_inst; ++I) {
         const tincr_tda_instance &q = hin[I];
         if (q.n_atoms <= 0 || q.n_orb <= 0 || q.n_occ <= 0 || q.n_virt <= 0 || q.n_occ + q.n_virt > q.n_orb ||
@@ -1306,51 +1328,83 @@ int Ctx::solve_batch(int n_inst, const tincr_tda_instance *hin, int max_iter, do
         o_pv += (long long)b.nr * ((long long)b.v * b.ko + 2LL * n * b.kv + 2LL * n * b.k2 + (long long)b.v * b.k2);
         b.off_ao = o_ao; o_ao += N + 1;
         b.off_aoatom = o_aoatom; o_aoatom += n;
+        if (b.lc) { hGlrOff[I] = o_glra; o_glra += (long long)N * N; }
+        offPos[I] = o_pos; o_pos += b.nr;
         mmax_all = std::max(mmax_all, b.mmax);
         nr_max = std::max(nr_max, b.nr);
         nmax_atoms = std::max(nmax_atoms, N);
-        // host-side copies into the packed arrays
-        check_finite(q.c, (size_t)n * w_, "c");
-        check_finite(q.s, (size_t)n * n, "s");
-        check_finite(q.orbe, (size_t)w_, "orbe");
-        check_finite(q.gamma, (size_t)N * N, "gamma");
-        hC.insert(hC.end(), q.c, q.c + (size_t)n * w_);
-        hS.insert(hS.end(), q.s, q.s + (size_t)n * n);
-        hG.insert(hG.end(), q.gamma, q.gamma + (size_t)N * N);
-        if (b.lc) {
-            check_finite(q.gamma_lr, (size_t)N * N, "gamma_lr");
-            hGlrOff[I] = (long long)hGlr.size();
-            hGlr.insert(hGlr.end(), q.gamma_lr, q.gamma_lr + (size_t)N * N);
-        }
+    }
+    // pass 2, one instance per task: copies into the page-locked staging buffers with the finiteness
+    // check, orbital-energy differences and the guess positions
+    w.pinC.reserve(o_c);
+    w.pinS.reserve(o_s);
+    w.pinG.reserve(o_gam);
+    w.pinGlr.reserve(o_glra);
+    w.pinOm.reserve(o_om);
+    hAo.resize(o_ao);
+    hAoAtom.resize(o_aoatom);
+    hPos.resize(o_pos);
+    std::vector<unsigned char> bad(n_inst, 0);
+#pragma omp parallel for schedule(dynamic, 4) num_threads(12)
+    for (int I = 0; I < n_inst; ++I) {
+        const tincr_tda_instance &q = hin[I];
+        const BtInst &b = w.h[I];
+        const int n = b.n, w_ = b.o + b.v, N = b.N;
+        auto copy = [&](double *dst, const double *src, size_t cnt, unsigned char flag) {
+            bool ok = true;
+            for (size_t k = 0; k < cnt; ++k) {
+                const double x = src[k];
+                ok &= std::isfinite(x);
+                dst[k] = x;
+            }
+            if (!ok) bad[I] |= flag;
+        };
+        copy(w.pinC.p + b.off_c, q.c, (size_t)n * w_, 1);
+        copy(w.pinS.p + b.off_s, q.s, (size_t)n * n, 2);
+        copy(w.pinG.p + b.off_gam, q.gamma, (size_t)N * N, 4);
+        if (b.lc) copy(w.pinGlr.p + hGlrOff[I], q.gamma_lr, (size_t)N * N, 8);
+        for (int k = 0; k < w_; ++k)
+            if (!std::isfinite(q.orbe[k])) bad[I] |= 16;
         int off = 0;
         for (int A = 0; A < N; ++A) {
-            hAo.push_back(off);
-            for (int k = 0; k < q.orbs_per_atom[A]; ++k) hAoAtom.push_back(A);
+            hAo[b.off_ao + A] = off;
+            for (int k = 0; k < q.orbs_per_atom[A]; ++k) hAoAtom[b.off_aoatom + off + k] = A;
             off += q.orbs_per_atom[A];
         }
-        hAo.push_back(off);
+        hAo[b.off_ao + N] = off;
         // omega_ia = e_a - e_i (excited_states/utils.rs:8-22) and the guess positions (stable ties)
-        std::vector<double> om(b.ov);
+        double *om = w.pinOm.p + b.off_omega;
         for (int i = 0; i < b.o; ++i)
             for (int x = 0; x < b.v; ++x) om[(size_t)i * b.v + x] = q.orbe[b.o + x] - q.orbe[i];
-        hOm.insert(hOm.end(), om.begin(), om.end());
         std::vector<int> ord(b.ov);
         std::iota(ord.begin(), ord.end(), 0);
         std::stable_sort(ord.begin(), ord.end(), [&](int x, int y) { return om[x] < om[y]; });
-        for (int r = 0; r < b.nr; ++r) hPos.push_back(ord[r]);
+        for (int r = 0; r < b.nr; ++r) hPos[offPos[I] + r] = ord[r];
     }
+    for (int I = 0; I < n_inst; ++I)
+        if (bad[I]) {
+            static const char *names[5] = {"c", "s", "gamma", "gamma_lr", "orbe"};
+            int f = 0;
+            while (!((bad[I] >> f) & 1)) ++f;
+            fail(TINCR_NONFINITE, "solve_batch: instance " + std::to_string(I) + ": non-finite value in " + names[f]);
+        }
     // device arrays
+    auto upload_pinned = [&](DevBuf<double> &d, const PinnedBuf &h, long long count) {
+        d.reserve(std::max<long long>(1, count));
+        if (count > 0)
+            TINCR_CUDA(cudaMemcpyAsync(d.p, h.p, (size_t)count * sizeof(double), cudaMemcpyHostToDevice, stream));
+    };
     upload_any(stream, w.inst, w.h);
     w.state.reserve(n_inst);
-    upload_vec(stream, w.C, hC);
+    upload_pinned(w.C, w.pinC, o_c);
     w.SC.reserve(std::max<long long>(1, o_c));
-    upload_vec(stream, w.S, hS);
+    upload_pinned(w.S, w.pinS, o_s);
     w.blk.reserve(std::max<long long>(1, o_blk));
     w.glr.reserve(std::max<long long>(1, o_glr));
-    upload_vec(stream, w.glr_atoms, hGlr);
+    upload_pinned(w.glr_atoms, w.pinGlr, o_glra);
     upload_any(stream, w.off_glr_atoms, hGlrOff);
-    upload_vec(stream, w.gam, hG);
-    upload_vec(stream, w.omega, hOm);
+    upload_pinned(w.gam, w.pinG, o_gam);
+    upload_pinned(w.omega, w.pinOm, o_om);
     w.V.reserve(o_v);
     w.AV.reserve(o_v);
     w.R.reserve(o_r);
@@ -1455,7 +1509,7 @@ int Ctx::solve_batch(int n_inst, const tincr_tda_instance *hin, int max_iter, do
     bt_pack_kernel<<<n_inst, BT_T, 0, stream>>>(a);
     count_launch(stream, "bt_pack");
     check_launch("bt_pack");
-    if (!hGlr.empty()) {
+    if (o_glra > 0) {
         bt_expand_kernel<<<n_inst, BT_T, 0, stream>>>(a, w.glr_atoms.p, w.off_glr_atoms.p);
         count_launch(stream, "bt_expand");
         check_launch("bt_expand");
