@@ -3,15 +3,16 @@
 // C[M x N] = A[M x K] B[N x K]^T with A and B in three split-BF16 planes each (planes.cuh),
 // accumulated as the six plane products A0B0 + A0B1 + A1B0 + A0B2 + A2B0 + A1B1.
 //
-// CTA = 192 threads, one 128 x 128 output tile, K consumed in 64-element (128-byte) blocks:
-//   * warp 4 / lane 0: TMA producer, six boxes (A0, A1, A2, B0, B1, B2; 128 rows x 64 bf16, 128-byte
+// CTA = 320 threads, one 128 x 128 output tile, K consumed in 64-element (128-byte) blocks:
+//   * warp 8 / lane 0: TMA producer, six boxes (A0, A1, A2, B0, B1, B2; 128 rows x 64 bf16, 128-byte
 //     swizzle) per stage into a 2-stage ring, completion on the stage's "full" mbarrier;
-//   * warp 5 / lane 0: MMA issuer, 4 K=16 steps x 6 products per block (tcgen05.mma.cta_group::1
+//   * warp 9 / lane 0: MMA issuer, 4 K=16 steps x 6 products per block (tcgen05.mma.cta_group::1
 //     .kind::f16, M = N = 128) into one of two TMEM accumulator pairs (ping-pong): the hi x hi product
 //     in one accumulator, the five smaller products in the other; tcgen05.commit to the stage's
 //     "empty" and the pair's "full" mbarrier;
-//   * warps 0-3: fold each K block's pair into FP32 running sums held in registers (warp w owns
-//     TMEM lanes 32w..32w+31 = tile rows, one row per thread), then the epilogue functor.
+//   * warps 0-7: fold each K block's pair into FP32 running sums held in registers (warp w owns
+//     TMEM lanes 32 (w % 4) .. + 31 = tile rows, one row per thread, and columns 64 (w / 4) .. + 63),
+//     then the epilogue functor.
 // The dominant accumulator takes only 4 MMAs per block before the CUDA cores add it with
 // round-to-nearest, and the small products accumulate apart from it, which keeps long K (up to
 // 2 n_orb) from building up a one-sided accumulation error; the fold overlaps the next block's MMAs.
@@ -27,7 +28,8 @@
 
 namespace tincr {
 
-constexpr int TC_M = 128, TC_N = 128, TC_K = 64, TC_STAGES = 2, TC_T = 192;
+constexpr int TC_M = 128, TC_N = 128, TC_K = 64, TC_STAGES = 2, TC_T = 320;
+constexpr int TC_FOLD_WARPS = 8;                         // warps 0-7 fold and run the epilogue
 constexpr int TC_TILE = TC_M * TC_K * 2;                  // 16 KB (128 rows x 128 bytes)
 constexpr int TC_STAGE = 2 * N_PLANES * TC_TILE;          // A0, A1, A2, B0, B1, B2
 constexpr int TC_SMEM = TC_STAGES * TC_STAGE + 1024 + 256;
@@ -151,7 +153,7 @@ gemm_planes_tc_kernel(const __grid_constant__ TcMaps maps, int M, int N, int Kpa
         }
         for (int a = 0; a < 2; ++a) {
             mbar_init(&accf[a], 1);
-            mbar_init(&acce[a], 4);          // one arrival per folding warp
+            mbar_init(&acce[a], TC_FOLD_WARPS);   // one arrival per folding warp
         }
         mbar_init(done, 1);
         asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
@@ -166,7 +168,7 @@ gemm_planes_tc_kernel(const __grid_constant__ TcMaps maps, int M, int N, int Kpa
     asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
     const uint32_t tmem = *tmem_slot;
 
-    if (warp == 4) {
+    if (warp == TC_FOLD_WARPS) {
         if (lane == 0) {
             int issued = 0;
             bool ok = true;
@@ -191,7 +193,7 @@ gemm_planes_tc_kernel(const __grid_constant__ TcMaps maps, int M, int N, int Kpa
                 for (int kb = (issued > TC_STAGES ? issued - TC_STAGES : 0); kb < issued; ++kb)
                     mbar_wait(&full[kb % TC_STAGES], (kb / TC_STAGES) & 1);
         }
-    } else if (warp == 5) {
+    } else if (warp == TC_FOLD_WARPS + 1) {
         if (lane == 0) {
             for (int kb = 0; kb < nk; ++kb) {
                 const int s = kb % TC_STAGES, a = kb & 1;
@@ -227,10 +229,13 @@ gemm_planes_tc_kernel(const __grid_constant__ TcMaps maps, int M, int N, int Kpa
             mbar_wait(done, 0);   // no MMA is in flight once the issuer leaves (also after a failure)
         }
     } else {
-        // folding warps 0-3: row m0 + 32 warp + lane, columns n0 .. n0 + 127
-        float sum[TC_N];
+        // folding warps 0-7: row m0 + 32 (warp % 4) + lane (TMEM lane quarter of the warp), columns
+        // n0 + 64 (warp / 4) .. + 63: two warps per lane quarter halve the fold and epilogue per thread
+        constexpr int HN = TC_N / 2;
+        const int quarter = warp & 3, half = warp >> 2;
+        float sum[HN];
 #pragma unroll
-        for (int j = 0; j < TC_N; ++j) sum[j] = 0.f;
+        for (int j = 0; j < HN; ++j) sum[j] = 0.f;
         bool ok = true;
         for (int kb = 0; kb < nk; ++kb) {
             const int a = kb & 1;
@@ -240,9 +245,10 @@ gemm_planes_tc_kernel(const __grid_constant__ TcMaps maps, int M, int N, int Kpa
                 break;
             }
             asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-            const uint32_t t0 = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(a * 2 * TC_N);
+            const uint32_t t0 =
+                tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(a * 2 * TC_N) + (uint32_t)(half * HN);
 #pragma unroll
-            for (int c0 = 0; c0 < TC_N; c0 += 16) {
+            for (int c0 = 0; c0 < HN; c0 += 16) {
                 uint32_t rm[16], rx[16];
                 tmem_ld16(t0 + (uint32_t)c0, rm);
                 tmem_ld16(t0 + (uint32_t)(TC_N + c0), rx);
@@ -254,14 +260,14 @@ gemm_planes_tc_kernel(const __grid_constant__ TcMaps maps, int M, int N, int Kpa
             __syncwarp();
             if (lane == 0) mbar_arrive(&acce[a]);
         }
-        const int row = m0 + warp * 32 + lane;
+        const int row = m0 + quarter * 32 + lane;
         if (ok && row < M) {
 #pragma unroll
-            for (int c0 = 0; c0 < TC_N; c0 += 8) {
+            for (int c0 = 0; c0 < HN; c0 += 8) {
                 F8 v;
 #pragma unroll
                 for (int j = 0; j < 8; ++j) v.x[j] = sum[c0 + j];
-                epi.run8(b, row, n0 + c0, N, v);
+                epi.run8(b, row, n0 + half * HN + c0, N, v);
             }
         }
     }
