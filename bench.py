@@ -388,6 +388,19 @@ def ctx_device(ctx):
     return int(os.environ.get("LOCAL_RANK", "0"))
 
 
+def tile_summary(table):
+    """How many instance shapes chose each tile shape, per plane GEMM step of the mixed batch."""
+    out = {"instance_shapes": len(table)}
+    for st in ("H", "F", "G", "AX"):
+        cnt = {}
+        for t in table:
+            sh = t["shapes"][st]
+            if sh is not None:
+                cnt[sh] = cnt.get(sh, 0) + 1
+        out[st] = cnt
+    return out
+
+
 def run_fmo(args, ctx):
     """Batched LE / CT TDA of the 64-acene aggregate plus the S1 gradient, mixed and FP64 forms
     (monomers/s)."""
@@ -444,6 +457,7 @@ def run_fmo(args, ctx):
         "s1_monomer": km,
         "max_abs_s1_grad_err_eh_per_bohr": float(np.abs(gm - g64).max()) if km == k64 else None,
         "davidson_iterations_max": int(max(x["iterations"] for x in rm)),
+        "plane_tile_autotuner": tile_summary(ctx.batch_tile_table()),
     })
     if args.cpu_baseline:
         total, sample = fmo_cpu_sample(mons, inst, labels, s1_monomer=km)
@@ -576,7 +590,8 @@ def run_fmo_once(args):
         rc, r = fmo.solve_batch(ctx, inst, FMO_MAX_ITER, FMO_TOL, prec)
     ms, nl = ctx.last_timing()
     print(json.dumps({"mode": "fmo", "precision": args.precision, "instances": len(inst), "status": rc, "ms": ms,
-                      "launches": nl}))
+                      "launches": nl, "plane_tile_autotuner": tile_summary(ctx.batch_tile_table()),
+                      "plane_tile_table": ctx.batch_tile_table()}))
     ctx.close()
 
 

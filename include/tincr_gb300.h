@@ -199,6 +199,19 @@ typedef struct {
 int tincr_tda_solve_batch(tincr_ctx *ctx, int n_inst, const tincr_tda_instance *inst, int max_iter,
                           double tolerance, int precision, tincr_tda_result *res);
 
+/* The tile shapes of the batch's mixed-form plane GEMMs, as chosen by the autotuner.  No counterpart
+ * in tincr (rayon runs one monomer per thread).  The first TINCR_PREC_BF16X3 batch that contains an
+ * instance shape (n_atoms, n_orb, n_occ, n_virt, long-range flag) times the four tile shapes
+ * 64x64, 64x32, 32x64 and 32x32 (rows x columns of the output per CTA) for each of its four plane
+ * GEMM steps (H = [C_o;SC_o]X, F, G, AX) on that shape's instances and keeps the fastest; later
+ * batches reuse the choice (the table lives for the process).  TINCR_GB300_BATCH_TILES=<shape>
+ * forces one shape and skips the tuner.  Results do not depend on the shape.
+ * Writes up to `capacity` entries: entries[9 i ..] = n_atoms, n_orb, n_occ, n_virt, lc, then the
+ * chosen shape index (0-3 in the order above, -1 when the step does not run: F and G without
+ * long-range correction) for the four steps; us[16 i + 4 step + shape] (may be NULL) = measured
+ * microseconds per repetition of that shape's tiles.  *n_entries = the table's size. */
+int tincr_batch_tile_table(const tincr_ctx *ctx, int capacity, int *n_entries, int *entries, double *us);
+
 /* A.X product that allocates no device memory.  No counterpart in tincr: it exists for callers
  * that own all device memory themselves (pool or arena allocators of an MD or FMO driver) or that
  * cannot accept the implicit device synchronisation of cudaMalloc/cudaFree between their kernels.

@@ -119,3 +119,39 @@ def fmo_oracle_engine(case, k):
     glr = d.gamma_lr[:na, na:] if case["lc"] else np.zeros((na, sl.n_atoms))
     eng = OT.CtEngine(om, qov, d.gamma, qoo_h, qvv_l, glr, sh.n_occ, sl.n_virt)
     return eng, d.system.xyz
+
+
+def scc_arrays(args):
+    """Host SCC of one geometry -> the arrays a TDA set-up needs.  `args` = (numbers, xyz in bohr,
+    lc); top-level so that a spawn process pool can run it."""
+    z, xyz, lc = args
+    sy = gs.build_system(z, xyz, lc=lc)
+    g = gs.run_scc(sy, tol=1e-11)
+    return dict(orbs=g.orbs, s=g.s, orbe=g.orbe, gamma=g.gamma, gamma_lr=g.gamma_lr if lc else None)
+
+
+def displaced_scc(z, xyz, lc, h):
+    """SCC ground states at xyz + h e_c and xyz - h e_c for every Cartesian coordinate c, run in a
+    spawn process pool with one BLAS thread per worker.  Returns [(plus, minus)] per coordinate."""
+    import multiprocessing as mp
+    from concurrent.futures import ProcessPoolExecutor
+    jobs = []
+    for c in range(xyz.size):
+        for sgn in (1.0, -1.0):
+            x = xyz.copy()
+            x[c // 3, c % 3] += sgn * h
+            jobs.append((z, x, lc))
+    keys = ("OMP_NUM_THREADS", "OPENBLAS_NUM_THREADS", "MKL_NUM_THREADS")
+    saved = {k: os.environ.get(k) for k in keys}
+    os.environ.update({k: "1" for k in keys})
+    try:
+        with ProcessPoolExecutor(max_workers=min(16, os.cpu_count() or 1),
+                                 mp_context=mp.get_context("spawn")) as ex:
+            out = list(ex.map(scc_arrays, jobs, chunksize=4))
+    finally:
+        for k, v in saved.items():
+            if v is None:
+                os.environ.pop(k, None)
+            else:
+                os.environ[k] = v
+    return [(out[2 * c], out[2 * c + 1]) for c in range(xyz.size)]

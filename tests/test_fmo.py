@@ -176,3 +176,36 @@ def test_le_gradients_concurrent_match_single_context(gpu_ctx):
     _, flr = OG.ground_state_gradient(inp, der, True)
     ref = OG.tda_gradient(inp, der, 0, True, flr_dmd0=flr)
     assert np.abs(conc[k] - ref).max() < 1e-8
+
+
+@pytest.mark.gpu
+def test_batch_tile_autotuner(gpu_ctx, monkeypatch):
+    """The mixed batch's plane GEMM tile shapes: the autotuner records a choice for every instance
+    shape of the batch, and every forced tile shape gives the same energies, vectors and iteration
+    counts (each output element sees the same K order whatever the shape)."""
+    case = fmo_case(3, 1, 1)
+    monkeypatch.delenv("TINCR_GB300_BATCH_TILES", raising=False)
+    rc, ra = fmo.solve_batch(gpu_ctx, case["instances"], max_iter=150, tol=1e-6, precision=_lib.PREC_BF16X3)
+    assert rc == _lib.OK
+    table = gpu_ctx.batch_tile_table()
+    keys = {(t["n_atoms"], t["n_orb"], t["n_occ"], t["n_virt"]) for t in table}
+    for q in case["instances"]:
+        assert (q["n_atoms"], q["n_orb"], q["n_occ"], q["n_virt"]) in keys
+    for t in table:
+        assert t["shapes"]["H"] in gpu_ctx.TILE_SHAPES and t["shapes"]["AX"] in gpu_ctx.TILE_SHAPES
+        assert (t["shapes"]["F"] is None) == (not t["lc"])
+        for st, times in t["us"].items():
+            assert all(v > 0 for v in times.values())
+        print("tiles", t["n_atoms"], t["n_orb"], t["n_occ"], t["n_virt"], t["shapes"])
+    for shape in gpu_ctx.TILE_SHAPES:
+        monkeypatch.setenv("TINCR_GB300_BATCH_TILES", shape)
+        rc, rb = fmo.solve_batch(gpu_ctx, case["instances"], max_iter=150, tol=1e-6, precision=_lib.PREC_BF16X3)
+        assert rc == _lib.OK
+        for a, b in zip(ra, rb):
+            assert a["iterations"] == b["iterations"]
+            assert np.array_equal(a["energies"], b["energies"])
+            assert np.array_equal(np.abs(a["coefficients"]), np.abs(b["coefficients"]))
+    monkeypatch.setenv("TINCR_GB300_BATCH_TILES", "48x48")
+    with pytest.raises(_lib.TincrError) as e:
+        fmo.solve_batch(gpu_ctx, case["instances"], precision=_lib.PREC_BF16X3)
+    assert e.value.status == _lib.BAD_ARG

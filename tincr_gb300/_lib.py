@@ -33,6 +33,7 @@ SIGNATURES = {
     "tincr_last_solve_stats": (C.c_int, [C.c_void_p, C.POINTER(C.c_longlong), _ip, _dp]),
     "tincr_set_precision": (C.c_int, [C.c_void_p, C.c_int]),
     "tincr_tda_solve_batch": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_double, C.c_int, C.c_void_p]),
+    "tincr_batch_tile_table": (C.c_int, [C.c_void_p, C.c_int, _ip, _ip, _dp]),
     "tincr_davidson_history": (C.c_int, [C.c_void_p, C.c_int, _ip, _ip, _ip, _dp, _ip, _ip]),
     "tincr_subspace_eigh": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _dp, _dp, _dp, _ip]),
     "tincr_gemm_fp64_tensor": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, _dp, _dp, _dp]),
@@ -149,6 +150,29 @@ class Context:
                                                    iptr(pr)))
         return [dict(iter=int(it[i]), n_sub=int(ns[i]), max_residual=float(mr[i]), roots_left=int(rl[i]),
                      precision=int(pr[i])) for i in range(k)]
+
+    TILE_SHAPES = ("64x64", "64x32", "32x64", "32x32")
+    PLANE_STEPS = ("H", "F", "G", "AX")
+
+    def batch_tile_table(self):
+        """The batch autotuner's table: list of dict(n_atoms, n_orb, n_occ, n_virt, lc,
+        shapes={step: shape or None}, us={step: {shape: microseconds}})."""
+        n = C.c_int()
+        self.check(self.lib.tincr_batch_tile_table(self.h, 0, C.byref(n), None, None))
+        k = n.value
+        ent = np.zeros((max(k, 1), 9), np.int32)
+        us = np.zeros((max(k, 1), 4, 4))
+        self.check(self.lib.tincr_batch_tile_table(self.h, k, C.byref(n), iptr(ent), dptr(us)))
+        out = []
+        for i in range(min(k, n.value)):
+            e = ent[i]
+            shapes = {st: (self.TILE_SHAPES[e[5 + p]] if e[5 + p] >= 0 else None)
+                      for p, st in enumerate(self.PLANE_STEPS)}
+            times = {st: {sh: float(us[i, p, q]) for q, sh in enumerate(self.TILE_SHAPES)}
+                     for p, st in enumerate(self.PLANE_STEPS) if e[5 + p] >= 0}
+            out.append(dict(n_atoms=int(e[0]), n_orb=int(e[1]), n_occ=int(e[2]), n_virt=int(e[3]), lc=bool(e[4]),
+                            shapes=shapes, us=times))
+        return out
 
     def subspace_eigh(self, a, k):
         """k lowest eigenpairs of the symmetric matrix a (upper triangle read): (w [k], y [k, m], on_device)."""

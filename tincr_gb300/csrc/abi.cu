@@ -188,6 +188,12 @@ int tincr_tda_solve_batch(tincr_ctx *ctx, int n_inst, const tincr_tda_instance *
     return guarded(ctx, [&](tincr::Ctx &c) { return c.solve_batch(n_inst, inst, max_iter, tolerance, precision, res); });
 }
 
+int tincr_batch_tile_table(const tincr_ctx *ctx, int capacity, int *n_entries, int *entries, double *us) {
+    if (!ctx || !ctx->impl || capacity < 0 || !n_entries) return TINCR_BAD_ARG;
+    *n_entries = tincr::bp_table_entries(capacity, entries, us);
+    return TINCR_OK;
+}
+
 int tincr_set_parameters(tincr_ctx *ctx, int n_kinds, const int *kind_z, const int *kind_norb, const int *kind_l,
                          const int *kind_m, const double *kind_hubbard, const double *kind_occ, int n_knots,
                          const double *sk_knots, const double *sk_coef, int rep_ntmax, const int *rep_nt,

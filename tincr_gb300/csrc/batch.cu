@@ -18,8 +18,13 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <cstdio>
+#include <cstdlib>
 #include <functional>
+#include <map>
+#include <mutex>
 #include <numeric>
+#include <tuple>
 #include <vector>
 
 #ifdef _OPENMP
@@ -403,8 +408,9 @@ __global__ void bt_scale_rows_kernel(BtArrays a) {
 }
 
 // ----------------------------------------------------------------------------------------------
-// mixed form: grouped three-plane split-BF16 GEMM (64 x 64 tiles, warp MMA, six plane products,
-// FP32 folded every 32 of K)
+// mixed form: grouped three-plane split-BF16 GEMM (BM x BN tiles, warp MMA, six plane products,
+// FP32 folded every 32 of K).  The tile shape of each instance and product step is chosen by the
+// autotuner below, keyed on the instance's shape.
 // ----------------------------------------------------------------------------------------------
 
 inline int pad32(int k) { return (k + 31) / 32 * 32; }
@@ -417,11 +423,22 @@ struct BtPlaneOp {
     const double *X;
 };
 
-constexpr int BP_T = 128, BP_K = 32, BP_LD = BP_K + 8, BP_TILE = 64 * BP_LD;
-constexpr int BP_SMEM = 2 * 2 * N_PLANES * BP_TILE * 2;   // 2 stages x {A, B} x planes x bytes
+constexpr int BP_T = 128, BP_K = 32, BP_LD = BP_K + 8;
+// tile shapes (rows of A x rows of B per CTA) the autotuner chooses from
+constexpr int BP_SHAPES = 4;
+constexpr int BP_BM[BP_SHAPES] = {64, 64, 32, 32};
+constexpr int BP_BN[BP_SHAPES] = {64, 32, 64, 32};
+constexpr int bp_smem(int bm, int bn) { return 2 * N_PLANES * (bm + bn) * BP_LD * 2; }   // 2 stages, bytes
 
-template <class Step>
+// Four warps in a 2 x 2 arrangement, each computing a (BM/2) x (BN/2) block from m16n8k16 MMAs.
+// Every output element sees the same K order (32-deep slices, two MMA k-steps each, folded after
+// every slice) whatever the tile shape, so the results do not depend on the shape.
+template <class Step, int BM, int BN>
 __global__ void __launch_bounds__(BP_T) bt_plane_kernel(const int4 *__restrict__ tiles, Step step) {
+    constexpr int MI = BM / 32, NJ = BN / 16;          // 16-row and 8-column fragments per warp
+    constexpr int STAGE = N_PLANES * (BM + BN) * BP_LD;
+    constexpr int CHUNKS = N_PLANES * (BM + BN) * (BP_K / 8);   // 16-byte pieces per stage
+    static_assert(CHUNKS % BP_T == 0, "stage load must divide evenly over the CTA");
     extern __shared__ __align__(16) unsigned char bp_raw[];
     bf16 *sm = reinterpret_cast<bf16 *>(bp_raw);
     const int4 t = tiles[blockIdx.x];
@@ -430,32 +447,36 @@ __global__ void __launch_bounds__(BP_T) bt_plane_kernel(const int4 *__restrict__
     const long long ps = step.a.ps;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int wm = warp >> 1, wn = warp & 1, g = lane >> 2, tg = lane & 3;
-    const int m0 = t.z * 64, n0 = t.w * 64;
-    auto tile = [&](int s, int which) { return sm + (s * 2 * N_PLANES + which) * BP_TILE; };
+    const int m0 = t.z * BM, n0 = t.w * BN;
+    auto tileA = [&](int s, int q) { return sm + s * STAGE + q * BM * BP_LD; };
+    auto tileB = [&](int s, int q) { return sm + s * STAGE + N_PLANES * BM * BP_LD + q * BN * BP_LD; };
     auto load_stage = [&](int s, int k0) {
 #pragma unroll
-        for (int q = 0; q < 12; ++q) {
-            const int idx = tid + q * BP_T;         // 0 .. 1535: 6 tiles x 64 rows x 4 chunks
-            const int which = idx >> 8, within = idx & 255;
-            const int r = within >> 2, c = (within & 3) * 8;
+        for (int q = 0; q < CHUNKS / BP_T; ++q) {
+            const int idx = tid + q * BP_T;
+            const int row = idx >> 2, c = (idx & 3) * 8;   // row of the stacked A planes, then B planes
             const bf16 *base;
-            int ld, row0, lim;
-            if (which < N_PLANES) { base = op.A + which * ps; ld = op.lda; row0 = m0; lim = op.M; }
-            else                  { base = op.B + (which - N_PLANES) * ps; ld = op.ldb; row0 = n0; lim = op.N; }
-            const int gr = row0 + r;
-            cp_async16(tile(s, which) + r * BP_LD + c, base + (long long)(gr < lim ? gr : 0) * ld + k0 + c,
-                       gr < lim ? 16 : 0);
+            bf16 *dst;
+            int ld, gr, lim;
+            if (row < N_PLANES * BM) {
+                const int pl = row / BM, r = row % BM;
+                base = op.A + pl * ps; ld = op.lda; gr = m0 + r; lim = op.M; dst = tileA(s, pl) + r * BP_LD + c;
+            } else {
+                const int pl = (row - N_PLANES * BM) / BN, r = (row - N_PLANES * BM) % BN;
+                base = op.B + pl * ps; ld = op.ldb; gr = n0 + r; lim = op.N; dst = tileB(s, pl) + r * BP_LD + c;
+            }
+            cp_async16(dst, base + (long long)(gr < lim ? gr : 0) * ld + k0 + c, gr < lim ? 16 : 0);
         }
         cp_async_commit();
     };
     // acc: FP32 running sums; pm: the hi x hi product of one 32-deep K slice, px: the five smaller
     // plane products (kept apart so that the tensor core's accumulation of the small terms cannot
     // shift the dominant one); both folded into acc with round-to-nearest adds every slice
-    float acc[2][4][4], pm[2][4][4], px[2][4][4];
+    float acc[MI][NJ][4], pm[MI][NJ][4], px[MI][NJ][4];
 #pragma unroll
-    for (int i = 0; i < 2; ++i)
+    for (int i = 0; i < MI; ++i)
 #pragma unroll
-        for (int j = 0; j < 4; ++j)
+        for (int j = 0; j < NJ; ++j)
 #pragma unroll
             for (int e = 0; e < 4; ++e) acc[i][j][e] = pm[i][j][e] = px[i][j][e] = 0.f;
     const int nk = op.Kpad / BP_K;
@@ -467,28 +488,28 @@ __global__ void __launch_bounds__(BP_T) bt_plane_kernel(const int4 *__restrict__
         if (kb + 1 < nk) load_stage(s ^ 1, (kb + 1) * BP_K);
 #pragma unroll
         for (int kk = 0; kk < BP_K; kk += 16) {
-            unsigned af[2][N_PLANES][4];
+            unsigned af[MI][N_PLANES][4];
 #pragma unroll
-            for (int i = 0; i < 2; ++i)
+            for (int i = 0; i < MI; ++i)
 #pragma unroll
                 for (int q = 0; q < N_PLANES; ++q) {
-                    const bf16 *pa = tile(s, q) + (wm * 32 + i * 16 + g) * BP_LD + kk + tg * 2;
+                    const bf16 *pa = tileA(s, q) + (wm * (BM / 2) + i * 16 + g) * BP_LD + kk + tg * 2;
                     af[i][q][0] = *(const unsigned *)(pa);
                     af[i][q][1] = *(const unsigned *)(pa + 8 * BP_LD);
                     af[i][q][2] = *(const unsigned *)(pa + 8);
                     af[i][q][3] = *(const unsigned *)(pa + 8 * BP_LD + 8);
                 }
 #pragma unroll
-            for (int j = 0; j < 4; ++j) {
+            for (int j = 0; j < NJ; ++j) {
                 unsigned bf[N_PLANES][2];
 #pragma unroll
                 for (int q = 0; q < N_PLANES; ++q) {
-                    const bf16 *pb = tile(s, N_PLANES + q) + (wn * 32 + j * 8 + g) * BP_LD + kk + tg * 2;
+                    const bf16 *pb = tileB(s, q) + (wn * (BN / 2) + j * 8 + g) * BP_LD + kk + tg * 2;
                     bf[q][0] = *(const unsigned *)(pb);
                     bf[q][1] = *(const unsigned *)(pb + 8);
                 }
 #pragma unroll
-                for (int i = 0; i < 2; ++i) {
+                for (int i = 0; i < MI; ++i) {
                     mma_bf16(pm[i][j], af[i][0], bf[0]);
                     mma_bf16(px[i][j], af[i][0], bf[1]);
                     mma_bf16(px[i][j], af[i][1], bf[0]);
@@ -499,9 +520,9 @@ __global__ void __launch_bounds__(BP_T) bt_plane_kernel(const int4 *__restrict__
             }
         }
 #pragma unroll
-        for (int i = 0; i < 2; ++i)
+        for (int i = 0; i < MI; ++i)
 #pragma unroll
-            for (int j = 0; j < 4; ++j)
+            for (int j = 0; j < NJ; ++j)
 #pragma unroll
                 for (int e = 0; e < 4; ++e) {
                     acc[i][j][e] += pm[i][j][e] + px[i][j][e];
@@ -510,13 +531,13 @@ __global__ void __launch_bounds__(BP_T) bt_plane_kernel(const int4 *__restrict__
         __syncthreads();
     }
 #pragma unroll
-    for (int i = 0; i < 2; ++i)
+    for (int i = 0; i < MI; ++i)
 #pragma unroll
-        for (int j = 0; j < 4; ++j)
+        for (int j = 0; j < NJ; ++j)
 #pragma unroll
             for (int e = 0; e < 4; ++e) {
-                const int m = m0 + wm * 32 + i * 16 + g + (e >= 2 ? 8 : 0);
-                const int n = n0 + wn * 32 + j * 8 + tg * 2 + (e & 1);
+                const int m = m0 + wm * (BM / 2) + i * 16 + g + (e >= 2 ? 8 : 0);
+                const int n = n0 + wn * (BN / 2) + j * 8 + tg * 2 + (e & 1);
                 if (m < op.M && n < op.N) step.epi(op, m, n, acc[i][j][e]);
             }
 }
@@ -1222,6 +1243,9 @@ struct PinnedBuf {
     }
 };
 
+// the four plane GEMM steps of the mixed product
+enum BpStep { BP_P1 = 0, BP_P2 = 1, BP_P4 = 2, BP_P5 = 3, BP_STEPS = 4 };
+
 struct BatchWork {
     std::vector<BtInst> h;
     PinnedBuf pinC, pinS, pinG, pinGlr, pinOm;   // staging of the instance inputs
@@ -1230,7 +1254,10 @@ struct BatchWork {
     DevBuf<double> C, SC, S, blk, glr, glr_atoms, gam, omega, V, AV, R, Rk, T, sub, H, F, D, u, err, Y;
     DevBuf<int> ao_off, ao_atom, pos, active;
     DevBuf<long long> off_glr_atoms;
-    DevBuf<int4> t_sc, t1, t2, t4, t5, p1, p2, p4, p5;
+    DevBuf<int4> t_sc, t1, t2, t4, t5;
+    DevBuf<int4> pt[BP_STEPS][BP_SHAPES];   // plane GEMM tiles per product step and tile shape
+    size_t npt[BP_STEPS][BP_SHAPES] = {};
+    DevBuf<int4> tune_tiles[BP_SHAPES];
     DevBuf<bf16> Pl;
     DevBuf<float> glr32, blk32, D32;
     cudaGraphExec_t graph = nullptr;
@@ -1260,19 +1287,185 @@ static void bt_launch(Ctx &c, const DevBuf<int4> &tiles, size_t n_tiles, const S
     c.prof_end(slot, flops, 0.0);
 }
 
-template <class Step>
-static void bt_plane_launch(Ctx &c, const DevBuf<int4> &tiles, size_t n_tiles, const Step &step, int family) {
-    if (n_tiles == 0) return;
-    int slot = c.prof_begin(family);
-    static bool attr = false;
-    if (!attr) {
-        TINCR_CUDA(cudaFuncSetAttribute(bt_plane_kernel<Step>, cudaFuncAttributeMaxDynamicSharedMemorySize, BP_SMEM));
-        attr = true;
-    }
-    bt_plane_kernel<Step><<<(unsigned)n_tiles, BP_T, BP_SMEM, c.stream>>>(tiles.p, step);
-    count_launch(c.stream, "bt_plane");
+template <class Step, int BM, int BN>
+static void bp_launch(cudaStream_t st, const int4 *tiles, size_t n, const Step &step) {
+    static const bool attr = [] {
+        TINCR_CUDA(cudaFuncSetAttribute(bt_plane_kernel<Step, BM, BN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        bp_smem(BM, BN)));
+        return true;
+    }();
+    (void)attr;
+    bt_plane_kernel<Step, BM, BN><<<(unsigned)n, BP_T, bp_smem(BM, BN), st>>>(tiles, step);
+    count_launch(st, "bt_plane");
     check_launch("bt_plane");
-    c.prof_end(slot, 0.0, 0.0);
+}
+
+template <class Step>
+static void bp_launch_shape(cudaStream_t st, int shape, const int4 *tiles, size_t n, const Step &step) {
+    if (n == 0) return;
+    switch (shape) {
+    case 0: bp_launch<Step, 64, 64>(st, tiles, n, step); break;
+    case 1: bp_launch<Step, 64, 32>(st, tiles, n, step); break;
+    case 2: bp_launch<Step, 32, 64>(st, tiles, n, step); break;
+    default: bp_launch<Step, 32, 32>(st, tiles, n, step); break;
+    }
+}
+
+// one plane step: a launch per tile shape in use
+template <class Step>
+static void bt_plane_launch(Ctx &c, BatchWork &w, int p, const Step &step, int family) {
+    for (int sh = 0; sh < BP_SHAPES; ++sh) {
+        if (w.npt[p][sh] == 0) continue;
+        const int slot = c.prof_begin(family);
+        bp_launch_shape(c.stream, sh, w.pt[p][sh].p, w.npt[p][sh], step);
+        c.prof_end(slot, 0.0, 0.0);
+    }
+}
+
+// ----------------------------------------------------------------------------------------------
+// autotuner of the plane GEMM tile shapes
+// ----------------------------------------------------------------------------------------------
+// The instances of an FMO batch come in a few shapes (monomers of each ring count, pairs of them).
+// For each shape (atoms, AOs, occupied, virtual, long-range flag) and each plane step, the tuner
+// times the four tile shapes on the batch's own instances of that shape, all vector slots, the
+// tile list repeated until the 64 x 64 grid has at least four CTAs per SM, and keeps the fastest
+// (64 x 64 unless another is more than 2% faster).  Smaller tiles waste less of a tile on
+// 96 - 204-row operands; larger ones load less per output.  The table lives for the process.
+
+struct BpKey {
+    int device, n_atoms, n_orb, n_occ, n_virt, lc;
+    bool operator<(const BpKey &o) const {
+        return std::tie(device, n_atoms, n_orb, n_occ, n_virt, lc) <
+               std::tie(o.device, o.n_atoms, o.n_orb, o.n_occ, o.n_virt, o.lc);
+    }
+};
+struct BpChoice {
+    int shape[BP_STEPS];                 // -1: the step does not run for this shape
+    double us[BP_STEPS][BP_SHAPES];      // measured time of each candidate per repetition of the tiles, us
+};
+static std::mutex g_bp_mu;
+static std::map<BpKey, BpChoice> g_bp_table;
+
+static BpKey bp_key(int device, const BtInst &b) { return BpKey{device, b.N, b.n, b.o, b.v, b.lc}; }
+
+static bool bp_step_runs(const BtInst &b, int p) { return (p != BP_P2 && p != BP_P4) || b.lc; }
+
+// tiles of every vector slot of instance I for step p in tile shape sh
+static void bp_tiles(const BtInst &b, int I, int p, int sh, std::vector<int4> &out) {
+    if (!bp_step_runs(b, p)) return;
+    const int n2 = 2 * b.n;
+    const int M = p == BP_P5 ? b.o : n2, N = p == BP_P2 ? n2 : b.v;
+    for (int s = 0; s < b.nr; ++s)
+        for (int tm = 0; tm < ceil_div(M, BP_BM[sh]); ++tm)
+            for (int tn = 0; tn < ceil_div(N, BP_BN[sh]); ++tn) out.push_back(make_int4(I, s, tm, tn));
+}
+
+// forced shape from TINCR_GB300_BATCH_TILES (64x64, 64x32, 32x64, 32x32), or -1 for the tuner
+static int bp_forced_shape() {
+    const char *e = getenv("TINCR_GB300_BATCH_TILES");
+    if (!e || !*e || !strcmp(e, "auto")) return -1;
+    for (int sh = 0; sh < BP_SHAPES; ++sh) {
+        char name[16];
+        snprintf(name, sizeof name, "%dx%d", BP_BM[sh], BP_BN[sh]);
+        if (!strcmp(e, name)) return sh;
+    }
+    fail(TINCR_BAD_ARG, std::string("TINCR_GB300_BATCH_TILES: unknown tile shape ") + e);
+    return -1;
+}
+
+template <class Step>
+static void bp_probe(cudaStream_t st, int sh, const int4 *tiles, size_t n, const Step &step) {
+    bp_launch_shape(st, sh, tiles, n, step);
+}
+
+// Tune every instance shape of the batch missing from the table.  Runs after the guesses and before
+// the first iteration: everything the probes write (H, F, G planes, Coulomb diagonals, the products of
+// the guesses) is written again by the first iteration before it is read.
+static void bp_autotune(Ctx &c, BatchWork &w, const BtArrays &a, int n_sm) {
+    std::map<BpKey, std::vector<int>> todo;
+    {
+        std::lock_guard<std::mutex> lk(g_bp_mu);
+        for (int I = 0; I < (int)w.h.size(); ++I) {
+            const BpKey k = bp_key(c.device, w.h[I]);
+            if (!g_bp_table.count(k)) todo[k].push_back(I);
+        }
+    }
+    if (todo.empty()) return;
+    constexpr int REPS = 3;
+    std::vector<cudaEvent_t> ev(2 * BP_STEPS * BP_SHAPES * (REPS + 1));
+    for (auto &e : ev) TINCR_CUDA(cudaEventCreate(&e));
+    for (auto &kv : todo) {
+        const BtInst &b0 = w.h[kv.second[0]];
+        BpChoice ch{};
+        for (int p = 0; p < BP_STEPS; ++p) {
+            ch.shape[p] = -1;
+            if (!bp_step_runs(b0, p)) continue;
+            std::vector<int4> base0;
+            for (int I : kv.second) bp_tiles(w.h[I], I, p, 0, base0);
+            const size_t reps = std::min<size_t>(64, std::max<size_t>(1, (4 * (size_t)n_sm + base0.size() - 1) / base0.size()));
+            size_t cnt[BP_SHAPES];
+            for (int sh = 0; sh < BP_SHAPES; ++sh) {
+                std::vector<int4> one, all;
+                for (int I : kv.second) bp_tiles(w.h[I], I, p, sh, one);
+                for (size_t r = 0; r < reps; ++r) all.insert(all.end(), one.begin(), one.end());
+                cnt[sh] = all.size();
+                upload_any(c.stream, w.tune_tiles[sh], all);
+            }
+            for (int sh = 0; sh < BP_SHAPES; ++sh)
+                for (int r = 0; r <= REPS; ++r) {   // r = 0 warms up
+                    cudaEvent_t *e = &ev[2 * ((p * BP_SHAPES + sh) * (REPS + 1) + r)];
+                    TINCR_CUDA(cudaEventRecord(e[0], c.stream));
+                    const int4 *t = w.tune_tiles[sh].p;
+                    switch (p) {
+                    case BP_P1: bp_probe(c.stream, sh, t, cnt[sh], BtP1{a}); break;
+                    case BP_P2: bp_probe(c.stream, sh, t, cnt[sh], BtP2{a}); break;
+                    case BP_P4: bp_probe(c.stream, sh, t, cnt[sh], BtP4{a}); break;
+                    default: bp_probe(c.stream, sh, t, cnt[sh], BtP5{a}); break;
+                    }
+                    TINCR_CUDA(cudaEventRecord(e[1], c.stream));
+                }
+            c.sync();   // the tile lists of the next step reuse the buffers
+            float best = 0.f;
+            for (int sh = 0; sh < BP_SHAPES; ++sh) {
+                float t = 1e30f;
+                for (int r = 1; r <= REPS; ++r) {
+                    cudaEvent_t *e = &ev[2 * ((p * BP_SHAPES + sh) * (REPS + 1) + r)];
+                    float ms = 0.f;
+                    TINCR_CUDA(cudaEventElapsedTime(&ms, e[0], e[1]));
+                    t = std::min(t, ms);
+                }
+                ch.us[p][sh] = 1000.0 * t / (double)reps;
+                if (sh == 0 || t < 0.98f * best) {
+                    best = t;
+                    ch.shape[p] = sh;
+                }
+            }
+        }
+        std::lock_guard<std::mutex> lk(g_bp_mu);
+        g_bp_table[kv.first] = ch;
+    }
+    for (auto &e : ev) cudaEventDestroy(e);
+}
+
+int bp_table_entries(int capacity, int *entries, double *us) {
+    std::lock_guard<std::mutex> lk(g_bp_mu);
+    int n = 0;
+    for (const auto &kv : g_bp_table) {
+        if (n < capacity) {
+            const BpKey &k = kv.first;
+            const BpChoice &ch = kv.second;
+            if (entries) {
+                int *e = entries + 9 * n;
+                e[0] = k.n_atoms; e[1] = k.n_orb; e[2] = k.n_occ; e[3] = k.n_virt; e[4] = k.lc;
+                for (int p = 0; p < BP_STEPS; ++p) e[5 + p] = ch.shape[p];
+            }
+            if (us)
+                for (int p = 0; p < BP_STEPS; ++p)
+                    for (int sh = 0; sh < BP_SHAPES; ++sh) us[(n * BP_STEPS + p) * BP_SHAPES + sh] = ch.us[p][sh];
+        }
+        ++n;
+    }
+    return n;
 }
 
 int Ctx::solve_batch(int n_inst, const tincr_tda_instance *hin, int max_iter, double tol, int precision,
@@ -1447,29 +1640,8 @@ int Ctx::solve_batch(int n_inst, const tincr_tda_instance *hin, int max_iter, do
     upload_any(stream, w.t2, t2);
     upload_any(stream, w.t4, t4);
     upload_any(stream, w.t5, t5);
-    // plane GEMM tiles of the mixed form (64 x 64)
-    std::vector<int4> p1, p2, p4, p5;
+    // split-BF16 planes of the mixed form (their tile tables follow the guesses and the autotuner)
     if (mixed) {
-        for (int I = 0; I < n_inst; ++I) {
-            const BtInst &b = w.h[I];
-            const int n2 = 2 * b.n;
-            for (int s = 0; s < b.nr; ++s) {
-                for (int tm = 0; tm < ceil_div(n2, 64); ++tm)
-                    for (int tn = 0; tn < ceil_div(b.v, 64); ++tn) {
-                        p1.push_back(make_int4(I, s, tm, tn));
-                        if (b.lc) p4.push_back(make_int4(I, s, tm, tn));
-                    }
-                if (b.lc)
-                    for (int tm = 0; tm < ceil_div(n2, 64); ++tm)
-                        for (int tn = 0; tn < ceil_div(n2, 64); ++tn) p2.push_back(make_int4(I, s, tm, tn));
-                for (int tm = 0; tm < ceil_div(b.o, 64); ++tm)
-                    for (int tn = 0; tn < ceil_div(b.v, 64); ++tn) p5.push_back(make_int4(I, s, tm, tn));
-            }
-        }
-        upload_any(stream, w.p1, p1);
-        upload_any(stream, w.p2, p2);
-        upload_any(stream, w.p4, p4);
-        upload_any(stream, w.p5, p5);
         w.Pl.reserve(N_PLANES * (o_pc + o_pv));
         TINCR_CUDA(cudaMemsetAsync(w.Pl.p, 0, N_PLANES * (o_pc + o_pv) * sizeof(bf16), stream));   // K padding stays zero
         for (auto &b : w.h) b.off_pv += o_pc;
@@ -1525,13 +1697,40 @@ int Ctx::solve_batch(int n_inst, const tincr_tda_instance *hin, int max_iter, do
     bt_guess_kernel<<<n_inst, BT_T, 0, stream>>>(a, w.pos.p);
     count_launch(stream, "bt_guess");
     check_launch("bt_guess");
+    const dim3 gv(nr_max, n_inst);
+    if (mixed) {
+        // tile shape of every instance and plane step: forced, or from the autotuner's table
+        const int forced = bp_forced_shape();
+        if (forced < 0) {
+            TINCR_CUDA(cudaMemsetAsync(w.D32.p, 0, o_d * sizeof(float), stream));
+            bt_split_x_kernel<<<gv, BT_T, 0, stream>>>(a);
+            count_launch(stream, "bt_split_x");
+            check_launch("bt_split_x");
+            bp_autotune(*this, w, a, n_sm);
+        }
+        std::vector<int4> pt[BP_STEPS][BP_SHAPES];
+        {
+            std::lock_guard<std::mutex> lk(g_bp_mu);
+            for (int I = 0; I < n_inst; ++I) {
+                const BpChoice *ch = forced < 0 ? &g_bp_table.at(bp_key(device, w.h[I])) : nullptr;
+                for (int p = 0; p < BP_STEPS; ++p) {
+                    const int sh = ch ? ch->shape[p] : forced;
+                    if (sh >= 0) bp_tiles(w.h[I], I, p, sh, pt[p][sh]);
+                }
+            }
+        }
+        for (int p = 0; p < BP_STEPS; ++p)
+            for (int sh = 0; sh < BP_SHAPES; ++sh) {
+                w.npt[p][sh] = pt[p][sh].size();
+                if (!pt[p][sh].empty()) upload_any(stream, w.pt[p][sh], pt[p][sh]);
+            }
+    }
 
     const size_t sub_smem = bt_subspace_smem(mmax_all);
     TINCR_CUDA(cudaFuncSetAttribute(bt_subspace_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sub_smem));
     const size_t coul_smem = (size_t)nmax_atoms * sizeof(double);
     if (coul_smem > 48 * 1024)
         TINCR_CUDA(cudaFuncSetAttribute(bt_coulomb_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)coul_smem));
-    const dim3 gv(nr_max, n_inst);
 
     // one Davidson iteration of every running instance (captured once as a graph)
     auto iteration = [&]() {
@@ -1558,19 +1757,19 @@ int Ctx::solve_batch(int n_inst, const tincr_tda_instance *hin, int max_iter, do
         bt_split_x_kernel<<<gv, BT_T, 0, stream>>>(a);
         count_launch(stream, "bt_split_x");
         check_launch("bt_split_x");
-        bt_plane_launch(*this, w.p1, p1.size(), BtP1{a}, TINCR_KF_AO_TRANSFORM);
-        bt_plane_launch(*this, w.p2, p2.size(), BtP2{a}, TINCR_KF_AO_EXCHANGE);   // + LC Coulomb diagonals
+        bt_plane_launch(*this, w, BP_P1, BtP1{a}, TINCR_KF_AO_TRANSFORM);
+        bt_plane_launch(*this, w, BP_P2, BtP2{a}, TINCR_KF_AO_EXCHANGE);   // + LC Coulomb diagonals
         bt_diag_kernel<<<gv, BT_T, 0, stream>>>(a, BT_MIXED);                  // non-LC Coulomb diagonals
         count_launch(stream, "bt_diag");
         check_launch("bt_diag");
         bt_coulomb_kernel<<<gv, BT_T, coul_smem, stream>>>(a, BT_MIXED);
         count_launch(stream, "bt_coulomb");
         check_launch("bt_coulomb");
-        bt_plane_launch(*this, w.p4, p4.size(), BtP4{a}, TINCR_KF_AO_EXCHANGE);
+        bt_plane_launch(*this, w, BP_P4, BtP4{a}, TINCR_KF_AO_EXCHANGE);
         bt_gt_nolc_kernel<<<gv, BT_T, 0, stream>>>(a);
         count_launch(stream, "bt_gt_nolc");
         check_launch("bt_gt_nolc");
-        bt_plane_launch(*this, w.p5, p5.size(), BtP5{a}, TINCR_KF_AO_TRANSFORM);
+        bt_plane_launch(*this, w, BP_P5, BtP5{a}, TINCR_KF_AO_TRANSFORM);
         TINCR_CUDA(cudaMemsetAsync(w.active.p, 0, sizeof(int), stream));
         bt_subspace_kernel<<<n_inst, BT_T, sub_smem, stream>>>(a);
         count_launch(stream, "bt_subspace");

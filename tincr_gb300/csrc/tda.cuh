@@ -33,6 +33,8 @@ constexpr double MIXED_TOL_FLOOR = 1e-6;
 
 struct BatchWork;                      // batched LE / CT TDA workspace (batch.cu)
 void release_batch(BatchWork *w);
+// entries of the batch tile-shape autotuner's table (9 ints and 16 times each); returns the count
+int bp_table_entries(int capacity, int *entries, double *us);
 
 struct Ctx {
     int device = 0;
