@@ -31,12 +31,16 @@
 #include <omp.h>
 #endif
 
+#include <cooperative_groups.h>
+
 #include "batch.cuh"
 #include "gemm_f64.cuh"
 #include "planes.cuh"
 #include "tda.cuh"
 
 namespace tincr {
+
+namespace cg = cooperative_groups;
 
 constexpr int BT_T = 256;
 constexpr int BT_MAXR = 6;   // roots per instance (subspace up to 90, Jacobi in shared memory)
@@ -329,13 +333,15 @@ __global__ void bt_guess_kernel(BtArrays a, const int *__restrict__ pos) {
 }
 
 // Coulomb diagonals d3_mu = M[mu][n+mu], d2_mu = M[n+mu][mu] of M = H [C_v;SC_v]^T, one warp per row
-// (non-LC instances in the products, every instance in the final pass)
-__global__ void bt_diag_kernel(BtArrays a, int mode) {
-    const int I = blockIdx.y, b = blockIdx.x;
+// (non-LC and, in the mixed form, block-structured instances in the products, every instance in the
+// final pass)
+__global__ void bt_diag_kernel(BtArrays a, int mode, int I0) {
+    const int I = I0 + blockIdx.y, b = blockIdx.x;
     const BtInst in = a.inst[I];
     const double *X;
     if (!bt_vector(a, in, I, b, mode == BT_FINAL, &X)) return;
-    if (mode != BT_FINAL && in.lc) return;   // the exchange GEMM's epilogue captures them
+    // the exchange GEMM's epilogue captures them for LC instances, unless it skips their blocks
+    if (mode != BT_FINAL && in.lc && !(mode == BT_MIXED && in.nh)) return;
     const int n = in.n, v = in.v;
     const double *H = a.H + in.off_h + (long long)b * 2 * n * v;
     const double *rv = a.blk + in.off_blk + 2LL * n * in.o;
@@ -355,9 +361,9 @@ __global__ void bt_diag_kernel(BtArrays a, int mode) {
 // y_A = 1/2 sum_{mu in A}(d3 + d2) (= q_ov X per atom), z = gamma y; z onto F's off-diagonal-block
 // diagonals (FP64 form, LC) or kept per AO (non-LC, and the mixed form); in the final pass y is the
 // transition charge of the root.
-__global__ void bt_coulomb_kernel(BtArrays a, int mode) {
+__global__ void bt_coulomb_kernel(BtArrays a, int mode, int I0) {
     extern __shared__ double ysh[];
-    const int I = blockIdx.y, b = blockIdx.x;
+    const int I = I0 + blockIdx.y, b = blockIdx.x;
     const BtInst in = a.inst[I];
     const double *X;
     const bool final_pass = mode == BT_FINAL;
@@ -392,8 +398,8 @@ __global__ void bt_coulomb_kernel(BtArrays a, int mode) {
 }
 
 // non-LC: G_b = diag(z, z) [C_v;SC_v]  (written over H_b)
-__global__ void bt_scale_rows_kernel(BtArrays a) {
-    const int I = blockIdx.y, b = blockIdx.x;
+__global__ void bt_scale_rows_kernel(BtArrays a, int I0) {
+    const int I = I0 + blockIdx.y, b = blockIdx.x;
     const BtInst in = a.inst[I];
     const double *X;
     if (in.lc || !bt_vector(a, in, I, b, false, &X)) return;
@@ -574,8 +580,8 @@ __global__ void bt_const_planes_kernel(BtArrays a) {
 }
 
 // X^T planes of the new trial vectors
-__global__ void bt_split_x_kernel(BtArrays a) {
-    const int I = blockIdx.y, b = blockIdx.x;
+__global__ void bt_split_x_kernel(BtArrays a, int I0) {
+    const int I = I0 + blockIdx.y, b = blockIdx.x;
     const BtInst in = a.inst[I];
     const double *X;
     if (!bt_vector(a, in, I, b, false, &X)) return;
@@ -601,7 +607,7 @@ struct BtP1 {
     }
     __device__ void epi(const BtPlaneOp &op, int m, int n, float acc) const {
         const BtInst &in = *op.in;
-        if (!in.lc) a.H[in.off_h + (long long)op.b * 2 * in.n * in.v + (long long)m * in.v + n] = (double)acc;
+        if (!in.lc || in.nh) a.H[in.off_h + (long long)op.b * 2 * in.n * in.v + (long long)m * in.v + n] = (double)acc;
         bt_split_store(a, bt_pv_h(in, op.b) + (long long)m * in.kv + n, acc);
     }
 };
@@ -623,9 +629,11 @@ struct BtP2 {
         const BtInst &in = *op.in;
         const int n = in.n;
         const int rr = r < n ? r : r - n, cc = c < n ? c : c - n;
-        double *d = a.D + in.off_d;   // Coulomb diagonals of M from the same accumulator
-        if (r < n && c == r + n) d[(long long)op.b * n + r] = (double)acc;
-        if (r >= n && c == r - n) d[(long long)(in.nr + op.b) * n + c] = (double)acc;
+        if (!in.nh) {   // Coulomb diagonals of M from the same accumulator (bt_diag_kernel otherwise)
+            double *d = a.D + in.off_d;
+            if (r < n && c == r + n) d[(long long)op.b * n + r] = (double)acc;
+            if (r >= n && c == r - n) d[(long long)(in.nr + op.b) * n + c] = (double)acc;
+        }
         const float f = -0.25f * a.glr32[in.off_glr + (long long)rr * n + cc] * acc;
         bt_split_store(a, bt_pv_f(in, op.b) + (long long)r * in.k2 + c, f);
     }
@@ -654,8 +662,8 @@ struct BtP4 {
 };
 
 // non-LC: G = diag(z, z) [C_v;SC_v] as transposed planes
-__global__ void bt_gt_nolc_kernel(BtArrays a) {
-    const int I = blockIdx.y, b = blockIdx.x;
+__global__ void bt_gt_nolc_kernel(BtArrays a, int I0) {
+    const int I = I0 + blockIdx.y, b = blockIdx.x;
     const BtInst in = a.inst[I];
     const double *X;
     if (in.lc || !bt_vector(a, in, I, b, false, &X)) return;
@@ -676,7 +684,7 @@ struct BtP5 {
         const double *X;
         if (!bt_vector(a, in, I, b, false, &X)) return false;
         op.in = &a.inst[I]; op.I = I; op.b = b; op.X = X;
-        op.M = in.o; op.N = in.v; op.Kpad = in.k2;
+        op.M = in.o; op.N = in.v; op.Kpad = in.nh ? in.k5 : in.k2;   // rows n+nh.. of G meet C_o = 0
         op.A = a.P + bt_pc_lswt(in); op.lda = in.k2;
         op.B = a.P + bt_pv_gt(in, b); op.ldb = in.k2;
         return true;
@@ -1015,17 +1023,55 @@ __device__ void bt_eig_lowest(int m, int nr, double *A, double *W, double *w, do
     __syncthreads();
 }
 
+// The subspace step runs on thread-block clusters of BT_CL CTAs.  A heavy instance (several roots
+// on a long vector) takes a whole cluster: its CTAs own interleaved blocks of BT_T components of
+// every ov-long vector and combine their partial sums through distributed shared memory (added in
+// rank order, so every CTA holds the same bits and takes the same decisions); the small
+// eigenproblem is solved by the cluster's first CTA and copied by the others.  Light instances (one CT root) take one CTA each, four to a
+// cluster, where splitting would repeat the eigensolver more than it divides the vector work.
+constexpr int BT_CL = 4;
+
 // shared memory of the subspace kernel for subspaces up to mmax: the projected matrix, eigensolver
-// scratch (4 m + 5 nr m <= mmax^2 doubles since mmax = 15 nr), reductions and Gram-Schmidt dots
+// scratch (4 m + 5 nr m <= mmax^2 doubles since mmax = 15 nr), reductions, Gram-Schmidt dots, two
+// cluster exchange buffers and the new projected columns
 inline size_t bt_subspace_smem(int mmax) {
-    return (2 * (size_t)mmax * mmax + 8 * BT_MAXR * (BT_T / 32) + mmax + BT_MAXR + 16 + BT_MAXR) * sizeof(double);
+    const size_t cb = (size_t)mmax * BT_MAXR + 8;
+    return (2 * (size_t)mmax * mmax + 8 * BT_MAXR * (BT_T / 32) + mmax + BT_MAXR + 16 + BT_MAXR + 3 * cb) *
+           sizeof(double);
 }
 
-// Ritz vectors and residuals of NR roots over this thread's components; sq[r] += |Rk_r|^2 partials
+// Sum over the cluster's CTAs of the n values each CTA holds in `mine` (shared memory): out[k] =
+// the partials of ranks 0, 1, ... added in that order, so every CTA receives the same bits (a CTA
+// working alone copies its values).  Callers alternate between two `mine` buffers: a CTA writes a
+// buffer again only after the next call's cluster barrier, which every CTA reaches after its reads
+// of this call.
+__device__ __forceinline__ void bt_cluster_sum(const cg::cluster_group &cl, bool coop, double *mine, int n,
+                                               double *out) {
+    if (coop) cl.sync();
+    else __syncthreads();
+    for (int k = threadIdx.x; k < n; k += BT_T) {
+        double s = mine[k];
+        if (coop) {
+            s = 0.0;
+#pragma unroll
+            for (int r = 0; r < BT_CL; ++r) s += *cl.map_shared_rank(mine + k, r);
+        }
+        out[k] = s;
+    }
+    __syncthreads();
+}
+
+// heavy instances (about nr^2 ov FP64 work per iteration at or above this) take a whole cluster in
+// the subspace step
+constexpr long long BT_HEAVY = 8192;
+
+// Ritz vectors and residuals of NR roots over this CTA's components (x0, x0 + xs, ...);
+// sq[r] += |Rk_r|^2 partials
 template <int NR>
-__device__ __forceinline__ void bt_ritz(int m, long long ov, const double *V, const double *AV, const double *Yev,
-                                        const double *u, double *R, double *Rk, double (&sq)[BT_MAXR]) {
-    for (long long x = threadIdx.x; x < ov; x += BT_T) {
+__device__ __forceinline__ void bt_ritz(int m, long long ov, long long x0, long long xs, const double *V,
+                                        const double *AV, const double *Yev, const double *u, double *R, double *Rk,
+                                        double (&sq)[BT_MAXR]) {
+    for (long long x = x0; x < ov; x += xs) {
         double rv[NR], av[NR];
 #pragma unroll
         for (int r = 0; r < NR; ++r) rv[r] = av[r] = 0.0;
@@ -1048,17 +1094,28 @@ __device__ __forceinline__ void bt_ritz(int m, long long ov, const double *V, co
     }
 }
 
-__global__ void __launch_bounds__(BT_T) bt_subspace_kernel(BtArrays a) {
-    const int I = blockIdx.x;
+// cl_inst[c]: the work of cluster c, {I, -1, -1, -1} with .y = -2 for one heavy instance I on the
+// whole cluster, or up to four light instances (-1 = none), one per CTA
+__global__ void __cluster_dims__(BT_CL, 1, 1) __launch_bounds__(BT_T)
+    bt_subspace_kernel(BtArrays a, const int4 *__restrict__ cl_inst) {
+    const cg::cluster_group cl = cg::this_cluster();
+    const int rank = (int)cl.block_rank();
+    const int4 cw = cl_inst[blockIdx.x / BT_CL];
+    const bool coop = cw.y == -2;
+    const int I = coop ? cw.x : rank == 0 ? cw.x : rank == 1 ? cw.y : rank == 2 ? cw.z : cw.w;
+    if (I < 0) return;                     // light cluster with fewer than four instances
+    const int part_rank = coop ? rank : 0, ncl = coop ? BT_CL : 1;
+    const bool lead = part_rank == 0;      // writes the instance's shared results
     const int tid = threadIdx.x;
     const BtInst in = a.inst[I];
     __shared__ BtState st;
     __shared__ int s_sel[BT_MAXR], s_nsel, s_action, s_mcur;
-    __shared__ double s_u[BT_MAXR], s_err[BT_MAXR];
+    __shared__ double s_u[BT_MAXR], s_err[BT_MAXR], s_sq[BT_MAXR], s_nrm;
     if (tid == 0) st = a.state[I];
     __syncthreads();
-    if (st.status != BT_RUNNING) return;
+    if (st.status != BT_RUNNING) return;   // the same state in every CTA of a heavy instance's cluster
     const long long ov = in.ov;
+    const long long x0 = (long long)part_rank * BT_T + tid, xs = (long long)ncl * BT_T;   // this CTA's components
     const int nr = in.nr, mmax = in.mmax;
     double *V = a.V + in.off_v, *AV = a.AV + in.off_v;
     double *R = a.R + in.off_r, *Rk = a.Rk + in.off_r, *T = a.T + in.off_r;
@@ -1067,33 +1124,58 @@ __global__ void __launch_bounds__(BT_T) bt_subspace_kernel(BtArrays a) {
     const int m = st.m, m_done = st.m_done;
 
     extern __shared__ double smem[];
+    const size_t cbn = (size_t)mmax * BT_MAXR + 8;
     double *A = smem, *Z = A + (size_t)mmax * mmax;
     double *red = Z + (size_t)mmax * mmax;
     double *cdot = red + 8 * BT_MAXR * (BT_T / 32);
     double *wev = cdot + mmax + BT_MAXR + 16;
+    double *cbuf[2] = {wev + BT_MAXR, wev + BT_MAXR + cbn};
+    double *pnew = cbuf[1] + cbn;
+    int ph = 0;   // exchange buffer of the next cluster sum
 
-    // 1. new columns of the projected matrix: P[i][j] = V_i . AV_j, j in [m_done, m)
+    // 1. new columns of the projected matrix: P[i][j] = V_i . AV_j, j in [m_done, m), one warp per
+    //    entry over this CTA's components, summed over the cluster
+    const int kn = m - m_done;
     {
         const int warp = tid >> 5, lane = tid & 31, nw = BT_T / 32;
-        const int kn = m - m_done;
+        double *part = cbuf[ph];
         for (int e = warp; e < m * kn; e += nw) {
             const int i = e / kn, j = m_done + e % kn;
             const double *x = V + (long long)i * ov, *y = AV + (long long)j * ov;
             double s = 0.0;
-            for (long long t = lane; t < ov; t += 32) s += x[t] * y[t];
+            for (long long b0 = (long long)part_rank * BT_T; b0 < ov; b0 += xs)
+                for (int l = lane; l < BT_T; l += 32) {
+                    const long long t = b0 + l;
+                    if (t < ov) s += x[t] * y[t];
+                }
             for (int off = 16; off; off >>= 1) s += __shfl_down_sync(0xffffffffu, s, off);
-            if (lane == 0) P[(long long)i * mmax + j] = s;
+            if (lane == 0) part[e] = s;
+        }
+        bt_cluster_sum(cl, coop, part, m * kn, pnew);
+        ph ^= 1;
+    }
+    if (lead)
+        for (int e = tid; e < m * kn; e += BT_T) P[(long long)(e / kn) * mmax + m_done + e % kn] = pnew[e];
+    // 2. eigenpairs of the upper triangle (davidson.rs:89-93): old columns from the previous
+    //    iterations, new ones from this step.  The lead CTA solves; the other CTAs of a heavy
+    //    instance's cluster copy its eigenpairs.
+    double *Yev = Z + 4 * m;   // eigenvector r at Yev[r * m + i]
+    if (lead) {
+        for (int e = tid; e < m * m; e += BT_T) {
+            const int i = e / m, j = e % m, lo = i < j ? i : j, hi = i < j ? j : i;
+            A[e] = hi >= m_done ? pnew[lo * kn + hi - m_done] : P[(long long)lo * mmax + hi];
+        }
+        __syncthreads();
+        bt_eig_lowest(m, nr, A, Z, wev, red);
+    }
+    if (coop) {
+        cl.sync();   // the lead's eigenpairs are final (it does not write them again in this step)
+        if (!lead) {
+            const double *yr = cl.map_shared_rank(Yev, 0), *wr = cl.map_shared_rank(wev, 0);
+            for (int e = tid; e < nr * m; e += BT_T) Yev[e] = yr[e];
+            if (tid < nr) wev[tid] = wr[tid];
         }
     }
-    __syncthreads();
-    // 2. eigenpairs of the upper triangle (davidson.rs:89-93)
-    for (int e = tid; e < m * m; e += BT_T) {
-        const int i = e / m, j = e % m;
-        A[e] = i <= j ? P[(long long)i * mmax + j] : P[(long long)j * mmax + i];
-    }
-    __syncthreads();
-    bt_eig_lowest(m, nr, A, Z, wev, red);
-    const double *Yev = Z + 4 * m;   // eigenvector r at Yev[r * m + i]
     if (tid < nr) s_u[tid] = wev[tid];
     __syncthreads();
     // 3. Ritz vectors R_r = sum_i y_ir V_i and residuals Rk_r = sum_i y_ir AV_i - u_r R_r (:101-107),
@@ -1102,25 +1184,30 @@ __global__ void __launch_bounds__(BT_T) bt_subspace_kernel(BtArrays a) {
 #pragma unroll
     for (int r = 0; r < BT_MAXR; ++r) sq[r] = 0.0;
     switch (nr) {
-    case 1: bt_ritz<1>(m, ov, V, AV, Yev, s_u, R, Rk, sq); break;
-    case 2: bt_ritz<2>(m, ov, V, AV, Yev, s_u, R, Rk, sq); break;
-    case 3: bt_ritz<3>(m, ov, V, AV, Yev, s_u, R, Rk, sq); break;
-    case 4: bt_ritz<4>(m, ov, V, AV, Yev, s_u, R, Rk, sq); break;
-    case 5: bt_ritz<5>(m, ov, V, AV, Yev, s_u, R, Rk, sq); break;
-    default: bt_ritz<BT_MAXR>(m, ov, V, AV, Yev, s_u, R, Rk, sq); break;
+    case 1: bt_ritz<1>(m, ov, x0, xs, V, AV, Yev, s_u, R, Rk, sq); break;
+    case 2: bt_ritz<2>(m, ov, x0, xs, V, AV, Yev, s_u, R, Rk, sq); break;
+    case 3: bt_ritz<3>(m, ov, x0, xs, V, AV, Yev, s_u, R, Rk, sq); break;
+    case 4: bt_ritz<4>(m, ov, x0, xs, V, AV, Yev, s_u, R, Rk, sq); break;
+    case 5: bt_ritz<5>(m, ov, x0, xs, V, AV, Yev, s_u, R, Rk, sq); break;
+    default: bt_ritz<BT_MAXR>(m, ov, x0, xs, V, AV, Yev, s_u, R, Rk, sq); break;
     }
     bt_block_sum<BT_MAXR>(sq, red);
-    // 4. convergence and the next action (:109-178)
+    if (tid < BT_MAXR) cbuf[ph][tid] = sq[tid];
+    bt_cluster_sum(cl, coop, cbuf[ph], BT_MAXR, s_sq);
+    ph ^= 1;
+    // 4. convergence and the next action (:109-178), taken identically by every CTA
     if (tid == 0) {
         st.products += m - m_done;
         int cvd = 0;
         bool finite = true;
         double mx = 0.0;
         for (int r = 0; r < nr; ++r) {
-            const double e = sqrt(sq[r]);
+            const double e = sqrt(s_sq[r]);
             s_err[r] = e;
-            a.u[in.off_u + r] = s_u[r];
-            a.err[in.off_u + r] = e;
+            if (lead) {
+                a.u[in.off_u + r] = s_u[r];
+                a.err[in.off_u + r] = e;
+            }
             if (!isfinite(e) || !isfinite(s_u[r])) finite = false;
             if (e < a.tol) ++cvd;
             mx = fmax(mx, e);
@@ -1157,7 +1244,7 @@ __global__ void __launch_bounds__(BT_T) bt_subspace_kernel(BtArrays a) {
         for (int j = 0; j < kadd; ++j) {
             const int r = s_sel[j];
             const double w = s_u[r];
-            for (long long x = tid; x < ov; x += BT_T) {
+            for (long long x = x0; x < ov; x += xs) {
                 double d = w - om[x];
                 if (fabs(d) < 1.0e-4) d = 1.0;
                 T[(long long)j * ov + x] = Rk[(long long)r * ov + x] / d;
@@ -1167,11 +1254,12 @@ __global__ void __launch_bounds__(BT_T) bt_subspace_kernel(BtArrays a) {
         for (int j = 0; j < kadd; ++j) {
             double *t = T + (long long)j * ov;
             const int mc = s_mcur;
+            double *part = cbuf[ph];
             for (int i0 = 0; i0 < mc; i0 += 8) {
                 double c8[8];
 #pragma unroll
                 for (int q = 0; q < 8; ++q) c8[q] = 0.0;
-                for (long long x = tid; x < ov; x += BT_T) {
+                for (long long x = x0; x < ov; x += xs) {
                     const double tx = t[x];
 #pragma unroll
                     for (int q = 0; q < 8; ++q)
@@ -1180,25 +1268,29 @@ __global__ void __launch_bounds__(BT_T) bt_subspace_kernel(BtArrays a) {
                 bt_block_sum8(c8, red);
 #pragma unroll
                 for (int q = 0; q < 8; ++q)
-                    if (tid == q) cdot[i0 + q] = c8[q];
+                    if (tid == q) part[i0 + q] = c8[q];
             }
-            __syncthreads();
+            bt_cluster_sum(cl, coop, part, mc, cdot);
+            ph ^= 1;
             double nr2[1] = {0.0};
-            for (long long x = tid; x < ov; x += BT_T) {
+            for (long long x = x0; x < ov; x += xs) {
                 double s = t[x];
                 for (int i = 0; i < mc; ++i) s -= cdot[i] * V[(long long)i * ov + x];
                 t[x] = s;
                 nr2[0] += s * s;
             }
             bt_block_sum<1>(nr2, red);
-            const double nrm = sqrt(nr2[0]);
+            if (tid == 0) cbuf[ph][0] = nr2[0];
+            bt_cluster_sum(cl, coop, cbuf[ph], 1, &s_nrm);
+            ph ^= 1;
+            const double nrm = sqrt(s_nrm);
             if (!isfinite(nrm)) {
                 if (tid == 0) st.status = BT_NONFINITE;
                 break;
             }
             if (nrm > 1.0e-8 && mc < mmax) {
                 const double inv = 1.0 / nrm;
-                for (long long x = tid; x < ov; x += BT_T) V[(long long)mc * ov + x] = t[x] * inv;
+                for (long long x = x0; x < ov; x += xs) V[(long long)mc * ov + x] = t[x] * inv;
                 __syncthreads();
                 if (tid == 0) s_mcur = mc + 1;
             }
@@ -1206,8 +1298,9 @@ __global__ void __launch_bounds__(BT_T) bt_subspace_kernel(BtArrays a) {
         }
         if (tid == 0) st.m = s_mcur;
     } else if (s_action == 2) {
-        // 6. collapse onto the Ritz vectors (:172-176)
-        for (long long x = tid; x < (long long)nr * ov; x += BT_T) V[x] = R[x];
+        // 6. collapse onto the Ritz vectors (:172-176), this CTA's components
+        for (int r = 0; r < nr; ++r)
+            for (long long x = x0; x < ov; x += xs) V[(long long)r * ov + x] = R[(long long)r * ov + x];
         if (tid == 0) {
             st.dim_sub = nr;
             st.m = nr;
@@ -1215,8 +1308,8 @@ __global__ void __launch_bounds__(BT_T) bt_subspace_kernel(BtArrays a) {
             st.collapses += 1;
         }
     }
-    __syncthreads();
-    if (tid == 0) {
+    if (coop) cl.sync();   // no CTA leaves while another may still read its exchange buffers
+    if (tid == 0 && lead) {
         a.state[I] = st;
         if (st.status == BT_RUNNING) atomicAdd(a.active, 1);
     }
@@ -1254,15 +1347,25 @@ struct BatchWork {
     DevBuf<double> C, SC, S, blk, glr, glr_atoms, gam, omega, V, AV, R, Rk, T, sub, H, F, D, u, err, Y;
     DevBuf<int> ao_off, ao_atom, pos, active;
     DevBuf<long long> off_glr_atoms;
-    DevBuf<int4> t_sc, t1, t2, t4, t5;
-    DevBuf<int4> pt[BP_STEPS][BP_SHAPES];   // plane GEMM tiles per product step and tile shape
-    size_t npt[BP_STEPS][BP_SHAPES] = {};
+    DevBuf<int4> t_sc;
+    // Instances run in two groups, heavy (several roots on long vectors) then light, whose
+    // iterations are two concurrent branches of the iteration graph; per group:
+    DevBuf<int4> t1[2], t2[2], t4[2], t5[2];           // FP64 product tiles
+    size_t nt1[2] = {}, nt2[2] = {}, nt4[2] = {}, nt5[2] = {};
+    DevBuf<int4> pt[2][BP_STEPS][BP_SHAPES];           // plane GEMM tiles per product step and tile shape
+    size_t npt[2][BP_STEPS][BP_SHAPES] = {};
+    DevBuf<int4> cl_inst[2];                           // work of each cluster of the subspace step
     DevBuf<int4> tune_tiles[BP_SHAPES];
     DevBuf<bf16> Pl;
     DevBuf<float> glr32, blk32, D32;
-    cudaGraphExec_t graph = nullptr;
+    cudaStream_t hi = nullptr, side = nullptr;         // branches of the heavy (high priority) and light groups
+    cudaEvent_t fork = nullptr, join_hi = nullptr, join_side = nullptr;
     ~BatchWork() {
-        if (graph) cudaGraphExecDestroy(graph);
+        if (fork) cudaEventDestroy(fork);
+        if (join_hi) cudaEventDestroy(join_hi);
+        if (join_side) cudaEventDestroy(join_side);
+        if (hi) cudaStreamDestroy(hi);
+        if (side) cudaStreamDestroy(side);
     }
 };
 
@@ -1278,11 +1381,12 @@ static void upload_any(cudaStream_t st, DevBuf<T> &d, const std::vector<T> &h) {
 }
 
 template <bool TA, bool TB, class Step>
-static void bt_launch(Ctx &c, const DevBuf<int4> &tiles, size_t n_tiles, const Step &step, int family, double flops) {
+static void bt_launch(Ctx &c, cudaStream_t st, const DevBuf<int4> &tiles, size_t n_tiles, const Step &step, int family,
+                      double flops) {
     if (n_tiles == 0) return;
     int slot = c.prof_begin(family);
-    bt_gemm_kernel<TA, TB, Step><<<(unsigned)n_tiles, GB_T, 0, c.stream>>>(tiles.p, step);
-    count_launch(c.stream, "bt_gemm");
+    bt_gemm_kernel<TA, TB, Step><<<(unsigned)n_tiles, GB_T, 0, st>>>(tiles.p, step);
+    count_launch(st, "bt_gemm");
     check_launch("bt_gemm");
     c.prof_end(slot, flops, 0.0);
 }
@@ -1313,11 +1417,11 @@ static void bp_launch_shape(cudaStream_t st, int shape, const int4 *tiles, size_
 
 // one plane step: a launch per tile shape in use
 template <class Step>
-static void bt_plane_launch(Ctx &c, BatchWork &w, int p, const Step &step, int family) {
+static void bt_plane_launch(Ctx &c, cudaStream_t st, BatchWork &w, int g, int p, const Step &step, int family) {
     for (int sh = 0; sh < BP_SHAPES; ++sh) {
-        if (w.npt[p][sh] == 0) continue;
+        if (w.npt[g][p][sh] == 0) continue;
         const int slot = c.prof_begin(family);
-        bp_launch_shape(c.stream, sh, w.pt[p][sh].p, w.npt[p][sh], step);
+        bp_launch_shape(st, sh, w.pt[g][p][sh].p, w.npt[g][p][sh], step);
         c.prof_end(slot, 0.0, 0.0);
     }
 }
@@ -1350,14 +1454,35 @@ static BpKey bp_key(int device, const BtInst &b) { return BpKey{device, b.N, b.n
 
 static bool bp_step_runs(const BtInst &b, int p) { return (p != BP_P2 && p != BP_P4) || b.lc; }
 
-// tiles of every vector slot of instance I for step p in tile shape sh
+// Does [lo, hi) meet [a0, a1) or [b0, b1)?
+static bool bp_meets(int lo, int hi, int a0, int a1, int b0, int b1) {
+    return (lo < a1 && hi > a0) || (lo < b1 && hi > b0);
+}
+
+// Tiles of every vector slot of instance I for step p in tile shape sh.  With the block structure
+// of a CT dimer (C_o zero on AOs >= nh, C_v zero on AOs < nh) the tiles that only hold zeros, or
+// values that the next step multiplies by zeros, are left out (their planes keep the zeros they
+// were cleared to):
+//   H = [C_o;SC_o] X: rows nh..n-1 are zero;
+//   F: only rows {mu, n+mu : mu < nh} and columns {nu, n+nu : nu >= nh} reach AX, the other rows
+//      of M are zero or meet C_o = 0 in AX, the other columns are zero or meet C_v = 0 in G;
+//   G = F [SC_v;C_v] + z: rows n+nh.. meet C_o = 0 in AX (which stops its K there).
 static void bp_tiles(const BtInst &b, int I, int p, int sh, std::vector<int4> &out) {
     if (!bp_step_runs(b, p)) return;
-    const int n2 = 2 * b.n;
+    const int n = b.n, n2 = 2 * n, nh = b.nh, BM = BP_BM[sh], BN = BP_BN[sh];
     const int M = p == BP_P5 ? b.o : n2, N = p == BP_P2 ? n2 : b.v;
     for (int s = 0; s < b.nr; ++s)
-        for (int tm = 0; tm < ceil_div(M, BP_BM[sh]); ++tm)
-            for (int tn = 0; tn < ceil_div(N, BP_BN[sh]); ++tn) out.push_back(make_int4(I, s, tm, tn));
+        for (int tm = 0; tm < ceil_div(M, BM); ++tm)
+            for (int tn = 0; tn < ceil_div(N, BN); ++tn) {
+                if (nh) {
+                    const int r0 = tm * BM, r1 = r0 + BM, c0 = tn * BN, c1 = c0 + BN;
+                    if (p == BP_P1 && !bp_meets(r0, r1, 0, nh, n, n2)) continue;
+                    if (p == BP_P2 && !(bp_meets(r0, r1, 0, nh, n, n + nh) && bp_meets(c0, c1, nh, n, n + nh, n2)))
+                        continue;
+                    if (p == BP_P4 && r0 >= n + nh) continue;
+                }
+                out.push_back(make_int4(I, s, tm, tn));
+            }
 }
 
 // forced shape from TINCR_GB300_BATCH_TILES (64x64, 64x32, 32x64, 32x32), or -1 for the tuner
@@ -1477,6 +1602,20 @@ int Ctx::solve_batch(int n_inst, const tincr_tda_instance *hin, int max_iter, do
     if (!batch) batch = new BatchWork();
     BatchWork &w = *batch;
     w.h.assign(n_inst, BtInst{});
+    // internal order: heavy instances first (group 0), then light ones (group 1); order[I] is the
+    // caller's index of internal instance I
+    std::vector<int> order;
+    order.reserve(n_inst);
+    int g_lo[3] = {0, 0, n_inst};   // group g holds internal instances [g_lo[g], g_lo[g + 1])
+    for (int pass = 0; pass < 2; ++pass)
+        for (int k = 0; k < n_inst; ++k) {
+            const long long nr = hin[k].n_roots, ov = (long long)hin[k].n_occ * hin[k].n_virt;
+            if ((nr * nr * ov >= BT_HEAVY) == (pass == 0)) order.push_back(k);
+        }
+    for (int k = 0; k < n_inst; ++k) {
+        const long long nr = hin[k].n_roots, ov = (long long)hin[k].n_occ * hin[k].n_virt;
+        if (nr * nr * ov >= BT_HEAVY) ++g_lo[1];
+    }
     std::vector<int> hAo, hAoAtom, hPos;
     std::vector<long long> hGlrOff(n_inst, 0), offPos(n_inst, 0);
     long long o_c = 0, o_s = 0, o_blk = 0, o_glr = 0, o_gam = 0, o_om = 0, o_v = 0, o_r = 0, o_sub = 0, o_h = 0, o_f = 0,
@@ -1485,11 +1624,11 @@ int Ctx::solve_batch(int n_inst, const tincr_tda_instance *hin, int max_iter, do
     int o_ao = 0, o_aoatom = 0, mmax_all = 1, nr_max = 1, nmax_atoms = 1;
     // pass 1: validation and the packed offsets of every instance
     for (int I = 0; I < n_inst; ++I) {
-        const tincr_tda_instance &q = hin[I];
+        const tincr_tda_instance &q = hin[order[I]];
         if (q.n_atoms <= 0 || q.n_orb <= 0 || q.n_occ <= 0 || q.n_virt <= 0 || q.n_occ + q.n_virt > q.n_orb ||
             q.n_roots <= 0 || q.n_roots > BT_MAXR || (long long)q.n_roots > (long long)q.n_occ * q.n_virt ||
             !q.orbs_per_atom || !q.c || !q.s || !q.orbe || !q.gamma || !q.xyz)
-            fail(TINCR_BAD_ARG, "solve_batch: instance " + std::to_string(I) + " is malformed (n_roots <= 6)");
+            fail(TINCR_BAD_ARG, "solve_batch: instance " + std::to_string(order[I]) + " is malformed (n_roots <= 6)");
         BtInst &b = w.h[I];
         b.n = q.n_orb; b.o = q.n_occ; b.v = q.n_virt; b.N = q.n_atoms;
         b.nr = q.n_roots; b.mmax = 15 * q.n_roots; b.lc = q.gamma_lr != nullptr; b.max_iter = max_iter;
@@ -1540,8 +1679,8 @@ int Ctx::solve_batch(int n_inst, const tincr_tda_instance *hin, int max_iter, do
     std::vector<unsigned char> bad(n_inst, 0);
 #pragma omp parallel for schedule(dynamic, 4) num_threads(12)
     for (int I = 0; I < n_inst; ++I) {
-        const tincr_tda_instance &q = hin[I];
-        const BtInst &b = w.h[I];
+        const tincr_tda_instance &q = hin[order[I]];
+        BtInst &b = w.h[I];
         const int n = b.n, w_ = b.o + b.v, N = b.N;
         auto copy = [&](double *dst, const double *src, size_t cnt, unsigned char flag) {
             bool ok = true;
@@ -1553,6 +1692,20 @@ int Ctx::solve_batch(int n_inst, const tincr_tda_instance *hin, int max_iter, do
             if (!ok) bad[I] |= flag;
         };
         copy(w.pinC.p + b.off_c, q.c, (size_t)n * w_, 1);
+        // block structure of a CT dimer: occupied MOs only on AOs < nh, virtual MOs only on AOs >= nh
+        {
+            int hi_o = 0, lo_v = n;
+            for (int mu = 0; mu < n; ++mu) {
+                const double *row = q.c + (size_t)mu * w_;
+                for (int k = 0; k < b.o; ++k)
+                    if (row[k] != 0.0) { hi_o = mu + 1; break; }
+                if (lo_v == n)
+                    for (int k = b.o; k < w_; ++k)
+                        if (row[k] != 0.0) { lo_v = mu; break; }
+            }
+            b.nh = (hi_o > 0 && hi_o < n && hi_o <= lo_v) ? hi_o : 0;
+            b.k5 = b.nh ? pad32(n + b.nh) : b.k2;
+        }
         copy(w.pinS.p + b.off_s, q.s, (size_t)n * n, 2);
         copy(w.pinG.p + b.off_gam, q.gamma, (size_t)N * N, 4);
         if (b.lc) copy(w.pinGlr.p + hGlrOff[I], q.gamma_lr, (size_t)N * N, 8);
@@ -1579,7 +1732,7 @@ int Ctx::solve_batch(int n_inst, const tincr_tda_instance *hin, int max_iter, do
             static const char *names[5] = {"c", "s", "gamma", "gamma_lr", "orbe"};
             int f = 0;
             while (!((bad[I] >> f) & 1)) ++f;
-            fail(TINCR_NONFINITE, "solve_batch: instance " + std::to_string(I) + ": non-finite value in " + names[f]);
+            fail(TINCR_NONFINITE, "solve_batch: instance " + std::to_string(order[I]) + ": non-finite value in " + names[f]);
         }
     // device arrays
     auto upload_pinned = [&](DevBuf<double> &d, const PinnedBuf &h, long long count) {
@@ -1605,6 +1758,8 @@ int Ctx::solve_batch(int n_inst, const tincr_tda_instance *hin, int max_iter, do
     w.T.reserve(o_r);
     w.sub.reserve(o_sub);
     w.H.reserve(o_h);
+    // the mixed form leaves the zero rows of block-structured H out: they must read as zeros
+    if (mixed) TINCR_CUDA(cudaMemsetAsync(w.H.p, 0, o_h * sizeof(double), stream));
     w.F.reserve(std::max<long long>(1, o_f));
     w.D.reserve(o_d);
     w.u.reserve(o_u);
@@ -1615,31 +1770,55 @@ int Ctx::solve_batch(int n_inst, const tincr_tda_instance *hin, int max_iter, do
     upload_any(stream, w.pos, hPos);
     w.active.reserve(1);
 
+    // clusters of the subspace step: each heavy instance on one cluster, the light ones four to a
+    // cluster; per group, roots per instance (grid of the per-vector kernels)
+    static_assert(BT_CL == 4, "a cluster's work is one int4");
+    unsigned sub_grid[2] = {0, 0};
+    int nr_grp[2] = {1, 1};
+    for (int g = 0; g < 2; ++g) {
+        std::vector<int4> cw;
+        for (int I = g_lo[g]; I < g_lo[g + 1]; ++I) nr_grp[g] = std::max(nr_grp[g], w.h[I].nr);
+        if (g == 0) {
+            for (int I = g_lo[0]; I < g_lo[1]; ++I) cw.push_back(make_int4(I, -2, -2, -2));
+        } else {
+            for (int k = g_lo[1]; k < g_lo[2]; k += BT_CL) {
+                int v[BT_CL];
+                for (int r = 0; r < BT_CL; ++r) v[r] = k + r < g_lo[2] ? k + r : -1;
+                cw.push_back(make_int4(v[0], v[1], v[2], v[3]));
+            }
+        }
+        sub_grid[g] = (unsigned)(cw.size() * BT_CL);
+        if (!cw.empty()) upload_any(stream, w.cl_inst[g], cw);
+    }
+
     // static tile tables
-    std::vector<int4> tsc, t1, t2, t4, t5;
+    std::vector<int4> tsc, t1[2], t2[2], t4[2], t5[2];
     for (int I = 0; I < n_inst; ++I) {
         const BtInst &b = w.h[I];
-        const int n2 = 2 * b.n;
+        const int n2 = 2 * b.n, g = I < g_lo[1] ? 0 : 1;
         for (int tm = 0; tm < ceil_div(b.n, GB_M); ++tm)
             for (int tn = 0; tn < ceil_div(b.o + b.v, GB_N); ++tn) tsc.push_back(make_int4(I, 0, tm, tn));
         for (int s = 0; s < b.nr; ++s) {
             for (int tm = 0; tm < ceil_div(n2, GB_M); ++tm)
                 for (int tn = 0; tn < ceil_div(b.v, GB_N); ++tn) {
-                    t1.push_back(make_int4(I, s, tm, tn));
-                    if (b.lc) t4.push_back(make_int4(I, s, tm, tn));
+                    t1[g].push_back(make_int4(I, s, tm, tn));
+                    if (b.lc) t4[g].push_back(make_int4(I, s, tm, tn));
                 }
             if (b.lc)
                 for (int tm = 0; tm < ceil_div(n2, GB_M); ++tm)
-                    for (int tn = 0; tn < ceil_div(n2, GB_N); ++tn) t2.push_back(make_int4(I, s, tm, tn));
+                    for (int tn = 0; tn < ceil_div(n2, GB_N); ++tn) t2[g].push_back(make_int4(I, s, tm, tn));
             for (int tm = 0; tm < ceil_div(b.o, GB_M); ++tm)
-                for (int tn = 0; tn < ceil_div(b.v, GB_N); ++tn) t5.push_back(make_int4(I, s, tm, tn));
+                for (int tn = 0; tn < ceil_div(b.v, GB_N); ++tn) t5[g].push_back(make_int4(I, s, tm, tn));
         }
     }
     upload_any(stream, w.t_sc, tsc);
-    upload_any(stream, w.t1, t1);
-    upload_any(stream, w.t2, t2);
-    upload_any(stream, w.t4, t4);
-    upload_any(stream, w.t5, t5);
+    for (int g = 0; g < 2; ++g) {
+        w.nt1[g] = t1[g].size(); w.nt2[g] = t2[g].size(); w.nt4[g] = t4[g].size(); w.nt5[g] = t5[g].size();
+        if (w.nt1[g]) upload_any(stream, w.t1[g], t1[g]);
+        if (w.nt2[g]) upload_any(stream, w.t2[g], t2[g]);
+        if (w.nt4[g]) upload_any(stream, w.t4[g], t4[g]);
+        if (w.nt5[g]) upload_any(stream, w.t5[g], t5[g]);
+    }
     // split-BF16 planes of the mixed form (their tile tables follow the guesses and the autotuner)
     if (mixed) {
         w.Pl.reserve(N_PLANES * (o_pc + o_pv));
@@ -1676,7 +1855,7 @@ int Ctx::solve_batch(int n_inst, const tincr_tda_instance *hin, int max_iter, do
         check_launch("bt_sc32");
         prof_end(slot, 0.0, 0.0);
     } else {
-        bt_launch<false, false>(*this, w.t_sc, tsc.size(), BtStepSC{a}, TINCR_KF_OTHER, 0.0);
+        bt_launch<false, false>(*this, stream, w.t_sc, tsc.size(), BtStepSC{a}, TINCR_KF_OTHER, 0.0);
     }
     bt_pack_kernel<<<n_inst, BT_T, 0, stream>>>(a);
     count_launch(stream, "bt_pack");
@@ -1698,32 +1877,35 @@ int Ctx::solve_batch(int n_inst, const tincr_tda_instance *hin, int max_iter, do
     count_launch(stream, "bt_guess");
     check_launch("bt_guess");
     const dim3 gv(nr_max, n_inst);
+    const dim3 gvg[2] = {dim3(nr_grp[0], g_lo[1] - g_lo[0]), dim3(nr_grp[1], g_lo[2] - g_lo[1])};
     if (mixed) {
         // tile shape of every instance and plane step: forced, or from the autotuner's table
         const int forced = bp_forced_shape();
         if (forced < 0) {
             TINCR_CUDA(cudaMemsetAsync(w.D32.p, 0, o_d * sizeof(float), stream));
-            bt_split_x_kernel<<<gv, BT_T, 0, stream>>>(a);
+            bt_split_x_kernel<<<gv, BT_T, 0, stream>>>(a, 0);
             count_launch(stream, "bt_split_x");
             check_launch("bt_split_x");
             bp_autotune(*this, w, a, n_sm);
         }
-        std::vector<int4> pt[BP_STEPS][BP_SHAPES];
+        std::vector<int4> pt[2][BP_STEPS][BP_SHAPES];
         {
             std::lock_guard<std::mutex> lk(g_bp_mu);
             for (int I = 0; I < n_inst; ++I) {
                 const BpChoice *ch = forced < 0 ? &g_bp_table.at(bp_key(device, w.h[I])) : nullptr;
+                const int g = I < g_lo[1] ? 0 : 1;
                 for (int p = 0; p < BP_STEPS; ++p) {
                     const int sh = ch ? ch->shape[p] : forced;
-                    if (sh >= 0) bp_tiles(w.h[I], I, p, sh, pt[p][sh]);
+                    if (sh >= 0) bp_tiles(w.h[I], I, p, sh, pt[g][p][sh]);
                 }
             }
         }
-        for (int p = 0; p < BP_STEPS; ++p)
-            for (int sh = 0; sh < BP_SHAPES; ++sh) {
-                w.npt[p][sh] = pt[p][sh].size();
-                if (!pt[p][sh].empty()) upload_any(stream, w.pt[p][sh], pt[p][sh]);
-            }
+        for (int g = 0; g < 2; ++g)
+            for (int p = 0; p < BP_STEPS; ++p)
+                for (int sh = 0; sh < BP_SHAPES; ++sh) {
+                    w.npt[g][p][sh] = pt[g][p][sh].size();
+                    if (!pt[g][p][sh].empty()) upload_any(stream, w.pt[g][p][sh], pt[g][p][sh]);
+                }
     }
 
     const size_t sub_smem = bt_subspace_smem(mmax_all);
@@ -1731,64 +1913,97 @@ int Ctx::solve_batch(int n_inst, const tincr_tda_instance *hin, int max_iter, do
     const size_t coul_smem = (size_t)nmax_atoms * sizeof(double);
     if (coul_smem > 48 * 1024)
         TINCR_CUDA(cudaFuncSetAttribute(bt_coulomb_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)coul_smem));
+    if (!w.side) {
+        int least = 0, greatest = 0;
+        TINCR_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+        TINCR_CUDA(cudaStreamCreateWithPriority(&w.hi, cudaStreamNonBlocking, greatest));
+        TINCR_CUDA(cudaStreamCreateWithPriority(&w.side, cudaStreamNonBlocking, least));
+        TINCR_CUDA(cudaEventCreateWithFlags(&w.fork, cudaEventDisableTiming));
+        TINCR_CUDA(cudaEventCreateWithFlags(&w.join_hi, cudaEventDisableTiming));
+        TINCR_CUDA(cudaEventCreateWithFlags(&w.join_side, cudaEventDisableTiming));
+    }
 
-    // one Davidson iteration of every running instance (captured once as a graph)
-    auto iteration = [&]() {
-        bt_launch<false, false>(*this, w.t1, t1.size(), BtStep1{a, false}, TINCR_KF_AO_TRANSFORM, 0.0);
-        bt_launch<false, true>(*this, w.t2, t2.size(), BtStep2{a}, TINCR_KF_AO_EXCHANGE, 0.0);
-        bt_diag_kernel<<<gv, BT_T, 0, stream>>>(a, 0);
-        count_launch(stream, "bt_diag");
+    // one Davidson iteration of the running instances of group g on stream st
+    auto iteration = [&](cudaStream_t st, int g) {
+        if (g_lo[g] == g_lo[g + 1]) return;
+        const int I0 = g_lo[g];
+        bt_launch<false, false>(*this, st, w.t1[g], w.nt1[g], BtStep1{a, false}, TINCR_KF_AO_TRANSFORM, 0.0);
+        bt_launch<false, true>(*this, st, w.t2[g], w.nt2[g], BtStep2{a}, TINCR_KF_AO_EXCHANGE, 0.0);
+        bt_diag_kernel<<<gvg[g], BT_T, 0, st>>>(a, 0, I0);
+        count_launch(st, "bt_diag");
         check_launch("bt_diag");
-        bt_coulomb_kernel<<<gv, BT_T, coul_smem, stream>>>(a, 0);
-        count_launch(stream, "bt_coulomb");
+        bt_coulomb_kernel<<<gvg[g], BT_T, coul_smem, st>>>(a, 0, I0);
+        count_launch(st, "bt_coulomb");
         check_launch("bt_coulomb");
-        bt_launch<false, false>(*this, w.t4, t4.size(), BtStep4{a}, TINCR_KF_AO_EXCHANGE, 0.0);
-        bt_scale_rows_kernel<<<gv, BT_T, 0, stream>>>(a);
-        count_launch(stream, "bt_scale_rows");
+        bt_launch<false, false>(*this, st, w.t4[g], w.nt4[g], BtStep4{a}, TINCR_KF_AO_EXCHANGE, 0.0);
+        bt_scale_rows_kernel<<<gvg[g], BT_T, 0, st>>>(a, I0);
+        count_launch(st, "bt_scale_rows");
         check_launch("bt_scale_rows");
-        bt_launch<true, false>(*this, w.t5, t5.size(), BtStep5{a}, TINCR_KF_AO_TRANSFORM, 0.0);
-        TINCR_CUDA(cudaMemsetAsync(w.active.p, 0, sizeof(int), stream));
-        bt_subspace_kernel<<<n_inst, BT_T, sub_smem, stream>>>(a);
-        count_launch(stream, "bt_subspace");
+        bt_launch<true, false>(*this, st, w.t5[g], w.nt5[g], BtStep5{a}, TINCR_KF_AO_TRANSFORM, 0.0);
+        bt_subspace_kernel<<<sub_grid[g], BT_T, sub_smem, st>>>(a, w.cl_inst[g].p);
+        count_launch(st, "bt_subspace");
         check_launch("bt_subspace");
     };
     // the mixed-form iteration: split-BF16 plane GEMMs, FP64 Coulomb diagonals and subspace step
-    auto iteration_mixed = [&]() {
-        bt_split_x_kernel<<<gv, BT_T, 0, stream>>>(a);
-        count_launch(stream, "bt_split_x");
+    auto iteration_mixed = [&](cudaStream_t st, int g) {
+        if (g_lo[g] == g_lo[g + 1]) return;
+        const int I0 = g_lo[g];
+        bt_split_x_kernel<<<gvg[g], BT_T, 0, st>>>(a, I0);
+        count_launch(st, "bt_split_x");
         check_launch("bt_split_x");
-        bt_plane_launch(*this, w, BP_P1, BtP1{a}, TINCR_KF_AO_TRANSFORM);
-        bt_plane_launch(*this, w, BP_P2, BtP2{a}, TINCR_KF_AO_EXCHANGE);   // + LC Coulomb diagonals
-        bt_diag_kernel<<<gv, BT_T, 0, stream>>>(a, BT_MIXED);                  // non-LC Coulomb diagonals
-        count_launch(stream, "bt_diag");
+        bt_plane_launch(*this, st, w, g, BP_P1, BtP1{a}, TINCR_KF_AO_TRANSFORM);
+        bt_plane_launch(*this, st, w, g, BP_P2, BtP2{a}, TINCR_KF_AO_EXCHANGE);   // + LC Coulomb diagonals
+        bt_diag_kernel<<<gvg[g], BT_T, 0, st>>>(a, BT_MIXED, I0);                  // non-LC Coulomb diagonals
+        count_launch(st, "bt_diag");
         check_launch("bt_diag");
-        bt_coulomb_kernel<<<gv, BT_T, coul_smem, stream>>>(a, BT_MIXED);
-        count_launch(stream, "bt_coulomb");
+        bt_coulomb_kernel<<<gvg[g], BT_T, coul_smem, st>>>(a, BT_MIXED, I0);
+        count_launch(st, "bt_coulomb");
         check_launch("bt_coulomb");
-        bt_plane_launch(*this, w, BP_P4, BtP4{a}, TINCR_KF_AO_EXCHANGE);
-        bt_gt_nolc_kernel<<<gv, BT_T, 0, stream>>>(a);
-        count_launch(stream, "bt_gt_nolc");
+        bt_plane_launch(*this, st, w, g, BP_P4, BtP4{a}, TINCR_KF_AO_EXCHANGE);
+        bt_gt_nolc_kernel<<<gvg[g], BT_T, 0, st>>>(a, I0);
+        count_launch(st, "bt_gt_nolc");
         check_launch("bt_gt_nolc");
-        bt_plane_launch(*this, w, BP_P5, BtP5{a}, TINCR_KF_AO_TRANSFORM);
-        TINCR_CUDA(cudaMemsetAsync(w.active.p, 0, sizeof(int), stream));
-        bt_subspace_kernel<<<n_inst, BT_T, sub_smem, stream>>>(a);
-        count_launch(stream, "bt_subspace");
+        bt_plane_launch(*this, st, w, g, BP_P5, BtP5{a}, TINCR_KF_AO_TRANSFORM);
+        bt_subspace_kernel<<<sub_grid[g], BT_T, sub_smem, st>>>(a, w.cl_inst[g].p);
+        count_launch(st, "bt_subspace");
         check_launch("bt_subspace");
+    };
+    // One iteration of both groups.  The groups are independent, so in the graph they are two
+    // concurrent branches: the heavy group, whose iterations are more and whose subspace step is
+    // bound by the latency of its small eigenproblems, at high priority, and the light group at low
+    // priority filling the SMs the heavy one leaves.  With kernel timing on, both run in turn on the
+    // main stream.
+    auto both = [&](const std::function<void(cudaStream_t, int)> &body, bool fork) {
+        TINCR_CUDA(cudaMemsetAsync(w.active.p, 0, sizeof(int), stream));
+        if (fork) {
+            TINCR_CUDA(cudaEventRecord(w.fork, stream));
+            TINCR_CUDA(cudaStreamWaitEvent(w.hi, w.fork, 0));
+            TINCR_CUDA(cudaStreamWaitEvent(w.side, w.fork, 0));
+            body(w.hi, 0);
+            body(w.side, 1);
+            TINCR_CUDA(cudaEventRecord(w.join_hi, w.hi));
+            TINCR_CUDA(cudaEventRecord(w.join_side, w.side));
+            TINCR_CUDA(cudaStreamWaitEvent(stream, w.join_hi, 0));
+            TINCR_CUDA(cudaStreamWaitEvent(stream, w.join_side, 0));
+        } else {
+            body(stream, 0);
+            body(stream, 1);
+        }
     };
     // run an iteration function (as a CUDA graph unless kernel timing is on) until no instance is
     // running or `limit` iterations are done; returns the iterations run
-    auto run_loop = [&](const std::function<void()> &body, int limit) {
+    auto run_loop = [&](const std::function<void(cudaStream_t, int)> &body, int limit) {
         int its = 0, active = n_inst;
         if (!profiling) {
             cudaGraph_t g = nullptr;
             cudaGraphExec_t exec = nullptr;
             TINCR_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
             const long long before = g_launches;
-            body();
+            both(body, true);
             const long long per_iter = g_launches - before;
             g_launches = before;
             TINCR_CUDA(cudaStreamEndCapture(stream, &g));
-            TINCR_CUDA(cudaGraphInstantiate(&exec, g, 0));
+            TINCR_CUDA(cudaGraphInstantiate(&exec, g, cudaGraphInstantiateFlagUseNodePriority));
             cudaGraphDestroy(g);
             while (active > 0 && its < limit) {
                 TINCR_CUDA(cudaGraphLaunch(exec, stream));
@@ -1800,7 +2015,7 @@ int Ctx::solve_batch(int n_inst, const tincr_tda_instance *hin, int max_iter, do
             cudaGraphExecDestroy(exec);
         } else {
             while (active > 0 && its < limit) {
-                body();
+                both(body, false);
                 ++its;
                 TINCR_CUDA(cudaMemcpyAsync(&active, w.active.p, sizeof(int), cudaMemcpyDeviceToHost, stream));
                 sync();
@@ -1825,11 +2040,12 @@ int Ctx::solve_batch(int n_inst, const tincr_tda_instance *hin, int max_iter, do
         run_loop(iteration, max_iter);
     }
     // final pass: transition charges of the Ritz vectors
-    bt_launch<false, false>(*this, w.t1, t1.size(), BtStep1{a, true}, TINCR_KF_OTHER, 0.0);
-    bt_diag_kernel<<<gv, BT_T, 0, stream>>>(a, 1);
+    for (int g = 0; g < 2; ++g)
+        bt_launch<false, false>(*this, stream, w.t1[g], w.nt1[g], BtStep1{a, true}, TINCR_KF_OTHER, 0.0);
+    bt_diag_kernel<<<gv, BT_T, 0, stream>>>(a, 1, 0);
     count_launch(stream, "bt_diag");
     check_launch("bt_diag");
-    bt_coulomb_kernel<<<gv, BT_T, coul_smem, stream>>>(a, 1);
+    bt_coulomb_kernel<<<gv, BT_T, coul_smem, stream>>>(a, 1, 0);
     count_launch(stream, "bt_coulomb");
     check_launch("bt_coulomb");
     TINCR_CUDA(cudaEventRecord(ev1, stream));
@@ -1846,8 +2062,8 @@ int Ctx::solve_batch(int n_inst, const tincr_tda_instance *hin, int max_iter, do
     last_products = 0;
     for (int I = 0; I < n_inst; ++I) {
         const BtInst &b = w.h[I];
-        const tincr_tda_instance &q = hin[I];
-        tincr_tda_result &o = res[I];
+        const tincr_tda_instance &q = hin[order[I]];
+        tincr_tda_result &o = res[order[I]];
         const BtState &s = hs[I];
         o.iterations = s.iter;
         o.status = s.status == BT_CONVERGED ? TINCR_OK

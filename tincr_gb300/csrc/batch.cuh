@@ -44,6 +44,10 @@ struct BtInst {
     int ko, kv, k2;
     long long off_pc;        // [C_o;SC_o] 2n x ko | [C_v;SC_v] 2n x kv | [SC_v;C_v]^T v x k2 | [SC_o;C_o]^T o x k2
     long long off_pv;        // per slot: X^T v x ko | H 2n x kv | F 2n x k2 | G^T v x k2
+    // Block structure of a CT pair direction's dimer: occupied MOs vanish on AOs >= nh and virtual
+    // MOs on AOs < nh (0: no such structure).  The mixed form then skips the product blocks that
+    // are zero or multiplied by zeros; k5 = pad(n + nh) is the K of the last product step.
+    int nh, k5;
 };
 
 // Dynamic Davidson state of one instance (davidson.rs:53-185 bookkeeping).
