@@ -826,47 +826,58 @@ __device__ __forceinline__ int bt_sturm(const double *d, const double *esq, int 
 __device__ void bt_eig_lowest(int m, int nr, double *A, double *W, double *w, double *red) {
     double *d = W, *e = d + m, *beta = e + m, *p = beta + m, *Y = p + m, *F = Y + (size_t)nr * m;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    // 1. tridiagonalisation (one reflection per column k, acting on rows/columns k+1..m-1)
+    // 1. tridiagonalisation (one reflection per column k, acting on rows/columns k+1..m-1).  Four
+    //    barriers per column; the FP64 latency chains are kept short: the column norm, the
+    //    reflection scalars and u^T p on warp 0 alone (shuffle reductions, no cross-warp step), and
+    //    p = bet A' u with G threads per row (G = 8, 4, 2 for trailing blocks up to 32, 64, 128 rows).
     for (int k = 0; k + 2 < m; ++k) {
         const int n1 = m - k - 1;
-        double s2[1] = {0.0};
-        for (int i = 1 + tid; i < n1; i += BT_T) {
-            const double x = A[(k + 1 + i) * m + k];
-            s2[0] += x * x;
-        }
-        bt_block_sum<1>(s2, red);
-        if (s2[0] == 0.0) {   // the same in every thread
-            if (tid == 0) { beta[k] = 0.0; e[k] = A[(k + 1) * m + k]; d[k] = A[k * m + k]; }
-            __syncthreads();
-            continue;
-        }
-        if (tid == 0) {   // H = I - bet u u^T, u = x - alpha e_1 (one thread: FP64 chains are slow)
-            const double x0 = A[(k + 1) * m + k];
-            const double nx = sqrt(x0 * x0 + s2[0]);
-            const double alpha = x0 > 0.0 ? -nx : nx;
-            A[(k + 1) * m + k] = x0 - alpha;
-            beta[k] = 1.0 / (alpha * (alpha - x0));
-            e[k] = alpha;
-            d[k] = A[k * m + k];
+        double *u = A + (size_t)(k + 1) * m + k;   // u_i = u[i * m], i < n1 (column k below the diagonal)
+        if (warp == 0) {
+            double s2 = 0.0;
+            for (int i = 1 + lane; i < n1; i += 32) s2 += u[(size_t)i * m] * u[(size_t)i * m];
+            for (int off = 16; off; off >>= 1) s2 += __shfl_xor_sync(0xffffffffu, s2, off);
+            if (lane == 0) {   // H = I - bet u u^T, u = x - alpha e_1
+                const double x0 = u[0];
+                d[k] = A[(size_t)k * m + k];
+                if (s2 == 0.0) {
+                    beta[k] = 0.0;
+                    e[k] = x0;
+                } else {
+                    const double nx = sqrt(x0 * x0 + s2);
+                    const double alpha = x0 > 0.0 ? -nx : nx;
+                    u[0] = x0 - alpha;
+                    beta[k] = 1.0 / (alpha * (alpha - x0));
+                    e[k] = alpha;
+                }
+            }
         }
         __syncthreads();
         const double bet = beta[k];
-        for (int i = tid; i < n1; i += BT_T) {              // p = bet A' u
-            const double *row = A + (size_t)(k + 1 + i) * m + (k + 1);
+        if (bet == 0.0) continue;   // the same in every thread
+        {
+            const int G = n1 <= 32 ? 8 : n1 <= 64 ? 4 : 2;
+            const int row = tid / G, sub = tid % G;
             double acc = 0.0;
-            for (int j = 0; j < n1; ++j) acc += row[j] * A[(k + 1 + j) * m + k];
-            p[i] = bet * acc;
+            if (row < n1) {
+                const double *ar = A + (size_t)(k + 1 + row) * m + (k + 1);
+                for (int j = sub; j < n1; j += G) acc += ar[j] * u[(size_t)j * m];
+            }
+            for (int off = G >> 1; off; off >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, off);
+            if (sub == 0 && row < n1) p[row] = bet * acc;
         }
         __syncthreads();
-        double up[1] = {0.0};
-        for (int i = tid; i < n1; i += BT_T) up[0] += A[(k + 1 + i) * m + k] * p[i];
-        bt_block_sum<1>(up, red);
-        const double K = 0.5 * bet * up[0];
-        for (int i = tid; i < n1; i += BT_T) p[i] -= K * A[(k + 1 + i) * m + k];   // q = p - K u
+        if (warp == 0) {   // q = p - K u, K = bet u^T p / 2
+            double up = 0.0;
+            for (int i = lane; i < n1; i += 32) up += u[(size_t)i * m] * p[i];
+            for (int off = 16; off; off >>= 1) up += __shfl_xor_sync(0xffffffffu, up, off);
+            const double K = 0.5 * bet * up;
+            for (int i = lane; i < n1; i += 32) p[i] -= K * u[(size_t)i * m];
+        }
         __syncthreads();
         for (int t = tid; t < n1 * n1; t += BT_T) {          // A' -= u q^T + q u^T
             const int i = t / n1, j = t % n1;
-            A[(k + 1 + i) * m + (k + 1 + j)] -= A[(k + 1 + i) * m + k] * p[j] + p[i] * A[(k + 1 + j) * m + k];
+            A[(size_t)(k + 1 + i) * m + (k + 1 + j)] -= u[(size_t)i * m] * p[j] + p[i] * u[(size_t)j * m];
         }
         __syncthreads();
     }

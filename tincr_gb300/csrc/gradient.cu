@@ -219,17 +219,40 @@ __global__ void cg_update_kernel(long long len, double alpha, const double *p, c
 }
 
 // the same update with alpha = rr / pAp formed on the device (pAp left there by dot_kernel)
-__global__ void cg_update_dev_kernel(long long len, double rr, const double *pAp, const double *p, const double *Ap,
-                                     double *x, double *r) {
-    const double alpha = rr / *pAp;
+// Device-side CG state: s[0] = r.r, s[1] = p.Ap, s[2] = the new r.r, s[3] = beta; flag[0] = 0 while
+// running, 1 once converged, 2 on a non-finite step; flag[1] = iterations done.  Every thread
+// forms alpha from the same two values, so all take the same decision.
+
+// x += alpha p ; r -= alpha Ap, alpha = r.r / p.Ap (skipped once the recursion has stopped)
+__global__ void cg_update_dev_kernel(long long len, const double *s, const int *flag, const double *p,
+                                     const double *Ap, double *x, double *r) {
+    if (flag[0] != 0) return;
+    const double alpha = s[0] / s[1];
+    if (!isfinite(alpha)) return;   // cg_check_kernel records it
     GRID_STRIDE(t, len) {
         x[t] += alpha * p[t];
         r[t] -= alpha * Ap[t];
     }
 }
 
-// p = beta p + r
-__global__ void cg_dir_kernel(long long len, double beta, double *p, const double *r) {
+// the convergence test of helpers.rs:1146-1223 (r.r <= conv) and the next beta
+__global__ void cg_check_kernel(double *s, int *flag, double conv) {
+    if (flag[0] != 0) return;
+    flag[1] += 1;
+    if (!isfinite(s[0] / s[1])) {
+        flag[0] = 2;
+    } else if (s[2] <= conv) {
+        flag[0] = 1;
+    } else {
+        s[3] = s[2] / s[0];
+        s[0] = s[2];
+    }
+}
+
+// p = beta p + r (skipped once the recursion has stopped)
+__global__ void cg_dir_kernel(long long len, const double *s, const int *flag, double *p, const double *r) {
+    if (flag[0] != 0) return;
+    const double beta = s[3];
     GRID_STRIDE(t, len) p[t] = beta * p[t] + r[t];
 }
 
@@ -496,7 +519,7 @@ int Ctx::zvector_cg(int variant, const double *R, double *Z, int max_iter, doubl
     const long long len = ov;
     gcg.reserve(5 * (size_t)len + 8);
     double *r = gcg.p, *p = r + len, *Ap = p + len, *tmp = Ap + len, *Xt = tmp + len, *dots = Xt + len;
-    double h_dots[2] = {0.0, 0.0};
+    int h_flag[2] = {0, 0};
     auto op = [&](const double *x, double *out) {
         // tincr: TDA matrix A for LC (mult_av_lc: 2 Coulomb - exchange), A+B without exchange otherwise
         // (mult_av_nolc: 4 Coulomb).  Exact variant with LC: (A+B) = 4 Coulomb - (ij|ab) - (ib|ja).
@@ -512,43 +535,39 @@ int Ctx::zvector_cg(int variant, const double *R, double *Z, int max_iter, doubl
         count_launch(stream, "dot");
         check_launch("dot");
     };
-    auto dot = [&](const double *a, const double *b) {
-        dot_dev(a, b, dots);
-        double h = 0.0;
-        TINCR_CUDA(cudaMemcpyAsync(&h, dots, sizeof(double), cudaMemcpyDeviceToHost, stream));
-        sync();
-        return h;
-    };
     EW(zguess_kernel, len, len, R, d_omega.p, Z);          // bs = R / omega
-    // CG from the current Z (tincr: helpers.rs:1146-1223); the convergence test is FP64
+    int *flag = reinterpret_cast<int *>(dots + 4);
+    // CG from the current Z (tincr: helpers.rs:1146-1223); the convergence test is FP64.  The
+    // recursion runs on the device (alpha, beta and the test in device scalars); the host reads
+    // the flag every CG_SYNC iterations, and the iterations queued after convergence change nothing.
+    constexpr int CG_SYNC = 4;
     auto run = [&](int limit, int *done) {
         op(Z, Ap);
         EW(axpby3_kernel, len, len, 1.0, R, -1.0, Ap, 0.0, nullptr, r);   // r = R - A Z
         TINCR_CUDA(cudaMemcpyAsync(p, r, len * sizeof(double), cudaMemcpyDeviceToDevice, stream));
-        double rr = dot(r, r);
-        int st = TINCR_CG_MAXITER;
-        int k = 0;
-        // one host synchronisation per iteration: alpha = rr / pAp is formed on the device (the same
-        // FP64 division), and pAp and the new r.r come back together
-        for (k = 0; k < limit; ++k) {
-            op(p, Ap);
-            dot_dev(p, Ap, dots + 1);
-            EW(cg_update_dev_kernel, len, len, rr, dots + 1, p, Ap, Z, r);
-            dot_dev(r, r, dots + 2);
-            TINCR_CUDA(cudaMemcpyAsync(h_dots, dots + 1, 2 * sizeof(double), cudaMemcpyDeviceToHost, stream));
-            sync();
-            const double alpha = rr / h_dots[0], rr_new = h_dots[1];
-            if (!std::isfinite(alpha)) fail(TINCR_NONFINITE, "Z-vector CG: non-finite step");
-            if (rr_new <= conv) {
-                st = TINCR_OK;
-                ++k;
-                break;
+        dot_dev(r, r, dots);
+        TINCR_CUDA(cudaMemsetAsync(flag, 0, 2 * sizeof(int), stream));
+        int queued = 0;
+        while (queued < limit) {
+            const int batch = std::min(CG_SYNC, limit - queued);
+            for (int q = 0; q < batch; ++q) {
+                op(p, Ap);
+                dot_dev(p, Ap, dots + 1);
+                EW(cg_update_dev_kernel, len, len, dots, flag, p, Ap, Z, r);
+                dot_dev(r, r, dots + 2);
+                cg_check_kernel<<<1, 1, 0, stream>>>(dots, flag, conv);
+                count_launch(stream, "cg_check");
+                check_launch("cg_check");
+                EW(cg_dir_kernel, len, len, dots, flag, p, r);
             }
-            EW(cg_dir_kernel, len, len, rr_new / rr, p, r);
-            rr = rr_new;
+            queued += batch;
+            TINCR_CUDA(cudaMemcpyAsync(h_flag, flag, 2 * sizeof(int), cudaMemcpyDeviceToHost, stream));
+            sync();
+            if (h_flag[0] == 2) fail(TINCR_NONFINITE, "Z-vector CG: non-finite step");
+            if (h_flag[0] == 1) break;
         }
-        *done = k;
-        return st;
+        *done = h_flag[1];
+        return h_flag[0] == 1 ? TINCR_OK : TINCR_CG_MAXITER;
     };
     int it = 0, status;
     if (prec == TINCR_PREC_BF16X3) {
