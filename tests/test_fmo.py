@@ -124,9 +124,15 @@ def test_batch_mixed_within_bar(gpu_ctx):
     err = max(np.abs(a["energies"] - b["energies"]).max() for a, b in zip(r64, rm))
     print("mixed batch: max |dE| = %.2e Eh" % err)
     assert err < 1e-6
+    dq, dosc = 0.0, 0.0
     for a, b in zip(r64, rm):
-        ov = np.abs(np.einsum("xr,xr->r", a["coefficients"], b["coefficients"]))
-        assert np.abs(ov - 1.0).max() < 1e-6
+        ovs = np.einsum("xr,xr->r", a["coefficients"], b["coefficients"])
+        assert np.abs(np.abs(ovs) - 1.0).max() < 1e-6
+        # transition charges (sign of each root aligned) and oscillator strengths of the roots
+        dq = max(dq, np.abs(a["q_trans"] - b["q_trans"] * np.sign(ovs)[None, :]).max())
+        dosc = max(dosc, np.abs(a["osc"] - b["osc"]).max())
+    print("mixed batch: max |dq_trans| = %.2e, max |d osc| = %.2e" % (dq, dosc))
+    assert dq < 1e-5 and dosc < 1e-6
 
 
 @pytest.mark.gpu

@@ -579,12 +579,12 @@ __global__ void bt_const_planes_kernel(BtArrays a) {
     }
 }
 
-// X^T planes of the new trial vectors
-__global__ void bt_split_x_kernel(BtArrays a, int I0) {
+// X^T planes of the new trial vectors (or of the Ritz vectors in the final pass)
+__global__ void bt_split_x_kernel(BtArrays a, int I0, int final_pass) {
     const int I = I0 + blockIdx.y, b = blockIdx.x;
     const BtInst in = a.inst[I];
     const double *X;
-    if (!bt_vector(a, in, I, b, false, &X)) return;
+    if (!bt_vector(a, in, I, b, final_pass != 0, &X)) return;
     const long long base = bt_pv_slot(in, b);
     for (long long t = threadIdx.x; t < in.ov; t += blockDim.x) {
         const int i = int(t / in.v), x = int(t % in.v);
@@ -595,10 +595,11 @@ __global__ void bt_split_x_kernel(BtArrays a, int I0) {
 // 1. H = [C_o;SC_o] X: FP64 copy (Coulomb diagonals) and planes
 struct BtP1 {
     BtArrays a;
+    bool final_pass;   // Ritz vectors: the transition charges after convergence
     __device__ bool setup(int I, int b, BtPlaneOp &op) const {
         const BtInst &in = a.inst[I];
         const double *X;
-        if (!bt_vector(a, in, I, b, false, &X)) return false;
+        if (!bt_vector(a, in, I, b, final_pass, &X)) return false;
         op.in = &a.inst[I]; op.I = I; op.b = b;
         op.M = 2 * in.n; op.N = in.v; op.Kpad = in.ko;
         op.A = a.P + in.off_pc; op.lda = in.ko;
@@ -607,7 +608,8 @@ struct BtP1 {
     }
     __device__ void epi(const BtPlaneOp &op, int m, int n, float acc) const {
         const BtInst &in = *op.in;
-        if (!in.lc || in.nh) a.H[in.off_h + (long long)op.b * 2 * in.n * in.v + (long long)m * in.v + n] = (double)acc;
+        if (final_pass || !in.lc || in.nh)
+            a.H[in.off_h + (long long)op.b * 2 * in.n * in.v + (long long)m * in.v + n] = (double)acc;
         bt_split_store(a, bt_pv_h(in, op.b) + (long long)m * in.kv + n, acc);
     }
 };
@@ -1553,7 +1555,7 @@ static void bp_autotune(Ctx &c, BatchWork &w, const BtArrays &a, int n_sm) {
                     TINCR_CUDA(cudaEventRecord(e[0], c.stream));
                     const int4 *t = w.tune_tiles[sh].p;
                     switch (p) {
-                    case BP_P1: bp_probe(c.stream, sh, t, cnt[sh], BtP1{a}); break;
+                    case BP_P1: bp_probe(c.stream, sh, t, cnt[sh], BtP1{a, false}); break;
                     case BP_P2: bp_probe(c.stream, sh, t, cnt[sh], BtP2{a}); break;
                     case BP_P4: bp_probe(c.stream, sh, t, cnt[sh], BtP4{a}); break;
                     default: bp_probe(c.stream, sh, t, cnt[sh], BtP5{a}); break;
@@ -1894,7 +1896,7 @@ int Ctx::solve_batch(int n_inst, const tincr_tda_instance *hin, int max_iter, do
         const int forced = bp_forced_shape();
         if (forced < 0) {
             TINCR_CUDA(cudaMemsetAsync(w.D32.p, 0, o_d * sizeof(float), stream));
-            bt_split_x_kernel<<<gv, BT_T, 0, stream>>>(a, 0);
+            bt_split_x_kernel<<<gv, BT_T, 0, stream>>>(a, 0, 0);
             count_launch(stream, "bt_split_x");
             check_launch("bt_split_x");
             bp_autotune(*this, w, a, n_sm);
@@ -1959,10 +1961,10 @@ int Ctx::solve_batch(int n_inst, const tincr_tda_instance *hin, int max_iter, do
     auto iteration_mixed = [&](cudaStream_t st, int g) {
         if (g_lo[g] == g_lo[g + 1]) return;
         const int I0 = g_lo[g];
-        bt_split_x_kernel<<<gvg[g], BT_T, 0, st>>>(a, I0);
+        bt_split_x_kernel<<<gvg[g], BT_T, 0, st>>>(a, I0, 0);
         count_launch(st, "bt_split_x");
         check_launch("bt_split_x");
-        bt_plane_launch(*this, st, w, g, BP_P1, BtP1{a}, TINCR_KF_AO_TRANSFORM);
+        bt_plane_launch(*this, st, w, g, BP_P1, BtP1{a, false}, TINCR_KF_AO_TRANSFORM);
         bt_plane_launch(*this, st, w, g, BP_P2, BtP2{a}, TINCR_KF_AO_EXCHANGE);   // + LC Coulomb diagonals
         bt_diag_kernel<<<gvg[g], BT_T, 0, st>>>(a, BT_MIXED, I0);                  // non-LC Coulomb diagonals
         count_launch(st, "bt_diag");
@@ -2050,9 +2052,19 @@ int Ctx::solve_batch(int n_inst, const tincr_tda_instance *hin, int max_iter, do
     } else {
         run_loop(iteration, max_iter);
     }
-    // final pass: transition charges of the Ritz vectors
-    for (int g = 0; g < 2; ++g)
-        bt_launch<false, false>(*this, stream, w.t1[g], w.nt1[g], BtStep1{a, true}, TINCR_KF_OTHER, 0.0);
+    // final pass: transition charges of the Ritz vectors (H = [C_o;SC_o] R, then its Coulomb
+    // diagonals); a mixed solve forms H with the plane GEMM (its S C is FP32-accurate either way)
+    for (int g = 0; g < 2; ++g) {
+        if (g_lo[g] == g_lo[g + 1]) continue;
+        if (mixed && tol >= MIXED_TOL_FLOOR) {
+            bt_split_x_kernel<<<gvg[g], BT_T, 0, stream>>>(a, g_lo[g], 1);
+            count_launch(stream, "bt_split_x");
+            check_launch("bt_split_x");
+            bt_plane_launch(*this, stream, w, g, BP_P1, BtP1{a, true}, TINCR_KF_OTHER);
+        } else {
+            bt_launch<false, false>(*this, stream, w.t1[g], w.nt1[g], BtStep1{a, true}, TINCR_KF_OTHER, 0.0);
+        }
+    }
     bt_diag_kernel<<<gv, BT_T, 0, stream>>>(a, 1, 0);
     count_launch(stream, "bt_diag");
     check_launch("bt_diag");
