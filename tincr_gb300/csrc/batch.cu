@@ -954,15 +954,19 @@ __device__ void bt_eig_lowest(int m, int nr, double *A, double *W, double *w, do
             du2[i] = 0.0;
         }
         unsigned long long swp = 0, swp2 = 0;   // row interchanges (bit i)
+        // dd[i] receives the reciprocal of pivot i (one division per row; the solves only multiply)
         for (int i = 0; i + 1 < m; ++i) {
             if (fabs(dd[i]) >= fabs(dl[i])) {
                 if (fabs(dd[i]) < tiny) dd[i] = dd[i] < 0.0 ? -tiny : tiny;
-                const double l = dl[i] / dd[i];
+                const double rp = 1.0 / dd[i];
+                const double l = dl[i] * rp;
+                dd[i] = rp;
                 dl[i] = l;
                 dd[i + 1] -= l * du[i];
             } else {
-                const double l = dd[i] / dl[i];
-                dd[i] = dl[i];
+                const double rp = 1.0 / dl[i];
+                const double l = dd[i] * rp;
+                dd[i] = rp;
                 dl[i] = l;
                 const double t = du[i];
                 du[i] = dd[i + 1];
@@ -975,7 +979,7 @@ __device__ void bt_eig_lowest(int m, int nr, double *A, double *W, double *w, do
             }
         }
         if (fabs(dd[m - 1]) < tiny) dd[m - 1] = dd[m - 1] < 0.0 ? -tiny : tiny;
-        for (int i = 0; i < m; ++i) dd[i] = 1.0 / dd[i];   // reciprocal pivots: no division in the solves
+        dd[m - 1] = 1.0 / dd[m - 1];
         for (int i = 0; i < m; ++i) z[i] = 1.0 + 0.5 * (double)((i * (r + 1) * 7919 + 13 * r) % 97) / 97.0;
         for (int it = 0; it < 3; ++it) {
             for (int i = 0; i + 1 < m; ++i) {            // L^-1 with the interchanges
