@@ -16,6 +16,8 @@ The monomer ground states come from the host SCC of the isolated monomers (tincr
 the electrostatic embedding of the other monomers, src/fmo/scc; that step precedes the TDA path).
 """
 
+import weakref
+
 import numpy as np
 
 from . import _lib
@@ -120,35 +122,69 @@ class _Result(ct.Structure):
                 ("q_trans", ct.POINTER(ct.c_double)), ("iterations", ct.c_int), ("status", ct.c_int)]
 
 
+# tincr_tda_instance / tincr_tda_result as numpy records (same layout as the C structs: five ints and
+# padding to the pointer alignment, then seven pointers; five pointers, then two ints), so that a
+# batch of hundreds of instances is marshalled with array operations
+_INST_DT = np.dtype([("dims", np.int32, 5), ("pad", np.int32), ("ptr", np.uint64, 7)])
+_RES_DT = np.dtype([("ptr", np.uint64, 5), ("iterations", np.int32), ("status", np.int32)])
+assert _INST_DT.itemsize == ct.sizeof(_Instance) and _RES_DT.itemsize == ct.sizeof(_Result)
+
+
+def _f64(a):
+    return a if (a.dtype == np.float64 and a.flags.c_contiguous) else np.ascontiguousarray(a, dtype=np.float64)
+
+
+_ADDR = {}   # id(array) -> (weak reference, data address): the lookup numpy makes costs microseconds
+
+
+def _addr(a):
+    if a is None:
+        return 0
+    hit = _ADDR.get(id(a))
+    if hit is not None and hit[0]() is a:
+        return hit[1]
+    ptr = a.__array_interface__["data"][0]
+    if len(_ADDR) > 65536:
+        _ADDR.clear()
+    _ADDR[id(a)] = (weakref.ref(a), ptr)
+    return ptr
+
+
 def solve_batch(ctx, instances, max_iter=50, tol=1e-4, precision=_lib.PREC_FP64):
     """Run `tincr_tda_solve_batch`; returns (status, list of result dicts)."""
     n = len(instances)
     keep = []
-    arr = (_Instance * n)()
-    res = (_Result * n)()
-    outs = []
+    arr = np.zeros(n, _INST_DT)
     for k, q in enumerate(instances):
-        host = {}
-        for key in ("c", "s", "orbe", "gamma", "xyz"):
-            host[key] = np.ascontiguousarray(q[key], dtype=np.float64)
-        host["opa"] = np.ascontiguousarray(q["opa"], dtype=np.int32)
-        host["gamma_lr"] = None if q["gamma_lr"] is None else np.ascontiguousarray(q["gamma_lr"], dtype=np.float64)
-        keep.append(host)
-        arr[k] = _Instance(q["n_atoms"], q["n_orb"], q["n_occ"], q["n_virt"], q["n_roots"], _lib.iptr(host["opa"]),
-                           _lib.dptr(host["c"]), _lib.dptr(host["s"]), _lib.dptr(host["orbe"]),
-                           _lib.dptr(host["gamma"]), _lib.dptr(host["gamma_lr"]), _lib.dptr(host["xyz"]))
-        nr, ov = q["n_roots"], q["n_occ"] * q["n_virt"]
-        o = dict(energies=np.zeros(nr), coefficients=np.zeros((ov, nr)), osc=np.zeros(nr), tr_dip=np.zeros((3, nr)),
-                 q_trans=np.zeros((q["n_atoms"], nr)))
-        outs.append(o)
-        res[k] = _Result(_lib.dptr(o["energies"]), _lib.dptr(o["coefficients"]), _lib.dptr(o["osc"]),
-                         _lib.dptr(o["tr_dip"]), _lib.dptr(o["q_trans"]), 0, 0)
-    rc = ctx.lib.tincr_tda_solve_batch(ctx.h, n, ct.cast(arr, ct.c_void_p), int(max_iter), float(tol), int(precision),
-                                       ct.cast(res, ct.c_void_p))
+        c, s_, orbe, gam, xyz = _f64(q["c"]), _f64(q["s"]), _f64(q["orbe"]), _f64(q["gamma"]), _f64(q["xyz"])
+        glr = None if q["gamma_lr"] is None else _f64(q["gamma_lr"])
+        opa = q["opa"] if (q["opa"].dtype == np.int32 and q["opa"].flags.c_contiguous) else \
+            np.ascontiguousarray(q["opa"], dtype=np.int32)
+        keep.append((c, s_, orbe, gam, xyz, glr, opa))
+        arr[k] = ((q["n_atoms"], q["n_orb"], q["n_occ"], q["n_virt"], q["n_roots"]), 0,
+                  (_addr(opa), _addr(c), _addr(s_), _addr(orbe), _addr(gam), _addr(glr), _addr(xyz)))
+    dims = arr["dims"].astype(np.int64)
+    nr, ov, na = dims[:, 4], dims[:, 2] * dims[:, 3], dims[:, 0]
+    # one block per output kind, instance k at its offset
+    sizes = np.stack([nr, ov * nr, nr, 3 * nr, na * nr])
+    offs = np.concatenate([np.zeros((5, 1), np.int64), np.cumsum(sizes, axis=1)], axis=1)
+    blocks = [np.zeros(int(offs[j, -1])) for j in range(5)]
+    res = np.zeros(n, _RES_DT)
+    for j in range(5):
+        res["ptr"][:, j] = _addr(blocks[j]) + 8 * offs[j, :-1].astype(np.uint64)
+    rc = ctx.lib.tincr_tda_solve_batch(ctx.h, n, arr.ctypes.data, int(max_iter), float(tol), int(precision),
+                                       res.ctypes.data)
     ctx.check(rc, allow=(_lib.OK, _lib.NOT_CONVERGED))
+    outs = []
+    e, cf, osc, td, qt = blocks
+    o0 = offs[:, :-1].tolist()
+    o1 = offs[:, 1:].tolist()
+    its, sts = res["iterations"].tolist(), res["status"].tolist()
     for k in range(n):
-        outs[k]["iterations"] = res[k].iterations
-        outs[k]["status"] = res[k].status
+        r_, v_, a_ = int(nr[k]), int(ov[k]), int(na[k])
+        outs.append(dict(energies=e[o0[0][k]:o1[0][k]], coefficients=cf[o0[1][k]:o1[1][k]].reshape(v_, r_),
+                         osc=osc[o0[2][k]:o1[2][k]], tr_dip=td[o0[3][k]:o1[3][k]].reshape(3, r_),
+                         q_trans=qt[o0[4][k]:o1[4][k]].reshape(a_, r_), iterations=its[k], status=sts[k]))
     return rc, outs
 
 
