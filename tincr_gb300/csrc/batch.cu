@@ -1808,14 +1808,15 @@ int Ctx::solve_batch(int n_inst, const tincr_tda_instance *hin, int max_iter, do
         if (!cw.empty()) upload_any(stream, w.cl_inst[g], cw);
     }
 
-    // static tile tables
+    // static tile tables (the FP64 product tables only when an FP64 product runs)
+    const bool fp64_products = !(mixed && tol >= MIXED_TOL_FLOOR);
     std::vector<int4> tsc, t1[2], t2[2], t4[2], t5[2];
     for (int I = 0; I < n_inst; ++I) {
         const BtInst &b = w.h[I];
         const int n2 = 2 * b.n, g = I < g_lo[1] ? 0 : 1;
         for (int tm = 0; tm < ceil_div(b.n, GB_M); ++tm)
             for (int tn = 0; tn < ceil_div(b.o + b.v, GB_N); ++tn) tsc.push_back(make_int4(I, 0, tm, tn));
-        for (int s = 0; s < b.nr; ++s) {
+        for (int s = 0; s < (fp64_products ? b.nr : 0); ++s) {
             for (int tm = 0; tm < ceil_div(n2, GB_M); ++tm)
                 for (int tn = 0; tn < ceil_div(b.v, GB_N); ++tn) {
                     t1[g].push_back(make_int4(I, s, tm, tn));
@@ -2088,16 +2089,21 @@ int Ctx::solve_batch(int n_inst, const tincr_tda_instance *hin, int max_iter, do
     int worst = TINCR_OK;
     last_products = 0;
     for (int I = 0; I < n_inst; ++I) {
-        const BtInst &b = w.h[I];
-        const tincr_tda_instance &q = hin[order[I]];
-        tincr_tda_result &o = res[order[I]];
         const BtState &s = hs[I];
+        tincr_tda_result &o = res[order[I]];
         o.iterations = s.iter;
         o.status = s.status == BT_CONVERGED ? TINCR_OK
                  : s.status == BT_NONFINITE ? TINCR_NONFINITE : TINCR_NOT_CONVERGED;
         if (o.status == TINCR_NONFINITE) worst = TINCR_NONFINITE;
         else if (o.status == TINCR_NOT_CONVERGED && worst == TINCR_OK) worst = TINCR_NOT_CONVERGED;
         last_products += s.products;
+    }
+    // per-instance outputs, one task per instance (the coefficients are transposed to tincr's layout)
+#pragma omp parallel for schedule(dynamic, 4) num_threads(12)
+    for (int I = 0; I < n_inst; ++I) {
+        const BtInst &b = w.h[I];
+        const tincr_tda_instance &q = hin[order[I]];
+        tincr_tda_result &o = res[order[I]];
         const double *u = hu.data() + b.off_u, *Rr = hR.data() + b.off_r, *Y = hY.data() + b.off_y;
         if (o.energies)
             for (int r = 0; r < b.nr; ++r) o.energies[r] = u[r];
