@@ -245,37 +245,33 @@ bool eigh_lowest_upper(int n, const double *a, int k, double *w, double *y) {
     // 1. T = Q^T A Q.  Reflection c acts on rows/columns c+1..n-1; its vector u (with u_0 = x0 - alpha)
     //    replaces row c to the right of the diagonal (= column c below it), where the back-
     //    transformation reads it.  The full symmetric trailing block is kept up to date.
-    //    Rows are dealt to threads in blocks of eight (one cache line of p per thread).
-//    Step c: (i) the owner of row c forms the reflection from row c (already updated) into uv (two
-    //    buffers by step parity);
-    //    barrier; (ii) p = beta A' u on the owned rows and partial u.p; barrier; (iii) K = beta u.p / 2,
-    //    q = p - K u, rows -= u q^T + q u^T; the owner of row c+1 updates that row first and forms the
-    //    next reflection before the barrier that closes the step.
+    //    Rows are dealt to threads in blocks of eight (one cache line of p per thread).  One barrier
+    //    and one pass over the owned rows per step: after the barrier, K = beta u.p / 2 and
+    //    q = p - K u on every thread; row c+1 is formed privately by every thread from the old values
+    //    (the same arithmetic, so the same bits), which gives the next reflection u' without a
+    //    second barrier; then each owned row gets rows -= u q^T + q u^T and, in the same pass, its
+    //    entry of the next p' = beta' A'' u' and of u'.p' (buffers of the step's parity).  The owner
+    //    of row c+1 stores it after the next barrier, when no thread reads the old row.
     const int T = tridiag_threads(n);
-    std::vector<double> part(64, 0.0);
-    std::vector<char> skip(n, 0);
-    auto reflect = [&](int c) {   // from row c, columns c+1..n-1
-        double *u = &A[(size_t)c * n + c + 1];
-        const int n1 = n - c - 1;
-        const double x0 = u[0];
+    std::vector<double> part(2 * 64, 0.0), pp(2 * (size_t)n);
+    // the reflection of row c from its updated entries row[c..n-1] (row[0] = the diagonal):
+    // writes u (row[1..], with u_0 = x0 - alpha) and returns beta (0: nothing to reflect)
+    auto reflect = [](double *row, int n1, double &dc, double &ec) {
+        const double x0 = row[1];
         double s2 = 0.0;
-        for (int i = 1; i < n1; ++i) s2 += u[i] * u[i];
-        d[c] = A[(size_t)c * n + c];
+        for (int i = 2; i <= n1; ++i) s2 += row[i] * row[i];
+        dc = row[0];
         if (s2 == 0.0) {
-            beta[c] = 0.0;
-            e[c] = x0;
-            skip[c] = 1;
-            return;
+            ec = x0;
+            return 0.0;
         }
         const double nx = std::sqrt(x0 * x0 + s2);
         const double alpha = x0 > 0.0 ? -nx : nx;
-        beta[c] = 1.0 / (alpha * (alpha - x0));
-        e[c] = alpha;
-        u[0] = x0 - alpha;
-        double *ub = uv.data() + (size_t)(c & 1) * n;   // alternates: step c - 1 may still read the other
-        for (int i = 0; i < n1; ++i) ub[c + 1 + i] = u[i];
+        ec = alpha;
+        row[1] = x0 - alpha;
+        return 1.0 / (alpha * (alpha - x0));
     };
-    if (n >= 3) reflect(0);
+    if (n >= 3) {
 #pragma omp parallel num_threads(T) if (T > 1)
     {
 #ifdef _OPENMP
@@ -283,42 +279,95 @@ bool eigh_lowest_upper(int n, const double *a, int k, double *w, double *y) {
 #else
         const int nt = 1, me = 0;
 #endif
-        std::vector<double> q(n);
-        for (int c = 0; c + 2 < n; ++c) {
-            if (skip[c]) {   // identical on every thread: written before the previous barrier
-                if (((c + 1) >> 3) % nt == me && c + 3 < n) reflect(c + 1);
-#pragma omp barrier
-                continue;
-            }
-            const double bet = beta[c];
-            const double *u = uv.data() + (size_t)(c & 1) * n;
+        std::vector<double> q(n), nxt(n), cur(n);   // cur: row c (u in cur[1..]), nxt: row c+1 being formed
+        for (int j = 0; j < n; ++j) cur[j] = A[j];  // row 0 (c = 0)
+        double d0, e0;
+        double bet = reflect(cur.data(), n - 1, d0, e0);   // the same on every thread
+        if (me == 0) {
+            d[0] = d0;
+            e[0] = e0;
+        }
+        // row this thread owns whose reflection it still has to store (row 0: thread 0, after the
+        // first barrier, since every thread copies the old row 0 first)
+        int pending = me == 0 ? 0 : -1;
+        // p = beta A' u of step 0 on the owned rows (later steps form theirs while updating)
+        if (bet != 0.0) {
             double up = 0.0;
-            for (int i = c + 1; i < n; ++i) {
+            for (int i = 1; i < n; ++i) {
                 if ((i >> 3) % nt != me) continue;
-                const double acc = dot8(&A[(size_t)i * n + c + 1], u + c + 1, n - c - 1);
-                p[i] = bet * acc;
-                up += u[i] * p[i];
+                pp[i] = bet * dot8(&A[(size_t)i * n + 1], cur.data() + 1, n - 1);
+                up += cur[i] * pp[i];
             }
             part[me] = up;
-#pragma omp barrier
-            double ut = 0.0;
-            for (int t = 0; t < nt; ++t) ut += part[t];
-            const double K = 0.5 * bet * ut;
-            for (int j = c + 1; j < n; ++j) q[j] = p[j] - K * u[j];
-            auto update = [&](int i) {
-                double *row = &A[(size_t)i * n];
-                const double ui = u[i], qi = q[i];
-#pragma omp simd
-                for (int j = c + 1; j < n; ++j) row[j] -= ui * q[j] + qi * u[j];
-            };
-            if (((c + 1) >> 3) % nt == me) {
-                update(c + 1);
-                if (c + 3 < n) reflect(c + 1);
-            }
-            for (int i = c + 2; i < n; ++i)
-                if ((i >> 3) % nt == me) update(i);
-#pragma omp barrier
         }
+        for (int c = 0; c + 2 < n; ++c) {
+            const double *u = cur.data() - c;   // u[i] for i = c+1..n-1
+            const double *p = pp.data() + (size_t)(c & 1) * n;
+            const double *pt = part.data() + (c & 1) * 64;
+            double *pn = pp.data() + (size_t)((c + 1) & 1) * n;
+            double *ptn = part.data() + ((c + 1) & 1) * 64;
+#pragma omp barrier
+            if (pending >= 0) {   // row c, formed in the previous step: past the barrier nobody reads it
+                for (int j = c; j < n; ++j) A[(size_t)c * n + j] = cur[j - c];
+                pending = -1;
+            }
+            // row c+1 (columns c+1..n-1) after this step's update, on every thread
+            const int r = c + 1;
+            double K = 0.0;
+            if (bet != 0.0) {
+                double ut = 0.0;
+                for (int t = 0; t < nt; ++t) ut += pt[t];
+                K = 0.5 * bet * ut;
+                for (int j = c + 1; j < n; ++j) q[j] = p[j] - K * u[j];
+                const double ur = u[r], qr = q[r];
+                for (int j = r; j < n; ++j) nxt[j - r] = A[(size_t)r * n + j] - (ur * q[j] + qr * u[j]);
+            } else {
+                for (int j = r; j < n; ++j) nxt[j - r] = A[(size_t)r * n + j];
+            }
+            double dr = 0.0, er = 0.0, betn = 0.0;
+            if (c + 3 < n) betn = reflect(nxt.data(), n - r - 1, dr, er);
+            // owned rows c+2..: this step's update and, in the same pass, the next step's p
+            const double *un = nxt.data() - r;   // next u[i] for i = r+1..n-1
+            double upn = 0.0;
+            for (int i = c + 2; i < n; ++i) {
+                if ((i >> 3) % nt != me) continue;
+                double *row = &A[(size_t)i * n];
+                if (bet != 0.0) {
+                    const double ui = u[i], qi = q[i];
+                    row[c + 1] -= ui * q[c + 1] + qi * u[c + 1];
+                    if (betn != 0.0) {
+                        double acc = 0.0;
+#pragma omp simd reduction(+ : acc)
+                        for (int j = c + 2; j < n; ++j) {
+                            const double x = row[j] - (ui * q[j] + qi * u[j]);
+                            row[j] = x;
+                            acc += x * un[j];
+                        }
+                        pn[i] = betn * acc;
+                        upn += un[i] * pn[i];
+                    } else {
+#pragma omp simd
+                        for (int j = c + 2; j < n; ++j) row[j] -= ui * q[j] + qi * u[j];
+                    }
+                } else if (betn != 0.0) {
+                    pn[i] = betn * dot8(row + c + 2, un + c + 2, n - c - 2);
+                    upn += un[i] * pn[i];
+                }
+            }
+            ptn[me] = upn;
+            if (me == 0) {
+                beta[c] = bet;
+                if (c + 3 < n) { d[r] = dr; e[r] = er; }
+            }
+            std::swap(cur, nxt);   // cur = row c+1, cur[0] its diagonal
+            bet = betn;
+            if ((r >> 3) % nt == me) pending = r;
+        }
+        if (pending >= 0) {
+            const int r = pending;
+            for (int j = r; j < n; ++j) A[(size_t)r * n + j] = cur[j - r];
+        }
+    }
     }
     if (n >= 2) {
         d[n - 2] = A[(size_t)(n - 2) * n + n - 2];
