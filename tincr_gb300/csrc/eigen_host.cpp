@@ -7,6 +7,7 @@
 // The subspace is at most 15 * n_roots wide, so this stays a small host step between device phases.
 #include <algorithm>
 #include <cmath>
+#include <cstring>
 #include <numeric>
 #include <vector>
 
@@ -184,33 +185,44 @@ namespace {
 // leading principal minors N_i = (d_i - x) N_{i-1} - e_{i-1}^2 N_{i-2} (a division-free recurrence,
 // backward stable like the pivot form: each step's rounding is a relative perturbation of d_i - x
 // and of e_{i-1}^2).  An exact zero becomes a tiny value of the opposite sign; both terms are
-// rescaled by a power of two when the newest leaves [2^-400, 2^400].
-int sturm_count(const double *d, const double *bsq, int n, double x) {
-    double n0 = 1.0, n1 = d[0] - x;
-    if (n1 == 0.0) n1 = -0x1p-100;
-    int c = std::signbit(n1) ? 1 : 0;
+// rescaled by a power of two when the newest leaves [2^-400, 2^400].  Counted at SLICE points at
+// once: independent recurrences interleaved, so that their floating-point latencies overlap.  The
+// range test reads the exponent bits; the exact rescaling exponent comes from ilogb in the rare
+// branch that needs it.
+constexpr int SLICE = 4;   // points per multisection step
+
+void sturm_count_multi(const double *d, const double *bsq, int n, const double *x, int *cnt) {
+    double n0[SLICE], n1[SLICE];
+    for (int q = 0; q < SLICE; ++q) {
+        n0[q] = 1.0;
+        n1[q] = d[0] - x[q];
+        if (n1[q] == 0.0) n1[q] = -0x1p-100;
+        cnt[q] = std::signbit(n1[q]) ? 1 : 0;
+    }
     for (int i = 1; i < n; ++i) {
-        double n2 = (d[i] - x) * n1 - bsq[i - 1] * n0;
-        if (n2 == 0.0) {
-            n2 = -0x1p-100 * n1;
-        } else {
-            const int ex = std::ilogb(n2);
-            if (ex > 400 || ex < -400) {
-                const double sc = std::ldexp(1.0, -ex);
-                n1 *= sc;
+        const double di = d[i], bi = bsq[i - 1];
+        for (int q = 0; q < SLICE; ++q) {
+            double n2 = (di - x[q]) * n1[q] - bi * n0[q];
+            unsigned long long bits;
+            std::memcpy(&bits, &n2, sizeof bits);
+            const int bex = (int)((bits >> 52) & 0x7ff);   // biased exponent (0: zero or subnormal)
+            if (n2 == 0.0) {
+                n2 = -0x1p-100 * n1[q];
+            } else if (bex > 1023 + 400 || bex < 1023 - 400) {
+                const double sc = std::ldexp(1.0, -std::ilogb(n2));
+                n1[q] *= sc;
                 n2 *= sc;
             }
+            cnt[q] += std::signbit(n1[q]) != std::signbit(n2) ? 1 : 0;
+            n0[q] = n1[q];
+            n1[q] = n2;
         }
-        c += std::signbit(n1) != std::signbit(n2) ? 1 : 0;
-        n0 = n1;
-        n1 = n2;
     }
-    return c;
 }
 
-// threads for the tridiagonalisation: two barriers per reflection pay off from n ~ 128.  Eight
-// threads come within 10% of sixteen on a 16-core Grace host (n = 300: 1.45 ms vs 1.35 ms) and leave
-// cores to the CUDA driver and the caller, so a preempted thread does not stall every barrier.
+// threads for the tridiagonalisation: the per-step barrier pays off from n ~ 128.  Eight threads come
+// within 10% of twelve and sixteen on a 16-core Grace host and leave cores to the CUDA driver and
+// the caller, so a preempted thread does not stall every barrier.
 int tridiag_threads(int n) {
 #ifdef _OPENMP
     return n >= 128 ? std::min(8, omp_get_max_threads()) : 1;
@@ -402,12 +414,21 @@ bool eigh_lowest_upper(int n, const double *a, int k, double *w, double *y) {
     {
 #pragma omp for schedule(dynamic, 1)
     for (int r = 0; r < k; ++r) {
+        // multisection: SLICE interior points per step cut [x_lo, x_hi] into SLICE + 1 parts
         double x_lo = lo, x_hi = hi;
         for (int it = 0; it < 200; ++it) {
             if (x_hi - x_lo <= 2.0 * eps * std::max(std::fabs(x_lo), std::fabs(x_hi)) + 4.0 * pivmin) break;
-            const double mid = 0.5 * (x_lo + x_hi);
-            if (sturm_count(d.data(), bsq.data(), n, mid) > r) x_hi = mid;
-            else x_lo = mid;
+            double xs[SLICE];
+            int cs[SLICE];
+            const double h = (x_hi - x_lo) / (SLICE + 1);
+            for (int q = 0; q < SLICE; ++q) xs[q] = x_lo + h * (q + 1);
+            sturm_count_multi(d.data(), bsq.data(), n, xs, cs);
+            int f = 0;   // first point with more than r eigenvalues below it
+            while (f < SLICE && cs[f] <= r) ++f;
+            const double a = f > 0 ? xs[f - 1] : x_lo, b = f < SLICE ? xs[f] : x_hi;
+            if (!(a > x_lo || b < x_hi)) break;   // no representable progress left
+            x_lo = a;
+            x_hi = b;
         }
         w[r] = 0.5 * (x_lo + x_hi);
     }
