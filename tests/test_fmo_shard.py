@@ -1,0 +1,102 @@
+"""Multi-rank FMO work list (CPU, gloo, world size 2): the shards cover every instance once, are
+balanced by estimated cost, and the all-gather returns the whole result list in the caller's order
+on every rank.  The per-rank solver is a stand-in that derives each result from its instance, so no
+GPU is needed; the GPU batch itself is covered by test_fmo.py."""
+
+import os
+import socket
+
+import numpy as np
+import pytest
+
+from tincr_gb300 import _lib
+from tincr_gb300 import fmo
+
+
+def _instances(n=23, seed=5):
+    rng = np.random.default_rng(seed)
+    out = []
+    for k in range(n):
+        o, v = int(rng.integers(8, 52)), int(rng.integers(8, 52))
+        out.append(dict(n_occ=o, n_virt=v, n_roots=int(rng.choice([1, 4])), tag=k))
+    return out
+
+
+def _fake_solver(ctx, inst, **kw):
+    return _lib.OK, [dict(energies=np.array([0.1 * q["tag"]]), tag=q["tag"]) for q in inst]
+
+
+def test_shards_cover_and_balance():
+    inst = _instances()
+    for world in (1, 2, 3, 4):
+        shards = [fmo.shard_instances(inst, world, r) for r in range(world)]
+        flat = sorted(k for s in shards for k in s)
+        assert flat == list(range(len(inst)))
+        loads = [sum(fmo.instance_cost(inst[k]) for k in s) for s in shards]
+        # LPT: the largest load exceeds the mean by at most the largest single instance
+        assert max(loads) - sum(loads) / world <= max(fmo.instance_cost(q) for q in inst)
+
+
+def _rank_main(rank, world, port, q):
+    import torch.distributed as dist
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    try:
+        inst = _instances()
+        rc, full = fmo.solve_batch_sharded(None, inst, world, rank, solver=_fake_solver)
+        q.put((rank, rc, [r["tag"] for r in full], [float(r["energies"][0]) for r in full]))
+    finally:
+        dist.destroy_process_group()
+
+
+def test_sharded_results_gathered_in_order():
+    torch = pytest.importorskip("torch")
+    import torch.multiprocessing as mp
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        port = s.getsockname()[1]
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    procs = [ctx.Process(target=_rank_main, args=(r, 2, port, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    got = [q.get(timeout=120) for _ in procs]
+    for p in procs:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    n = len(_instances())
+    for rank, rc, tags, es in got:
+        assert rc == _lib.OK
+        assert tags == list(range(n))
+        assert np.allclose(es, 0.1 * np.arange(n))
+
+
+def _bench_rank(rank, world, port, q):
+    import torch.distributed as dist
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    try:
+        import bench
+        q.put((rank, bench.barrier_and_max(1.5 + rank, world)))
+    finally:
+        dist.destroy_process_group()
+
+
+def test_bench_timing_is_max_over_ranks():
+    """bench.py's N > 1 path (replicas of the single-system step): barrier, then the slowest rank's
+    time on every rank."""
+    pytest.importorskip("torch")
+    import torch.multiprocessing as mp
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        port = s.getsockname()[1]
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    procs = [ctx.Process(target=_bench_rank, args=(r, 2, port, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    got = sorted(q.get(timeout=120) for _ in procs)
+    for p in procs:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    assert [v for _, v in got] == [2.5, 2.5]

@@ -188,6 +188,53 @@ def solve_batch(ctx, instances, max_iter=50, tol=1e-4, precision=_lib.PREC_FP64)
     return rc, outs
 
 
+def instance_cost(q):
+    """Estimated work of one instance: n_roots o v (o + v), the exchange contraction of tincr's
+    product per trial vector (the quantity the work list is balanced on)."""
+    o, v = int(q["n_occ"]), int(q["n_virt"])
+    return int(q["n_roots"]) * o * v * (o + v)
+
+
+def shard_instances(instances, world, rank):
+    """Indices (ascending) of the instances rank `rank` of `world` solves: longest-processing-time
+    assignment by `instance_cost` (the most expensive instance first to the least loaded rank, ties
+    to the lower rank), the same on every rank without communication."""
+    if world <= 1:
+        return list(range(len(instances)))
+    load = [0] * world
+    owner = [0] * len(instances)
+    for k in sorted(range(len(instances)), key=lambda k: (-instance_cost(instances[k]), k)):
+        r = min(range(world), key=lambda x: (load[x], x))
+        owner[k] = r
+        load[r] += instance_cost(instances[k])
+    return [k for k in range(len(instances)) if owner[k] == rank]
+
+
+def solve_batch_sharded(ctx, instances, world, rank, solver=None, **kw):
+    """The FMO work list split over `world` ranks (one GPU each): every rank solves its shard with
+    `solve_batch` (or `solver`), then one all-gather of the per-instance results (energies,
+    coefficients, transition charges, dipoles, oscillator strengths) gives every rank the whole
+    list, in the caller's order, as the exciton Hamiltonian needs it.  Needs an initialised
+    torch.distributed process group when world > 1 (gloo suffices: the results are host arrays).
+    Returns (worst status over all ranks, list of result dicts)."""
+    solver = solver or solve_batch
+    mine = shard_instances(instances, world, rank)
+    rc, out = solver(ctx, [instances[k] for k in mine], **kw) if mine else (_lib.OK, [])
+    if world <= 1:
+        return rc, out
+    import torch.distributed as dist
+    parts = [None] * world
+    dist.all_gather_object(parts, (mine, rc, out))
+    full = [None] * len(instances)
+    worst = _lib.OK
+    for idx, rc_r, out_r in parts:
+        for k, o in zip(idx, out_r):
+            full[k] = o
+        if rc_r == _lib.NONFINITE or (rc_r == _lib.NOT_CONVERGED and worst == _lib.OK):
+            worst = rc_r
+    return worst, full
+
+
 def le_gradients(monomers, results, states, n_streams=8, variant="reference", contexts=None,
                  precision=_lib.PREC_FP64):
     """Excitation-energy gradients of locally excited states, the LE terms of tincr's FMO exciton
