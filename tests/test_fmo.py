@@ -116,7 +116,7 @@ def test_batch_not_converged_and_bad_input(gpu_ctx):
 @pytest.mark.gpu
 def test_batch_mixed_within_bar(gpu_ctx):
     """Mixed form (three-plane split-BF16 GEMMs, FP64 subspace): every root of every instance within
-    1e-6 Eh of the FP64 batch (spec bar)."""
+    1e-6 Eh of the FP64 batch (the mixed-form target)."""
     case = fmo_case(3, 1, 1)
     rc64, r64 = fmo.solve_batch(gpu_ctx, case["instances"], max_iter=150, tol=1e-6)
     rcm, rm = fmo.solve_batch(gpu_ctx, case["instances"], max_iter=150, tol=1e-6, precision=_lib.PREC_BF16X3)

@@ -78,7 +78,7 @@ def test_digit_gemm_zero_rows_and_nonfinite(gpu_ctx):
 def test_mixed_davidson_digit_and_fp64_subspace_agree(gpu_ctx, monkeypatch):
     """water27 LC-TDA, 6 roots to residual 1e-5, mixed form: the subspace products as digit GEMMs or
     in FP64 give the same Davidson history and roots within 1e-7 Eh (both carry the mixed A.X
-    operator's error; the spec bar against FP64 is 1e-6 Eh)."""
+    operator's error; the mixed-form target against FP64 is 1e-6 Eh)."""
     c = synthetic_case("water27", True)
 
     def run(ctx):

@@ -4,7 +4,7 @@
   (ground_state.rs / excited_state.rs) on the same roots (installed with tincr_tda_set_states):
   1e-9 Eh/bohr; and the full chain GPU Davidson -> gradient at 1e-6 Eh/bohr.
 * variant "exact" against the oracle's exact variant, and against central finite differences of
-  the excitation energy (+-1e-4 bohr): 1e-5 Eh/bohr, the spec bar.
+  the excitation energy (+-1e-4 bohr): 1e-5 Eh/bohr, the gradient accuracy target.
 """
 
 import numpy as np
@@ -147,7 +147,7 @@ def test_gradient_call_order_and_arguments(gpu_ctx):
                                              ("polyene8", False, "reference")])
 def test_mixed_gradient_within_bar(gpu_ctx, name, lc, variant):
     """After a mixed solve the gradient's contractions and Z-vector run mixed: S1 gradient within
-    1e-5 Eh/bohr (spec bar) of the gradient after an FP64 solve of the same roots."""
+    1e-5 Eh/bohr (the gradient accuracy target) of the gradient after an FP64 solve of the same roots."""
     z, x = _molecule(name)
     sy = gs.build_system(z, x, lc=lc)
     g = gs.run_scc(sy, tol=1e-11)

@@ -2,7 +2,7 @@
 against the oracle on the same inputs.
 
 Tolerances: FP64 path, so transition charges and products agree to a few ulp-scale relative
-errors (1e-12 relative); Davidson energies to 1e-10 Eh (spec bar 1e-8 for FP64) and
+errors (1e-12 relative); Davidson energies to 1e-10 Eh (the FP64 target is 1e-8) and
 eigenvectors up to sign (|overlap| = 1 within 1e-7)."""
 
 import numpy as np
@@ -210,7 +210,7 @@ def test_mixed_products_close_to_fp64(gpu_ctx, name):
 @pytest.mark.parametrize("name", ["water27", "uracil"])
 def test_mixed_davidson_energies_within_bar(monkeypatch, name, plane):
     """Mixed form at tolerance 1e-6 (mixed operator only): every root within 1e-6 Eh of the FP64 GPU
-    roots (spec bar), with either plane GEMM."""
+    roots (the mixed-form target), with either plane GEMM."""
     monkeypatch.setenv("TINCR_GB300_PLANE_GEMM", plane)
     ctx = _lib.Context(0)
     try:
