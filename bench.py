@@ -530,7 +530,32 @@ def cpu_sample(sy, g, n_products, n_iters, cg_iters, sample_vectors=2):
 
 def cpu_baseline(sy, g, n_iters, n_products, cg_iters):
     total, threads, sample = cpu_sample(sy, g, int(n_products), int(round(n_iters)), int(cg_iters))
-    return {"value": total, "unit": "s", "cores": threads, "kind": "port", "sample": sample}
+    out = {"value": total, "unit": "s", "cores": threads, "kind": "port", "sample": sample}
+    out["single_thread"] = cpu_single_thread(int(n_products), int(round(n_iters)), int(cg_iters))
+    return out
+
+
+def cpu_single_thread(n_products, n_iters, cg_iters):
+    """The same sample with one thread: a child process whose BLAS and OpenMP pools have one thread
+    (set before numpy loads), one A.X product in the sample."""
+    import subprocess
+    import sys
+    env = dict(os.environ, OMP_NUM_THREADS="1", OPENBLAS_NUM_THREADS="1", MKL_NUM_THREADS="1")
+    cmd = [sys.executable, os.path.abspath(__file__), "--mode", "cpu-sample", "--ref-products", str(n_products),
+           "--ref-iters", str(n_iters), "--ref-cg", str(cg_iters)]
+    try:
+        r = subprocess.run(cmd, env=env, capture_output=True, text=True, timeout=600)
+        d = json.loads(r.stdout.strip().splitlines()[-1])
+        return {"value": d["value"], "unit": "s", "cores": 1}
+    except Exception as e:   # the baseline is reported, not required
+        return {"unavailable": str(e)[:200]}
+
+
+def run_cpu_sample(args):
+    """--mode cpu-sample: the CPU sample of one step in this process (no GPU), one A.X product."""
+    sy, g = workload()
+    total, threads, sample = cpu_sample(sy, g, args.ref_products, args.ref_iters, args.ref_cg, sample_vectors=1)
+    print(json.dumps({"value": total, "threads": threads, "sample": sample}))
 
 
 def OT_lowest(mons, k):
@@ -627,7 +652,7 @@ def main():
     ap.add_argument("--ref-products", type=int, default=369)
     ap.add_argument("--ref-iters", type=int, default=40)
     ap.add_argument("--ref-cg", type=int, default=14)
-    ap.add_argument("--mode", default="solve", choices=["solve", "products", "fmo"])
+    ap.add_argument("--mode", default="solve", choices=["solve", "products", "fmo", "cpu-sample"])
     ap.add_argument("--k", type=int, default=4)
     args = ap.parse_args()
     if args.mode == "products":
@@ -635,6 +660,9 @@ def main():
         return
     if args.mode == "fmo":
         run_fmo_once(args)
+        return
+    if args.mode == "cpu-sample":
+        run_cpu_sample(args)
         return
     out = run_reference(args) if args.impl == "reference" else run_gpu(args)
     if out is not None:
