@@ -193,15 +193,18 @@ struct BtStep2 {
         const BtInst &in = *op.in;
         const int n = in.n, n2 = 2 * n;
         const int rr = r < n ? r : r - n, cc = c < n ? c : c - n;
-        double *d = a.D + in.off_d;
-        if (r < n && c == r + n) d[(long long)op.b * n + r] = acc;
-        if (r >= n && c == r - n) d[(long long)(in.nr + op.b) * n + c] = acc;
+        if (!in.nh) {   // Coulomb diagonals (bt_diag_kernel for block-structured instances)
+            double *d = a.D + in.off_d;
+            if (r < n && c == r + n) d[(long long)op.b * n + r] = acc;
+            if (r >= n && c == r - n) d[(long long)(in.nr + op.b) * n + c] = acc;
+        }
         a.F[in.off_f + (long long)op.b * n2 * n2 + (long long)r * n2 + c] =
             -0.25 * a.glr[in.off_glr + (long long)rr * n + cc] * acc;
     }
 };
 
-// 4. G_b = F_b [SC_v;C_v]   (2n x v, written over H_b)
+// 4. G_b = F_b [SC_v;C_v]   (2n x v, written over H_b); block-structured instances add the Coulomb
+//    term z o [C_v;SC_v] here instead of through F's diagonals (their F tiles there are skipped)
 struct BtStep4 {
     BtArrays a;
     __device__ bool setup(int I, int b, BtOp &op) const {
@@ -217,6 +220,11 @@ struct BtStep4 {
     }
     __device__ void epi(const BtOp &op, int m, int n, double acc) const {
         const BtInst &in = *op.in;
+        if (in.nh) {
+            const int nn = in.n;
+            acc += a.D[in.off_d + (long long)(2 * in.nr + op.b) * nn + (m < nn ? m : m - nn)] *
+                   a.blk[in.off_blk + 2LL * nn * in.o + (long long)m * in.v + n];
+        }
         a.H[in.off_h + (long long)op.b * 2 * in.n * in.v + (long long)m * in.v + n] = acc;
     }
 };
@@ -230,7 +238,7 @@ struct BtStep5 {
         if (!bt_vector(a, in, I, b, false, &X)) return false;
         op.in = &a.inst[I]; op.I = I; op.b = b; op.X = X;
         const int n2 = 2 * in.n;
-        op.M = in.o; op.N = in.v; op.K = n2;
+        op.M = in.o; op.N = in.v; op.K = in.nh ? in.n + in.nh : n2;   // rows n+nh.. of G meet C_o = 0
         op.A = a.blk + in.off_blk + (long long)n2 * (in.o + in.v); op.lda = in.o;        // [SC_o;C_o], transposed
         op.B = a.H + in.off_h + (long long)b * n2 * in.v; op.ldb = in.v;
         return true;
@@ -341,7 +349,7 @@ __global__ void bt_diag_kernel(BtArrays a, int mode, int I0) {
     const double *X;
     if (!bt_vector(a, in, I, b, mode == BT_FINAL, &X)) return;
     // the exchange GEMM's epilogue captures them for LC instances, unless it skips their blocks
-    if (mode != BT_FINAL && in.lc && !(mode == BT_MIXED && in.nh)) return;
+    if (mode != BT_FINAL && in.lc && !in.nh) return;
     const int n = in.n, v = in.v;
     const double *H = a.H + in.off_h + (long long)b * 2 * n * v;
     const double *rv = a.blk + in.off_blk + 2LL * n * in.o;
@@ -385,7 +393,7 @@ __global__ void bt_coulomb_kernel(BtArrays a, int mode, int I0) {
         double z = 0.0;
         for (int B = 0; B < N; ++B) z += gam[(long long)A * N + B] * ysh[B];
         for (int mu = ao_off[A]; mu < ao_off[A + 1]; ++mu) {
-            if (in.lc && mode == BT_FP64) {
+            if (in.lc && mode == BT_FP64 && !in.nh) {
                 double *f = a.F + in.off_f + (long long)b * n2 * n2;
                 f[(long long)mu * n2 + n + mu] += z;
                 f[(long long)(n + mu) * n2 + mu] += z;
@@ -1778,6 +1786,8 @@ int Ctx::solve_batch(int n_inst, const tincr_tda_instance *hin, int max_iter, do
     // the mixed form leaves the zero rows of block-structured H out: they must read as zeros
     if (mixed) TINCR_CUDA(cudaMemsetAsync(w.H.p, 0, o_h * sizeof(double), stream));
     w.F.reserve(std::max<long long>(1, o_f));
+    // the FP64 exchange leaves the zero tiles of block-structured F out: they must read as zeros
+    if (!(mixed && tol >= MIXED_TOL_FLOOR) && o_f > 0) TINCR_CUDA(cudaMemsetAsync(w.F.p, 0, o_f * sizeof(double), stream));
     w.D.reserve(o_d);
     w.u.reserve(o_u);
     w.err.reserve(o_u);
@@ -1820,11 +1830,19 @@ int Ctx::solve_batch(int n_inst, const tincr_tda_instance *hin, int max_iter, do
             for (int tm = 0; tm < ceil_div(n2, GB_M); ++tm)
                 for (int tn = 0; tn < ceil_div(b.v, GB_N); ++tn) {
                     t1[g].push_back(make_int4(I, s, tm, tn));
-                    if (b.lc) t4[g].push_back(make_int4(I, s, tm, tn));
+                    if (b.lc && !(b.nh && tm * GB_M >= b.n + b.nh)) t4[g].push_back(make_int4(I, s, tm, tn));
                 }
+            // with the block structure: F tiles that only hold zeros or values multiplied by zeros
+            // are left out (as in the plane steps), G rows from n+nh are not needed
             if (b.lc)
                 for (int tm = 0; tm < ceil_div(n2, GB_M); ++tm)
-                    for (int tn = 0; tn < ceil_div(n2, GB_N); ++tn) t2[g].push_back(make_int4(I, s, tm, tn));
+                    for (int tn = 0; tn < ceil_div(n2, GB_N); ++tn) {
+                        const int r0 = tm * GB_M, c0 = tn * GB_N;
+                        if (b.nh && !(bp_meets(r0, r0 + GB_M, 0, b.nh, b.n, b.n + b.nh) &&
+                                      bp_meets(c0, c0 + GB_N, b.nh, b.n, b.n + b.nh, n2)))
+                            continue;
+                        t2[g].push_back(make_int4(I, s, tm, tn));
+                    }
             for (int tm = 0; tm < ceil_div(b.o, GB_M); ++tm)
                 for (int tn = 0; tn < ceil_div(b.v, GB_N); ++tn) t5[g].push_back(make_int4(I, s, tm, tn));
         }
