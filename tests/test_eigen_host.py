@@ -1,6 +1,7 @@
 """CPU test of the host subspace eigensolvers (tincr_gb300/csrc/eigen_host.cpp) against LAPACK
-(numpy.linalg.eigh): the full decomposition and the lowest-k solver (Householder, bisection,
-inverse iteration) on random, nearly degenerate and exactly degenerate symmetric matrices."""
+(numpy.linalg.eigh): the full decomposition and the lowest-k solver (Householder, multisection,
+inverse iteration) on random, nearly degenerate, exactly degenerate, diagonal and block-diagonal
+symmetric matrices, on one thread (n < 128) and on several."""
 
 import ctypes
 import os
@@ -56,6 +57,14 @@ def _cases(rng, n):
     ev = np.repeat(np.sort(rng.uniform(0.3, 1.5, (n + 1) // 2)), 2)[:n]
     yield (q * ev) @ q.T
     yield np.diag(np.sort(rng.uniform(0.2, 1.5, n))) + 1e-3 * (b + b.T)
+    # reflections with nothing to reflect: a diagonal matrix (every column), and two decoupled
+    # blocks (the column at the block edge), which the threaded reduction takes without an update
+    yield np.diag(rng.uniform(0.2, 1.5, n))
+    h = n // 2
+    c = b + b.T
+    c[:h, h:] = 0.0
+    c[h:, :h] = 0.0
+    yield c
 
 
 @pytest.mark.parametrize("n", [1, 2, 3, 17, 60, 150, 300])
