@@ -100,3 +100,63 @@ def test_bench_timing_is_max_over_ranks():
         p.join(timeout=60)
         assert p.exitcode == 0
     assert [v for _, v in got] == [2.5, 2.5]
+
+
+def test_batch_marshalling_layout():
+    """fmo.solve_batch marshals instances and result buffers as records with the C structs' layout:
+    a stand-in for the library reads every instance through its pointers and writes every result,
+    and each value lands in the right instance's arrays."""
+    import ctypes as ct
+    rng = np.random.default_rng(3)
+    inst = []
+    for k in range(7):
+        na, o, v, nr = 2 + k % 3, 3 + k, 2 + (k * 2) % 5, 1 + k % 4
+        n = o + v + 1
+        inst.append(dict(n_atoms=na, n_orb=n, n_occ=o, n_virt=v, n_roots=nr,
+                         opa=np.full(na, 1, np.int32), c=rng.standard_normal((n, o + v)),
+                         s=rng.standard_normal((n, n)), orbe=rng.standard_normal(o + v),
+                         gamma=rng.standard_normal((na, na)),
+                         gamma_lr=None if k % 2 else rng.standard_normal((na, na)),
+                         xyz=rng.standard_normal((na, 3))))
+
+    class Lib:
+        def tincr_tda_solve_batch(self, h, n, arr_addr, max_iter, tol, prec, res_addr):
+            arr = (fmo._Instance * n).from_address(arr_addr)
+            res = (fmo._Result * n).from_address(res_addr)
+            for k in range(n):
+                q = arr[k]
+                o, v, nr, na = q.n_occ, q.n_virt, q.n_roots, q.n_atoms
+                assert q.c[0] == inst[k]["c"][0, 0] and q.s[1] == inst[k]["s"].reshape(-1)[1]
+                assert q.orbe[o + v - 1] == inst[k]["orbe"][-1] and q.xyz[3 * na - 1] == inst[k]["xyz"][-1, -1]
+                assert bool(q.gamma_lr) == (inst[k]["gamma_lr"] is not None)
+                r = res[k]
+                for i in range(nr):
+                    r.energies[i] = 100 * k + i
+                    r.osc[i] = -k
+                for i in range(o * v * nr):
+                    r.coefficients[i] = k + 1e-3 * i
+                for i in range(3 * nr):
+                    r.tr_dip[i] = 7 * k
+                for i in range(na * nr):
+                    r.q_trans[i] = 11 * k + i
+                r.iterations = 5 + k
+                r.status = 0
+            return 0
+
+    class Ctx:
+        lib = Lib()
+        h = None
+
+        def check(self, rc, allow=()):
+            assert rc in allow
+
+    rc, out = fmo.solve_batch(Ctx(), inst, 50, 1e-4, _lib.PREC_BF16X3)
+    assert rc == _lib.OK
+    for k, (q, r) in enumerate(zip(inst, out)):
+        nr, ov = q["n_roots"], q["n_occ"] * q["n_virt"]
+        assert np.array_equal(r["energies"], 100 * k + np.arange(nr))
+        assert r["coefficients"].shape == (ov, nr)
+        assert np.allclose(r["coefficients"].reshape(-1), k + 1e-3 * np.arange(ov * nr))
+        assert np.all(r["osc"] == -k) and np.all(r["tr_dip"] == 7 * k) and r["tr_dip"].shape == (3, nr)
+        assert np.array_equal(r["q_trans"].reshape(-1), 11 * k + np.arange(q["n_atoms"] * nr))
+        assert r["iterations"] == 5 + k and r["status"] == 0
