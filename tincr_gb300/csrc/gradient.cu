@@ -219,9 +219,10 @@ __global__ void cg_update_kernel(long long len, double alpha, const double *p, c
 }
 
 // the same update with alpha = rr / pAp formed on the device (pAp left there by dot_kernel)
-// Device-side CG state: s[0] = r.r, s[1] = p.Ap, s[2] = the new r.r, s[3] = beta; flag[0] = 0 while
-// running, 1 once converged, 2 on a non-finite step; flag[1] = iterations done.  Every thread
-// forms alpha from the same two values, so all take the same decision.
+// Device-side CG state: s[0] = r.r (r.z when preconditioned), s[1] = p.Ap, s[2] = the new r.r,
+// s[3] = beta, s[4] = the new r.z; flag[0] = 0 while running, 1 once converged, 2 on a non-finite
+// step; flag[1] = iterations done.  Every thread forms alpha from the same two values, so all take
+// the same decision.
 
 // x += alpha p ; r -= alpha Ap, alpha = r.r / p.Ap (skipped once the recursion has stopped)
 __global__ void cg_update_dev_kernel(long long len, const double *s, const int *flag, const double *p,
@@ -236,7 +237,7 @@ __global__ void cg_update_dev_kernel(long long len, const double *s, const int *
 }
 
 // the convergence test of helpers.rs:1146-1223 (r.r <= conv) and the next beta
-__global__ void cg_check_kernel(double *s, int *flag, double conv) {
+__global__ void cg_check_kernel(double *s, int *flag, double conv, int precond) {
     if (flag[0] != 0) return;
     flag[1] += 1;
     if (!isfinite(s[0] / s[1])) {
@@ -244,8 +245,9 @@ __global__ void cg_check_kernel(double *s, int *flag, double conv) {
     } else if (s[2] <= conv) {
         flag[0] = 1;
     } else {
-        s[3] = s[2] / s[0];
-        s[0] = s[2];
+        const double next = precond ? s[4] : s[2];
+        s[3] = next / s[0];
+        s[0] = next;
     }
 }
 
@@ -536,16 +538,23 @@ int Ctx::zvector_cg(int variant, const double *R, double *Z, int max_iter, doubl
         check_launch("dot");
     };
     EW(zguess_kernel, len, len, R, d_omega.p, Z);          // bs = R / omega
-    int *flag = reinterpret_cast<int *>(dots + 4);
-    // CG from the current Z (tincr: helpers.rs:1146-1223); the convergence test is FP64.  The
+    int *flag = reinterpret_cast<int *>(dots + 6);
+    // CG from the current Z (tincr: helpers.rs:1146-1223); the convergence test is FP64 on r.r.  The
     // recursion runs on the device (alpha, beta and the test in device scalars); the host reads
     // the flag every CG_SYNC iterations, and the iterations queued after convergence change nothing.
+    // The mixed form preconditions with diag(omega), the dominant part of the operator's diagonal
+    // (tincr's CG is unpreconditioned): the same stopping rule on the same residual, so Z agrees to
+    // that tolerance, in fewer iterations.  The FP64 form keeps tincr's recursion.
     constexpr int CG_SYNC = 4;
+    double *zr = tmp;   // preconditioned residual
     auto run = [&](int limit, int *done) {
+        const bool pre = prec == TINCR_PREC_BF16X3;
+        const double *dir = pre ? zr : r;
         op(Z, Ap);
         EW(axpby3_kernel, len, len, 1.0, R, -1.0, Ap, 0.0, nullptr, r);   // r = R - A Z
-        TINCR_CUDA(cudaMemcpyAsync(p, r, len * sizeof(double), cudaMemcpyDeviceToDevice, stream));
-        dot_dev(r, r, dots);
+        if (pre) EW(zguess_kernel, len, len, r, d_omega.p, zr);
+        TINCR_CUDA(cudaMemcpyAsync(p, dir, len * sizeof(double), cudaMemcpyDeviceToDevice, stream));
+        dot_dev(r, dir, dots);
         TINCR_CUDA(cudaMemsetAsync(flag, 0, 2 * sizeof(int), stream));
         int queued = 0;
         while (queued < limit) {
@@ -555,10 +564,14 @@ int Ctx::zvector_cg(int variant, const double *R, double *Z, int max_iter, doubl
                 dot_dev(p, Ap, dots + 1);
                 EW(cg_update_dev_kernel, len, len, dots, flag, p, Ap, Z, r);
                 dot_dev(r, r, dots + 2);
-                cg_check_kernel<<<1, 1, 0, stream>>>(dots, flag, conv);
+                if (pre) {
+                    EW(zguess_kernel, len, len, r, d_omega.p, zr);
+                    dot_dev(r, zr, dots + 4);
+                }
+                cg_check_kernel<<<1, 1, 0, stream>>>(dots, flag, conv, pre ? 1 : 0);
                 count_launch(stream, "cg_check");
                 check_launch("cg_check");
-                EW(cg_dir_kernel, len, len, dots, flag, p, r);
+                EW(cg_dir_kernel, len, len, dots, flag, p, dir);
             }
             queued += batch;
             TINCR_CUDA(cudaMemcpyAsync(h_flag, flag, 2 * sizeof(int), cudaMemcpyDeviceToHost, stream));
