@@ -1394,11 +1394,6 @@ struct BatchWork {
     }
 };
 
-static void upload_vec(cudaStream_t st, DevBuf<double> &d, const std::vector<double> &h) {
-    d.reserve(std::max<size_t>(1, h.size()));
-    if (!h.empty()) TINCR_CUDA(cudaMemcpyAsync(d.p, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice, st));
-}
-
 template <class T>
 static void upload_any(cudaStream_t st, DevBuf<T> &d, const std::vector<T> &h) {
     d.reserve(std::max<size_t>(1, h.size()));
