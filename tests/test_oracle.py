@@ -226,3 +226,14 @@ def test_reference_lc_gradient_differs_from_fd_by_zvector_operator():
     _, g_ref_nolc, _ = oracle_gradient(nums, xyz, False, variant="reference")
     _, g_ex_nolc, _ = oracle_gradient(nums, xyz, False, variant="exact")
     assert np.abs(g_ref_nolc - g_ex_nolc).max() < 1e-14
+
+
+def test_apb_product_known_answer():
+    """(A+B).v with long-range exchange on tincr's 2 x 2 active-space known answer
+    (not_refactored_tests/solver.rs:1478-1634, `test_apbv_fortran`: four unit trial vectors, the
+    stored products bp_ref): the operator of the exact-variant Z-vector, to rounding."""
+    d = golden("kat_test_apbv_fortran")
+    bs = d["bs"]
+    out = np.stack([OG.mult_apb_lc(d["gamma"], d["gamma_lr"], d["qtrans_ov"], d["qtrans_oo"], d["qtrans_vv"],
+                                   d["omega0"], bs[:, :, k]) for k in range(bs.shape[2])], axis=2)
+    assert np.abs(out - d["bp_ref"]).max() < 1e-14
