@@ -50,3 +50,22 @@ def test_binding_signatures_cover_header(libpath):
 def test_build_targets_sm103a_only():
     from tincr_gb300 import build
     assert build.ARCH == ["-gencode", "arch=compute_103a,code=sm_103a"]
+
+
+def _declared_arities():
+    """Number of parameters of every entry point in the header (comments stripped)."""
+    text = re.sub(r"/\*.*?\*/", "", open(HEADER).read(), flags=re.S)
+    out = {}
+    for m in re.finditer(r"^\s*(?:const\s+)?\w+\s*\*?\s*(tincr_\w+)\s*\(([^)]*)\)\s*;", text, re.M):
+        params = [p.strip() for p in m.group(2).split(",") if p.strip() and p.strip() != "void"]
+        out[m.group(1)] = len(params)
+    return out
+
+
+def test_binding_arities_match_header():
+    """The ctypes argument lists have as many entries as the C declarations have parameters."""
+    from tincr_gb300 import _lib
+    ar = _declared_arities()
+    assert set(ar) == set(_lib.SIGNATURES)
+    for name, (_, args) in _lib.SIGNATURES.items():
+        assert len(args) == ar[name], (name, len(args), ar[name])
