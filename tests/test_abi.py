@@ -69,3 +69,25 @@ def test_binding_arities_match_header():
     assert set(ar) == set(_lib.SIGNATURES)
     for name, (_, args) in _lib.SIGNATURES.items():
         assert len(args) == ar[name], (name, len(args), ar[name])
+
+
+def test_batch_struct_layouts_match_header(tmp_path):
+    """tincr_tda_instance / tincr_tda_result as the C compiler lays them out equal the ctypes (and
+    numpy record) layouts the Python mirror passes."""
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    src = tmp_path / "lay.c"
+    src.write_text('#include <stdio.h>\n#include <stddef.h>\n#include "tincr_gb300.h"\n'
+                   'int main(void) { printf("%zu %zu %zu %zu %zu %zu\\n", sizeof(tincr_tda_instance), '
+                   'offsetof(tincr_tda_instance, orbs_per_atom), offsetof(tincr_tda_instance, xyz), '
+                   'sizeof(tincr_tda_result), offsetof(tincr_tda_result, iterations), '
+                   'offsetof(tincr_tda_result, status)); return 0; }\n')
+    exe = tmp_path / "lay"
+    subprocess.run([cc, str(src), "-I", os.path.join(ROOT, "include"), "-o", str(exe)], check=True)
+    got = [int(v) for v in subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()]
+    from tincr_gb300 import fmo
+    I, R = fmo._Instance, fmo._Result
+    assert got == [ctypes.sizeof(I), I.orbs_per_atom.offset, I.xyz.offset, ctypes.sizeof(R), R.iterations.offset,
+                   R.status.offset]
+    assert fmo._INST_DT.itemsize == got[0] and fmo._RES_DT.itemsize == got[3]
