@@ -3,16 +3,19 @@
 // loop (basis.rs:170-238, PairChargeTransfer::prepare_ct_tda / run_ct_tda in
 // src/excited_states/tda/ct_pair.rs:12-180) as one device-resident lockstep block Davidson.
 //
-// Per iteration (a CUDA graph replayed until no instance is running):
-//   1. H  = [C_o;SC_o] X                      grouped FP64 GEMM, tiles over (instance, vector)
+// Per iteration (a CUDA graph replayed until no instance is running; heavy and light instances are
+// two concurrent branches of it):
+//   1. H  = [C_o;SC_o] X                      grouped GEMM (FP64 tiles, or split-BF16 planes in the
+//                                             mixed form), tiles over (instance, vector)
 //   2. F  = -1/4 gamma_lr o (H [C_v;SC_v]^T)  grouped GEMM with the Hadamard epilogue (LC instances),
 //      or the two Coulomb diagonals only     (non-LC instances)
 //   3. y = q_ov X per atom, z = gamma y       one CTA per (instance, vector)
 //   4. G  = F [SC_v;C_v]                      grouped GEMM (LC) or row scaling by z (non-LC)
 //   5. AX = [SC_o;C_o]^T G + omega o X        grouped GEMM with the omega epilogue
-//   6. subspace step                          one CTA per instance: projections, FP64 Jacobi
-//      eigensolver, Ritz vectors and residuals, convergence test, preconditioning, Gram-Schmidt,
-//      collapse (davidson.rs:83-178)
+//   6. subspace step                          a 4-CTA cluster per heavy instance, one CTA per light
+//      one: projections, FP64 eigensolver (Householder, multisection, inverse iteration), Ritz
+//      vectors and residuals, convergence test, preconditioning, Gram-Schmidt, collapse
+//      (davidson.rs:83-178)
 // Every CTA of steps 1-6 reads its instance's state first and returns when the instance has
 // converged or has no new vector in that slot.
 #include <algorithm>
@@ -731,7 +734,7 @@ __global__ void bt_restart_kernel(BtArrays a) {
 }
 
 // ----------------------------------------------------------------------------------------------
-// subspace step: one CTA per instance
+// subspace step
 // ----------------------------------------------------------------------------------------------
 
 // sum over the CTA of NV values per thread; every thread receives the totals.  The warp partials
