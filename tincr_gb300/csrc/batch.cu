@@ -46,7 +46,7 @@ namespace tincr {
 namespace cg = cooperative_groups;
 
 constexpr int BT_T = 256;
-constexpr int BT_MAXR = 6;   // roots per instance (subspace up to 90, Jacobi in shared memory)
+constexpr int BT_MAXR = 6;   // roots per instance (subspace up to 90, its projected matrix in shared memory)
 
 struct BtArrays {
     const BtInst *inst;
