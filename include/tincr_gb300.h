@@ -215,14 +215,19 @@ int tincr_batch_tile_table(const tincr_ctx *ctx, int capacity, int *n_entries, i
 /* A.X product that allocates no device memory.  No counterpart in tincr: it exists for callers
  * that own all device memory themselves (pool or arena allocators of an MD or FMO driver) or that
  * cannot accept the implicit device synchronisation of cudaMalloc/cudaFree between their kernels.
- * X_dev and AX_dev are caller-owned DEVICE buffers of k trial vectors, vector-major [k][n_occ*n_virt]
- * (element i*n_virt + a of each vector); the operator is the one set by tincr_tda_setup, FP64.
- * Temporaries live in one file-scope device array of 32 MiB (held by every GPU that loads the
- * library until exit); systems needing more than that per trial vector (8 (4 n v + 3 n) bytes,
- * + 32 n^2 bytes with long-range correction, n = n_orb, v = n_virt) are rejected with
- * TINCR_BAD_ARG.  The first call on a device looks up that array's device address (make it before
- * any stream capture).  All calls on a GPU share the array: calls whose GPU work overlaps race and
- * must be serialised by the caller.  Synchronises the context's stream before returning. */
+ * X_dev and AX_dev are caller-owned DEVICE buffers (device or managed memory of the context's GPU;
+ * anything else is rejected with TINCR_BAD_ARG) of k trial vectors, vector-major
+ * [k][n_occ*n_virt] (element i*n_virt + a of each vector); the operator is the one set by
+ * tincr_tda_setup, FP64.  Temporaries live in one file-scope device array of 32 MiB (held by every
+ * GPU that loads the library until exit); systems needing more than that per trial vector
+ * (8 (4 n v + 3 n) bytes, + 32 n^2 bytes with long-range correction, n = n_orb, v = n_virt) are
+ * rejected with TINCR_BAD_ARG.  The first call on a tincr context looks up that array's device
+ * address (make it before any stream capture).  The array exists once per CUDA context, so all
+ * calls in one CUDA context (normally the device's primary context) share it: calls whose GPU work
+ * overlaps race and must be serialised by the caller.  Ordering: the call runs after all work queued
+ * before it on the legacy default stream (and so on every blocking stream); writes of X_dev and
+ * uses of AX_dev on the caller's non-blocking streams must be complete before the call.
+ * Synchronises the context's stream before returning. */
 int tincr_tda_products_noalloc(tincr_ctx *ctx, int k, const double *X_dev, double *AX_dev);
 
 /* ---- analytic gradients ---------------------------------------------------------------------- */

@@ -37,14 +37,49 @@ def test_shards_cover_and_balance():
         assert max(loads) - sum(loads) / world <= max(fmo.instance_cost(q) for q in inst)
 
 
+def _gloo_allgather(world):
+    import torch.distributed as dist
+
+    def gather(obj):
+        parts = [None] * world
+        dist.all_gather_object(parts, obj)
+        return parts
+    return gather
+
+
 def _rank_main(rank, world, port, q):
     import torch.distributed as dist
     os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
     dist.init_process_group("gloo", rank=rank, world_size=world)
     try:
         inst = _instances()
-        rc, full = fmo.solve_batch_sharded(None, inst, world, rank, solver=_fake_solver)
+        rc, full = fmo.solve_batch_sharded(None, inst, world, rank, allgather=_gloo_allgather(world),
+                                           solver=_fake_solver)
         q.put((rank, rc, [r["tag"] for r in full], [float(r["energies"][0]) for r in full]))
+    finally:
+        dist.destroy_process_group()
+
+
+def _failing_solver(ctx, inst, **kw):
+    """Rank 1's shard raises as the library does for a non-finite input; rank 0's shard reports
+    NOT_CONVERGED."""
+    import torch.distributed as dist
+    if dist.get_rank() == 1:
+        raise _lib.TincrError(_lib.NONFINITE, "planted non-finite input")
+    return _lib.NOT_CONVERGED, [dict(energies=np.array([0.0]), tag=q["tag"]) for q in inst]
+
+
+def _failing_rank_main(rank, world, port, q):
+    import torch.distributed as dist
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    try:
+        try:
+            fmo.solve_batch_sharded(None, _instances(), world, rank, allgather=_gloo_allgather(world),
+                                    solver=_failing_solver)
+            q.put((rank, None, "no error"))
+        except _lib.TincrError as e:
+            q.put((rank, e.status, str(e)))
     finally:
         dist.destroy_process_group()
 
@@ -69,6 +104,36 @@ def test_sharded_results_gathered_in_order():
         assert rc == _lib.OK
         assert tags == list(range(n))
         assert np.allclose(es, 0.1 * np.arange(n))
+
+
+def test_failed_shard_raises_on_every_rank():
+    """A rank whose solve raises still joins the all-gather; every rank then raises the same error
+    (the most severe status), so no rank waits in the collective for the failed one."""
+    pytest.importorskip("torch")
+    import torch.multiprocessing as mp
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        port = s.getsockname()[1]
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    procs = [ctx.Process(target=_failing_rank_main, args=(r, 2, port, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    got = sorted(q.get(timeout=120) for _ in procs)
+    for p in procs:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    for rank, status, msg in got:
+        assert status == _lib.NONFINITE, msg
+        assert "planted non-finite input" in msg and "rank 1" in msg
+
+
+def test_worst_status_folds_every_code():
+    assert fmo.worst_status([]) == _lib.OK
+    assert fmo.worst_status([_lib.OK, _lib.NOT_CONVERGED]) == _lib.NOT_CONVERGED
+    assert fmo.worst_status([_lib.NOT_CONVERGED, _lib.CG_MAXITER, _lib.OK]) == _lib.CG_MAXITER
+    assert fmo.worst_status([_lib.CUDA_ERR, _lib.NONFINITE, _lib.BAD_ARG]) == _lib.CUDA_ERR
+    assert fmo.worst_status([_lib.OK, 42]) == 42
 
 
 def _bench_rank(rank, world, port, q):

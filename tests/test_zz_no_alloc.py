@@ -22,14 +22,15 @@ pytestmark = pytest.mark.gpu
 
 
 def _noalloc(ctx, x_vecmajor):
+    """Copy the vectors to the device on torch's default stream and call the entry point at once:
+    the call orders itself after the legacy default stream, so no host synchronisation is needed
+    before it (it synchronises its own stream before returning)."""
     import torch
     xd = torch.from_numpy(np.ascontiguousarray(x_vecmajor)).to("cuda")
     ad = torch.empty_like(xd)
-    torch.cuda.synchronize()
     rc = ctx.lib.tincr_tda_products_noalloc(ctx.h, xd.shape[0], ctypes.c_void_p(xd.data_ptr()),
                                             ctypes.c_void_p(ad.data_ptr()))
     ctx.check(rc)
-    torch.cuda.synchronize()
     return ad.cpu().numpy()
 
 
@@ -60,3 +61,23 @@ def test_noalloc_rejects_systems_beyond_the_scratch_size(gpu_ctx):
         _noalloc(gpu_ctx, np.zeros((1, s.dim)))
     assert e.value.status == _lib.BAD_ARG
     assert "scratch" in str(e.value)
+
+
+def test_noalloc_rejects_host_pointers(gpu_ctx):
+    """A host buffer passed in place of device memory is refused before any kernel runs."""
+    pytest.importorskip("torch")
+    import torch
+    c = fixture_case("uracil", True)
+    s = T.ExcitedStateSystem(gpu_ctx, c["opa"], c["orbs"], c["s"], c["orbe"], c["n_occ"], c["n_virt"], c["gamma"],
+                             c["gamma_lr"], c["xyz"])
+    s.prepare_tda()
+    host = np.zeros((1, s.dim))
+    dev = torch.zeros((1, s.dim), dtype=torch.float64, device="cuda")
+    for x_ptr, ax_ptr in ((host.ctypes.data, dev.data_ptr()), (dev.data_ptr(), host.ctypes.data)):
+        rc = gpu_ctx.lib.tincr_tda_products_noalloc(gpu_ctx.h, 1, ctypes.c_void_p(x_ptr), ctypes.c_void_p(ax_ptr))
+        assert rc == _lib.BAD_ARG
+        assert "device memory" in gpu_ctx.lib.tincr_last_error(gpu_ctx.h).decode()
+    # the context is still usable afterwards
+    x = np.random.default_rng(1).standard_normal((s.dim, 1))
+    ref = s.compute_products(x)
+    assert np.abs(_noalloc(gpu_ctx, x.T).T - ref).max() < 1e-12 * max(1.0, np.abs(ref).max())

@@ -9,12 +9,17 @@
 // G and the Coulomb diagonals of the product, see tda.cu) in one file-scope device array of fixed
 // size, so it calls no cudaMalloc, cudaFree or allocating library routine.
 //
-// The scratch array is shared by every call in the process on a given GPU and keeps the contents
-// of the last call; nothing in it has to start at zero (every element a call reads was written by
-// that same call).  Calls whose GPU work overlaps (from several host threads, or on several
-// contexts of the same GPU) race on it and must be serialised by the caller.
-#include <mutex>
-
+// A __device__ array exists once per CUDA context: every call made in the same context (normally
+// the device's primary context, which all tincr contexts on that device share) uses the same
+// array, and it keeps the contents of the last call.  Nothing in it has to start at zero (every
+// element a call reads was written by that same call).  Calls in one CUDA context whose GPU work
+// overlaps (from several host threads, or from several tincr contexts on the same GPU) race on it
+// and must be serialised by the caller.
+//
+// Ordering: the product runs on the tincr context's own (non-blocking) stream.  It first makes that
+// stream wait for all work queued so far on the legacy default stream (and so on every blocking
+// stream), and it synchronises its own stream before returning.  Work that writes X_dev, or still
+// uses AX_dev, on a non-blocking stream of the caller must be complete before the call.
 #include "gemm_f64.cuh"
 #include "kernels.cuh"
 #include "ops.cuh"
@@ -26,25 +31,37 @@ namespace tincr {
 constexpr size_t NOALLOC_SCRATCH_DOUBLES = size_t(4) << 20;
 static __device__ __align__(256) double g_noalloc_scratch[NOALLOC_SCRATCH_DOUBLES];
 
-// Device address of the scratch array, looked up once per device (the symbol's host-side name is
-// only a stand-in and must never be handed to a kernel).
-static std::mutex g_scratch_mutex;
-static double *g_scratch_addr[64] = {};
-
-static double *scratch_on(int device) {
-    if (device < 0 || device >= 64) fail(TINCR_BAD_ARG, "noalloc: device index out of range");
-    std::lock_guard<std::mutex> lock(g_scratch_mutex);
-    if (!g_scratch_addr[device]) {
+// Device address of the scratch array in the current CUDA context, looked up at the first call on
+// each tincr context, with that context's device current (the symbol's host-side name is only a
+// stand-in and must never be handed to a kernel).  A tincr context lives in one CUDA context, so the
+// cached address stays valid for as long as the tincr context does.
+static double *scratch_of(Ctx &c) {
+    if (!c.noalloc_scratch) {
         int cur = -1;
         TINCR_CUDA(cudaGetDevice(&cur));
-        if (cur != device) fail(TINCR_BAD_ARG, "noalloc: device is not current");
+        if (cur != c.device) fail(TINCR_BAD_ARG, "noalloc: the context's device is not current");
         void *p = nullptr;
         cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
         if (e != cudaSuccess || !p)
             fail(TINCR_CUDA_ERR, std::string("noalloc: cudaGetSymbolAddress failed: ") + cudaGetErrorString(e));
-        g_scratch_addr[device] = static_cast<double *>(p);
+        c.noalloc_scratch = static_cast<double *>(p);
     }
-    return g_scratch_addr[device];
+    return c.noalloc_scratch;
+}
+
+// A caller buffer must be device (or managed) memory of the context's device: a host pointer handed
+// to the kernels would fault the GPU instead of failing the call.
+static void check_device_pointer(const Ctx &c, const void *p, const char *what) {
+    cudaPointerAttributes a{};
+    cudaError_t e = cudaPointerGetAttributes(&a, p);
+    if (e != cudaSuccess) {
+        cudaGetLastError();   // clear the error this query recorded
+        fail(TINCR_BAD_ARG, std::string("noalloc: ") + what + " is not a CUDA pointer");
+    }
+    if (a.type != cudaMemoryTypeDevice && a.type != cudaMemoryTypeManaged)
+        fail(TINCR_BAD_ARG, std::string("noalloc: ") + what + " is not device memory");
+    if (a.type == cudaMemoryTypeDevice && a.device != c.device)
+        fail(TINCR_BAD_ARG, std::string("noalloc: ") + what + " lives on another device");
 }
 
 // Scratch doubles needed for one trial vector: H and G (2n x v), F (2n x 2n, with exchange),
@@ -64,11 +81,17 @@ void products_noalloc(Ctx &c, int k, const double *X, double *AX) {
         fail(TINCR_BAD_ARG, "noalloc: system too large for the fixed scratch (needs " + std::to_string(need * 8) +
                                 " bytes per trial vector, have " + std::to_string(NOALLOC_SCRATCH_DOUBLES * 8) + ")");
     if ((size_t)c.n_atoms * sizeof(double) > 48 * 1024) fail(TINCR_BAD_ARG, "noalloc: too many atoms");
-    double *base = scratch_on(c.device);
+    check_device_pointer(c, X, "X_dev");
+    check_device_pointer(c, AX, "AX_dev");
+    double *base = scratch_of(c);
     const int n = c.n_orb, o = c.n_occ, v = c.n_virt;
     const long long ov = c.ov;
     double *H = base, *G = H + 2LL * n * v, *d3 = G + 2LL * n * v, *d2 = d3 + n, *z = d2 + n, *F = z + n;
     cudaStream_t st = c.stream;
+    // order after the work queued on the legacy default stream (which itself follows every blocking
+    // stream); ev0 is free here: it only brackets the timed regions of the other entry points
+    TINCR_CUDA(cudaEventRecord(c.ev0, cudaStreamLegacy));
+    TINCR_CUDA(cudaStreamWaitEvent(st, c.ev0, 0));
     for (int b = 0; b < k; ++b) {
         const double *xb = X + (long long)b * ov;
         double *ab = AX + (long long)b * ov;

@@ -41,6 +41,9 @@ struct Ctx {
     int n_sm = 0;
     cudaStream_t stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    // device address of noalloc.cu's fixed scratch array in this context, looked up by the first
+    // tincr_tda_products_noalloc call on the context (nullptr until then)
+    double *noalloc_scratch = nullptr;
     std::string err;
     double last_ms = 0.0;
     long long last_launches = 0;

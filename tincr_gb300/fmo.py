@@ -210,29 +210,65 @@ def shard_instances(instances, world, rank):
     return [k for k in range(len(instances)) if owner[k] == rank]
 
 
-def solve_batch_sharded(ctx, instances, world, rank, solver=None, **kw):
+# order in which statuses of different ranks are folded into one (later = worse)
+_SEVERITY = {_lib.OK: 0, _lib.NOT_CONVERGED: 1, _lib.CG_MAXITER: 2, _lib.NONFINITE: 3, _lib.BAD_ARG: 4,
+             _lib.CUDA_ERR: 5, _lib.NO_DEVICE: 6}
+
+
+def worst_status(codes):
+    """The most severe of several status codes (unknown codes rank above every known one)."""
+    worst = _lib.OK
+    for c in codes:
+        if _SEVERITY.get(c, 99) > _SEVERITY.get(worst, 99):
+            worst = c
+    return worst
+
+
+def solve_batch_sharded(ctx, instances, world, rank, allgather=None, solver=None, **kw):
     """The FMO work list split over `world` ranks (one GPU each): every rank solves its shard with
     `solve_batch` (or `solver`), then one all-gather of the per-instance results (energies,
     coefficients, transition charges, dipoles, oscillator strengths) gives every rank the whole
-    list, in the caller's order, as the exciton Hamiltonian needs it.  Needs an initialised
-    torch.distributed process group when world > 1 (gloo suffices: the results are host arrays).
-    Returns (worst status over all ranks, list of result dicts)."""
+    list, in the caller's order, as the exciton Hamiltonian needs it.
+
+    `allgather(obj) -> list of every rank's obj, in rank order` is the caller's collective (for
+    instance torch.distributed.all_gather_object over gloo: the results are host arrays); it is
+    required when world > 1, so this module needs no communication library of its own.
+
+    Every rank takes part in the all-gather even when its own solve failed: a rank whose solver
+    raised sends its status and message instead of results, and after the collective every rank
+    raises the same error (a TincrError with the most severe status of the failed ranks, or a
+    RuntimeError when a rank failed outside the library).  No rank is left waiting in the
+    collective for one that raised.  Returns (worst status over all ranks, list of result dicts)."""
     solver = solver or solve_batch
     mine = shard_instances(instances, world, rank)
-    rc, out = solver(ctx, [instances[k] for k in mine], **kw) if mine else (_lib.OK, [])
+    failure = None
+    try:
+        rc, out = solver(ctx, [instances[k] for k in mine], **kw) if mine else (_lib.OK, [])
+    except _lib.TincrError as e:
+        if world <= 1:
+            raise
+        rc, out, failure = e.status, None, (e.status, "rank %d: %s" % (rank, e))
+    except Exception as e:   # noqa: BLE001 - reported to every rank below, then raised there
+        if world <= 1:
+            raise
+        rc, out, failure = None, None, (None, "rank %d: %s: %s" % (rank, type(e).__name__, e))
     if world <= 1:
         return rc, out
-    import torch.distributed as dist
-    parts = [None] * world
-    dist.all_gather_object(parts, (mine, rc, out))
+    if allgather is None:
+        raise ValueError("solve_batch_sharded: world > 1 needs an allgather collective")
+    parts = allgather((mine, rc, out, failure))
+    failures = [p[3] for p in parts if p[3] is not None]
+    if failures:
+        msg = "; ".join(m for _, m in failures)
+        codes = [s for s, _ in failures if s is not None]
+        if len(codes) == len(failures):
+            raise _lib.TincrError(worst_status(codes), msg)
+        raise RuntimeError("sharded FMO solve failed: " + msg)
     full = [None] * len(instances)
-    worst = _lib.OK
-    for idx, rc_r, out_r in parts:
+    for idx, _, out_r, _ in parts:
         for k, o in zip(idx, out_r):
             full[k] = o
-        if rc_r == _lib.NONFINITE or (rc_r == _lib.NOT_CONVERGED and worst == _lib.OK):
-            worst = rc_r
-    return worst, full
+    return worst_status(p[1] for p in parts), full
 
 
 def le_gradients(monomers, results, states, n_streams=8, variant="reference", contexts=None,
