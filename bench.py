@@ -235,7 +235,7 @@ def run_gpu(args):
     else:
         peak = peaks.get("bf16_tflops", 1900.0)
         peak_note = ("measured bf16_tflops" if "bf16_tflops" in peaks else "fallback 1.9 PFLOP/s") + \
-            "; achieved counts the algorithmic 2MNK once, the tensor pipe executes 3 split products"
+            "; achieved counts the algorithmic 2MNK once, the tensor pipe executes 6 split-BF16 plane products per MAC"
         bound, kernel = "tensor", "AO-exchange contractions (gemm_planes_tc, tcgen05 split-BF16, A.X steps 2 and 4)"
     # DRAM bytes per launch of the exchange family: ncu bytes per product vector (capture in
     # profiles/) times the vectors per launch of this step (2 launches per chunk)

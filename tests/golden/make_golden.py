@@ -99,7 +99,9 @@ def convert_kats(src):
 
 
 if __name__ == "__main__":
-    src = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    if len(sys.argv) != 2:
+        sys.exit("usage: python make_golden.py <path of the tincr source tree>")
+    src = sys.argv[1]
     convert_data(src)
     convert_kats(src)
     print("golden fixtures written to", HERE)

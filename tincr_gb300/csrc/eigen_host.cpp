@@ -2,7 +2,10 @@
 //
 // Householder reduction to tridiagonal form followed by the implicit-shift QL iteration, with
 // accumulated transformations (the method of Wilkinson & Reinsch, "Handbook for Automatic
-// Computation, Vol. II: Linear Algebra", routines tred2/tql2).  Only the upper triangle of the
+// Computation, Vol. II: Linear Algebra", routines tred2/tql2).  eigh_upper follows the structure of
+// the public-domain JAMA transcription of those two routines (JAMA: A Java Matrix Package, NIST and
+// The MathWorks, 1999, class EigenvalueDecomposition, methods tred2 and tql2), with row-major
+// storage and the input read from the upper triangle.  Only the upper triangle of the
 // input is read, like `eigh(UPLO::Upper)` in tincr's Davidson (src/excited_states/solvers/davidson.rs:93).
 // The subspace is at most 15 * n_roots wide, so this stays a small host step between device phases.
 #include <algorithm>

@@ -100,7 +100,9 @@ def main(src, out):
 
 
 if __name__ == "__main__":
-    src = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    if len(sys.argv) not in (2, 3):
+        sys.exit("usage: python make_params.py <path of the tincr source tree> [output .npz]")
+    src = sys.argv[1]
     out = sys.argv[2] if len(sys.argv) > 2 else os.path.join(os.path.dirname(os.path.abspath(__file__)),
                                                               "hcno_params.npz")
     main(src, out)
