@@ -15,8 +15,12 @@ largest energy and gradient differences between the two.
 `value` is device time per step (CUDA events on the library stream, inputs resident in HBM);
 `e2e` is the same step through the C ABI with host buffers (setup upload, solve, parameter upload,
 gradient, result copies).
-`--impl reference` times the CPU restatement of tincr's algorithm (the oracle, numpy + the host
-BLAS with all host threads) on a bounded sample of the same workload and scales it to one step.
+`cpu_baseline` (this arm) times the CPU restatement of tincr's algorithm (the oracle, numpy + the
+host BLAS with all host threads) on a bounded sample of the water step, scaled to the step's counts;
+the FMO work list is timed in full.  `--impl reference` runs the complete CPU step once, measured
+(Davidson to convergence with its own iteration count, then the S1 gradients), and the whole FMO work
+list.  `parity` holds the per-root errors against the oracle's results on the same inputs
+(tests/golden/water128.npz, acene64.npz).
 Under torchrun (N > 1) every rank runs an independent replica (the path does not shard one
 system); rank 0 prints the JSON line with the max over ranks.
 """
@@ -187,7 +191,8 @@ def run_gpu(args):
         if profile:
             ctx.set_profiling(False)
         return dict(dev_ms=dev_ms, launches=launches, iters=iters, products=prods, stats=stats,
-                    energies=r["ci_eigenvalues"].copy(), grad=grad.copy(), cg=gr.last_cg_iterations)
+                    energies=r["ci_eigenvalues"].copy(), f=r["oscillator_strengths"].copy(), grad=grad.copy(),
+                    cg=gr.last_cg_iterations)
 
     with ClockSampler(local) as clocks:
         t0 = time.perf_counter()
@@ -289,12 +294,10 @@ def run_gpu(args):
         "warmup": args.warmup, "ms_per_step": step_s * 1e3, "higher_is_better": False,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64" if prec == _lib.PREC_FP64 else "bf16x3+f64",
         "data": "synthetic (seeded (H2O)128 cluster, host SCC ground state)",
-        "config": {"workload": "water128-lctda-20roots+S1grad", "n_orb": int(sy.n_orbs), "n_occ": int(sy.n_occ),
-                   "n_virt": int(sy.n_virt), "n_roots": N_ROOTS, "tol": TOL, "max_iter": MAX_ITER,
-                   "r_lr_bohr": R_LR, "precision": args.precision, "gradient": "S1, tincr formulas",
-                   "l2": "flushed (256 MB write) between steps",
-                   "parallelism": "replicas" if world > 1 else "single-gpu",
-                   "davidson_iterations": main["iters"][-1], "zvector_cg_iterations": main["cg"]},
+        "config": workload_config(sy, world),
+        "precision": args.precision,
+        "counts": {"davidson_iterations": main["iters"][-1], "products": int(main["products"] / args.steps),
+                   "zvector_cg_iterations": main["cg"]},
         "e2e": {"value": e2e_s, "unit": "s", "h2d_bytes_per_step": int(h2d_bytes),
                 "d2h_bytes_per_step": int(d2h_bytes)},
         "gpu_launches": int(main["launches"]),
@@ -306,6 +309,7 @@ def run_gpu(args):
         "lowest_energies_eh": [float(e) for e in main["energies"][:3]],
         "wall_s": wall,
     }
+    out["parity"] = water_parity(g, main, ref64)
     if args.fmo:
         out["fmo"] = run_fmo(args, ctx)
     if ref64 is not None:
@@ -313,6 +317,38 @@ def run_gpu(args):
                            "speedup_of_mixed": float(np.mean(ref64["dev_ms"])) / max(1e-9, float(np.mean(main["dev_ms"]))),
                            "max_abs_energy_err_eh": float(np.abs(main["energies"] - ref64["energies"]).max()),
                            "max_abs_grad_err_eh_per_bohr": float(np.abs(main["grad"] - ref64["grad"]).max())}
+    return out
+
+
+def golden(name):
+    """A committed oracle fixture of the benchmark workloads (tests/golden/make_bench_fixtures.py)."""
+    path = os.path.join(ROOT, "tests", "golden", name + ".npz")
+    return np.load(path) if os.path.exists(path) else None
+
+
+def water_parity(g, main, ref64):
+    """Per-root errors of this run against the oracle's results on the same inputs (computed once on
+    the CPU, tests/golden/water128.npz): energies and oscillator strengths per root, the largest S1
+    gradient error, for the timed precision and for the FP64 form."""
+    fx = golden("water128")
+    if fx is None:
+        return {"unavailable": "fixture tests/golden/water128.npz missing"}
+    d_orbe = float(np.abs(g.orbe - fx["orbe"]).max())
+    if d_orbe > 1e-8:
+        return {"unavailable": "ground state differs from the fixture's (orbital energies %.1e)" % d_orbe}
+    ref_g = fx["grad_ground"] + fx["grad_excited"]
+    out = {"oracle": "tests/golden/water128.npz: numpy restatement of tincr on the same inputs, roots converged to "
+                     "residual %g (%d Davidson iterations, %d products, corrections re-orthogonalised)"
+                     % (float(fx["tol"]), int(fx["iterations"]), int(fx["n_products"])),
+           "bars": {"fp64_energy_eh": 1e-8, "mixed_energy_eh": 1e-6, "gradient_eh_per_bohr": 1e-5},
+           "per_root_energy_err_eh": [float(x) for x in np.abs(main["energies"] - fx["energies"])],
+           "per_root_f_err": [float(x) for x in np.abs(main["f"] - fx["f"])],
+           "max_grad_err_eh_per_bohr": float(np.abs(main["grad"] - ref_g).max())}
+    if ref64 is not None:
+        out["fp64_per_root_energy_err_eh"] = [float(x) for x in np.abs(ref64["energies"] - fx["energies"])]
+        out["fp64_max_f_err"] = float(np.abs(ref64["f"] - fx["f"]).max())
+        out["fp64_max_grad_err_eh_per_bohr"] = float(np.abs(ref64["grad"] - ref_g).max())
+        out["fp64_davidson_iterations"] = int(ref64["iters"][-1])
     return out
 
 
@@ -330,58 +366,44 @@ def fmo_workload():
     return mons, pairs, inst, labels
 
 
-def oracle_le_gradient_seconds(m, state=0):
-    """tincr's LE excitation gradient of one monomer (oracle: dense derivative tensors, Z-vector,
-    f_v / f_lr contractions), timed."""
+def _cpu_helpers():
+    """The oracle and its input builders (test infrastructure, used only by the CPU legs)."""
+    tests = os.path.join(ROOT, "tests")
+    if tests not in sys.path:
+        sys.path.insert(0, tests)
+    import cases
     from oracle import gradients as OG
     from oracle import tda as OT
-    from tincr_gb300 import groundstate as gs
-    sy, g = m.system, m.ground
+    return cases, OG, OT
+
+
+def fmo_cpu_reference(mons, inst, labels):
+    """tincr's FMO step on the CPU, measured in full: the TDA of every instance of the work list
+    with tincr's engines (oracle `TdaEngine` per monomer, `CtEngine` per pair direction; numpy +
+    the host BLAS), then the LE excitation gradient of the aggregate's lowest LE root (dense
+    derivative tensors, Z-vector, f_v / f_lr contractions).  Returns (seconds, description)."""
+    cases, OG, OT = _cpu_helpers()
+    case = dict(monomers=mons, labels=labels, lc=True)
     t0 = time.perf_counter()
-    qov, qoo, qvv = OT.trans_charges(sy.ao_offset, g.orbs, g.s, sy.occ_indices, sy.virt_indices)
-    om = OT.orbe_differences(g.orbe[sy.occ_indices], g.orbe[sy.virt_indices])
-    eng = OT.TdaEngine(om, qov, g.gamma, qoo, qvv, g.gamma_lr, sy.n_occ, sy.n_virt)
-    r = OT.run_tda_engine(eng, sy.xyz, FMO_N_LE, FMO_MAX_ITER, FMO_TOL)
+    res = []
+    for k, q in enumerate(inst):
+        eng, xyz = cases.fmo_oracle_engine(case, k)
+        res.append(OT.run_tda_engine(eng, xyz, q["n_roots"], FMO_MAX_ITER, FMO_TOL))
     t_tda = time.perf_counter() - t0
     t0 = time.perf_counter()
+    n_mon = len(mons)
+    k1 = int(np.argmin([res[k]["energies"][0] for k in range(n_mon)]))
+    sy, g = mons[k1].system, mons[k1].ground
+    q = OT.trans_charges(sy.ao_offset, g.orbs, g.s, sy.occ_indices, sy.virt_indices)
+    inp = cases.oracle_gradient_inputs(sy, g, True, res[k1]["energies"], res[k1]["coefficients"], q)
     der = OG.derivative_tensors(sy.numbers, sy.xyz, sy.ao_offset, sy.ao_atom, sy.hubbard, sy.r_lr, sy.params)
-    inp = dict(p=g.p, p0=g.p0, h_coul_x=g.h_coul_x, gamma=g.gamma, dq=g.dq, s=g.s, ao_atom=sy.ao_atom,
-               numbers=sy.numbers, xyz=sy.xyz, params=sy.params, gamma_lr_ao=gs.atom_to_ao(sy, g.gamma_lr),
-               orbe=g.orbe, occ=sy.occ_indices, virt=sy.virt_indices, ci_eigenvalues=r["energies"],
-               ci_coefficients=r["coefficients"], q_ov=qov, q_oo=qoo, q_vv=qvv, gamma_lr=g.gamma_lr,
-               orbs=g.orbs, gamma_ao=gs.atom_to_ao(sy, g.gamma))
     _, flr = OG.ground_state_gradient(inp, der, True)
-    OG.tda_gradient(inp, der, state, True, flr_dmd0=flr)
-    return time.perf_counter() - t0
-
-
-def fmo_cpu_sample(mons, inst, labels, n_le_sample=8, n_ct_sample=32, s1_monomer=None):
-    """tincr's per-instance TDA (oracle engines, numpy + host BLAS) on a few LE and CT instances,
-    scaled to the whole work list by instance kind, plus the LE gradient of the S1 monomer."""
-    from oracle import tda as OT
-    t_le, t_ct = [], []
-    le = [k for k, l in enumerate(labels) if l[0] == "LE"][:n_le_sample]
-    ct = [k for k, l in enumerate(labels) if l[0] == "CT"][:n_ct_sample]
-    for k in le + ct:
-        q = inst[k]
-        t0 = time.perf_counter()
-        no, nv = q["n_occ"], q["n_virt"]
-        ao = np.concatenate([[0], np.cumsum(q["opa"])])
-        qov, qoo, qvv = OT.trans_charges(ao, q["c"], q["s"], np.arange(no), np.arange(no, no + nv))
-        om = OT.orbe_differences(q["orbe"][:no], q["orbe"][no:])
-        eng = OT.TdaEngine(om, qov, q["gamma"], qoo, qvv, q["gamma_lr"], no, nv)
-        OT.run_tda_engine(eng, q["xyz"], q["n_roots"], FMO_MAX_ITER, FMO_TOL)
-        (t_le if labels[k][0] == "LE" else t_ct).append(time.perf_counter() - t0)
+    OG.tda_gradient(inp, der, 0, True, flr_dmd0=flr)
+    t_grad = time.perf_counter() - t0
     n_le = sum(1 for l in labels if l[0] == "LE")
-    n_ct = len(labels) - n_le
-    total = n_le * float(np.mean(t_le)) + n_ct * float(np.mean(t_ct))
-    sample = ("oracle TDA of %d LE and %d CT instances (%.3f s / %.3f s each), scaled to %d LE + %d CT instances"
-              % (len(t_le), len(t_ct), np.mean(t_le), np.mean(t_ct), n_le, n_ct))
-    if s1_monomer is not None:
-        t_g = oracle_le_gradient_seconds(mons[s1_monomer])
-        total += t_g
-        sample += "; oracle LE gradient of the S1 monomer (%.2f s)" % t_g
-    return total, sample
+    sample = ("measured in full: oracle TDA of all %d instances (%d LE, %d CT; %.2f s) + the LE gradient of the "
+              "lowest LE root (monomer %d, %.2f s)" % (len(inst), n_le, len(inst) - n_le, t_tda, k1, t_grad))
+    return t_tda + t_grad, sample
 
 
 def ctx_device(ctx):
@@ -459,8 +481,23 @@ def run_fmo(args, ctx):
         "davidson_iterations_max": int(max(x["iterations"] for x in rm)),
         "plane_tile_autotuner": tile_summary(ctx.batch_tile_table()),
     })
+    fx = golden("acene64")
+    if fx is not None:
+        orbe = np.concatenate([m.ground.orbe for m in mons])
+        if np.abs(orbe - fx["monomer_orbe"]).max() <= 1e-8:
+            em = np.concatenate([r["energies"] for r in rm])
+            e64 = np.concatenate([r["energies"] for r in r64])
+            out["parity"] = {
+                "oracle": "tests/golden/acene64.npz: oracle engines on every instance, same inputs",
+                "mixed_max_energy_err_eh": float(np.abs(em - fx["energies"]).max()),
+                "fp64_max_energy_err_eh": float(np.abs(e64 - fx["energies"]).max()),
+                "fp64_iterations_equal": [r["iterations"] for r in r64] == fx["iterations"].tolist(),
+                "mixed_s1_le_grad_err_eh_per_bohr": float(np.abs(gm - fx["s1_le_gradient"]).max())
+                if km == int(fx["s1_monomer"]) else None,
+                "fp64_s1_le_grad_err_eh_per_bohr": float(np.abs(g64 - fx["s1_le_gradient"]).max())
+                if k64 == int(fx["s1_monomer"]) else None}
     if args.cpu_baseline:
-        total, sample = fmo_cpu_sample(mons, inst, labels, s1_monomer=km)
+        total, sample = fmo_cpu_reference(mons, inst, labels)
         out["cpu_baseline"] = {"value": len(mons) / total, "unit": "monomers/s", "step_s": total,
                                "cores": os.cpu_count(), "kind": "port", "sample": sample}
     return out
@@ -558,47 +595,90 @@ def run_cpu_sample(args):
     print(json.dumps({"value": total, "threads": threads, "sample": sample}))
 
 
-def OT_lowest(mons, k):
-    """Lowest LE root of monomer k from the oracle's Davidson (picks the S1 monomer on the CPU)."""
-    from oracle import tda as OT
-    sy, g = mons[k].system, mons[k].ground
-    qov, qoo, qvv = OT.trans_charges(sy.ao_offset, g.orbs, g.s, sy.occ_indices, sy.virt_indices)
-    om = OT.orbe_differences(g.orbe[sy.occ_indices], g.orbe[sy.virt_indices])
-    eng = OT.TdaEngine(om, qov, g.gamma, qoo, qvv, g.gamma_lr, sy.n_occ, sy.n_virt)
-    return float(OT.run_tda_engine(eng, sy.xyz, 1, FMO_MAX_ITER, FMO_TOL)["energies"][0])
+def cpu_reference_step(sy, g):
+    """tincr's complete step on the CPU, measured: the oracle (numpy + the host BLAS, all host
+    threads) runs transition charges, the Davidson to convergence at the bench settings (its own
+    products and iterations; tincr's `System::run_tda`, src/excited_states/tda/mod.rs:74-131), the
+    moments, then the S1 ground-state and excitation gradients of tincr's formulas
+    (src/gradients/ground_state.rs:12-137, src/gradients/excited_state.rs:56-487), with the
+    derivative-tensor rows of one atom at a time built on the way (the same per-coordinate f_v /
+    f_lr work as tincr's loops, src/gradients/helpers.rs:47-188, without holding [3N, n, n]).
+    The Davidson orthogonalises each correction twice: with tincr's single Gram-Schmidt pass the
+    restated solve of this cluster loses the orthogonality of its basis after the subspace collapse
+    and stops at spurious near-zero roots (oracle.tda.davidson); the second pass costs one more
+    matrix-vector pass per correction, under 1% of the step, and gives the roots the GPU path finds."""
+    cases, OG, OT = _cpu_helpers()
+    occ, virt = sy.occ_indices, sy.virt_indices
+    t0 = time.perf_counter()
+    q = OT.trans_charges(sy.ao_offset, g.orbs, g.s, occ, virt)
+    om = OT.orbe_differences(g.orbe[occ], g.orbe[virt])
+    eng = OT.TdaEngine(om, q[0], g.gamma, q[1], q[2], g.gamma_lr, sy.n_occ, sy.n_virt)
+    r = OT.run_tda_engine(eng, sy.xyz, N_ROOTS, MAX_ITER, TOL, reorthogonalize=True)
+    t_tda = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    inp = cases.oracle_gradient_inputs(sy, g, True, r["energies"], r["coefficients"], q)
+    del eng, q
+    rows = OG.AtomRows(sy.numbers, sy.xyz, sy.ao_offset, sy.ao_atom, sy.hubbard, sy.r_lr, sy.params)
+    st = {}
+    OG.gradients_by_atom(inp, rows, 0, True, stats=st)
+    t_grad = time.perf_counter() - t0
+    return dict(seconds=t_tda + t_grad, tda_s=t_tda, gradient_s=t_grad, davidson_iterations=int(r["iterations"]),
+                products=int(r["n_products"]), zvector_cg_iterations=int(st.get("cg_iterations", 0)),
+                lowest_energies_eh=[float(e) for e in r["energies"][:3]])
+
+
+def workload_config(sy, world):
+    """The `config` object of both arms (the workload: what is computed, not how)."""
+    return {"workload": "water128-lctda-20roots+S1grad", "n_orb": int(sy.n_orbs), "n_occ": int(sy.n_occ),
+            "n_virt": int(sy.n_virt), "n_roots": N_ROOTS, "tol": TOL, "max_iter": MAX_ITER, "r_lr_bohr": R_LR,
+            "gradient": "S1, tincr formulas", "l2": "GPU arm: flushed (256 MB write) between steps",
+            "parallelism": "replicas" if world > 1 else "single-gpu"}
 
 
 def run_reference(args):
+    """`--impl reference`: tincr's algorithm on the host CPU (the oracle port; tincr itself is
+    Rust and cannot be built here).  Rank 0 alone works.  Warm-up: `--warmup` reference-form A.X
+    products.  Timed: the complete step once, measured end to end (`cpu_reference_step`); its wall
+    time is the line's value, spread evenly over the `--steps` steps of the line (ms_per_step), so
+    the steps' total equals the time the run actually took.  The FMO object times the whole
+    64-acene work list and the S1 LE gradient the same way."""
     rank, world, local = dist_env()
     if rank != 0:
         return None
+    cases, OG, OT = _cpu_helpers()
     sy, g = workload()
-    # products, Davidson iterations and CG iterations of the FP64 GPU step at these settings (same
-    # algorithm, same guesses)
-    vals = []
-    sample = ""
-    threads = os.cpu_count()
+    q = OT.trans_charges(sy.ao_offset, g.orbs, g.s, sy.occ_indices, sy.virt_indices)
+    om = OT.orbe_differences(g.orbe[sy.occ_indices], g.orbe[sy.virt_indices])
+    eng = OT.TdaEngine(om, q[0], g.gamma, q[1], q[2], g.gamma_lr, sy.n_occ, sy.n_virt)
+    x = np.random.default_rng(0).standard_normal((len(om), 1))
     for _ in range(args.warmup):
-        cpu_sample(sy, g, args.ref_products, args.ref_iters, args.ref_cg, sample_vectors=1)
-    for _ in range(args.steps):
-        total, threads, sample = cpu_sample(sy, g, args.ref_products, args.ref_iters, args.ref_cg, sample_vectors=1)
-        vals.append(total)
-    v = float(np.mean(vals))
+        eng.apply(x)
+    del eng, q
+    rec = cpu_reference_step(sy, g)
+    v = rec["seconds"]
+    threads = os.cpu_count()
+    sample = ("measured in full, once: trans_charges + Davidson to convergence (%d iterations, %d reference-form A.X "
+              "products, corrections orthogonalised twice, %.1f s) + S1 ground-state and excitation gradients atom by atom (Z-vector %d CG iterations, "
+              "derivative rows and f_v / f_lr per coordinate, %.1f s); the wall time is spread evenly over the %d "
+              "steps" % (rec["davidson_iterations"], rec["products"], rec["tda_s"], rec["zvector_cg_iterations"],
+                         rec["gradient_s"], args.steps))
     fmo_ref = None
     if args.fmo:
         mons, pairs, inst, labels = fmo_workload()
-        k1 = int(np.argmin([OT_lowest(mons, k) for k in range(len(mons))]))
-        total, fsample = fmo_cpu_sample(mons, inst, labels, s1_monomer=k1)
+        total, fsample = fmo_cpu_reference(mons, inst, labels)
         fmo_ref = {"workload": "acene64-fmo-le4-ct1", "value_monomers_per_s": len(mons) / total,
-                   "unit": "monomers/s", "step_s": total, "cores": os.cpu_count(), "kind": "port",
-                   "sample": fsample}
-    return {"impl": "reference", "metric": METRIC, "fmo": fmo_ref, "value": v, "unit": "s", "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": v * 1e3, "higher_is_better": False, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded (H2O)128 cluster, host SCC ground state)",
-            "config": {"workload": "water128-lctda-20roots+S1grad", "n_roots": N_ROOTS, "tol": TOL,
-                       "max_iter": MAX_ITER},
-            "cpu_baseline": {"value": v, "unit": "s", "cores": threads, "kind": "port", "sample": sample},
-            "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+                   "unit": "monomers/s", "step_s": total, "cores": threads, "kind": "port", "sample": fsample}
+    return {"impl": "reference", "metric": METRIC, "value": v, "unit": "s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": v * 1e3 / max(1, args.steps), "higher_is_better": False,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded (H2O)128 cluster, host SCC ground state)",
+            "config": workload_config(sy, world),
+            "counts": {k: rec[k] for k in ("davidson_iterations", "products", "zvector_cg_iterations")},
+            "lowest_energies_eh": rec["lowest_energies_eh"],
+            "cpu_baseline": {"value": v, "unit": "s", "cores": threads, "kind": "port", "sample": sample,
+                             "tda_s": rec["tda_s"], "gradient_s": rec["gradient_s"]},
+            "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "fmo": fmo_ref}
 
 
 def run_fmo_once(args):
@@ -649,9 +729,10 @@ def main():
     ap.add_argument("--no-fmo", dest="fmo", action="store_false")
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
-    ap.add_argument("--ref-products", type=int, default=369)
-    ap.add_argument("--ref-iters", type=int, default=40)
-    ap.add_argument("--ref-cg", type=int, default=14)
+    # counts of the step a `--mode cpu-sample` child scales its sample to (passed by the GPU arm)
+    ap.add_argument("--ref-products", type=int, default=None)
+    ap.add_argument("--ref-iters", type=int, default=None)
+    ap.add_argument("--ref-cg", type=int, default=None)
     ap.add_argument("--mode", default="solve", choices=["solve", "products", "fmo", "cpu-sample"])
     ap.add_argument("--k", type=int, default=4)
     args = ap.parse_args()
@@ -662,6 +743,8 @@ def main():
         run_fmo_once(args)
         return
     if args.mode == "cpu-sample":
+        if None in (args.ref_products, args.ref_iters, args.ref_cg):
+            ap.error("--mode cpu-sample needs --ref-products, --ref-iters and --ref-cg")
         run_cpu_sample(args)
         return
     out = run_reference(args) if args.impl == "reference" else run_gpu(args)

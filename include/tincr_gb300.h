@@ -109,6 +109,13 @@ typedef enum {
 
 /* Turn per-family kernel timing on (1) or off (0); turning it on clears the statistics. */
 int tincr_set_profiling(tincr_ctx *ctx, int enable);
+/* Test hook of the failure path, no counterpart in tincr.  Every mbarrier wait of the tcgen05 plane
+ * GEMM gives up after 2 s, records an error code, drains the copies and MMAs it has in flight, frees
+ * its TMEM and returns; the next host synchronisation of the call reports TINCR_CUDA_ERR.  This sets
+ * the limit of the first wait of the MMA issuer for this context's later launches: 0 gives up at
+ * once (the other waits of the CTA keep their 2 s limit and run out in turn), a negative value
+ * restores the default. */
+int tincr_debug_tc_first_wait(tincr_ctx *ctx, long long limit_ns);
 /* Accumulated device ms, launches, algorithmic FLOPs and algorithmic bytes of one family. */
 int tincr_kernel_stats(const tincr_ctx *ctx, int family, double *ms, long long *launches, double *flops,
                        double *bytes);

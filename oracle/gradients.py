@@ -35,14 +35,22 @@ def gamma_gradients_atomwise(xyz, c):
     n = len(xyz)
     g1 = np.zeros((3 * n, n, n))
     for i in range(n):
-        for j in range(n):
-            if i == j:
-                continue
-            rv = xyz[i] - xyz[j]
-            r = np.linalg.norm(rv)
-            cv = c[i, j]
-            dg = 2.0 * cv / PI_SQRT * np.exp(-(cv * r) ** 2) / r - erf(cv * r) / r ** 2
-            g1[3 * i:3 * i + 3, i, j] = rv / r * dg
+        g1[3 * i:3 * i + 3] = gamma_gradient_rows(i, xyz, c)
+    return g1
+
+
+def gamma_gradient_rows(i, xyz, c):
+    """Rows 3i..3i+2 of `gamma_gradients_atomwise`: [3, N, N], nonzero only in row i."""
+    n = len(xyz)
+    g1 = np.zeros((3, n, n))
+    for j in range(n):
+        if i == j:
+            continue
+        rv = xyz[i] - xyz[j]
+        r = np.linalg.norm(rv)
+        cv = c[i, j]
+        dg = 2.0 * cv / PI_SQRT * np.exp(-(cv * r) ** 2) / r - erf(cv * r) / r ** 2
+        g1[:, i, j] = rv / r * dg
     return g1
 
 
@@ -52,15 +60,24 @@ def gamma_gradients_ao(g1, ao_atom):
     n_orb = len(ao_atom)
     g1_ao = np.zeros((3 * n_atoms, n_orb, n_orb))
     for i in range(n_atoms):
-        mu = np.where(ao_atom == i)[0]
-        for j in range(n_atoms):
-            if i == j:
-                continue
-            nu = np.where(ao_atom == j)[0]
-            for k in range(3):
-                g1_ao[3 * i + k][np.ix_(mu, nu)] = g1[3 * i + k, i, j]
-                g1_ao[3 * i + k][np.ix_(nu, mu)] = g1[3 * i + k, i, j]
+        g1_ao[3 * i:3 * i + 3] = gamma_gradient_ao_rows(i, g1[3 * i:3 * i + 3], ao_atom)
     return g1_ao
+
+
+def gamma_gradient_ao_rows(i, g1_rows, ao_atom):
+    """Rows 3i..3i+2 of `gamma_gradients_ao` from the atomwise rows [3, N, N] of atom i."""
+    n_atoms = g1_rows.shape[1]
+    n_orb = len(ao_atom)
+    out = np.zeros((3, n_orb, n_orb))
+    mu = np.where(ao_atom == i)[0]
+    for j in range(n_atoms):
+        if i == j:
+            continue
+        nu = np.where(ao_atom == j)[0]
+        for k in range(3):
+            out[k][np.ix_(mu, nu)] = g1_rows[k, i, j]
+            out[k][np.ix_(nu, mu)] = g1_rows[k, i, j]
+    return out
 
 
 # ----------------------------------------------------------------------------------------------
@@ -317,27 +334,39 @@ def ground_state_gradient(inp, der, lc):
     Returns (gradient [3N], f_lr_dmd0 or None).
     """
     n_atoms = len(inp["numbers"])
-    n_orb = inp["p"].shape[0]
+    gd = ground_state_densities(inp)
+    return ground_state_contract(inp, der, gd, lc, n_atoms,
+                                 gradient_v_rep(inp["numbers"], inp["xyz"], inp["params"]))
+
+
+def ground_state_densities(inp):
+    """The coordinate-independent operands of the ground-state gradient (`ground_state.rs:40-96`)."""
     p = inp["p"]
     ao_atom = inp["ao_atom"]
     esp = inp["gamma"] @ inp["dq"]
     esp_ao = esp[ao_atom]
     coulomb_mat = (esp_ao[:, None] + esp_ao[None, :]) * 0.5
-    coulomb_x_p = (p * coulomb_mat).reshape(-1)
-    p_flat = p.reshape(-1)
     dq = inp["dq"]
-    dq_x_dq = (dq[:, None] * dq[None, :]).reshape(-1)
-    w = 0.5 * (p @ inp["h_coul_x"] @ p).reshape(-1)
+    return dict(p_flat=p.reshape(-1), coulomb_x_p=(p * coulomb_mat).reshape(-1),
+                dq_x_dq=(dq[:, None] * dq[None, :]).reshape(-1),
+                w=0.5 * (p @ inp["h_coul_x"] @ p).reshape(-1), diff_p=p - inp["p0"])
+
+
+def ground_state_contract(inp, der, gd, lc, n_atoms, v_rep):
+    """Contraction of the derivative tensors `der` (all 3N rows, or the rows of one atom with
+    n_atoms = 1) with the ground-state operands `gd` (`ground_state.rs:97-136`); `v_rep` is the
+    repulsive gradient of the same rows.  Returns (gradient rows, f_lr_dmd0 rows or None)."""
+    n_orb = inp["p"].shape[0]
     gs2 = der["grad_s"].reshape(3 * n_atoms, -1)
     gh2 = der["grad_h0"].reshape(3 * n_atoms, -1)
-    grad = gh2 @ p_flat
-    grad -= gs2 @ w
-    grad += gs2 @ coulomb_x_p
-    grad += der["grad_gamma"].reshape(3 * n_atoms, -1) @ dq_x_dq
-    grad = grad + gradient_v_rep(inp["numbers"], inp["xyz"], inp["params"])
+    grad = gh2 @ gd["p_flat"]
+    grad -= gs2 @ gd["w"]
+    grad += gs2 @ gd["coulomb_x_p"]
+    grad += der["grad_gamma"].reshape(3 * n_atoms, -1) @ gd["dq_x_dq"]
+    grad = grad + v_rep
     flr_dmd0 = None
     if lc:
-        diff_p = p - inp["p0"]
+        diff_p = gd["diff_p"]
         flr_dmd0 = f_lr(diff_p, inp["s"], der["grad_s"], inp["gamma_lr_ao"], der["grad_gamma_lr_ao"],
                         n_atoms, n_orb)
         grad = grad - 0.25 * flr_dmd0.reshape(3 * n_atoms, -1) @ diff_p.reshape(-1)
@@ -345,7 +374,16 @@ def ground_state_gradient(inp, der, lc):
 
 
 def tda_gradient(inp, der, state, lc, flr_dmd0=None, stats=None, variant="reference"):
-    """`tda_gradient_lc` / `tda_gradient_nolc` (`src/gradients/excited_state.rs:56-487`).
+    """`tda_gradient_lc` / `tda_gradient_nolc` (`src/gradients/excited_state.rs:56-487`):
+    `tda_gradient_densities`, then `tda_gradient_contract` over all 3N derivative rows."""
+    d = tda_gradient_densities(inp, state, lc, stats=stats, variant=variant)
+    return tda_gradient_contract(inp, der, d, lc, flr_dmd0, inp["q_ov"].shape[0])
+
+
+def tda_gradient_densities(inp, state, lc, stats=None, variant="reference"):
+    """The coordinate-independent part of `tda_gradient_lc` / `tda_gradient_nolc`
+    (`src/gradients/excited_state.rs:56-430`): Z-vector, W, and the AO densities the derivative
+    tensors are contracted with.  Returns dict(diff_p, m = T_vv - T_oo + Z_AO, w_ao, x_ao).
 
     variant="reference" follows tincr exactly.  For LC, tincr solves the Z-vector equation with
     the TDA matrix A (`mult_av_lc`, 2 Coulomb - one exchange) and uses Hav for W_ij[Z]; the
@@ -416,13 +454,6 @@ def tda_gradient(inp, der, state, lc, flr_dmd0=None, stats=None, variant="refere
     w[:no, no:] = w_ia
     w[no:, :no] = w_ai
     w[no:, no:] = w_ab
-    n_orb = inp["s"].shape[0]
-    diff_p = inp["p"] - inp["p0"]
-    s = inp["s"]
-    f_dmd0 = f_v(diff_p, s, der["grad_s"], inp["gamma_ao"], der["grad_gamma_ao"], n_atoms, n_orb)
-    grad_h = der["grad_h0"] + f_dmd0
-    if lc:
-        grad_h = grad_h - 0.5 * flr_dmd0
     orbs = inp["orbs"]
     c_o = orbs[:, occ]
     c_v = orbs[:, virt]
@@ -431,15 +462,78 @@ def tda_gradient(inp, der, state, lc, flr_dmd0=None, stats=None, variant="refere
     z_ao = c_o @ z_ia @ c_v.T
     w_ao = orbs @ np.triu(w) @ orbs.T
     x_ao = c_o @ xs @ c_v.T
+    if stats is not None:
+        stats["z_ia"] = z_ia
+        stats["w"] = w
+    return dict(diff_p=inp["p"] - inp["p0"], m=(t_vv - t_oo + z_ao).reshape(-1), w_ao=w_ao, x_ao=x_ao)
+
+
+def tda_gradient_contract(inp, der, d, lc, flr_dmd0, n_atoms):
+    """Contraction of the derivative tensors `der` (all 3N rows, or the rows of one atom with
+    n_atoms = 1) with the densities of `tda_gradient_densities` (`excited_state.rs:432-486`, LC;
+    `:232-256`, non-LC); flr_dmd0 holds f_lr(P - P0) for the same rows (LC)."""
+    n_orb = inp["s"].shape[0]
+    s = inp["s"]
+    diff_p, m, w_ao, x_ao = d["diff_p"], d["m"], d["w_ao"], d["x_ao"]
+    f_dmd0 = f_v(diff_p, s, der["grad_s"], inp["gamma_ao"], der["grad_gamma_ao"], n_atoms, n_orb)
+    grad_h = der["grad_h0"] + f_dmd0
+    if lc:
+        grad_h = grad_h - 0.5 * flr_dmd0
     f = f_v(x_ao, s, der["grad_s"], inp["gamma_ao"], der["grad_gamma_ao"], n_atoms, n_orb)
-    m = (t_vv - t_oo + z_ao).reshape(-1)
     grad = grad_h.reshape(3 * n_atoms, -1) @ m
     grad = grad - der["grad_s"].reshape(3 * n_atoms, -1) @ w_ao.reshape(-1)
     grad = grad + 2.0 * f.reshape(3 * n_atoms, -1) @ x_ao.reshape(-1)
     if lc:
         flr_p = f_lr(x_ao.T, s, der["grad_s"], inp["gamma_lr_ao"], der["grad_gamma_lr_ao"], n_atoms, n_orb)
         grad = grad - flr_p.reshape(3 * n_atoms, -1) @ x_ao.reshape(-1)
-    if stats is not None:
-        stats["z_ia"] = z_ia
-        stats["w"] = w
     return grad
+
+
+# ----------------------------------------------------------------------------------------------
+# the same gradients one atom at a time (memory O(n_orb^2) instead of O(3N n_orb^2))
+# ----------------------------------------------------------------------------------------------
+
+class AtomRows:
+    """Derivative-tensor rows of one atom at a time: the 3-row blocks of `derivative_tensors`
+    (dS, dH0, dgamma, dgamma_AO, dgamma_lr_AO) for atom i, built on request."""
+
+    def __init__(self, numbers, xyz, ao_offset, ao_atom, hubbard, r_lr, params, orientation="reference"):
+        self.numbers, self.xyz, self.ao_offset, self.ao_atom = numbers, xyz, ao_offset, ao_atom
+        self.params, self.orientation, self.r_lr = params, orientation, r_lr
+        self.c0 = gamma_c(hubbard, 0.0)
+        self.clr = gamma_c(hubbard, r_lr) if r_lr > 0.0 else None
+        self.v_rep = gradient_v_rep(numbers, xyz, params)
+
+    def __call__(self, i):
+        gs, gh = slako.h0_and_s_gradient_rows(i, self.numbers, self.xyz, self.ao_offset, self.params,
+                                              orientation=self.orientation)
+        g1 = gamma_gradient_rows(i, self.xyz, self.c0)
+        out = dict(grad_s=gs, grad_h0=gh, grad_gamma=g1, grad_gamma_ao=gamma_gradient_ao_rows(i, g1, self.ao_atom))
+        if self.clr is not None:
+            g1lr = gamma_gradient_rows(i, self.xyz, self.clr)
+            out["grad_gamma_lr"] = g1lr
+            out["grad_gamma_lr_ao"] = gamma_gradient_ao_rows(i, g1lr, self.ao_atom)
+        return out
+
+
+def gradient_rows(inp, rows, i, gd, d, lc):
+    """Ground-state and excitation gradient of atom i (3 components each) from its derivative rows:
+    the same formulas as `ground_state_gradient` and `tda_gradient`, with the operands `gd`
+    (`ground_state_densities`) and `d` (`tda_gradient_densities`, or None for the ground state
+    only)."""
+    blk = rows(i)
+    g, flr = ground_state_contract(inp, blk, gd, lc, 1, rows.v_rep[3 * i:3 * i + 3])
+    x = None if d is None else tda_gradient_contract(inp, blk, d, lc, flr, 1)
+    return g, x
+
+
+def gradients_by_atom(inp, rows, state, lc, variant="reference", stats=None):
+    """Ground-state and excitation gradients [3N] each, atom by atom (`gradient_rows`), equal to
+    `ground_state_gradient` + `tda_gradient` without the [3N, n_orb, n_orb] tensors."""
+    gd = ground_state_densities(inp)
+    d = tda_gradient_densities(inp, state, lc, stats=stats, variant=variant)
+    n_atoms = len(inp["numbers"])
+    ggs, gex = np.zeros(3 * n_atoms), np.zeros(3 * n_atoms)
+    for i in range(n_atoms):
+        ggs[3 * i:3 * i + 3], gex[3 * i:3 * i + 3] = gradient_rows(inp, rows, i, gd, d, lc)
+    return ggs, gex

@@ -95,38 +95,59 @@ def h0_and_s_gradients(numbers, xyz, ao_offset, params, orientation="reference")
     gs = np.zeros((3 * n_atoms, n_orb, n_orb))
     gh = np.zeros((3 * n_atoms, n_orb, n_orb))
     for i in range(n_atoms):
-        ei = params.element(numbers[i])
-        for j in range(n_atoms):
-            if i == j:
-                continue
-            d = xyz[j] - xyz[i]
-            if np.linalg.norm(d) >= PROXIMITY_CUTOFF:
-                continue
-            ej = params.element(numbers[j])
-            zi, zj = int(numbers[i]), int(numbers[j])
-            centre1_is_i = zi < zj or (zi == zj and (orientation == "reference" or i < j))
-            if centre1_is_i:
-                # gradient w.r.t. r = pos_j - pos_i, turned into d/dR_i by a minus sign (`:218-248`)
-                key = (zi, zj)
-                _, gS = sk_block(params.sk_knots, params.sk_coef[key + ("s",)], params.sk_present[key],
-                                 ei.l, ei.m, ej.l, ej.m, d[None, :], grad=True)
-                _, gH = sk_block(params.sk_knots, params.sk_coef[key + ("h",)], params.sk_present[key],
-                                 ei.l, ei.m, ej.l, ej.m, d[None, :], grad=True)
-                bs, bh = -gS[0], -gH[0]
-            else:
-                # centres swapped: r = pos_i - pos_j, orbitals (j, i) (`:249-277`)
-                key = (zj, zi)
-                _, gS = sk_block(params.sk_knots, params.sk_coef[key + ("s",)], params.sk_present[key],
-                                 ej.l, ej.m, ei.l, ei.m, -d[None, :], grad=True)
-                _, gH = sk_block(params.sk_knots, params.sk_coef[key + ("h",)], params.sk_present[key],
-                                 ej.l, ej.m, ei.l, ei.m, -d[None, :], grad=True)
-                bs, bh = gS[0].transpose(0, 2, 1), gH[0].transpose(0, 2, 1)
-            mu = slice(ao_offset[i], ao_offset[i + 1])
+        h0_and_s_gradient_rows(i, numbers, xyz, ao_offset, params, orientation,
+                               out_s=gs[3 * i:3 * i + 3], out_h=gh[3 * i:3 * i + 3])
+    return gs, gh
+
+
+def h0_and_s_gradient_rows(i, numbers, xyz, ao_offset, params, orientation="reference", out_s=None, out_h=None):
+    """Rows 3i..3i+2 of the dense dS/dR and dH0/dR of `h0_and_s_gradients` (the loop body of
+    `src/scc/h0_and_s.rs:203-296` for one atom i): [3, n_orb, n_orb] each, written into out_s /
+    out_h when given (zeros elsewhere).  The partner atoms j are evaluated in batches of the same
+    element and centre order (one spline evaluation per batch)."""
+    n_atoms = len(numbers)
+    n_orb = int(ao_offset[-1])
+    gs = np.zeros((3, n_orb, n_orb)) if out_s is None else out_s
+    gh = np.zeros((3, n_orb, n_orb)) if out_h is None else out_h
+    ei = params.element(numbers[i])
+    zi = int(numbers[i])
+    groups = {}
+    for j in range(n_atoms):
+        if i == j:
+            continue
+        d = xyz[j] - xyz[i]
+        if np.linalg.norm(d) >= PROXIMITY_CUTOFF:
+            continue
+        zj = int(numbers[j])
+        centre1_is_i = zi < zj or (zi == zj and (orientation == "reference" or i < j))
+        groups.setdefault((zj, centre1_is_i), []).append(j)
+    mu = slice(ao_offset[i], ao_offset[i + 1])
+    for (zj, centre1_is_i), js in groups.items():
+        ej = params.element(zj)
+        d = xyz[js] - xyz[i][None, :]
+        if centre1_is_i:
+            # gradient w.r.t. r = pos_j - pos_i, turned into d/dR_i by a minus sign (`:218-248`)
+            key = (zi, zj)
+            _, gS = sk_block(params.sk_knots, params.sk_coef[key + ("s",)], params.sk_present[key],
+                             ei.l, ei.m, ej.l, ej.m, d, grad=True)
+            _, gH = sk_block(params.sk_knots, params.sk_coef[key + ("h",)], params.sk_present[key],
+                             ei.l, ei.m, ej.l, ej.m, d, grad=True)
+            bs_all, bh_all = -gS, -gH
+        else:
+            # centres swapped: r = pos_i - pos_j, orbitals (j, i) (`:249-277`)
+            key = (zj, zi)
+            _, gS = sk_block(params.sk_knots, params.sk_coef[key + ("s",)], params.sk_present[key],
+                             ej.l, ej.m, ei.l, ei.m, -d, grad=True)
+            _, gH = sk_block(params.sk_knots, params.sk_coef[key + ("h",)], params.sk_present[key],
+                             ej.l, ej.m, ei.l, ei.m, -d, grad=True)
+            bs_all, bh_all = gS.transpose(0, 1, 3, 2), gH.transpose(0, 1, 3, 2)
+        for t, j in enumerate(js):
             nu = slice(ao_offset[j], ao_offset[j + 1])
-            gs[3 * i:3 * i + 3, mu, nu] = bs
-            gs[3 * i:3 * i + 3, nu, mu] = bs.transpose(0, 2, 1)
-            gh[3 * i:3 * i + 3, mu, nu] = bh
-            gh[3 * i:3 * i + 3, nu, mu] = bh.transpose(0, 2, 1)
+            bs, bh = bs_all[t], bh_all[t]
+            gs[:, mu, nu] = bs
+            gs[:, nu, mu] = bs.transpose(0, 2, 1)
+            gh[:, mu, nu] = bh
+            gh[:, nu, mu] = bh.transpose(0, 2, 1)
     return gs, gh
 
 

@@ -151,11 +151,12 @@ class CtEngine(TdaEngine):
         return fock + two_el - k_x                                             # `:250`
 
 
-def run_tda_engine(eng, xyz, n_roots, max_iter, tolerance, history=None):
+def run_tda_engine(eng, xyz, n_roots, max_iter, tolerance, history=None, reorthogonalize=False):
     """`run_tda` / `run_ct_tda` around an existing engine: Davidson from `initial_subspace`,
     transition charges, Mulliken dipoles, oscillator strengths (ct_pair.rs:129-180)."""
     guess = initial_subspace(eng.omega, n_roots)
-    e, x, iters = davidson(eng, guess, n_roots, tolerance, max_iter, history=history)
+    e, x, iters = davidson(eng, guess, n_roots, tolerance, max_iter, history=history,
+                           reorthogonalize=reorthogonalize)
     q_trans = eng.q_ov @ x
     mu = mulliken_dipoles(q_trans, xyz)
     return dict(energies=e, coefficients=x, q_trans=q_trans, tr_dipoles=mu, f=oscillator_strength(e, mu),
@@ -166,11 +167,33 @@ class DavidsonError(RuntimeError):
     """`DavidsonError` (`solvers/davidson.rs:28-37`)."""
 
 
-def davidson(engine, guess, n_roots, tolerance, max_iter, history=None):
+def davidson(engine, guess, n_roots, tolerance, max_iter, history=None, reorthogonalize=False):
     """Block Davidson (`src/excited_states/solvers/davidson.rs:53-185`).
 
     Returns (eigenvalues [n_roots], eigenvectors [dim, n_roots], iterations).
+
+    tincr orthogonalises each correction against the basis with one classical Gram-Schmidt pass
+    (`:162-168`).  When a correction lies almost in the span of the basis, one pass leaves it with a
+    component of order (machine epsilon x its norm / the remainder's norm) inside that span, the
+    basis stops being orthonormal, and the Rayleigh-Ritz step can return spurious Ritz values near
+    zero (Rayleigh quotients of near-null combinations of nearly dependent columns) with small
+    residuals, which pass the convergence test.  `reorthogonalize=True` repeats the pass once
+    ("twice is enough"), which keeps the basis orthonormal to rounding; it is not tincr's statement
+    and serves to compute converged reference roots where the single pass fails.
     """
+    steps = davidson_steps(engine, guess, n_roots, tolerance, max_iter, history=history,
+                           reorthogonalize=reorthogonalize)
+    while True:
+        try:
+            next(steps)
+        except StopIteration as done:
+            return done.value
+
+
+def davidson_steps(engine, guess, n_roots, tolerance, max_iter, history=None, reorthogonalize=False):
+    """`davidson` as a generator: yields the iteration index after every iteration that does not
+    end the solve; the generator's return value is (eigenvalues, eigenvectors, iterations).  Lets a
+    caller time or interleave the iterations of one solve."""
     dim = engine.get_size()
     guess = np.array(guess, dtype=np.float64)
     dim_sub_origin = guess.shape[1]
@@ -198,12 +221,15 @@ def davidson(engine, guess, n_roots, tolerance, max_iter, history=None):
             dim_sub += roots_lft
             for vec in add:                                                    # `:162-168`
                 orth = vec - guess @ (guess.T @ vec)
+                if reorthogonalize:
+                    orth = orth - guess @ (guess.T @ orth)
                 nrm = np.linalg.norm(orth)
                 if nrm > 1.0e-8:
                     guess = np.concatenate([guess, (orth / nrm)[:, None]], axis=1)
         else:                                                                  # `:172-176`
             dim_sub = dim_sub_origin
             guess = ritz[:, :dim_sub].copy()
+        yield i
     raise DavidsonError("Davidson Algorithm did not converge!")
 
 
@@ -228,14 +254,15 @@ def oscillator_strength(energies, tr_dipoles):
 
 
 def run_tda(omega, q_ov, gamma, xyz, n_roots, max_iter, tolerance, q_oo=None, q_vv=None, gamma_lr=None,
-            n_occ=None, n_virt=None, history=None):
+            n_occ=None, n_virt=None, history=None, reorthogonalize=False):
     """`System::run_tda` (`src/excited_states/tda/mod.rs:74-131`) without the file output.
 
     Returns dict(energies, coefficients [o*v, n_roots], q_trans, tr_dipoles, f, iterations, n_products).
     """
     eng = TdaEngine(omega, q_ov, gamma, q_oo, q_vv, gamma_lr, n_occ, n_virt)
     guess = initial_subspace(omega, n_roots)
-    e, x, iters = davidson(eng, guess, n_roots, tolerance, max_iter, history=history)
+    e, x, iters = davidson(eng, guess, n_roots, tolerance, max_iter, history=history,
+                           reorthogonalize=reorthogonalize)
     q_trans = q_ov @ x
     mu = mulliken_dipoles(q_trans, xyz)
     f = oscillator_strength(e, mu)

@@ -155,3 +155,17 @@ def displaced_scc(z, xyz, lc, h):
             else:
                 os.environ[k] = v
     return [(out[2 * c], out[2 * c + 1]) for c in range(xyz.size)]
+
+
+def oracle_gradient_inputs(sy, g, lc, energies, coefficients, q=None):
+    """The `inp` dict of the oracle gradients for a host system `sy` with ground state `g` and the
+    roots (energies [n], coefficients [o*v, n]); q = (q_ov, q_oo, q_vv) when already computed."""
+    from oracle import tda as OT
+    occ, virt = sy.occ_indices, sy.virt_indices
+    qov, qoo, qvv = q if q is not None else OT.trans_charges(sy.ao_offset, g.orbs, g.s, occ, virt)
+    return dict(p=g.p, p0=g.p0, h_coul_x=g.h_coul_x, gamma=g.gamma, dq=g.dq, s=g.s, ao_atom=sy.ao_atom,
+                numbers=sy.numbers, xyz=sy.xyz, params=sy.params,
+                gamma_lr_ao=gs.atom_to_ao(sy, g.gamma_lr) if lc else None,
+                orbe=g.orbe, occ=occ, virt=virt, ci_eigenvalues=np.asarray(energies),
+                ci_coefficients=np.asarray(coefficients), q_ov=qov, q_oo=qoo, q_vv=qvv,
+                gamma_lr=g.gamma_lr if lc else None, orbs=g.orbs, gamma_ao=gs.atom_to_ao(sy, g.gamma))

@@ -237,3 +237,34 @@ def test_apb_product_known_answer():
     out = np.stack([OG.mult_apb_lc(d["gamma"], d["gamma_lr"], d["qtrans_ov"], d["qtrans_oo"], d["qtrans_vv"],
                                    d["omega0"], bs[:, :, k]) for k in range(bs.shape[2])], axis=2)
     assert np.abs(out - d["bp_ref"]).max() < 1e-14
+
+
+@pytest.mark.parametrize("name,lc,variant", [("naphthalene", True, "reference"), ("naphthalene", False, "reference"),
+                                             ("water8", True, "exact")])
+def test_gradient_by_atom_equals_dense(name, lc, variant):
+    """The atom-by-atom oracle gradient (one atom's derivative rows at a time, used at benchmark
+    sizes where the [3N, n, n] tensors do not fit) equals the dense restatement."""
+    from cases import oracle_gradient_inputs
+    from oracle import gradients as OG
+    from oracle import tda as OT
+    from tincr_gb300 import geometry as G
+    from tincr_gb300 import groundstate as gs
+    z, x = G.acene(2) if name == "naphthalene" else G.water_cluster(2, 2, 2)
+    sy = gs.build_system(z, G.to_bohr(x), lc=lc)
+    g = gs.run_scc(sy, tol=1e-10)
+    occ, virt = sy.occ_indices, sy.virt_indices
+    q = OT.trans_charges(sy.ao_offset, g.orbs, g.s, occ, virt)
+    om = OT.orbe_differences(g.orbe[occ], g.orbe[virt])
+    a = OT.tda_full_matrix(om, q[0], g.gamma, q[1], q[2], g.gamma_lr if lc else None, sy.n_occ, sy.n_virt)
+    e, xv = np.linalg.eigh(a)
+    inp = oracle_gradient_inputs(sy, g, lc, e[:3], xv[:, :3], q)
+    orient = "reference" if variant == "reference" else "index"
+    der = OG.derivative_tensors(sy.numbers, sy.xyz, sy.ao_offset, sy.ao_atom, sy.hubbard, sy.r_lr, sy.params,
+                                orientation=orient)
+    ggs, flr = OG.ground_state_gradient(inp, der, lc)
+    gex = OG.tda_gradient(inp, der, 1, lc, flr_dmd0=flr, variant=variant)
+    rows = OG.AtomRows(sy.numbers, sy.xyz, sy.ao_offset, sy.ao_atom, sy.hubbard, sy.r_lr, sy.params,
+                       orientation=orient)
+    ggs2, gex2 = OG.gradients_by_atom(inp, rows, 1, lc, variant=variant)
+    assert np.abs(ggs2 - ggs).max() < 1e-13
+    assert np.abs(gex2 - gex).max() < 1e-13

@@ -38,6 +38,7 @@ SIGNATURES = {
     "tincr_subspace_eigh": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _dp, _dp, _dp, _ip]),
     "tincr_gemm_fp64_tensor": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, _dp, _dp, _dp]),
     "tincr_set_profiling": (C.c_int, [C.c_void_p, C.c_int]),
+    "tincr_debug_tc_first_wait": (C.c_int, [C.c_void_p, C.c_longlong]),
     "tincr_kernel_stats": (C.c_int, [C.c_void_p, C.c_int, _dp, C.POINTER(C.c_longlong), _dp, _dp]),
     "tincr_trans_charges": (C.c_int, [C.c_void_p, C.c_int, _ip, C.c_int, _dp, _dp, C.c_int, C.c_int, C.c_int,
                                       C.c_int, _dp, _dp, _dp]),

@@ -120,6 +120,13 @@ int tincr_davidson_history(const tincr_ctx *ctx, int capacity, int *n_steps, int
     return TINCR_OK;
 }
 
+int tincr_debug_tc_first_wait(tincr_ctx *ctx, long long limit_ns) {
+    return guarded(ctx, [&](tincr::Ctx &c) {
+        c.tc_first_wait_ns = limit_ns < 0 ? -1 : limit_ns;
+        return TINCR_OK;
+    });
+}
+
 int tincr_set_profiling(tincr_ctx *ctx, int enable) {
     return guarded(ctx, [&](tincr::Ctx &c) {
         c.sync();

@@ -733,6 +733,26 @@ __global__ void bt_restart_kernel(BtArrays a) {
     }
 }
 
+// Device-side control of the iteration loop (a CUDA graph WHILE node replays one iteration until
+// no instance runs).  loop[0] = iterations run in the current phase, loop[1] = its limit,
+// loop[2] = iterations of the phase before (the mixed phase, when an FP64 phase follows it).
+__global__ void bt_loop_init_kernel(int *loop, int limit, int after_prev) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    const int prev = after_prev ? loop[0] : 0;
+    loop[2] = prev;
+    loop[1] = after_prev ? max(1, limit - prev) : max(1, limit);
+    loop[0] = 0;
+}
+
+// End of one iteration: count it and keep the loop going while an instance runs and the limit is
+// not reached (the same rule as a host loop reading the running count after every iteration).
+__global__ void bt_loop_next_kernel(const int *active, int *loop, cudaGraphConditionalHandle handle) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    const int its = loop[0] + 1;
+    loop[0] = its;
+    cudaGraphSetConditional(handle, (*active > 0 && its < loop[1]) ? 1u : 0u);
+}
+
 // ----------------------------------------------------------------------------------------------
 // subspace step
 // ----------------------------------------------------------------------------------------------
@@ -1374,6 +1394,7 @@ struct BatchWork {
     DevBuf<BtState> state;
     DevBuf<double> C, SC, S, blk, glr, glr_atoms, gam, omega, V, AV, R, Rk, T, sub, H, F, D, u, err, Y;
     DevBuf<int> ao_off, ao_atom, pos, active;
+    DevBuf<int> loop;                                  // device loop control (bt_loop_init_kernel)
     DevBuf<long long> off_glr_atoms;
     DevBuf<int4> t_sc;
     // Instances run in two groups, heavy (several roots on long vectors) then light, whose
@@ -1794,6 +1815,7 @@ int Ctx::solve_batch(int n_inst, const tincr_tda_instance *hin, int max_iter, do
     upload_any(stream, w.ao_atom, hAoAtom);
     upload_any(stream, w.pos, hPos);
     w.active.reserve(1);
+    w.loop.reserve(3);
 
     // clusters of the subspace step: each heavy instance on one cluster, the light ones four to a
     // cluster; per group, roots per instance (grid of the per-vector kernels)
@@ -2024,54 +2046,84 @@ int Ctx::solve_batch(int n_inst, const tincr_tda_instance *hin, int max_iter, do
             body(stream, 1);
         }
     };
-    // run an iteration function (as a CUDA graph unless kernel timing is on) until no instance is
-    // running or `limit` iterations are done; returns the iterations run
-    auto run_loop = [&](const std::function<void(cudaStream_t, int)> &body, int limit) {
-        int its = 0, active = n_inst;
+    // Run an iteration function until no instance is running or the limit is reached.  Without
+    // kernel timing the whole loop is one CUDA graph: a WHILE node whose body is one iteration of
+    // both groups followed by bt_loop_next_kernel, which decides on the device whether the body runs
+    // again, so no host round trip separates the iterations.  With kernel timing on (per-family
+    // events), the iterations run from the host one by one.  `after_prev`: the limit counts the
+    // iterations of the previous loop (limit - previous, at least 1).  Returns the launches of one
+    // iteration (for the launch count, finished once the iteration counts are read back).
+    auto run_loop = [&](const std::function<void(cudaStream_t, int)> &body, int limit, bool after_prev) {
+        long long per_iter = 0;
         if (!profiling) {
-            cudaGraph_t g = nullptr;
+            bt_loop_init_kernel<<<1, 1, 0, stream>>>(w.loop.p, limit, after_prev ? 1 : 0);
+            count_launch(stream, "bt_loop_init");
+            check_launch("bt_loop_init");
+            cudaGraph_t graph = nullptr;
             cudaGraphExec_t exec = nullptr;
-            TINCR_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+            TINCR_CUDA(cudaGraphCreate(&graph, 0));
+            cudaGraphConditionalHandle handle;
+            TINCR_CUDA(cudaGraphConditionalHandleCreate(&handle, graph, 1, cudaGraphCondAssignDefault));
+            cudaGraphNodeParams cp{};
+            cp.type = cudaGraphNodeTypeConditional;
+            cp.conditional.handle = handle;
+            cp.conditional.type = cudaGraphCondTypeWhile;
+            cp.conditional.size = 1;
+            cudaGraphNode_t node;
+            TINCR_CUDA(cudaGraphAddNode(&node, graph, nullptr, nullptr, 0, &cp));
+            cudaGraph_t body_graph = cp.conditional.phGraph_out[0];
+            TINCR_CUDA(cudaStreamBeginCaptureToGraph(stream, body_graph, nullptr, nullptr, 0,
+                                                     cudaStreamCaptureModeThreadLocal));
             const long long before = g_launches;
             both(body, true);
-            const long long per_iter = g_launches - before;
+            bt_loop_next_kernel<<<1, 1, 0, stream>>>(w.active.p, w.loop.p, handle);
+            count_launch(stream, "bt_loop_next");
+            check_launch("bt_loop_next");
+            per_iter = g_launches - before;
             g_launches = before;
-            TINCR_CUDA(cudaStreamEndCapture(stream, &g));
-            TINCR_CUDA(cudaGraphInstantiate(&exec, g, cudaGraphInstantiateFlagUseNodePriority));
-            cudaGraphDestroy(g);
-            while (active > 0 && its < limit) {
-                TINCR_CUDA(cudaGraphLaunch(exec, stream));
-                g_launches += per_iter;
-                ++its;
-                TINCR_CUDA(cudaMemcpyAsync(&active, w.active.p, sizeof(int), cudaMemcpyDeviceToHost, stream));
-                sync();
-            }
+            cudaGraph_t captured = nullptr;
+            TINCR_CUDA(cudaStreamEndCapture(stream, &captured));
+            TINCR_CUDA(cudaGraphInstantiate(&exec, graph, cudaGraphInstantiateFlagUseNodePriority));
+            cudaGraphDestroy(graph);
+            TINCR_CUDA(cudaGraphLaunch(exec, stream));
+            // freed once the launch completes
             cudaGraphExecDestroy(exec);
         } else {
+            int its = 0, active = n_inst, prev = 0;
+            if (after_prev) {
+                TINCR_CUDA(cudaMemcpyAsync(&prev, w.loop.p, sizeof(int), cudaMemcpyDeviceToHost, stream));
+                sync();
+                limit = std::max(1, limit - prev);
+            }
             while (active > 0 && its < limit) {
                 both(body, false);
                 ++its;
                 TINCR_CUDA(cudaMemcpyAsync(&active, w.active.p, sizeof(int), cudaMemcpyDeviceToHost, stream));
                 sync();
             }
+            const int rec[3] = {its, limit, prev};
+            TINCR_CUDA(cudaMemcpyAsync(w.loop.p, rec, sizeof(rec), cudaMemcpyHostToDevice, stream));
+            sync();
         }
-        return its;
+        return per_iter;
     };
+    long long per_iter_first = 0, per_iter_second = 0;
     if (mixed && tol >= MIXED_TOL_FLOOR) {
-        run_loop(iteration_mixed, max_iter);
+        per_iter_first = run_loop(iteration_mixed, max_iter, false);
     } else if (mixed) {
         // the mixed operator resolves residuals down to MIXED_TOL_FLOOR: the mixed phase stops there
         a.tol = MIXED_TOL_FLOOR;
-        const int its = run_loop(iteration_mixed, max_iter);
+        per_iter_first = run_loop(iteration_mixed, max_iter, false);
         a.tol = tol;
         // FP64 polish: every instance restarts from its mixed Ritz vectors on the FP64 operator and
-        // may stop at its first Rayleigh-Ritz step; convergence and energies are those of FP64
+        // may stop at its first Rayleigh-Ritz step; convergence and energies are those of FP64.  The
+        // polish may take max_iter minus the mixed iterations (at least 1), counted on the device.
         bt_restart_kernel<<<n_inst, BT_T, 0, stream>>>(a);
         count_launch(stream, "bt_restart");
         check_launch("bt_restart");
-        run_loop(iteration, std::max(1, max_iter - its));
+        per_iter_second = run_loop(iteration, max_iter, true);
     } else {
-        run_loop(iteration, max_iter);
+        per_iter_first = run_loop(iteration, max_iter, false);
     }
     // final pass: transition charges of the Ritz vectors (H = [C_o;SC_o] R, then its Coulomb
     // diagonals); a mixed solve forms H with the plane GEMM (its S C is FP32-accurate either way)
@@ -2101,7 +2153,15 @@ int Ctx::solve_batch(int n_inst, const tincr_tda_instance *hin, int max_iter, do
     TINCR_CUDA(cudaMemcpyAsync(hu.data(), w.u.p, o_u * sizeof(double), cudaMemcpyDeviceToHost, stream));
     TINCR_CUDA(cudaMemcpyAsync(hR.data(), w.R.p, o_r * sizeof(double), cudaMemcpyDeviceToHost, stream));
     TINCR_CUDA(cudaMemcpyAsync(hY.data(), w.Y.p, o_y * sizeof(double), cudaMemcpyDeviceToHost, stream));
+    int loop_rec[3] = {0, 0, 0};
+    TINCR_CUDA(cudaMemcpyAsync(loop_rec, w.loop.p, sizeof(loop_rec), cudaMemcpyDeviceToHost, stream));
     sync();
+    // launches of the device loop(s): iterations of the last loop in loop_rec[0], of the loop before
+    // it (mixed phase followed by the FP64 polish) in loop_rec[2]
+    if (per_iter_second > 0)
+        g_launches += per_iter_first * loop_rec[2] + per_iter_second * loop_rec[0];
+    else
+        g_launches += per_iter_first * loop_rec[0];
     int worst = TINCR_OK;
     last_products = 0;
     for (int I = 0; I < n_inst; ++I) {

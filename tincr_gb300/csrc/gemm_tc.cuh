@@ -64,8 +64,11 @@ __device__ __forceinline__ unsigned long long global_ns() {
     asm volatile("mov.u64 %0, %%globaltimer;\n" : "=l"(t));
     return t;
 }
-// bounded wait for the completion of the phase with the given parity; false on timeout
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, unsigned parity) {
+// bounded wait for the completion of the phase with the given parity; false on timeout.  A limit of
+// 0 gives up without polling (the test hook of the failure path, see gemm_planes_tc_kernel).
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, unsigned parity,
+                                          unsigned long long limit_ns = TC_WAIT_NS) {
+    if (limit_ns == 0) return false;
     uint32_t a = smem_u32(bar);
     const unsigned long long t0 = global_ns();
     for (unsigned it = 0;; ++it) {
@@ -76,7 +79,7 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, unsigned parity) {
             : "r"(a), "r"(parity)
             : "memory");
         if (done) return true;
-        if ((it & 63) == 63 && global_ns() - t0 > TC_WAIT_NS) return false;
+        if ((it & 63) == 63 && global_ns() - t0 > limit_ns) return false;
     }
 }
 
@@ -131,7 +134,7 @@ struct TcMaps {
 template <class Epi>
 __global__ void __launch_bounds__(TC_T, 1)
 gemm_planes_tc_kernel(const __grid_constant__ TcMaps maps, int M, int N, int Kpad, int a_batched, int b_batched,
-                      Epi epi, int *err) {
+                      Epi epi, int *err, unsigned long long first_wait_ns) {
     extern __shared__ unsigned char tc_raw[];
     unsigned char *smem = (unsigned char *)(((uintptr_t)tc_raw + 1023) & ~(uintptr_t)1023);
     uint64_t *full = reinterpret_cast<uint64_t *>(smem + TC_STAGES * TC_STAGE);
@@ -197,7 +200,9 @@ gemm_planes_tc_kernel(const __grid_constant__ TcMaps maps, int M, int N, int Kpa
         if (lane == 0) {
             for (int kb = 0; kb < nk; ++kb) {
                 const int s = kb % TC_STAGES, a = kb & 1;
-                if (!mbar_wait(&full[s], (kb / TC_STAGES) & 1)) {
+                // first_wait_ns limits the first of these waits (TC_WAIT_NS unless a test shortens it
+                // to exercise the recovery: the producer drains its loads, the fold warps give up)
+                if (!mbar_wait(&full[s], (kb / TC_STAGES) & 1, kb == 0 ? first_wait_ns : TC_WAIT_NS)) {
                     atomicExch(err, 2);
                     break;
                 }
@@ -313,7 +318,7 @@ inline CUtensorMap plane_map(const bf16 *base, int rows, long long Kpad, long lo
 
 template <class Epi>
 void gemm_planes_tc(cudaStream_t st, int M, int N, int Kpad, PlaneOperand A, PlaneOperand B, int batch, Epi epi,
-                    int *d_err) {
+                    int *d_err, unsigned long long first_wait_ns = TC_WAIT_NS) {
     if (M <= 0 || N <= 0 || batch <= 0) return;
     if (Kpad <= 0 || Kpad % TC_K) fail(TINCR_BAD_ARG, "gemm_planes_tc: K not padded to 64");
     TcMaps maps;
@@ -327,7 +332,8 @@ void gemm_planes_tc(cudaStream_t st, int M, int N, int Kpad, PlaneOperand A, Pla
         attr = true;
     }
     dim3 grid(ceil_div(N, TC_N), ceil_div(M, TC_M), batch);
-    gemm_planes_tc_kernel<Epi><<<grid, TC_T, TC_SMEM, st>>>(maps, M, N, Kpad, A.sb ? 1 : 0, B.sb ? 1 : 0, epi, d_err);
+    gemm_planes_tc_kernel<Epi><<<grid, TC_T, TC_SMEM, st>>>(maps, M, N, Kpad, A.sb ? 1 : 0, B.sb ? 1 : 0, epi, d_err,
+                                                            first_wait_ns);
     count_launch(st, "gemm_planes_tc");
     check_launch("gemm_planes_tc");
 }

@@ -104,6 +104,7 @@ struct Ctx {
     DevBuf<double> mx_f64;
     long long mx_key = -1;
     DevBuf<int> d_tc_err;                 // error word of the tensor-core kernels' bounded waits
+    long long tc_first_wait_ns = -1;      // limit of the plane GEMM's first MMA-side wait (-1: the default)
     int *h_tc_err = nullptr;              // pinned copy, refreshed after tensor-core launches, read by sync()
     void tc_err_ensure();                 // allocate and clear d_tc_err
     void tc_err_watch();                  // queue the copy of d_tc_err to h_tc_err (checked at the next sync)

@@ -312,3 +312,88 @@ def le_gradients(monomers, results, states, n_streams=8, variant="reference", co
             for c in ctxs:
                 c.close()
     return out
+
+
+# ----------------------------------------------------------------------------------------------
+# exciton Hamiltonian inputs (upstream of the couplings: pair types, overlaps, gamma, pair SCC)
+# ----------------------------------------------------------------------------------------------
+
+# Sums of van der Waals radii in bohr for H, C, N, O: tincr's VDW_SUM table (UFF radii,
+# src/constants.rs:1389)
+VDW_SUM_BOHR = {(1, 1): 5.454, (1, 6): 6.366, (1, 7): 6.185, (1, 8): 6.128, (6, 6): 7.279, (6, 7): 7.098,
+                (6, 8): 7.041, (7, 7): 6.916, (7, 8): 6.860, (8, 8): 6.803}
+
+
+def is_real_pair(ma, mb, vdw_scaling=2.0):
+    """tincr's `get_pair_type` (src/fmo/pair.rs:35-53): a real pair when some atom pair is closer than
+    vdw_scaling times the sum of its van der Waals radii, otherwise an ESD pair."""
+    za, zb = ma.system.numbers, mb.system.numbers
+    lim = np.array([[VDW_SUM_BOHR[(min(int(x), int(y)), max(int(x), int(y)))] for y in zb] for x in za])
+    d = np.linalg.norm(ma.system.xyz[:, None, :] - mb.system.xyz[None, :, :], axis=-1)
+    return bool(np.any(d < vdw_scaling * lim))
+
+
+def _dimer_scc(args):
+    """Host SCC of one dimer (top-level for a spawn process pool): returns (orbs, orbe)."""
+    z, xyz, lc, r_lr, tol = args
+    sy = gs.build_system(z, xyz, lc=lc, r_lr=r_lr)
+    g = gs.run_scc(sy, tol=tol)
+    return g.orbs, g.orbe
+
+
+class ExcitonSetup:
+    """Everything the exciton Hamiltonian reads besides the LE / CT roots, produced on the host
+    (tincr's SuperSystem holds the same: src/fmo/supersystem.rs:248-305, src/fmo/pair.rs):
+
+    * pair types of every monomer pair (real pair / ESD, `is_real_pair`);
+    * the AO overlap blocks S_IJ between the monomers of every real pair and of every CT pair;
+    * the atomwise gamma and gamma_lr of the whole aggregate;
+    * the ground state (MO coefficients, energies) of every real pair's dimer, for the LCMO Fock
+      matrix (tincr's FMO pair SCC; here the isolated dimer, like the monomers).
+    `workers` > 1 runs the dimer SCCs in a spawn process pool."""
+
+    def __init__(self, monomers, ct_pairs, lc=True, scc_tol=1e-10, workers=1):
+        self.monomers = monomers
+        self.ct_pairs = list(ct_pairs)
+        n = len(monomers)
+        self.real = {}
+        for i in range(n):
+            for j in range(i + 1, n):
+                self.real[(i, j)] = is_real_pair(monomers[i], monomers[j])
+        sy0 = monomers[0].system
+        self.lc, self.r_lr = lc, sy0.r_lr
+        z = np.concatenate([m.system.numbers for m in monomers])
+        xyz = np.concatenate([m.system.xyz for m in monomers])
+        self.atom_offset = np.concatenate([[0], np.cumsum([m.system.n_atoms for m in monomers])]).astype(np.int64)
+        big = gs.build_system(z, xyz, lc=lc, r_lr=self.r_lr)
+        self.gamma = gs.gamma_atomwise(big, 0.0)
+        self.gamma_lr = gs.gamma_atomwise(big, self.r_lr) if lc else np.zeros_like(self.gamma)
+        need = sorted(set(k for k, v in self.real.items() if v) | set(tuple(sorted(p)) for p in self.ct_pairs))
+        self.s_blocks = {}
+        for i, j in need:
+            mi, mj = monomers[i], monomers[j]
+            sy = gs.build_system(np.concatenate([mi.system.numbers, mj.system.numbers]),
+                                 np.concatenate([mi.system.xyz, mj.system.xyz]), lc=lc, r_lr=self.r_lr)
+            s, _ = gs.h0_and_s(sy)
+            ni = mi.system.n_orbs
+            self.s_blocks[(i, j)] = np.ascontiguousarray(s[:ni, ni:])
+        jobs = []
+        self.real_pairs = sorted(k for k, v in self.real.items() if v)
+        for i, j in self.real_pairs:
+            mi, mj = monomers[i], monomers[j]
+            jobs.append((np.concatenate([mi.system.numbers, mj.system.numbers]),
+                         np.concatenate([mi.system.xyz, mj.system.xyz]), lc, self.r_lr, scc_tol))
+        if workers > 1 and len(jobs) > 1:
+            import multiprocessing as mp
+            from concurrent.futures import ProcessPoolExecutor
+            with ProcessPoolExecutor(max_workers=workers, mp_context=mp.get_context("spawn")) as ex:
+                out = list(ex.map(_dimer_scc, jobs, chunksize=4))
+        else:
+            out = [_dimer_scc(a) for a in jobs]
+        self.pair_scc = {k: o for k, o in zip(self.real_pairs, out)}
+
+    def s_block(self, i, j):
+        """AO overlap between monomers i and j (rows i)."""
+        if i < j:
+            return self.s_blocks[(i, j)]
+        return self.s_blocks[(j, i)].T
