@@ -206,6 +206,60 @@ typedef struct {
 int tincr_tda_solve_batch(tincr_ctx *ctx, int n_inst, const tincr_tda_instance *inst, int max_iter,
                           double tolerance, int precision, tincr_tda_result *res);
 
+/* ---- FMO exciton Hamiltonian ------------------------------------------------------------------ */
+
+/* One monomer of the aggregate with its locally excited (LE) roots. */
+typedef struct {
+    int n_atoms, n_orb, n_occ;       /* atoms; AOs (= MOs); occupied MOs (the first n_occ)          */
+    const int *orbs_per_atom;        /* [n_atoms]                                                     */
+    const double *c;                 /* [n_orb x n_orb] MO coefficients, columns = MOs                */
+    const double *s;                 /* [n_orb x n_orb] AO overlap                                    */
+    const double *orbe;              /* [n_orb] orbital energies                                      */
+    int n_le;                        /* LE roots of the monomer in the basis                          */
+    const double *le_energies;       /* [n_le]                                                        */
+    const double *le_coefficients;   /* [n_occ*n_virt x n_le] (tincr's ci_coefficients layout)        */
+    const double *le_q_trans;        /* [n_atoms x n_le] transition charges                           */
+} tincr_exciton_monomer;
+
+/* A monomer pair that is a real pair (tincr's get_pair_type, src/fmo/pair.rs:35-53) or carries CT
+ * states.  Pairs not listed are ESD pairs: Coulomb couplings only, and zero AO overlap (their atoms
+ * are farther apart than the Slater-Koster tables reach), so the exchange integrals that need their
+ * overlap vanish. */
+typedef struct {
+    int i, j;                        /* monomers, i < j                                               */
+    int real;                        /* 1: real pair (exchange couplings, LCMO Fock block), 0: ESD     */
+    const double *s_ij;              /* [n_orb_i x n_orb_j] AO overlap between the two monomers       */
+    const double *pair_orbs;         /* real pairs: [n_ij x n_ij] dimer MO coefficients (AOs of i, j) */
+    const double *pair_orbe;         /* real pairs: [n_ij] dimer orbital energies                     */
+} tincr_exciton_pair;
+
+/* One charge-transfer basis state: root `state` of the pair TDA with the hole on monomer h and the
+ * electron on monomer l. */
+typedef struct {
+    int h, l;
+    int state;                       /* root index in this direction's results                        */
+    int n_ct;                        /* roots of this direction                                       */
+    const double *energies;          /* [n_ct]                                                        */
+    const double *coefficients;      /* [n_occ(h)*n_virt(l) x n_ct]                                   */
+    const double *q_tr;              /* [(n_atoms(h) + n_atoms(l)) x n_ct], h's atoms first            */
+} tincr_exciton_ct;
+
+/* Replaces SuperSystem::create_exciton_hamiltonian_new (src/fmo/lcmo/basis.rs:449-503): the exciton
+ * matrix in the diabatic basis (every monomer's LE roots in monomer order, then the CT states as
+ * given), with tincr's couplings (exciton_coupling, src/fmo/lcmo/integrals.rs:17-79: le_le, le_ct_new
+ * with the LCMO Fock matrix of src/fmo/lcmo/hamiltonian.rs:12-152, ct_ct_new; restricted active space
+ * of 10 occupied and 10 virtual orbitals for the LE-CT and CT-CT exchange), then its lowest n_roots
+ * roots by tincr's Davidson on the dense matrix (guess from the diagonal, residual tolerance tol).
+ * gamma / gamma_lr: [n_atoms x n_atoms] atomwise matrices of the whole aggregate, monomers' atoms in
+ * monomer order.  precision: TINCR_PREC_FP64, or TINCR_PREC_BF16X3 (exchange integrals and LCMO GEMMs
+ * in FP32; matrix and Davidson in FP64).  Monomers of up to 102 AOs and 40 atoms, with at least 10
+ * occupied and 10 virtual orbitals.  h_out ([dim x dim]) and vectors ([dim x n_roots]) may be NULL.
+ * Returns TINCR_NOT_CONVERGED when max_iter is reached. */
+int tincr_exciton_states(tincr_ctx *ctx, int n_monomers, const tincr_exciton_monomer *monomers, int n_pairs,
+                         const tincr_exciton_pair *pairs, int n_ct, const tincr_exciton_ct *ct, int n_atoms,
+                         const double *gamma, const double *gamma_lr, int precision, int n_roots, double tol,
+                         int max_iter, double *h_out, double *energies, double *vectors, int *iterations);
+
 /* The tile shapes of the batch's mixed-form plane GEMMs, as chosen by the autotuner.  No counterpart
  * in tincr (rayon runs one monomer per thread).  The first TINCR_PREC_BF16X3 batch that contains an
  * instance shape (n_atoms, n_orb, n_occ, n_virt, long-range flag) times the four tile shapes

@@ -46,6 +46,9 @@ SIGNATURES = {
                                   _dp]),
     "tincr_tda_products": (C.c_int, [C.c_void_p, C.c_int, _dp, _dp, C.c_int]),
     "tincr_tda_products_noalloc": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]),
+    "tincr_exciton_states": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_void_p,
+                                       C.c_int, _dp, _dp, C.c_int, C.c_int, C.c_double, C.c_int, _dp, _dp, _dp,
+                                       _ip]),
     "tincr_tda_solve": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_double, C.c_int, _dp, _dp, _dp, _dp, _dp,
                                   _ip]),
     "tincr_set_parameters": (C.c_int, [C.c_void_p, C.c_int, _ip, _ip, _ip, _ip, _dp, _dp, C.c_int, _dp, _dp,

@@ -16,7 +16,8 @@ SRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "lib")
 LIB = os.path.join(OUT, "libtincr_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["abi.cu", "tda.cu", "gradient.cu", "noalloc.cu", "mixed.cu", "batch.cu", "eig_cluster.cu", "digits.cu", "eigen_host.cpp"]
+SOURCES = ["abi.cu", "tda.cu", "gradient.cu", "noalloc.cu", "mixed.cu", "batch.cu", "eig_cluster.cu", "digits.cu",
+           "exciton.cu", "eigen_host.cpp"]
 
 
 def _nvcc():

@@ -174,6 +174,16 @@ int tincr_tda_products(tincr_ctx *ctx, int k, const double *X, double *AX, int p
     });
 }
 
+int tincr_exciton_states(tincr_ctx *ctx, int n_monomers, const tincr_exciton_monomer *monomers, int n_pairs,
+                         const tincr_exciton_pair *pairs, int n_ct, const tincr_exciton_ct *ct, int n_atoms,
+                         const double *gamma, const double *gamma_lr, int precision, int n_roots, double tol,
+                         int max_iter, double *h_out, double *energies, double *vectors, int *iterations) {
+    return guarded(ctx, [&](tincr::Ctx &c) {
+        return c.exciton_states(n_monomers, monomers, n_pairs, pairs, n_ct, ct, n_atoms, gamma, gamma_lr, precision,
+                                n_roots, tol, max_iter, h_out, energies, vectors, iterations);
+    });
+}
+
 int tincr_tda_products_noalloc(tincr_ctx *ctx, int k, const double *X_dev, double *AX_dev) {
     return guarded(ctx, [&](tincr::Ctx &c) {
         tincr::products_noalloc(c, k, X_dev, AX_dev);

@@ -179,6 +179,10 @@ struct Ctx {
     int davidson(int n_roots, int max_iter, double tol, bool from_ritz, std::vector<double> &u, int *it_out);
     int solve_batch(int n_inst, const tincr_tda_instance *inst, int max_iter, double tol, int precision,
                     tincr_tda_result *res);
+    int exciton_states(int n_mono, const tincr_exciton_monomer *mono, int n_pairs, const tincr_exciton_pair *pairs,
+                       int n_ct, const tincr_exciton_ct *cts, int n_atoms_total, const double *gamma,
+                       const double *gamma_lr, int precision, int n_roots, double tol, int max_iter, double *h_out,
+                       double *energies, double *vectors, int *iterations);
 };
 
 // Lowest k eigenpairs of the m x m matrix P (upper triangle, leading dimension ldp) on one thread-block

@@ -393,7 +393,106 @@ class ExcitonSetup:
         self.pair_scc = {k: o for k, o in zip(self.real_pairs, out)}
 
     def s_block(self, i, j):
-        """AO overlap between monomers i and j (rows i)."""
+        """AO overlap between monomers i and j (rows i).  Pairs without a stored block are ESD pairs
+        whose atoms are all farther apart than the Slater-Koster grid reaches: their overlap is zero."""
+        key = (min(i, j), max(i, j))
+        if key not in self.s_blocks:
+            mi, mj = self.monomers[i], self.monomers[j]
+            d = np.linalg.norm(mi.system.xyz[:, None, :] - mj.system.xyz[None, :, :], axis=-1).min()
+            if d <= float(np.max(mi.system.params.sk_knots)):
+                raise KeyError("overlap of pair %s not computed" % (key,))
+            return np.zeros((mi.system.n_orbs, mj.system.n_orbs))
         if i < j:
             return self.s_blocks[(i, j)]
         return self.s_blocks[(j, i)].T
+
+
+class _ExMonomer(ct.Structure):
+    _fields_ = [("n_atoms", ct.c_int), ("n_orb", ct.c_int), ("n_occ", ct.c_int),
+                ("orbs_per_atom", ct.POINTER(ct.c_int)), ("c", ct.POINTER(ct.c_double)), ("s", ct.POINTER(ct.c_double)),
+                ("orbe", ct.POINTER(ct.c_double)), ("n_le", ct.c_int), ("le_energies", ct.POINTER(ct.c_double)),
+                ("le_coefficients", ct.POINTER(ct.c_double)), ("le_q_trans", ct.POINTER(ct.c_double))]
+
+
+class _ExPair(ct.Structure):
+    _fields_ = [("i", ct.c_int), ("j", ct.c_int), ("real", ct.c_int), ("s_ij", ct.POINTER(ct.c_double)),
+                ("pair_orbs", ct.POINTER(ct.c_double)), ("pair_orbe", ct.POINTER(ct.c_double))]
+
+
+class _ExCT(ct.Structure):
+    _fields_ = [("h", ct.c_int), ("l", ct.c_int), ("state", ct.c_int), ("n_ct", ct.c_int),
+                ("energies", ct.POINTER(ct.c_double)), ("coefficients", ct.POINTER(ct.c_double)),
+                ("q_tr", ct.POINTER(ct.c_double))]
+
+
+def _dp(a):
+    return None if a is None else a.ctypes.data_as(ct.POINTER(ct.c_double))
+
+
+def exciton_states(ctx, setup, results, labels, n_le, n_ct, n_roots=10, tol=1e-4, max_iter=100,
+                   precision=_lib.PREC_FP64, want_matrix=False):
+    """tincr's exciton Hamiltonian and its lowest roots on the GPU (`tincr_exciton_states`;
+    SuperSystem::create_exciton_hamiltonian_new, src/fmo/lcmo/basis.rs:449-503).
+
+    `results` / `labels`: the batch TDA results of the work list of `aggregate_instances` (LE
+    instances of every monomer, then both directions of every CT pair of `setup.ct_pairs`).  The basis
+    is n_le LE roots per monomer, then for every CT pair and root n < n_ct the states I -> J and
+    J -> I (basis.rs:180-238).  Returns dict(energies [n_roots], vectors [dim, n_roots], iterations,
+    status, matrix [dim, dim] when want_matrix)."""
+    mons = setup.monomers
+    keep = []
+    le_of = {}
+    ct_of = {}
+    for k, lab in enumerate(labels):
+        if lab[0] == "LE":
+            le_of[lab[1]] = results[k]
+        else:
+            ct_of[(lab[1], lab[2])] = results[k]
+    marr = (_ExMonomer * len(mons))()
+    for k, m in enumerate(mons):
+        sy, g = m.system, m.ground
+        r = le_of[m.index]
+        opa = np.ascontiguousarray(sy.orbs_per_atom, dtype=np.int32)
+        e = _f64(np.asarray(r["energies"])[:n_le])
+        cf = _f64(np.asarray(r["coefficients"])[:, :n_le])
+        qt = _f64(np.asarray(r["q_trans"])[:, :n_le])
+        c, s, orbe = _f64(g.orbs), _f64(g.s), _f64(g.orbe)
+        keep += [opa, e, cf, qt, c, s, orbe]
+        marr[k] = _ExMonomer(sy.n_atoms, sy.n_orbs, sy.n_occ, opa.ctypes.data_as(ct.POINTER(ct.c_int)), _dp(c),
+                             _dp(s), _dp(orbe), n_le, _dp(e), _dp(cf), _dp(qt))
+    plist = sorted(set(setup.real_pairs) | set(tuple(sorted(p)) for p in setup.ct_pairs))
+    parr = (_ExPair * max(1, len(plist)))()
+    for k, (i, j) in enumerate(plist):
+        sij = _f64(setup.s_block(i, j))
+        real = bool(setup.real.get((i, j), False))
+        po, pe = (setup.pair_scc[(i, j)] if real else (None, None))
+        po = None if po is None else _f64(po)
+        pe = None if pe is None else _f64(pe)
+        keep += [sij, po, pe]
+        parr[k] = _ExPair(i, j, int(real), _dp(sij), _dp(po), _dp(pe))
+    states = []
+    for i, j in setup.ct_pairs:
+        for n in range(n_ct):
+            for h, l in ((i, j), (j, i)):
+                states.append((h, l, n))
+    carr = (_ExCT * max(1, len(states)))()
+    for k, (h, l, n) in enumerate(states):
+        r = ct_of[(h, l)]
+        e, cf, qt = _f64(np.asarray(r["energies"])), _f64(np.asarray(r["coefficients"])), _f64(np.asarray(r["q_trans"]))
+        keep += [e, cf, qt]
+        carr[k] = _ExCT(h, l, n, len(e), _dp(e), _dp(cf), _dp(qt))
+    dim = sum(n_le for _ in mons) + len(states)
+    energies = np.zeros(n_roots)
+    vectors = np.zeros((dim, n_roots))
+    mat = np.zeros((dim, dim)) if want_matrix else None
+    its = ct.c_int(0)
+    g, glr = _f64(setup.gamma), _f64(setup.gamma_lr)
+    rc = ctx.lib.tincr_exciton_states(ctx.h, len(mons), ct.addressof(marr), len(plist), ct.addressof(parr),
+                                      len(states), ct.addressof(carr), g.shape[0], _dp(g), _dp(glr), int(precision),
+                                      int(n_roots), float(tol), int(max_iter), _dp(mat), _dp(energies), _dp(vectors),
+                                      ct.byref(its))
+    ctx.check(rc, allow=(_lib.OK, _lib.NOT_CONVERGED))
+    out = dict(energies=energies, vectors=vectors, iterations=its.value, status=rc)
+    if want_matrix:
+        out["matrix"] = mat
+    return out
