@@ -43,6 +43,9 @@ METRIC = "LC-TDA roots+S1 grad wall s (mixed vs FP64 GPU, <=1e-6 Eh); FMO monome
 N_ROOTS, MAX_ITER, TOL = 20, 450, 1e-4
 PRECISIONS = {"fp64": 0, "bf16x3": 1}   # tincr_precision values
 FMO_N_LE, FMO_N_CT, FMO_TOL, FMO_MAX_ITER = 4, 1, 1e-4, 150
+# exciton states: tincr's Davidson on the exciton matrix (src/fmo/lcmo/basis.rs:500: tolerance 1e-4,
+# 100 iterations), the lowest 10 states
+FMO_N_EXCITON, FMO_EX_TOL, FMO_EX_MAX_ITER = 10, 1e-4, 100
 R_LR = 1.0 / 0.3
 
 
@@ -377,12 +380,17 @@ def _cpu_helpers():
     return cases, OG, OT
 
 
-def fmo_cpu_reference(mons, inst, labels):
+def fmo_cpu_reference(mons, pairs, inst, labels, setup):
     """tincr's FMO step on the CPU, measured in full: the TDA of every instance of the work list
     with tincr's engines (oracle `TdaEngine` per monomer, `CtEngine` per pair direction; numpy +
-    the host BLAS), then the LE excitation gradient of the aggregate's lowest LE root (dense
-    derivative tensors, Z-vector, f_v / f_lr contractions).  Returns (seconds, description)."""
+    the host BLAS); the exciton Hamiltonian over those states (LCMO Fock matrix, then the matrix
+    rows shared out to one process per host core, as tincr shares them out to rayon threads,
+    src/fmo/lcmo/basis.rs:479-487) and its lowest 10 roots by tincr's Davidson; then the LE
+    excitation gradient of the aggregate's lowest LE root (dense derivative tensors, Z-vector,
+    f_v / f_lr contractions).  `setup` (pair types, overlaps, gamma, dimer ground states) is the
+    host set-up the GPU arm also reads, not timed.  Returns (seconds, description, exciton energies)."""
     cases, OG, OT = _cpu_helpers()
+    from oracle import exciton as OX
     case = dict(monomers=mons, labels=labels, lc=True)
     t0 = time.perf_counter()
     res = []
@@ -390,6 +398,12 @@ def fmo_cpu_reference(mons, inst, labels):
         eng, xyz = cases.fmo_oracle_engine(case, k)
         res.append(OT.run_tda_engine(eng, xyz, q["n_roots"], FMO_MAX_ITER, FMO_TOL))
     t_tda = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    agg = OX.aggregate_of(mons, setup)
+    states = OX.basis_of(agg, labels, res, setup.ct_pairs, FMO_N_LE, FMO_N_CT)
+    h = OX.exciton_hamiltonian_rows(agg, states, os.cpu_count() or 1)
+    ex = OX.exciton_states(h, FMO_N_EXCITON, FMO_EX_TOL, FMO_EX_MAX_ITER)
+    t_ex = time.perf_counter() - t0
     t0 = time.perf_counter()
     n_mon = len(mons)
     k1 = int(np.argmin([res[k]["energies"][0] for k in range(n_mon)]))
@@ -401,9 +415,11 @@ def fmo_cpu_reference(mons, inst, labels):
     OG.tda_gradient(inp, der, 0, True, flr_dmd0=flr)
     t_grad = time.perf_counter() - t0
     n_le = sum(1 for l in labels if l[0] == "LE")
-    sample = ("measured in full: oracle TDA of all %d instances (%d LE, %d CT; %.2f s) + the LE gradient of the "
-              "lowest LE root (monomer %d, %.2f s)" % (len(inst), n_le, len(inst) - n_le, t_tda, k1, t_grad))
-    return t_tda + t_grad, sample
+    sample = ("measured in full: oracle TDA of all %d instances (%d LE, %d CT; %.2f s) + the exciton Hamiltonian "
+              "(%d states, rows on %d processes) and its lowest %d roots (%.2f s) + the LE gradient of the lowest LE "
+              "root (monomer %d, %.2f s)" % (len(inst), n_le, len(inst) - n_le, t_tda, len(states),
+                                              os.cpu_count() or 1, FMO_N_EXCITON, t_ex, k1, t_grad))
+    return t_tda + t_ex + t_grad, sample, np.asarray(ex[0])
 
 
 def ctx_device(ctx):
@@ -424,55 +440,70 @@ def tile_summary(table):
 
 
 def run_fmo(args, ctx):
-    """Batched LE / CT TDA of the 64-acene aggregate plus the S1 gradient, mixed and FP64 forms
-    (monomers/s)."""
+    """The 64-acene FMO step, mixed and FP64 forms (monomers/s): batched LE / CT TDA of the work
+    list, the exciton Hamiltonian and its lowest 10 states, and the S1 LE gradient."""
     from tincr_gb300 import _lib
     from tincr_gb300 import fmo
     t0 = time.perf_counter()
     mons, pairs, inst, labels = fmo_workload()
     t_setup = time.perf_counter() - t0
-    out = {"workload": "acene64-fmo-le4-ct1", "monomers": len(mons), "ct_pairs": len(pairs),
+    t0 = time.perf_counter()
+    setup = fmo.ExcitonSetup(mons, pairs, workers=min(16, os.cpu_count() or 1))
+    t_exsetup = time.perf_counter() - t0
+    out = {"workload": "acene64-fmo-le4-ct1-exciton10", "monomers": len(mons), "ct_pairs": len(pairs),
            "instances": len(inst), "tol": FMO_TOL, "max_iter": FMO_MAX_ITER,
-           "host_setup_s": t_setup}
+           "exciton": {"n_states": FMO_N_EXCITON, "tol": FMO_EX_TOL, "max_iter": FMO_EX_MAX_ITER,
+                       "basis": "%d LE per monomer + %d CT per pair direction" % (FMO_N_LE, FMO_N_CT),
+                       "real_pairs": len(setup.real_pairs)},
+           "host_setup_s": t_setup, "host_exciton_setup_s": t_exsetup}
     res = {}
     gctx = _lib.Context(ctx_device(ctx))
     n_mon = len(mons)
 
     def fmo_step(prec):
-        """Batched LE / CT TDA, then the gradient of S1, the lowest LE root of the aggregate
-        (its LE gradient, c = 1; the exciton couplings that would mix LE and CT states are not part
-        of this path)."""
+        """Batched LE / CT TDA; the exciton Hamiltonian over those states and its lowest 10 roots;
+        then the gradient of S1, the lowest LE root of the aggregate (its LE gradient, c = 1: the
+        CT and coupling terms of an exciton-state gradient are not built)."""
         rc, r = fmo.solve_batch(ctx, inst, FMO_MAX_ITER, FMO_TOL, prec)
         t_batch = ctx.last_timing()[0] / 1e3
+        ex = fmo.exciton_states(ctx, setup, r, labels, FMO_N_LE, FMO_N_CT, n_roots=FMO_N_EXCITON, tol=FMO_EX_TOL,
+                                max_iter=FMO_EX_MAX_ITER, precision=prec)
+        t_ex = ctx.last_timing()[0] / 1e3
         k1 = int(np.argmin([r[k]["energies"][0] for k in range(n_mon)]))
         states = [None] * n_mon
         states[k1] = 0
         g = fmo.le_gradients(mons, r[:n_mon], states, contexts=[gctx], precision=prec)
         t_grad = gctx.last_timing()[0] / 1e3
-        return rc, r, g[k1], k1, t_batch, t_grad
+        return rc, r, g[k1], k1, t_batch, t_grad, ex, t_ex
 
     for name, prec in (("bf16x3", _lib.PREC_BF16X3), ("fp64", _lib.PREC_FP64)):
         for _ in range(max(1, args.warmup)):
             fmo_step(prec)
-        dev, wall, tb, tg = [], [], [], []
+        dev, wall, tb, tg, te = [], [], [], [], []
         for _ in range(args.steps):
             t0 = time.perf_counter()
-            rc, r, g1, k1, t_batch, t_grad = fmo_step(prec)
+            rc, r, g1, k1, t_batch, t_grad, ex, t_ex = fmo_step(prec)
             wall.append(time.perf_counter() - t0)
-            dev.append(t_batch + t_grad)
+            dev.append(t_batch + t_ex + t_grad)
             tb.append(t_batch)
             tg.append(t_grad)
-        res[name] = (float(np.mean(dev)), float(np.mean(wall)), rc, r, g1, k1, float(np.mean(tb)), float(np.mean(tg)))
+            te.append(t_ex)
+        res[name] = (float(np.mean(dev)), float(np.mean(wall)), rc, r, g1, k1, float(np.mean(tb)), float(np.mean(tg)),
+                     ex, float(np.mean(te)))
     gctx.close()
-    dm, wm, rcm, rm, gm, km, tbm, tgm = res["bf16x3"]
-    d64, w64, rc64, r64, g64, k64, tb64, tg64 = res["fp64"]
+    dm, wm, rcm, rm, gm, km, tbm, tgm, exm, tem = res["bf16x3"]
+    d64, w64, rc64, r64, g64, k64, tb64, tg64, ex64, te64 = res["fp64"]
+    out["exciton"].update({
+        "energies_eh": [float(e) for e in exm["energies"]], "davidson_iterations": int(exm["iterations"]),
+        "status_ok": bool(exm["status"] == _lib.OK and ex64["status"] == _lib.OK),
+        "max_abs_energy_err_vs_fp64_eh": float(np.abs(exm["energies"] - ex64["energies"]).max())})
     out.update({
         "value_monomers_per_s": len(mons) / dm, "unit": "monomers/s",
-        "step_ms": dm * 1e3, "batch_tda_ms": tbm * 1e3, "s1_gradient_ms": tgm * 1e3,
+        "step_ms": dm * 1e3, "batch_tda_ms": tbm * 1e3, "exciton_ms": tem * 1e3, "s1_gradient_ms": tgm * 1e3,
         "instances_per_s": len(inst) / tbm,
         "e2e": {"value": len(mons) / wm, "unit": "monomers/s", "wall_ms": wm * 1e3},
         "fp64_gpu": {"value": len(mons) / d64, "step_ms": d64 * 1e3, "batch_tda_ms": tb64 * 1e3,
-                     "s1_gradient_ms": tg64 * 1e3, "e2e_wall_ms": w64 * 1e3},
+                     "exciton_ms": te64 * 1e3, "s1_gradient_ms": tg64 * 1e3, "e2e_wall_ms": w64 * 1e3},
         "speedup_mixed_vs_fp64": d64 / dm,
         "status_ok": bool(rcm == _lib.OK and rc64 == _lib.OK),
         "max_abs_energy_err_eh": float(max(np.abs(a["energies"] - b["energies"]).max() for a, b in zip(rm, r64))),
@@ -496,8 +527,15 @@ def run_fmo(args, ctx):
                 if km == int(fx["s1_monomer"]) else None,
                 "fp64_s1_le_grad_err_eh_per_bohr": float(np.abs(g64 - fx["s1_le_gradient"]).max())
                 if k64 == int(fx["s1_monomer"]) else None}
+            if "exciton_energies" in fx.files:
+                out["parity"]["exciton_oracle"] = ("oracle exciton Hamiltonian over the oracle's LE / CT roots, "
+                                                   "its Davidson at the same settings")
+                out["parity"]["mixed_exciton_energy_err_eh"] = [
+                    float(x) for x in np.abs(exm["energies"] - fx["exciton_energies"])]
+                out["parity"]["fp64_exciton_max_energy_err_eh"] = float(
+                    np.abs(ex64["energies"] - fx["exciton_energies"]).max())
     if args.cpu_baseline:
-        total, sample = fmo_cpu_reference(mons, inst, labels)
+        total, sample, _ = fmo_cpu_reference(mons, pairs, inst, labels, setup)
         out["cpu_baseline"] = {"value": len(mons) / total, "unit": "monomers/s", "step_s": total,
                                "cores": os.cpu_count(), "kind": "port", "sample": sample}
     return out
@@ -664,9 +702,11 @@ def run_reference(args):
                          rec["gradient_s"], args.steps))
     fmo_ref = None
     if args.fmo:
+        from tincr_gb300 import fmo
         mons, pairs, inst, labels = fmo_workload()
-        total, fsample = fmo_cpu_reference(mons, inst, labels)
-        fmo_ref = {"workload": "acene64-fmo-le4-ct1", "value_monomers_per_s": len(mons) / total,
+        setup = fmo.ExcitonSetup(mons, pairs, workers=os.cpu_count() or 1)
+        total, fsample, _ = fmo_cpu_reference(mons, pairs, inst, labels, setup)
+        fmo_ref = {"workload": "acene64-fmo-le4-ct1-exciton10", "value_monomers_per_s": len(mons) / total,
                    "unit": "monomers/s", "step_s": total, "cores": threads, "kind": "port", "sample": fsample}
     return {"impl": "reference", "metric": METRIC, "value": v, "unit": "s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": v * 1e3 / max(1, args.steps), "higher_is_better": False,

@@ -195,6 +195,34 @@ def diabatic_basis(agg, le_results, ct_results, ct_pairs, n_le, n_ct):
     return states
 
 
+def aggregate_of(monomers, setup):
+    """The Aggregate of an FMO set-up: `monomers` carry .index, .system (ao_offset, n_occ, n_atoms,
+    xyz, numbers) and .ground (orbs, orbe, s); `setup` carries .real {(I, J): bool}, .s_block(I, J),
+    .gamma, .gamma_lr and .pair_scc (the host set-up of the GPU path provides these)."""
+    frags = []
+    off = 0
+    for m in monomers:
+        sy, g = m.system, m.ground
+        frags.append(Frag(m.index, np.arange(off, off + sy.n_atoms), sy.ao_offset, g.orbs, g.orbe, g.s, sy.n_occ,
+                          sy.xyz, sy.numbers))
+        off += sy.n_atoms
+    types = {k: ("pair" if v else "esd") for k, v in setup.real.items()}
+    return Aggregate(frags, setup.s_block, setup.gamma, setup.gamma_lr, types, setup.pair_scc)
+
+
+def basis_of(agg, labels, results, ct_pairs, n_le, n_ct):
+    """`diabatic_basis` from a solved work list: labels[k] = ("LE", I) or ("CT", h, l), results[k]
+    a dict with energies, coefficients and (CT) q_trans."""
+    le, ct = {}, {}
+    for k, lab in enumerate(labels):
+        r = results[k]
+        if lab[0] == "LE":
+            le[lab[1]] = (r["energies"], r["coefficients"])
+        else:
+            ct[(lab[1], lab[2])] = (r["energies"], r["coefficients"], r["q_trans"])
+    return diabatic_basis(agg, le, ct, ct_pairs, n_le, n_ct)
+
+
 # ----------------------------------------------------------------------------------------------
 # transition charges between orbitals of two monomers
 # ----------------------------------------------------------------------------------------------
@@ -352,6 +380,50 @@ def exciton_hamiltonian(agg, states, fock=None, off=None):
     for i in range(dim):
         for j in range(i, dim):
             h[i, j] = exciton_coupling(agg, fock, off, states[i], states[j])
+    return h + h.T - np.diag(np.diag(h))
+
+
+_ROWS = {}
+
+
+def _rows_init(agg, states, fock, off):
+    _ROWS.update(agg=agg, states=states, fock=fock, off=off)
+
+
+def _row(i):
+    st = _ROWS["states"]
+    return i, [exciton_coupling(_ROWS["agg"], _ROWS["fock"], _ROWS["off"], st[i], st[j]) for j in range(i, len(st))]
+
+
+def exciton_hamiltonian_rows(agg, states, workers, fock=None, off=None):
+    """`exciton_hamiltonian` with the rows of the upper triangle shared out to `workers` processes,
+    as tincr shares them out to rayon threads (`states.par_iter()`, basis.rs:479-487).  Every element
+    is the same function of the same inputs, so the matrix equals the serial one.  The workers are
+    spawned with one BLAS thread each; the caller must run under a `__main__` guard."""
+    if fock is None:
+        fock, off = lcmo_fock(agg)
+    dim = len(states)
+    if workers <= 1:
+        return exciton_hamiltonian(agg, states, fock, off)
+    import multiprocessing as mp
+    import os
+    from concurrent.futures import ProcessPoolExecutor
+    names = ("OMP_NUM_THREADS", "OPENBLAS_NUM_THREADS", "MKL_NUM_THREADS")
+    saved = {k: os.environ.get(k) for k in names}
+    os.environ.update({k: "1" for k in names})
+    h = np.zeros((dim, dim))
+    try:
+        with ProcessPoolExecutor(max_workers=workers, mp_context=mp.get_context("spawn"), initializer=_rows_init,
+                                 initargs=(agg, states, fock, off)) as ex:
+            # long rows first, so the short ones fill in at the end
+            for i, row in ex.map(_row, range(dim), chunksize=max(1, dim // (16 * workers))):
+                h[i, i:] = row
+    finally:
+        for k, v in saved.items():
+            if v is None:
+                os.environ.pop(k, None)
+            else:
+                os.environ[k] = v
     return h + h.T - np.diag(np.diag(h))
 
 

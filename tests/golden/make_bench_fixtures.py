@@ -23,9 +23,12 @@ on this machine's CPU, once:
   pairs closer than 4.5 A x 1 CT root; tolerance 1e-4, max_iter 150): per-instance energies,
   oscillator strengths and Davidson iterations of the oracle engines (`TdaEngine` for a monomer,
   `CtEngine` for a pair direction: src/excited_states/solvers/mod.rs:59-269, davidson.rs:53-185),
-  and the excitation gradient of the lowest LE root of the aggregate (tincr's
-  `Monomer::tda_gradient_lc`, src/fmo/gradients/excited_state.rs:299-542).  Monomer orbital
-  energies are stored as an input check.
+  the excitation gradient of the lowest LE root of the aggregate (tincr's
+  `Monomer::tda_gradient_lc`, src/fmo/gradients/excited_state.rs:299-542), and the lowest 10
+  roots of the exciton Hamiltonian over those LE / CT states (oracle.exciton: LCMO Fock matrix,
+  couplings, tincr's Davidson at tolerance 1e-4 and 100 iterations, src/fmo/lcmo/basis.rs:449-503),
+  with the host set-up of the pair types, overlaps, gamma matrices and dimer ground states
+  (`fmo.ExcitonSetup`).  Monomer orbital energies are stored as an input check.
 """
 
 import os
@@ -89,9 +92,11 @@ def acene64():
     from cases import fmo_oracle_engine, oracle_gradient_inputs
     from oracle import gradients as OG
     from oracle import tda as OT
+    from oracle import exciton as OX
+    from tincr_gb300 import fmo
     mons, pairs, inst, labels = bench.fmo_workload()
     t0 = time.perf_counter()
-    e, f, its, nr = [], [], [], []
+    e, f, its, nr, res = [], [], [], [], []
     case = dict(monomers=mons, labels=labels, lc=True)
     for k, q in enumerate(inst):
         eng, _ = fmo_oracle_engine(case, k)
@@ -100,7 +105,17 @@ def acene64():
         f.append(r["f"])
         its.append(r["iterations"])
         nr.append(q["n_roots"])
+        res.append(r)
     t_tda = time.perf_counter() - t0
+    setup = fmo.ExcitonSetup(mons, pairs, workers=os.cpu_count() or 1)
+    t0 = time.perf_counter()
+    agg = OX.aggregate_of(mons, setup)
+    states = OX.basis_of(agg, labels, res, setup.ct_pairs, bench.FMO_N_LE, bench.FMO_N_CT)
+    h = OX.exciton_hamiltonian_rows(agg, states, os.cpu_count() or 1)
+    ex_e, _, ex_it = OX.exciton_states(h, bench.FMO_N_EXCITON, bench.FMO_EX_TOL, bench.FMO_EX_MAX_ITER)
+    t_ex = time.perf_counter() - t0
+    print("acene64 exciton: %d states, %d Davidson iterations, %.1f s, lowest %.8f Eh"
+          % (len(states), ex_it, t_ex, ex_e[0]))
     n_mon = len(mons)
     k1 = int(np.argmin([e[k][0] for k in range(n_mon)]))
     m = mons[k1]
@@ -122,7 +137,8 @@ def acene64():
                         n_roots=np.array(nr), kinds=np.array([0 if l[0] == "LE" else 1 for l in labels]),
                         monomer_orbe=np.concatenate([mm.ground.orbe for mm in mons]),
                         s1_monomer=k1, s1_le_gradient=gex, tol=bench.FMO_TOL, max_iter=bench.FMO_MAX_ITER,
-                        oracle_seconds=np.array([t_tda, t_grad]))
+                        exciton_energies=ex_e, exciton_iterations=ex_it, exciton_dim=len(states),
+                        oracle_seconds=np.array([t_tda, t_grad, t_ex]))
 
 
 if __name__ == "__main__":

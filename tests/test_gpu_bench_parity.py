@@ -9,12 +9,18 @@ once on the CPU and committed as fixtures (tests/golden/make_bench_fixtures.py).
     installed, the gradient within 1e-7 Eh/bohr (formula parity at full size, independent of the
     Davidson).
   - mixed form (split-BF16 tensor-core products, FP64 subspace) at the bench's residual 1e-4:
-    every root within 1e-6 Eh, oscillator strengths within 1e-5, the S1 gradient within
-    1e-5 Eh/bohr.
+    every root within 1e-6 Eh and the S1 gradient within 1e-5 Eh/bohr of the oracle. Oscillator
+    strengths are checked twice: within 1e-6 of the FP64 form run at the same residual 1e-4 (the
+    error of the mixed arithmetic), and within 5e-5 of the oracle's converged roots. At residual
+    1e-4 a root's vector is converged only to about the residual over the gap to its neighbours,
+    so its strength moves by up to ~1e-5 in either form (1.4e-5 on root 18 of 20).
 * the 64-acene FMO work list (632 LE / CT instances): every root of every instance within 1e-8 Eh
   (FP64, with the oracle's iteration count per instance, oscillator strengths within 1e-8) or
   1e-6 Eh (mixed, oscillator strengths within 1e-5), and the LE gradient of the aggregate's lowest
   root within 1e-5 Eh/bohr.
+* the exciton Hamiltonian of that aggregate (824 diabatic states: 4 LE per monomer, 1 CT per pair
+  direction) built from the GPU batch's roots, and its lowest 10 states: within 1e-8 Eh (FP64) or
+  1e-6 Eh (mixed) of the oracle's, which built the matrix from the oracle's own LE / CT roots.
 
 The inputs are rebuilt here from the same seeds with the host SCC; the orbital energies are first
 checked against the fixture's, so that a difference in the ground state cannot pass for a kernel
@@ -53,7 +59,7 @@ def acenes():
     mons, pairs, inst, labels = bench.fmo_workload()
     orbe = np.concatenate([m.ground.orbe for m in mons])
     assert np.abs(orbe - fx["monomer_orbe"]).max() < 1e-8, "monomer ground states differ from the fixture's"
-    return mons, inst, labels, fx
+    return mons, inst, labels, fx, pairs
 
 
 def _solve(ctx, sy, g, prec, fx, tol):
@@ -90,14 +96,18 @@ def test_water128_mixed_matches_oracle(gpu_ctx, water):
     _, r = _solve(gpu_ctx, sy, g, _lib.PREC_BF16X3, fx, bench.TOL)
     de = np.abs(r["e"] - fx["energies"])
     assert de.max() < 1e-6, "per-root |dE| %s" % de
-    assert np.abs(r["f"] - fx["f"]).max() < 1e-5
     ref = fx["grad_ground"] + fx["grad_excited"]
     assert np.abs(r["grad"] - ref).max() < 1e-5
+    _, r64 = _solve(gpu_ctx, sy, g, _lib.PREC_FP64, fx, bench.TOL)
+    df_prec = np.abs(r["f"] - r64["f"])
+    assert df_prec.max() < 1e-6, "per-root |df| against FP64 at the same residual %s" % df_prec
+    df = np.abs(r["f"] - fx["f"])
+    assert df.max() < 5e-5, "per-root |df| against the converged oracle roots %s" % df
 
 
 @pytest.mark.parametrize("prec", [_lib.PREC_FP64, _lib.PREC_BF16X3])
 def test_acene64_batch_matches_oracle(gpu_ctx, acenes, prec):
-    mons, inst, labels, fx = acenes
+    mons, inst, labels, fx, _ = acenes
     rc, res = fmo.solve_batch(gpu_ctx, inst, int(fx["max_iter"]), float(fx["tol"]), prec)
     assert rc == _lib.OK
     e = np.concatenate([r["energies"] for r in res])
@@ -116,3 +126,27 @@ def test_acene64_batch_matches_oracle(gpu_ctx, acenes, prec):
     states[k1] = 0
     g = fmo.le_gradients(mons, res[:n_mon], states, contexts=[gpu_ctx], precision=prec)
     assert np.abs(g[k1] - fx["s1_le_gradient"]).max() < 1e-5
+
+
+@pytest.fixture(scope="module")
+def exciton_setup(acenes):
+    import os
+    mons, inst, labels, fx, pairs = acenes
+    return fmo.ExcitonSetup(mons, pairs, workers=os.cpu_count() or 1)
+
+
+@pytest.mark.parametrize("prec", [_lib.PREC_FP64, _lib.PREC_BF16X3])
+def test_acene64_exciton_states_match_oracle(gpu_ctx, acenes, exciton_setup, prec):
+    import bench
+    mons, inst, labels, fx, _ = acenes
+    if "exciton_energies" not in fx.files:
+        pytest.skip("fixture without exciton energies")
+    rc, res = fmo.solve_batch(gpu_ctx, inst, int(fx["max_iter"]), float(fx["tol"]), prec)
+    assert rc == _lib.OK
+    out = fmo.exciton_states(gpu_ctx, exciton_setup, res, labels, bench.FMO_N_LE, bench.FMO_N_CT,
+                             n_roots=bench.FMO_N_EXCITON, tol=bench.FMO_EX_TOL, max_iter=bench.FMO_EX_MAX_ITER,
+                             precision=prec)
+    assert out["status"] == _lib.OK
+    assert out["vectors"].shape[0] == int(fx["exciton_dim"])
+    de = np.abs(out["energies"] - fx["exciton_energies"])
+    assert de.max() < (1e-8 if prec == _lib.PREC_FP64 else 1e-6), "per-state |dE| %s" % de

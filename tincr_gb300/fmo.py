@@ -16,6 +16,7 @@ The monomer ground states come from the host SCC of the isolated monomers (tincr
 the electrostatic embedding of the other monomers, src/fmo/scc; that step precedes the TDA path).
 """
 
+import os
 import weakref
 
 import numpy as np
@@ -386,8 +387,20 @@ class ExcitonSetup:
         if workers > 1 and len(jobs) > 1:
             import multiprocessing as mp
             from concurrent.futures import ProcessPoolExecutor
-            with ProcessPoolExecutor(max_workers=workers, mp_context=mp.get_context("spawn")) as ex:
-                out = list(ex.map(_dimer_scc, jobs, chunksize=4))
+            # one BLAS thread per worker: the workers already fill the cores, and a full-width BLAS
+            # pool in each of them oversubscribes the host by workers x cores threads
+            names = ("OMP_NUM_THREADS", "OPENBLAS_NUM_THREADS", "MKL_NUM_THREADS")
+            saved = {k: os.environ.get(k) for k in names}
+            os.environ.update({k: "1" for k in names})
+            try:
+                with ProcessPoolExecutor(max_workers=workers, mp_context=mp.get_context("spawn")) as ex:
+                    out = list(ex.map(_dimer_scc, jobs, chunksize=4))
+            finally:
+                for k, v in saved.items():
+                    if v is None:
+                        os.environ.pop(k, None)
+                    else:
+                        os.environ[k] = v
         else:
             out = [_dimer_scc(a) for a in jobs]
         self.pair_scc = {k: o for k, o in zip(self.real_pairs, out)}
