@@ -113,3 +113,26 @@ def test_lcmo_fock_without_real_pairs_is_diagonal(agg3):
                        {k: "esd" for k in agg.pair_types}, {})
     fock, off = OX.lcmo_fock(esd)
     assert np.allclose(fock, np.diag(np.concatenate([f.orbe for f in agg.frags])), atol=0, rtol=0)
+
+
+def test_dimer_scc_from_monomer_densities():
+    """The exciton set-up starts each dimer SCC from its two monomers' converged densities (tincr
+    starts a pair SCC from its monomers' charges); it must reach the ground state the neutral-atom
+    start reaches, and an SCC that misses its tolerance must say so (tincr panics there)."""
+    c = fmo_case(2, 1, 1)
+    a, b = c["monomers"]
+    sy = gs.build_system(np.concatenate([a.system.numbers, b.system.numbers]),
+                         np.concatenate([a.system.xyz, b.system.xyz]), lc=True, r_lr=a.system.r_lr)
+    ref = gs.run_scc(sy, tol=1e-10)
+    assert ref.converged
+    na = a.system.n_orbs
+    p_start = np.zeros_like(ref.p)
+    p_start[:na, :na] = a.ground.p
+    p_start[na:, na:] = b.ground.p
+    g = gs.run_scc(sy, tol=1e-10, p_start=p_start, require_convergence=True)
+    assert g.converged and g.iterations < ref.iterations
+    assert abs(g.energy - ref.energy) < 1e-9
+    assert np.abs(g.orbe - ref.orbe).max() < 1e-8
+    assert not gs.run_scc(sy, tol=1e-10, max_iter=2).converged
+    with pytest.raises(RuntimeError):
+        gs.run_scc(sy, tol=1e-10, max_iter=2, require_convergence=True)

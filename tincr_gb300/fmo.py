@@ -42,19 +42,29 @@ def build_monomers(numbers, xyz_bohr, monomer_of_atom, lc=True, r_lr=gs.LONG_RAN
     for k in np.unique(monomer_of_atom):
         at = np.nonzero(monomer_of_atom == k)[0]
         sy = gs.build_system(numbers[at], xyz_bohr[at], lc=lc, r_lr=r_lr)
-        mons.append(Monomer(int(k), at, sy, gs.run_scc(sy, tol=scc_tol)))
+        mons.append(Monomer(int(k), at, sy, gs.run_scc(sy, tol=scc_tol, require_convergence=True)))
     return mons
+
+
+def candidate_pairs(monomers, reach_bohr):
+    """Pairs (I, J), I < J, whose bounding spheres (centroid, largest centroid-atom distance) come
+    closer than `reach_bohr`: a superset of the pairs with an atom pair closer than that, found
+    without the atom-by-atom distances of every pair of a large aggregate."""
+    cen = np.array([m.system.xyz.mean(axis=0) for m in monomers])
+    rad = np.array([np.linalg.norm(m.system.xyz - c, axis=1).max() for m, c in zip(monomers, cen)])
+    d = np.linalg.norm(cen[:, None, :] - cen[None, :, :], axis=-1) - rad[:, None] - rad[None, :]
+    i, j = np.nonzero(np.triu(d < reach_bohr, 1))
+    return list(zip(i.tolist(), j.tolist()))
 
 
 def close_pairs(monomers, cutoff_bohr):
     """Pairs (I, J), I < J, whose smallest interatomic distance is below the cutoff."""
     out = []
-    for i, a in enumerate(monomers):
-        for j in range(i + 1, len(monomers)):
-            b = monomers[j]
-            d = np.linalg.norm(a.system.xyz[:, None, :] - b.system.xyz[None, :, :], axis=-1).min()
-            if d < cutoff_bohr:
-                out.append((i, j))
+    for i, j in candidate_pairs(monomers, cutoff_bohr):
+        a, b = monomers[i], monomers[j]
+        d = np.linalg.norm(a.system.xyz[:, None, :] - b.system.xyz[None, :, :], axis=-1).min()
+        if d < cutoff_bohr:
+            out.append((i, j))
     return out
 
 
@@ -335,10 +345,15 @@ def is_real_pair(ma, mb, vdw_scaling=2.0):
 
 
 def _dimer_scc(args):
-    """Host SCC of one dimer (top-level for a spawn process pool): returns (orbs, orbe)."""
-    z, xyz, lc, r_lr, tol = args
+    """Host SCC of one dimer (top-level for a spawn process pool): returns (orbs, orbe).  It starts
+    from the block-diagonal density of the two converged monomers, as tincr starts a pair SCC from
+    its monomers' charges (src/fmo/scc/pair.rs:112-124), and raises if it does not converge (tincr
+    panics, pair.rs:234-240): from the neutral-atom density a few dimers of a dense aggregate stall
+    past the iteration limit, and an unconverged dimer would hand machine-dependent orbitals to the
+    LCMO Fock matrix."""
+    z, xyz, lc, r_lr, tol, p_start = args
     sy = gs.build_system(z, xyz, lc=lc, r_lr=r_lr)
-    g = gs.run_scc(sy, tol=tol)
+    g = gs.run_scc(sy, tol=tol, p_start=p_start, require_convergence=True)
     return g.orbs, g.orbe
 
 
@@ -357,10 +372,10 @@ class ExcitonSetup:
         self.monomers = monomers
         self.ct_pairs = list(ct_pairs)
         n = len(monomers)
-        self.real = {}
-        for i in range(n):
-            for j in range(i + 1, n):
-                self.real[(i, j)] = is_real_pair(monomers[i], monomers[j])
+        self.real = {(i, j): False for i in range(n) for j in range(i + 1, n)}
+        reach = 2.0 * max(VDW_SUM_BOHR.values())   # no atom pair farther apart than this is a real pair
+        for i, j in candidate_pairs(monomers, reach):
+            self.real[(i, j)] = is_real_pair(monomers[i], monomers[j])
         sy0 = monomers[0].system
         self.lc, self.r_lr = lc, sy0.r_lr
         z = np.concatenate([m.system.numbers for m in monomers])
@@ -382,8 +397,12 @@ class ExcitonSetup:
         self.real_pairs = sorted(k for k, v in self.real.items() if v)
         for i, j in self.real_pairs:
             mi, mj = monomers[i], monomers[j]
+            ni, nj = mi.system.n_orbs, mj.system.n_orbs
+            p_start = np.zeros((ni + nj, ni + nj))
+            p_start[:ni, :ni] = mi.ground.p
+            p_start[ni:, ni:] = mj.ground.p
             jobs.append((np.concatenate([mi.system.numbers, mj.system.numbers]),
-                         np.concatenate([mi.system.xyz, mj.system.xyz]), lc, self.r_lr, scc_tol))
+                         np.concatenate([mi.system.xyz, mj.system.xyz]), lc, self.r_lr, scc_tol, p_start))
         if workers > 1 and len(jobs) > 1:
             import multiprocessing as mp
             from concurrent.futures import ProcessPoolExecutor

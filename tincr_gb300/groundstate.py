@@ -271,10 +271,14 @@ class GroundState:
     h_coul_x: np.ndarray       # converged SCC Hamiltonian (H0 + H1 o S + H^x)
     energy: float
     iterations: int
+    converged: bool = True
 
 
-def run_scc(sysm, tol=1e-10, max_iter=250, s_h0=None):
-    """Restricted closed-shell SCC to ||[F, P]|| < tol."""
+def run_scc(sysm, tol=1e-10, max_iter=250, s_h0=None, p_start=None, require_convergence=False):
+    """Restricted closed-shell SCC to ||[F, P]|| < tol, from the reference (neutral-atom) density or
+    from `p_start` (tincr starts a pair SCC from its monomers' charges, src/fmo/scc/pair.rs:112-124).
+    The result's `converged` says whether the test was met within max_iter iterations; with
+    `require_convergence` a miss raises RuntimeError (tincr panics there, pair.rs:234-240)."""
     s, h0 = s_h0 if s_h0 is not None else h0_and_s(sysm)
     gamma = gamma_atomwise(sysm, 0.0)
     gamma_lr = gamma_atomwise(sysm, sysm.r_lr) if sysm.lc else np.zeros_like(gamma)
@@ -283,9 +287,10 @@ def run_scc(sysm, tol=1e-10, max_iter=250, s_h0=None):
     w, v = np.linalg.eigh(s)
     x = (v / np.sqrt(w)) @ v.T
     n_occ = sysm.n_elec // 2
-    p = p0.copy()
+    p = p0.copy() if p_start is None else np.array(p_start, dtype=float)
     hist_f, hist_e = [], []
     it = 0
+    converged = False
     orbs = orbe = f = None
     for it in range(1, max_iter + 1):
         dp = p - p0
@@ -303,6 +308,7 @@ def run_scc(sysm, tol=1e-10, max_iter=250, s_h0=None):
             hist_f.pop(0)
             hist_e.pop(0)
         if it > 1 and errn < tol:
+            converged = True
             break
         m = len(hist_f)
         if m > 1:
@@ -324,6 +330,8 @@ def run_scc(sysm, tol=1e-10, max_iter=250, s_h0=None):
         orbs = x @ cp
         occ_c = orbs[:, :n_occ]
         p = 2.0 * occ_c @ occ_c.T
+    if require_convergence and not converged:
+        raise RuntimeError("SCC not converged to %g in %d iterations" % (tol, max_iter))
     # final diagonalisation of the converged Fock matrix
     orbe, cp = np.linalg.eigh(x.T @ f @ x)
     orbs = x @ cp
@@ -336,4 +344,4 @@ def run_scc(sysm, tol=1e-10, max_iter=250, s_h0=None):
         e_el += -0.125 * float(np.sum((s @ dp @ s) * dp * g_lr_ao) + np.sum((s @ dp) * (dp @ s) * g_lr_ao))
     return GroundState(s=s, h0=h0, gamma=gamma, gamma_lr=gamma_lr, orbs=np.ascontiguousarray(orbs),
                        orbe=orbe, p=p, p0=p0, dq=dq, h_coul_x=f, energy=e_el + repulsive_energy(sysm),
-                       iterations=it)
+                       iterations=it, converged=converged)
