@@ -1367,23 +1367,6 @@ __global__ void __cluster_dims__(BT_CL, 1, 1) __launch_bounds__(BT_T)
 // host
 // ----------------------------------------------------------------------------------------------
 
-// page-locked host staging buffer (grow-only): uploads from it are plain DMA
-struct PinnedBuf {
-    double *p = nullptr;
-    size_t n = 0;
-    void reserve(size_t count) {
-        if (count <= n && p) return;
-        if (p) cudaFreeHost(p);
-        p = nullptr;
-        n = 0;
-        TINCR_CUDA(cudaMallocHost(&p, std::max<size_t>(1, count) * sizeof(double)));
-        n = std::max<size_t>(1, count);
-    }
-    ~PinnedBuf() {
-        if (p) cudaFreeHost(p);
-    }
-};
-
 // the four plane GEMM steps of the mixed product
 enum BpStep { BP_P1 = 0, BP_P2 = 1, BP_P4 = 2, BP_P5 = 3, BP_STEPS = 4 };
 

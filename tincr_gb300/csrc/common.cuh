@@ -62,6 +62,26 @@ struct DevBuf {
     T *get() const { return p; }
 };
 
+// page-locked host staging buffer (grow-only): uploads from it are plain DMA
+struct PinnedBuf {
+    double *p = nullptr;
+    size_t n = 0;
+    PinnedBuf() = default;
+    PinnedBuf(const PinnedBuf &) = delete;
+    PinnedBuf &operator=(const PinnedBuf &) = delete;
+    void reserve(size_t count) {
+        if (count <= n && p) return;
+        if (p) cudaFreeHost(p);
+        p = nullptr;
+        n = 0;
+        TINCR_CUDA(cudaMallocHost(&p, (count ? count : 1) * sizeof(double)));
+        n = count ? count : 1;
+    }
+    ~PinnedBuf() {
+        if (p) cudaFreeHost(p);
+    }
+};
+
 inline int ceil_div(long long a, long long b) { return int((a + b - 1) / b); }
 
 }  // namespace tincr

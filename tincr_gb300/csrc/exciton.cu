@@ -24,6 +24,7 @@
 #include <algorithm>
 #include <cmath>
 #include <map>
+#include <unordered_map>
 #include <vector>
 
 #include "tda.cuh"
@@ -195,8 +196,28 @@ __global__ void ex_symmetrize_kernel(int n, double *H) {
 }
 
 // ----------------------------------------------------------------------------------------------
-// exchange jobs
+// exchange integrals
 // ----------------------------------------------------------------------------------------------
+//
+// An element (s, t) pairs occupied-side charges q^A_ij between columns P = [p0, p0 + np) of monomer
+// x1's C and Q = [q0, q0 + nq) of y1's C (atoms A of {x1, y1}) with virtual-side charges q^B_ab
+// between columns P' = [pa0, pa0 + na) of x2 and Q' = [qb0, qb0 + nb) of y2 (atoms B of {x2, y2}),
+// through the state vectors b1(i, a) of s and b2(j, b) of t:
+//   exchange = sum_{A, B} gamma_lr[A, B] sum_{a, j} U^A_aj W^B_aj,
+//   U^A_aj = sum_i q^A_ij b1(i, a) = 1/2 sum_{mu in A} (L1c[mu, a] R1s[mu, j] + L1s[mu, a] R1c[mu, j]),
+//   W^B_aj = sum_b q^B_ab b2(j, b) = 1/2 sum_{nu in B} (L2c[nu, a] R2s[nu, j] + L2s[nu, a] R2c[nu, j]),
+// with per-AO rows L1c = C_P b1, L1s = (S C)_P b1 (state s), R1c = C_Q, R1s = (S C)_Q, L2c = C_P',
+// L2s = (S C)_P', R2c = C_Q' b2^T, R2s = (S C)_Q' b2^T (state t); on the other monomer of a pair,
+// C is zero and S C is the cross product S_yx C_x.  The passes:
+//   1. side-1 arrays L1c, L1s per (state s, partner monomer) and side-2 arrays R2c, R2s per (state t,
+//      monomer set): batched small GEMMs (ex_gemm_kernel) into FP64 scratch;
+//   2. one CTA per side-2 group and ta x tj tile of (a, j) (ta tj <= 128) (ex_vu_kernel): the tile's
+//      L2 / R2 rows staged in shared memory, W formed there, then the gamma block in the staging area
+//      and V^A_aj = sum_B gamma_lr[A, B] W^B_aj accumulated in registers per block of atoms A and kept
+//      in shared memory; then for each element (s, t) of the group, s's L1 rows and the R1 rows
+//      staged, sum_A U^A_aj V^A_aj, block sum, added to H.
+// A side-2 group (t, its monomers, the side-1 monomers) serves every s paired with it: the four LE
+// states of a monomer against one LE or CT state share V, which is formed once.
 
 // Per-monomer device views: C and S C ([n x n], row-major, columns = MOs), atom range, AO offsets.
 struct ExMono {
@@ -205,186 +226,250 @@ struct ExMono {
     int n, n_atoms, atom0;
 };
 
-// One exchange tile: element (s, t); side 1 holds the charges between the occupied columns P of
-// monomer x1 and Q of y1, side 2 between the virtual columns P' of x2 and Q' of y2.
-//   b1(i, a) = X1[(i1 + i) * ld1 + a1 + a]  (state s: i over P, a over P')
-//   b2(j, b) = X2[(j2 + j) * ld2 + b2 + b]  (state t: j over Q, b over Q')
-// The tile covers a in [ta0, ta0 + ta), j in [tj0, tj0 + tj), ta * tj <= XJ_T.
-struct ExJob {
-    int s, t;
-    int x1, y1, x2, y2;
-    int p0, np, q0, pa0, qb0, nb;
-    int ta0, ta, tj0, tj;
-    const double *X1, *X2;
-    int ld1, i1, a1, ld2, j2, b2;
-    const double *cross_xy1, *cross_yx1;   // S_x1y1 C_y1 [n_x1 x n_y1], S_y1x1 C_x1 [n_y1 x n_x1] (x1 != y1)
-    const double *cross_xy2, *cross_yx2;   // the same for x2, y2
+// side-1 group: the occupied-side arrays of one state against one partner monomer
+struct ExS1 {
+    int x1, y1;                      // monomers (y1 == x1: one monomer)
+    int p0, np, q0, na;              // columns P of x1, Q of y1 (start), a extent
+    const double *X1;                // b1(i, a) = X1[(i1 + i) * ld1 + a1 + a]
+    int ld1, i1, a1;
+    const double *cross_yx1;         // S_y1x1 C_x1 [n_y1 x n_x1] (two monomers)
+    const double *cross_xy1;         // S_x1y1 C_y1 [n_x1 x n_y1] (two monomers)
+    long long own;                   // rows of x1: L1c at own, L1s at own + n_x1 na, [mu][a] (per state)
+    long long crs;                   // rows of y1: L1s at crs, [mu - n_x1][a] (per state and y1; L1c = 0)
 };
 
-constexpr int XJ_T = 128;          // threads = the largest (a, j) tile
-constexpr int XJ_TMAX = 16;        // largest tile side
-constexpr int XJ_AO = 2 * 102 + 4; // AOs of two monomers (largest supported monomer: 102 AOs)
-constexpr int XJ_ATOMS = 80;       // atoms of two monomers
-
-template <class T>
-struct XjSmem {
-    T L1[XJ_AO][XJ_TMAX], L2[XJ_AO][XJ_TMAX];   // Lc, Ls (side 1) or L'c, L's (side 2)
-    T R1[XJ_AO][XJ_TMAX], R2[XJ_AO][XJ_TMAX];   // Rc, Rs (side 1) or R'c, R's (side 2)
-    T V[XJ_ATOMS][XJ_T];                        // V^A = sum_B gamma_lr[A, B] W^B per (a, j)
-    T red[XJ_T / 32];
+// side-2 group: the virtual-side arrays and V of one state against one monomer set
+struct ExS2 {
+    int x1, y1;                      // side-1 monomers: the atoms A of V
+    int x2, y2;
+    int pa0, na, qb0, nb, nq;
+    int ta, tj;                      // tile sides over a and j (ta tj <= XJ_T)
+    const double *X2;                // b2(j, b) = X2[(j2 + j) * ld2 + b2 + b]
+    int ld2, j2, b2;
+    const double *cross_xy2, *cross_yx2;
+    long long own;                   // rows of y2 (x2 = y2: all rows): R2c at own, R2s at own + n_y2 nq, [nu][j]
+    long long crs;                   // rows of x2 when x2 != y2: R2s at crs, [nu][j] (per state and x2; R2c = 0)
 };
 
-// AO row mu of the fragment {x, y} (x's AOs first; y only when y != x): monomer and local row
-__device__ __forceinline__ void frag_row(const ExMono &mx, const ExMono &my, bool two, int mu, int &which, int &row) {
-    if (!two || mu < mx.n) {
-        which = 0;
-        row = mu;
-    } else {
-        which = 1;
-        row = mu - mx.n;
-    }
+struct ExEl {
+    int s, t;                        // matrix element (s < t)
+    int k1, k2;                      // side-1 and side-2 groups
+};
+
+constexpr int XJ_T = 128;            // threads per CTA: the largest (a, j) tile
+constexpr int XJ_TS = 16;            // largest tile side
+constexpr int XJ_AO = 2 * 102 + 4;   // AOs of two monomers (largest supported monomer: 102 AOs)
+constexpr int XJ_ATOMS = 80;         // atoms of two monomers (largest supported monomer: 40 atoms)
+
+__device__ __forceinline__ int ex_nao(const ExMono &x, const ExMono &y, bool two) { return x.n + (two ? y.n : 0); }
+__device__ __forceinline__ int ex_nat(const ExMono &x, const ExMono &y, bool two) {
+    return x.n_atoms + (two ? y.n_atoms : 0);
 }
 
+// Shared memory of ex_vu_kernel, by phase (every array [row][tile column]; byte offsets):
+//   A: W [0, W) | L2 / R2 staging [W, W + ST)
+//   B: W [0, W) | gamma block [W, W + G) | V [W + G, W + G + V)
+//   C: L1 / R1 staging [0, ST) | V
+// FP64: 215 KB, FP32: 108 KB.
 template <class T>
-__global__ void __launch_bounds__(XJ_T) ex_exchange_kernel(const ExJob *__restrict__ jobs, const ExMono *__restrict__ mono,
-                                                           const double *__restrict__ gamma_lr, int n_atoms_total,
-                                                           double *H, int n_states) {
-    extern __shared__ __align__(16) unsigned char xj_raw[];
-    XjSmem<T> &sm = *reinterpret_cast<XjSmem<T> *>(xj_raw);
-    const ExJob J = jobs[blockIdx.x];
-    const int tid = threadIdx.x;
-    const int ntile = J.ta * J.tj;
-    const int my_a = tid / J.tj, my_j = tid % J.tj;
-    const bool active = tid < ntile;
+struct ExVUSmem {
+    static constexpr size_t W_BYTES = sizeof(T) * XJ_ATOMS * XJ_T;
+    static constexpr size_t ST_BYTES = sizeof(T) * 4 * XJ_AO * XJ_TS;
+    static constexpr size_t G_BYTES = sizeof(T) * XJ_ATOMS * XJ_ATOMS;
+    static constexpr size_t V_OFF = W_BYTES + G_BYTES;
+    static constexpr size_t V_BYTES = sizeof(T) * XJ_ATOMS * XJ_T;
+    static constexpr size_t END =
+        W_BYTES + ST_BYTES > V_OFF + V_BYTES ? W_BYTES + ST_BYTES : V_OFF + V_BYTES;
+    static constexpr size_t BYTES = END + sizeof(double) * (XJ_T / 32);
+    static_assert(ST_BYTES <= V_OFF, "the side-1 staging of phase C would overlap V");
+    static_assert(BYTES <= 227 * 1024, "over the shared memory of one CTA");
+};
 
-    // ---- side 2 (virtual charges): L'c = P', L's = S P', R'c = Q' b2^T, R's = (S Q') b2^T ----
-    const ExMono m2x = mono[J.x2], m2y = mono[J.y2];
-    const bool two2 = J.x2 != J.y2;
-    const int nao2 = m2x.n + (two2 ? m2y.n : 0);
-    for (int e = tid; e < nao2 * J.ta; e += XJ_T) {
-        const int mu = e / J.ta, a = e % J.ta;
-        int w, r;
-        frag_row(m2x, m2y, two2, mu, w, r);
-        const int col = J.pa0 + J.ta0 + a;
-        T lc = T(0), ls = T(0);
-        if (w == 0) {
-            lc = (T)m2x.C[(long long)r * m2x.n + col];
-            ls = (T)m2x.SC[(long long)r * m2x.n + col];
-        } else {
-            ls = (T)J.cross_yx2[(long long)r * m2x.n + col];
+// one CTA per (side-2 group, ta x tj tile of (a, j)):
+//   V^A_aj = sum_B gamma_lr[A, B] W^B_aj, then for every element (s, t) of the group
+//   H[s, t] -= sum_A sum_aj U^A_aj(s) V^A_aj
+template <class T>
+__global__ void __launch_bounds__(XJ_T) ex_vu_kernel(const int4 *__restrict__ tiles, const ExS2 *__restrict__ keys,
+                                                     const int *__restrict__ el_begin, const ExEl *__restrict__ els,
+                                                     const ExS1 *__restrict__ k1s, const ExMono *__restrict__ mono,
+                                                     const double *__restrict__ gamma_lr, int n_atoms_total,
+                                                     const double *__restrict__ scr, double *H, int n_states) {
+    constexpr int CH = sizeof(T) == 4 ? 16 : 8;   // atoms A per register block
+    using L = ExVUSmem<T>;
+    extern __shared__ __align__(16) unsigned char xv_raw[];
+    T(*W)[XJ_T] = reinterpret_cast<T(*)[XJ_T]>(xv_raw);
+    T(*L2c)[XJ_TS] = reinterpret_cast<T(*)[XJ_TS]>(xv_raw + L::W_BYTES);
+    T(*L2s)[XJ_TS] = L2c + XJ_AO;
+    T(*R2c)[XJ_TS] = L2s + XJ_AO;
+    T(*R2s)[XJ_TS] = R2c + XJ_AO;
+    T(*G)[XJ_ATOMS] = reinterpret_cast<T(*)[XJ_ATOMS]>(xv_raw + L::W_BYTES);
+    T(*V)[XJ_T] = reinterpret_cast<T(*)[XJ_T]>(xv_raw + L::V_OFF);
+    T(*L1c)[XJ_TS] = reinterpret_cast<T(*)[XJ_TS]>(xv_raw);
+    T(*L1s)[XJ_TS] = L1c + XJ_AO;
+    T(*R1c)[XJ_TS] = L1s + XJ_AO;
+    T(*R1s)[XJ_TS] = R1c + XJ_AO;
+    double *red = reinterpret_cast<double *>(xv_raw + L::END);
+
+    const int4 tl = tiles[blockIdx.x];
+    const ExS2 K = keys[tl.x];
+    const int a0 = tl.y, j0 = tl.z, ta = K.ta, tj = K.tj;
+    const ExMono m1x = mono[K.x1], m1y = mono[K.y1], m2x = mono[K.x2], m2y = mono[K.y2];
+    const bool two1 = K.x1 != K.y1, two2 = K.x2 != K.y2;
+    const int nat1 = ex_nat(m1x, m1y, two1), nat2 = ex_nat(m2x, m2y, two2);
+    const int nao1 = ex_nao(m1x, m1y, two1), nao2 = ex_nao(m2x, m2y, two2);
+    const int al = threadIdx.x / tj, jl = threadIdx.x % tj;
+    const bool active = threadIdx.x < ta * tj && a0 + al < K.na && j0 + jl < K.nq;
+
+    // ---- phase A: L2 = C_P', (S C)_P' (S_y2x2 C_x2 on y2) and R2 (side-2 scratch); W ----
+#pragma unroll 4
+    for (int e = threadIdx.x; e < nao2 * ta; e += XJ_T) {
+        const int nu = e / ta, q = e % ta;
+        T c = T(0), sc = T(0);
+        if (a0 + q < K.na) {
+            const int col = K.pa0 + a0 + q;
+            if (nu < m2x.n) {
+                c = (T)m2x.C[(long long)nu * m2x.n + col];
+                sc = (T)m2x.SC[(long long)nu * m2x.n + col];
+            } else {
+                sc = (T)K.cross_yx2[(long long)(nu - m2x.n) * m2x.n + col];
+            }
         }
-        sm.L1[mu][a] = lc;
-        sm.L2[mu][a] = ls;
+        L2c[nu][q] = c;
+        L2s[nu][q] = sc;
     }
-    for (int e = tid; e < nao2 * J.tj; e += XJ_T) {
-        const int mu = e / J.tj, jj = e % J.tj;
-        int w, r;
-        frag_row(m2x, m2y, two2, mu, w, r);
-        const double *brow = J.X2 + (long long)(J.j2 + J.tj0 + jj) * J.ld2 + J.b2;
-        T rc = T(0), rs = T(0);
-        for (int b = 0; b < J.nb; ++b) {
-            const int col = J.qb0 + b;
-            const T bb = (T)brow[b];
-            if (two2) {
-                if (w == 1) {
-                    rc += (T)m2y.C[(long long)r * m2y.n + col] * bb;
-                    rs += (T)m2y.SC[(long long)r * m2y.n + col] * bb;
+    {
+        const int ny2 = two2 ? m2y.n : m2x.n;   // rows held by the per-state part
+        const double *rc = scr + K.own, *rs = rc + (long long)ny2 * K.nq;
+#pragma unroll 4
+        for (int e = threadIdx.x; e < nao2 * tj; e += XJ_T) {
+            const int nu = e / tj, q = e % tj;
+            T c = T(0), sc = T(0);
+            if (j0 + q < K.nq) {
+                const int j = j0 + q;
+                if (!two2) {
+                    c = (T)rc[(long long)nu * K.nq + j];
+                    sc = (T)rs[(long long)nu * K.nq + j];
+                } else if (nu < m2x.n) {
+                    sc = (T)scr[K.crs + (long long)nu * K.nq + j];
                 } else {
-                    rs += (T)J.cross_xy2[(long long)r * m2y.n + col] * bb;
+                    c = (T)rc[(long long)(nu - m2x.n) * K.nq + j];
+                    sc = (T)rs[(long long)(nu - m2x.n) * K.nq + j];
                 }
-            } else {
-                rc += (T)m2x.C[(long long)r * m2x.n + col] * bb;
-                rs += (T)m2x.SC[(long long)r * m2x.n + col] * bb;
             }
+            R2c[nu][q] = c;
+            R2s[nu][q] = sc;
         }
-        sm.R1[mu][jj] = rc;
-        sm.R2[mu][jj] = rs;
     }
-    // atoms of side 1 (for V's rows)
-    const ExMono m1x = mono[J.x1], m1y = mono[J.y1];
-    const bool two1 = J.x1 != J.y1;
-    const int nat1 = m1x.n_atoms + (two1 ? m1y.n_atoms : 0);
-    const int nat2 = m2x.n_atoms + (two2 ? m2y.n_atoms : 0);
     __syncthreads();
-    // V^A = sum_B gamma_lr[A, B] W^B, W^B_aj = 1/2 sum_{nu in B} (L'c R's + L's R'c)
-    if (active) {
-        for (int A = 0; A < nat1; ++A) sm.V[A][tid] = T(0);
+    for (int B = 0; B < nat2; ++B) {
+        const bool onx = B < m2x.n_atoms;
+        const ExMono &mb = onx ? m2x : m2y;
+        const int bl = onx ? B : B - m2x.n_atoms;
+        const int base = onx ? 0 : m2x.n;
+        T w = T(0);
+        if (active)
+            for (int nu = base + mb.ao_off[bl]; nu < base + mb.ao_off[bl + 1]; ++nu)
+                w += L2c[nu][al] * R2s[nu][jl] + L2s[nu][al] * R2c[nu][jl];
+        W[B][threadIdx.x] = T(0.5) * w;
+    }
+    __syncthreads();   // the staged rows are dead: the gamma block takes their place
+
+    // ---- phase B: gamma block, V = gamma W ----
+    const int nA = (nat1 + CH - 1) / CH * CH;
+#pragma unroll 4
+    for (int e = threadIdx.x; e < nat2 * nA; e += XJ_T) {
+        const int B = e / nA, A = e % nA;
+        T g = T(0);
+        if (A < nat1) {
+            const int gA = A < m1x.n_atoms ? m1x.atom0 + A : m1y.atom0 + (A - m1x.n_atoms);
+            const int gB = B < m2x.n_atoms ? m2x.atom0 + B : m2y.atom0 + (B - m2x.n_atoms);
+            g = (T)gamma_lr[(long long)gB * n_atoms_total + gA];   // gamma_lr is symmetric: A runs along a row
+        }
+        G[B][A] = g;
+    }
+    __syncthreads();
+    for (int A0 = 0; A0 < nat1; A0 += CH) {
+        T acc[CH];
+#pragma unroll
+        for (int k = 0; k < CH; ++k) acc[k] = T(0);
         for (int B = 0; B < nat2; ++B) {
-            const ExMono &mb = (B < m2x.n_atoms) ? m2x : m2y;
-            const int bl = (B < m2x.n_atoms) ? B : B - m2x.n_atoms;
-            const int base = (B < m2x.n_atoms) ? 0 : m2x.n;
-            T wv = T(0);
-            for (int nu = mb.ao_off[bl]; nu < mb.ao_off[bl + 1]; ++nu)
-                wv += sm.L1[base + nu][my_a] * sm.R2[base + nu][my_j] + sm.L2[base + nu][my_a] * sm.R1[base + nu][my_j];
-            wv *= T(0.5);
-            const int gB = mb.atom0 + bl;
+            const T w = W[B][threadIdx.x];
+#pragma unroll
+            for (int k = 0; k < CH; ++k) acc[k] += G[B][A0 + k] * w;
+        }
+#pragma unroll
+        for (int k = 0; k < CH; ++k)
+            if (A0 + k < nat1) V[A0 + k][threadIdx.x] = acc[k];
+    }
+    __syncthreads();   // W and the gamma block are dead: the side-1 rows take their place
+
+    // ---- phase C: per element, L1 (side-1 scratch), R1 = C_Q, (S C)_Q (S_x1y1 C_y1 on x1); U . V ----
+    const int eb = el_begin[tl.x], ee = el_begin[tl.x + 1];
+    for (int ei = eb; ei < ee; ++ei) {
+        const ExEl E = els[ei];
+        const ExS1 K1 = k1s[E.k1];
+        const double *l1c = scr + K1.own, *l1s = l1c + (long long)m1x.n * K1.na;
+#pragma unroll 4
+        for (int e = threadIdx.x; e < nao1 * ta; e += XJ_T) {
+            const int mu = e / ta, q = e % ta;
+            T c = T(0), sc = T(0);
+            if (a0 + q < K1.na) {
+                const int a = a0 + q;
+                if (mu < m1x.n) {
+                    c = (T)l1c[(long long)mu * K1.na + a];
+                    sc = (T)l1s[(long long)mu * K1.na + a];
+                } else {
+                    sc = (T)scr[K1.crs + (long long)(mu - m1x.n) * K1.na + a];
+                }
+            }
+            L1c[mu][q] = c;
+            L1s[mu][q] = sc;
+        }
+        if (ei == eb) {   // the same columns Q of y1 for every element of the group
+#pragma unroll 4
+            for (int e = threadIdx.x; e < nao1 * tj; e += XJ_T) {
+                const int mu = e / tj, q = e % tj;
+                T c = T(0), sc = T(0);
+                if (j0 + q < K.nq) {
+                    const int col = K1.q0 + j0 + q;
+                    if (!two1) {
+                        c = (T)m1x.C[(long long)mu * m1x.n + col];
+                        sc = (T)m1x.SC[(long long)mu * m1x.n + col];
+                    } else if (mu < m1x.n) {
+                        sc = (T)K1.cross_xy1[(long long)mu * m1y.n + col];
+                    } else {
+                        c = (T)m1y.C[(long long)(mu - m1x.n) * m1y.n + col];
+                        sc = (T)m1y.SC[(long long)(mu - m1x.n) * m1y.n + col];
+                    }
+                }
+                R1c[mu][q] = c;
+                R1s[mu][q] = sc;
+            }
+        }
+        __syncthreads();
+        T acc = T(0);
+        if (active) {
             for (int A = 0; A < nat1; ++A) {
-                const int gA = (A < m1x.n_atoms) ? m1x.atom0 + A : m1y.atom0 + (A - m1x.n_atoms);
-                sm.V[A][tid] += (T)gamma_lr[(long long)gA * n_atoms_total + gB] * wv;
+                const bool onx = A < m1x.n_atoms;
+                const ExMono &ma = onx ? m1x : m1y;
+                const int aloc = onx ? A : A - m1x.n_atoms;
+                const int base = onx ? 0 : m1x.n;
+                T u = T(0);
+                for (int mu = base + ma.ao_off[aloc]; mu < base + ma.ao_off[aloc + 1]; ++mu)
+                    u += L1c[mu][al] * R1s[mu][jl] + L1s[mu][al] * R1c[mu][jl];
+                acc += u * V[A][threadIdx.x];
             }
+            acc *= T(0.5);
         }
-    }
-    __syncthreads();
-    // ---- side 1 (occupied charges): Lc = P b1, Ls = (S P) b1, Rc = Q, Rs = S Q ----
-    const int nao1 = m1x.n + (two1 ? m1y.n : 0);
-    for (int e = tid; e < nao1 * J.ta; e += XJ_T) {
-        const int mu = e / J.ta, a = e % J.ta;
-        int w, r;
-        frag_row(m1x, m1y, two1, mu, w, r);
-        T lc = T(0), ls = T(0);
-        for (int i = 0; i < J.np; ++i) {
-            const int col = J.p0 + i;
-            const T bb = (T)J.X1[(long long)(J.i1 + i) * J.ld1 + J.a1 + J.ta0 + a];
-            if (w == 0) {
-                lc += (T)m1x.C[(long long)r * m1x.n + col] * bb;
-                ls += (T)m1x.SC[(long long)r * m1x.n + col] * bb;
-            } else {
-                ls += (T)J.cross_yx1[(long long)r * m1x.n + col] * bb;
-            }
+        double d = (double)acc;
+        for (int o = 16; o; o >>= 1) d += __shfl_xor_sync(0xffffffffu, d, o);
+        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = d;
+        __syncthreads();   // also: the next element's staging overwrites L1 only after every thread is done
+        if (threadIdx.x == 0) {
+            double tot = 0.0;
+            for (int w = 0; w < XJ_T / 32; ++w) tot += red[w];
+            atomicAdd(H + (long long)E.s * n_states + E.t, -tot);
         }
-        sm.L1[mu][a] = lc;
-        sm.L2[mu][a] = ls;
-    }
-    for (int e = tid; e < nao1 * J.tj; e += XJ_T) {
-        const int mu = e / J.tj, jj = e % J.tj;
-        int w, r;
-        frag_row(m1x, m1y, two1, mu, w, r);
-        const int col = J.q0 + J.tj0 + jj;
-        T rc = T(0), rs = T(0);
-        if (two1) {
-            if (w == 1) {
-                rc = (T)m1y.C[(long long)r * m1y.n + col];
-                rs = (T)m1y.SC[(long long)r * m1y.n + col];
-            } else {
-                rs = (T)J.cross_xy1[(long long)r * m1y.n + col];
-            }
-        } else {
-            rc = (T)m1x.C[(long long)r * m1x.n + col];
-            rs = (T)m1x.SC[(long long)r * m1x.n + col];
-        }
-        sm.R1[mu][jj] = rc;
-        sm.R2[mu][jj] = rs;
-    }
-    __syncthreads();
-    T acc = T(0);
-    if (active) {
-        for (int A = 0; A < nat1; ++A) {
-            const ExMono &ma = (A < m1x.n_atoms) ? m1x : m1y;
-            const int al = (A < m1x.n_atoms) ? A : A - m1x.n_atoms;
-            const int base = (A < m1x.n_atoms) ? 0 : m1x.n;
-            T u = T(0);
-            for (int mu = ma.ao_off[al]; mu < ma.ao_off[al + 1]; ++mu)
-                u += sm.L1[base + mu][my_a] * sm.R2[base + mu][my_j] + sm.L2[base + mu][my_a] * sm.R1[base + mu][my_j];
-            acc += T(0.5) * u * sm.V[A][tid];
-        }
-    }
-    for (int off = 16; off; off >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, off);
-    if ((tid & 31) == 0) sm.red[tid >> 5] = acc;
-    __syncthreads();
-    if (tid == 0) {
-        double tot = 0.0;
-        for (int w = 0; w < XJ_T / 32; ++w) tot += (double)sm.red[w];
-        atomicAdd(H + (long long)J.s * n_states + J.t, -tot);
     }
 }
 
@@ -470,16 +555,17 @@ __global__ void ex_row_norms_kernel(int k, int n, const double *__restrict__ a, 
     }
 }
 
-// v -= c^T V (c: m coefficients), then the norm into *nrm (one CTA)
+// v -= c^T V (c: m coefficients), one thread per component; each CTA's sum of squares into part[]
 __global__ void ex_orth_update_kernel(int m, int n, const double *__restrict__ V, const double *__restrict__ c,
-                                      double *v, double *nrm) {
+                                      double *v, double *part) {
     __shared__ double red[8];
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
     double s = 0.0;
-    for (int x = threadIdx.x; x < n; x += blockDim.x) {
+    if (x < n) {
         double y = v[x];
         for (int i = 0; i < m; ++i) y -= c[i] * V[(long long)i * n + x];
         v[x] = y;
-        s += y * y;
+        s = y * y;
     }
     for (int off = 16; off; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
     if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
@@ -487,8 +573,43 @@ __global__ void ex_orth_update_kernel(int m, int n, const double *__restrict__ V
     if (threadIdx.x == 0) {
         double t = 0.0;
         for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w];
+        part[blockIdx.x] = t;
+    }
+}
+
+// *nrm = sqrt(sum of the k partial sums), added in a fixed order
+__global__ void ex_norm_finish_kernel(int k, const double *__restrict__ part, double *nrm) {
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int i = 0; i < k; ++i) t += part[i];
         *nrm = sqrt(t);
     }
+}
+
+// out[i, x] = sum_k A[i, k] B[k, x] (k in order), one thread per output; A [M x K], B [K x N], out [M x N]
+// row-major (the Davidson's new products H v_i, Ritz vectors and Y^T AV)
+__global__ void ex_rowprod_kernel(int N, int K, const double *__restrict__ A, const double *__restrict__ B,
+                                  double *out) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, i = blockIdx.y;
+    if (x >= N) return;
+    const double *a = A + (long long)i * K;
+    double acc = 0.0;
+    for (int k = 0; k < K; ++k) acc += a[k] * B[(long long)k * N + x];
+    out[(long long)i * N + x] = acc;
+}
+
+// C[i, j] = A_i . B_j (rows of length K), one warp per entry (lane-strided sums, fixed shuffle order)
+__global__ void ex_dotmat_kernel(int M, int N, int K, const double *__restrict__ A, const double *__restrict__ B,
+                                 double *C) {
+    const long long w = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (w >= (long long)M * N) return;
+    const int i = (int)(w / N), j = (int)(w % N);
+    const double *a = A + (long long)i * K, *b = B + (long long)j * K;
+    double acc = 0.0;
+    for (int k = lane; k < K; k += 32) acc += a[k] * b[k];
+    for (int o = 16; o; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (lane == 0) C[(long long)i * N + j] = acc;
 }
 
 // c[i] = V_i . v (one CTA per i)
@@ -572,8 +693,6 @@ int Ctx::exciton_states(int n_mono, const tincr_exciton_monomer *mono, int n_pai
         check_finite(m.s, (size_t)m.n_orb * m.n_orb, "monomer S");
     }
     if (atoms_sum != n_atoms_total) fail(TINCR_BAD_ARG, "exciton_states: atom count differs from the monomers'");
-    check_finite(gamma, (size_t)n_atoms_total * n_atoms_total, "gamma");
-    check_finite(gamma_lr, (size_t)n_atoms_total * n_atoms_total, "gamma_lr");
 
     // concatenated C, S, orbital energies, AO offsets
     std::vector<long long> offC(n_mono + 1, 0), offAo(n_mono + 1, 0);
@@ -601,10 +720,37 @@ int Ctx::exciton_states(int n_mono, const tincr_exciton_monomer *mono, int n_pai
     upload_vec(stream, dAo, hAo);
     dSC.alloc(hC.size());
     TINCR_CUDA(cudaMemsetAsync(dSC.p, 0, hC.size() * sizeof(double), stream));
-    dG.alloc((size_t)n_atoms_total * n_atoms_total);
-    dGlr.alloc((size_t)n_atoms_total * n_atoms_total);
-    TINCR_CUDA(cudaMemcpyAsync(dG.p, gamma, dG.n * sizeof(double), cudaMemcpyHostToDevice, stream));
-    TINCR_CUDA(cudaMemcpyAsync(dGlr.p, gamma_lr, dGlr.n * sizeof(double), cudaMemcpyHostToDevice, stream));
+    // the large inputs (gamma, gamma_lr, the real pairs' dimer orbitals) go through the context's
+    // page-locked staging buffer: parallel host copies, then one DMA each
+    const size_t n_g = (size_t)n_atoms_total * n_atoms_total;
+    size_t pin_need = 2 * n_g;
+    for (int p = 0; p < n_pairs; ++p)   // (pairs with bad indices are rejected below)
+        if (pairs[p].real && pairs[p].i >= 0 && pairs[p].i < n_mono && pairs[p].j >= 0 && pairs[p].j < n_mono) {
+            const size_t nij = (size_t)nao[pairs[p].i] + nao[pairs[p].j];
+            pin_need += nij * nij + nij;
+        }
+    ex_pin.reserve(pin_need);
+    size_t pin_used = 0;
+    auto stage = [&](double *dst, const double *src, size_t n, const char *what) {
+        double *h = ex_pin.p + pin_used;
+        pin_used += n;
+        const long long chunk = 1 << 18, nc = ((long long)n + chunk - 1) / chunk;
+        long long bad = 0;
+#pragma omp parallel for schedule(static) num_threads(8) reduction(+ : bad)
+        for (long long c = 0; c < nc; ++c) {
+            const size_t a = (size_t)c * chunk, b = std::min(n, a + (size_t)chunk);
+            for (size_t x = a; x < b; ++x) {
+                h[x] = src[x];
+                bad += !std::isfinite(src[x]);
+            }
+        }
+        if (bad) fail(TINCR_NONFINITE, std::string("non-finite value in ") + what);
+        TINCR_CUDA(cudaMemcpyAsync(dst, h, n * sizeof(double), cudaMemcpyHostToDevice, stream));
+    };
+    dG.alloc(n_g);
+    dGlr.alloc(n_g);
+    stage(dG.p, gamma, n_g, "gamma");
+    stage(dGlr.p, gamma_lr, n_g, "gamma_lr");
 
     // pairs: type, S_xy, dimer SCC
     std::map<PairKey, int> pidx;
@@ -614,10 +760,16 @@ int Ctx::exciton_states(int n_mono, const tincr_exciton_monomer *mono, int n_pai
         if (q.real && (!q.pair_orbs || !q.pair_orbe)) fail(TINCR_BAD_ARG, "exciton_states: real pair without its SCC");
         pidx[PairKey{q.i, q.j}] = p;
     }
+    // dense pair lookup: the pair index of monomers (a, b), -1 when not listed
+    std::vector<int> pdense((size_t)n_mono * n_mono, -1);
+    for (auto &kv : pidx) {
+        pdense[(size_t)kv.first.i * n_mono + kv.first.j] = kv.second;
+        pdense[(size_t)kv.first.j * n_mono + kv.first.i] = kv.second;
+    }
     auto is_real = [&](int a, int b) {
         if (a == b) return false;
-        auto it = pidx.find(PairKey{std::min(a, b), std::max(a, b)});
-        return it != pidx.end() && pairs[it->second].real != 0;
+        const int p = pdense[(size_t)a * n_mono + b];
+        return p >= 0 && pairs[p].real != 0;
     };
     // cross products S_xy C_y (n_x x n_y) and S_yx C_x (n_y x n_x) of every listed pair
     std::vector<long long> offX(n_pairs + 1, 0);
@@ -635,9 +787,9 @@ int Ctx::exciton_states(int n_mono, const tincr_exciton_monomer *mono, int n_pai
     dCross.alloc(std::max<long long>(1, offX[n_pairs]));
     TINCR_CUDA(cudaMemsetAsync(dCross.p, 0, dCross.n * sizeof(double), stream));
     auto cross = [&](int x, int y) -> const double * {   // S_xy C_y, [n_x x n_y]
-        auto it = pidx.find(PairKey{std::min(x, y), std::max(x, y)});
-        if (it == pidx.end()) return nullptr;
-        const int p = it->second;
+        if (x == y) return nullptr;
+        const int p = pdense[(size_t)x * n_mono + y];
+        if (p < 0) return nullptr;
         const long long half = (long long)nao[pairs[p].i] * nao[pairs[p].j];
         return dCross.p + offX[p] + (x == pairs[p].i ? 0 : half);
     };
@@ -714,41 +866,92 @@ int Ctx::exciton_states(int n_mono, const tincr_exciton_monomer *mono, int n_pai
         prof_end(slot, 4.0 * ns * (double)n_atoms_total * 40.0, 0.0);
     }
 
-    // ---- exchange jobs ----
+    // ---- exchange integrals (see the kernels: side-1 groups, side-2 groups with V, elements) ----
     std::vector<ExMono> hm(n_mono);
     for (int k = 0; k < n_mono; ++k)
         hm[k] = ExMono{dC.p + offC[k], dSC.p + offC[k], dAo.p + offAo[k], nao[k], mono[k].n_atoms, atom0[k]};
     DevBuf<ExMono> dm;
     upload_vec(stream, dm, hm);
-    std::vector<ExJob> xj;
-    auto tile_side = [](int n, int &t) { t = n <= XJ_TMAX ? n : (n + ((n + XJ_TMAX - 1) / XJ_TMAX) - 1) / ((n + XJ_TMAX - 1) / XJ_TMAX); };
-    auto add_job = [&](int s, int t, int x1, int y1, int x2, int y2, int p0, int np, int q0, int nq, int pa0, int na,
-                       int qb0, int nb, const double *X1, int ld1, int i1, int a1, const double *X2, int ld2, int j2,
-                       int b2) {
-        int ta, tj;
-        tile_side(na, ta);
-        tile_side(nq, tj);
-        while (ta * tj > XJ_T) {
-            if (ta >= tj) --ta; else --tj;
-        }
-        for (int a0 = 0; a0 < na; a0 += ta)
-            for (int j0 = 0; j0 < nq; j0 += tj) {
-                ExJob J;
-                J.s = s; J.t = t; J.x1 = x1; J.y1 = y1; J.x2 = x2; J.y2 = y2;
-                J.p0 = p0; J.np = np; J.q0 = q0; J.pa0 = pa0; J.qb0 = qb0; J.nb = nb;
-                J.ta0 = a0; J.ta = std::min(ta, na - a0); J.tj0 = j0; J.tj = std::min(tj, nq - j0);
-                J.X1 = X1; J.X2 = X2; J.ld1 = ld1; J.i1 = i1; J.a1 = a1; J.ld2 = ld2; J.j2 = j2; J.b2 = b2;
-                J.cross_xy1 = x1 != y1 ? cross(x1, y1) : nullptr;
-                J.cross_yx1 = x1 != y1 ? cross(y1, x1) : nullptr;
-                J.cross_xy2 = x2 != y2 ? cross(x2, y2) : nullptr;
-                J.cross_yx2 = x2 != y2 ? cross(y2, x2) : nullptr;
-                // a pair that is not listed is an ESD pair, whose AO overlap is zero (its atoms are
-                // farther apart than the Slater-Koster tables reach): its charges, and the integral,
-                // vanish
-                if ((x1 != y1 && !J.cross_xy1) || (x2 != y2 && !J.cross_xy2)) continue;
-                xj.push_back(J);
-            }
+    auto nao_of = [&](int x, int y) { return (long long)nao[x] + (x != y ? nao[y] : 0); };
+    auto nat_of = [&](int x, int y) { return (long long)mono[x].n_atoms + (x != y ? mono[y].n_atoms : 0); };
+    std::vector<ExS1> k1v;
+    std::vector<ExS2> k2v;
+    std::vector<ExEl> elv;
+    // side arrays in one FP64 scratch: per state, the rows on its own monomer (C b, S C b), and per
+    // state and partner monomer, the cross rows (S_yx C_x b); each computed once and shared by every
+    // group that reads it
+    struct SideJob {
+        int kind;                    // 0: own side 1, 1: cross side 1, 2: own side 2, 3: cross side 2
+        int x, y;                    // monomer of the columns; monomer of the rows (cross) or x
+        int c0, nc, nout;            // columns [c0, c0 + nc) contracted; output columns (a or j)
+        const double *X;             // the state vector and its addressing (side 1: b1(i, a); side 2: b2(j, b))
+        int ld, r0;
+        long long off;
     };
+    std::vector<SideJob> sjobs;
+    long long scr = 0;
+    std::unordered_map<long long, long long> side_tab;
+    auto side_of = [&](int kind, int state, int mono_key, int variant, int x, int y, int c0, int nc, int nout,
+                       const double *X, int ld, int r0, long long rows) -> long long {
+        const long long key = (((long long)kind * ns + state) * (n_mono + 1) + mono_key) * 2 + variant;
+        auto it = side_tab.find(key);
+        if (it != side_tab.end()) return it->second;
+        const long long off = scr;
+        scr += rows * nout;
+        sjobs.push_back(SideJob{kind, x, y, c0, nc, nout, X, ld, r0, off});
+        side_tab.emplace(key, off);
+        return off;
+    };
+    auto k1_of = [&](int state, int variant, int x1, int y1, int p0, int np, int q0, int na, const double *X1, int ld1,
+                     int i1) -> int {
+        ExS1 K;
+        K.x1 = x1; K.y1 = y1; K.p0 = p0; K.np = np; K.q0 = q0; K.na = na;
+        K.X1 = X1; K.ld1 = ld1; K.i1 = i1; K.a1 = 0;
+        K.cross_yx1 = x1 != y1 ? cross(y1, x1) : nullptr;
+        K.cross_xy1 = x1 != y1 ? cross(x1, y1) : nullptr;
+        K.own = side_of(0, state, n_mono, variant, x1, x1, p0, np, na, X1, ld1, i1, 2LL * nao[x1]);
+        K.crs = x1 != y1 ? side_of(1, state, y1, variant, x1, y1, p0, np, na, X1, ld1, i1, nao[y1]) : -1;
+        k1v.push_back(K);
+        return (int)k1v.size() - 1;
+    };
+    // group tables keyed by (state, monomer): LE-LE side 1 (s, partner), LE-LE side 2 (t, side-1
+    // monomer), LE-CT side 1 (LE state, CT hole), LE-CT side 2 (CT state, LE monomer), CT-CT side 1
+    // (s, hole of t)
+    std::vector<int> tab[5];
+    for (auto &v : tab) v.assign((size_t)ns * n_mono, -1);
+    auto k1_cached = [&](int which, int state, int partner, int variant, int x1, int y1, int p0, int np, int q0, int na,
+                         const double *X1, int ld1, int i1) -> int {
+        int &id = tab[which][(size_t)state * n_mono + partner];
+        if (id < 0) id = k1_of(state, variant, x1, y1, p0, np, q0, na, X1, ld1, i1);
+        return id;
+    };
+    auto k2_of = [&](int which, int state, int key, int variant, int x1, int y1, int x2, int y2, int pa0, int na,
+                     int qb0, int nb, int nq, const double *X2, int ld2, int j2) -> int {
+        int *slot = which >= 0 ? &tab[which][(size_t)state * n_mono + key] : nullptr;
+        if (slot && *slot >= 0) return *slot;
+        ExS2 K;
+        K.x1 = x1; K.y1 = y1; K.x2 = x2; K.y2 = y2;
+        K.pa0 = pa0; K.na = na; K.qb0 = qb0; K.nb = nb; K.nq = nq;
+        auto side = [](int n) {   // near-equal parts of at most XJ_TS
+            const int parts = (n + XJ_TS - 1) / XJ_TS;
+            return (n + parts - 1) / parts;
+        };
+        K.ta = side(na);
+        K.tj = side(nq);
+        while (K.ta * K.tj > XJ_T) {
+            if (K.ta >= K.tj) --K.ta; else --K.tj;
+        }
+        K.X2 = X2; K.ld2 = ld2; K.j2 = j2; K.b2 = 0;
+        K.cross_xy2 = x2 != y2 ? cross(x2, y2) : nullptr;
+        K.cross_yx2 = x2 != y2 ? cross(y2, x2) : nullptr;
+        K.own = side_of(2, state, n_mono, variant, y2, y2, qb0, nb, nq, X2, ld2, j2, 2LL * nao[y2]);
+        K.crs = x2 != y2 ? side_of(3, state, x2, variant, y2, x2, qb0, nb, nq, X2, ld2, j2, nao[x2]) : -1;
+        const int id = (int)k2v.size();
+        k2v.push_back(K);
+        if (slot) *slot = id;
+        return id;
+    };
+    auto listed = [&](int a, int b) { return a == b || cross(a, b) != nullptr; };
     auto near = [&](int a, int b) { return a == b || is_real(a, b); };   // pair type Pair or None
     for (int s = 0; s < ns; ++s)
         for (int t = s + 1; t < ns; ++t) {
@@ -758,60 +961,117 @@ int Ctx::exciton_states(int n_mono, const tincr_exciton_monomer *mono, int n_pai
                 // le_le (integrals.rs:81-169): exchange for real pairs, full orbital spaces
                 if (A.hole == B.hole || !is_real(A.hole, B.hole)) continue;
                 const int I = A.hole, Jm = B.hole, oI = no[I], vI = nao[I] - oI, oJ = no[Jm], vJ = nao[Jm] - oJ;
-                add_job(s, t, I, Jm, I, Jm, 0, oI, 0, oJ, oI, vI, oJ, vJ, Xs, vI, 0, 0, Xt, vJ, 0, 0);
+                const int k1 = k1_cached(0, s, Jm, 0, I, Jm, 0, oI, 0, vI, Xs, vI, 0);
+                const int k2 = k2_of(1, t, I, 0, I, Jm, I, Jm, oI, vI, oJ, vJ, oJ, Xt, vJ, 0);
+                elv.push_back(ExEl{s, t, k1, k2});
             } else if (A.kind == 0 || B.kind == 0) {
                 // le_ct_2e_new (integrals.rs:602-727): exchange when the LE monomer is the hole, the
-                // electron or a real-pair neighbour of either; restricted active spaces
+                // electron or a real-pair neighbour of either; restricted active spaces.  A pair that
+                // is not listed is an ESD pair, whose AO overlap is zero (its atoms are farther apart
+                // than the Slater-Koster tables reach): its charges, and the integral, vanish.
                 const int le = A.kind == 0 ? s : t, ct = A.kind == 0 ? t : s;
                 const ExState &L = hst[le], &C = hst[ct];
                 const int I = L.hole, h = C.hole, l = C.elec;
-                if (!(near(I, h) || near(I, l))) continue;
+                if (!(near(I, h) || near(I, l)) || !listed(I, h) || !listed(I, l)) continue;
                 const int oI = no[I], vI = nao[I] - oI, oh = no[h], vl = nao[l] - no[l];
-                const int out_s = std::min(le, ct), out_t = std::max(le, ct);
-                add_job(out_s, out_t, I, h, I, l, oI - ACTIVE, ACTIVE, oh - ACTIVE, ACTIVE, oI, ACTIVE, no[l], ACTIVE,
-                        dX.p + xoff[le], vI, oI - ACTIVE, 0, dX.p + xoff[ct], vl, oh - ACTIVE, 0);
+                const int k1 = k1_cached(2, le, h, 1, I, h, oI - ACTIVE, ACTIVE, oh - ACTIVE, ACTIVE, dX.p + xoff[le],
+                                         vI, oI - ACTIVE);
+                const int k2 = k2_of(3, ct, I, 1, I, h, I, l, oI, ACTIVE, no[l], ACTIVE, ACTIVE, dX.p + xoff[ct], vl,
+                                     oh - ACTIVE);
+                elv.push_back(ExEl{std::min(le, ct), std::max(le, ct), k1, k2});
             } else {
                 // ct_ct_new (integrals.rs:733-878): exchange when the holes and the electrons are each on
                 // the same monomer or on a real pair; restricted active spaces
                 if (A.hole == B.hole && A.elec == B.elec) continue;
                 if (!(near(A.hole, B.hole) && near(A.elec, B.elec))) continue;
                 const int h1 = A.hole, l1 = A.elec, h2 = B.hole, l2 = B.elec;
+                if (!listed(h1, h2) || !listed(l1, l2)) continue;
                 const int v1 = nao[l1] - no[l1], v2 = nao[l2] - no[l2];
-                add_job(s, t, h1, h2, l1, l2, no[h1] - ACTIVE, ACTIVE, no[h2] - ACTIVE, ACTIVE, no[l1], ACTIVE, no[l2],
-                        ACTIVE, Xs, v1, no[h1] - ACTIVE, 0, Xt, v2, no[h2] - ACTIVE, 0);
+                const int k1 = k1_cached(4, s, h2, 1, h1, h2, no[h1] - ACTIVE, ACTIVE, no[h2] - ACTIVE, ACTIVE, Xs,
+                                         v1, no[h1] - ACTIVE);
+                const int k2 = k2_of(-1, t, 0, 1, h1, h2, l1, l2, no[l1], ACTIVE, no[l2], ACTIVE, ACTIVE, Xt, v2,
+                                     no[h2] - ACTIVE);
+                elv.push_back(ExEl{s, t, k1, k2});
             }
         }
-    if (!xj.empty()) {
-        DevBuf<ExJob> dxj;
-        upload_vec(stream, dxj, xj);
-        const size_t smem = fp32 ? sizeof(XjSmem<float>) : sizeof(XjSmem<double>);
-        static bool attr = false;
-        if (!attr) {
-            TINCR_CUDA(cudaFuncSetAttribute(ex_exchange_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                            (int)sizeof(XjSmem<float>)));
-            TINCR_CUDA(cudaFuncSetAttribute(ex_exchange_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                            (int)sizeof(XjSmem<double>)));
-            attr = true;
+    for (auto &v : tab) std::vector<int>().swap(v);
+    auto run_exchange = [&](auto zero) {
+        using T = decltype(zero);
+        if (elv.empty()) return;
+        // side arrays (FP64 scratch) by batched GEMMs
+        DevBuf<double> d1;
+        d1.alloc(std::max<long long>(1, scr));
+        TINCR_CUDA(cudaMemsetAsync(d1.p, 0, d1.n * sizeof(double), stream));
+        for (const SideJob &J : sjobs) {
+            const int nx = nao[J.x], ny = nao[J.y];
+            double *out = d1.p + J.off;
+            if (J.kind <= 1) {   // side 1: rows x C_P b1 or rows of y (S_yx C_x)_P b1; B(i, a) = X[(r0 + i) ld + a]
+                const double *B = J.X + (long long)J.r0 * J.ld;
+                if (J.kind == 0) {
+                    gb.gemm(nx, J.nout, J.nc, dC.p + offC[J.x] + J.c0, nx, 1, B, J.ld, 1, out, J.nout, 1.0);
+                    gb.gemm(nx, J.nout, J.nc, dSC.p + offC[J.x] + J.c0, nx, 1, B, J.ld, 1, out + (long long)nx * J.nout,
+                            J.nout, 1.0);
+                } else {
+                    gb.gemm(ny, J.nout, J.nc, cross(J.y, J.x) + J.c0, nx, 1, B, J.ld, 1, out, J.nout, 1.0);
+                }
+            } else {             // side 2: rows of x C_Q' b2^T or rows of y (S_yx C_x)_Q' b2^T; B(b, j) = X[(r0 + j) ld + b]
+                const double *B = J.X + (long long)J.r0 * J.ld;
+                if (J.kind == 2) {
+                    gb.gemm(nx, J.nout, J.nc, dC.p + offC[J.x] + J.c0, nx, 1, B, 1, J.ld, out, J.nout, 1.0);
+                    gb.gemm(nx, J.nout, J.nc, dSC.p + offC[J.x] + J.c0, nx, 1, B, 1, J.ld, out + (long long)nx * J.nout,
+                            J.nout, 1.0);
+                } else {
+                    gb.gemm(ny, J.nout, J.nc, cross(J.y, J.x) + J.c0, nx, 1, B, 1, J.ld, out, J.nout, 1.0);
+                }
+            }
+        }
+        gb.run(*this, sizeof(T) == 4, dJobs, dTiles, TINCR_KF_AO_EXCHANGE);
+        // elements sorted by side-2 group; one CTA per (group, tile) forms V and serves the group's elements
+        std::stable_sort(elv.begin(), elv.end(), [](const ExEl &a, const ExEl &b) { return a.k2 < b.k2; });
+        std::vector<int> el_begin(k2v.size() + 1, 0);
+        for (const ExEl &E : elv) ++el_begin[E.k2 + 1];
+        for (size_t k = 0; k < k2v.size(); ++k) el_begin[k + 1] += el_begin[k];
+        std::vector<int4> vt;
+        double fl = 0.0;
+        for (int k = 0; k < (int)k2v.size(); ++k) {
+            const ExS2 &K = k2v[k];
+            if (el_begin[k + 1] == el_begin[k]) continue;
+            for (int a0 = 0; a0 < K.na; a0 += K.ta)
+                for (int j0 = 0; j0 < K.nq; j0 += K.tj) vt.push_back(make_int4(k, a0, j0, 0));
+            fl += (2.0 * nat_of(K.x1, K.y1) * nat_of(K.x2, K.y2) +
+                   4.0 * nao_of(K.x1, K.y1) * (el_begin[k + 1] - el_begin[k])) * K.na * K.nq;
+        }
+        DevBuf<ExS1> dk1;
+        DevBuf<ExS2> dk2;
+        DevBuf<ExEl> del;
+        DevBuf<int> deb;
+        DevBuf<int4> dvt;
+        upload_vec(stream, dk1, k1v);
+        upload_vec(stream, dk2, k2v);
+        upload_vec(stream, del, elv);
+        upload_vec(stream, deb, el_begin);
+        upload_vec(stream, dvt, vt);
+        static bool attr[2] = {false, false};
+        if (!attr[sizeof(T) == 4]) {
+            TINCR_CUDA(cudaFuncSetAttribute(ex_vu_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                            (int)ExVUSmem<T>::BYTES));
+            attr[sizeof(T) == 4] = true;
         }
         const int slot = prof_begin(TINCR_KF_AO_EXCHANGE);
-        for (size_t j0 = 0; j0 < xj.size(); j0 += 1u << 20) {   // grid limit
-            const unsigned nb = (unsigned)std::min<size_t>(xj.size() - j0, 1u << 20);
-            if (fp32)
-                ex_exchange_kernel<float><<<nb, XJ_T, smem, stream>>>(dxj.p + j0, dm.p, dGlr.p, n_atoms_total, dH.p, ns);
-            else
-                ex_exchange_kernel<double><<<nb, XJ_T, smem, stream>>>(dxj.p + j0, dm.p, dGlr.p, n_atoms_total, dH.p, ns);
-            count_launch(stream, "ex_exchange");
-            check_launch("ex_exchange");
+        for (size_t t0 = 0; t0 < vt.size(); t0 += 1u << 20) {   // grid limit
+            const unsigned nb = (unsigned)std::min<size_t>(vt.size() - t0, 1u << 20);
+            ex_vu_kernel<T><<<nb, XJ_T, ExVUSmem<T>::BYTES, stream>>>(dvt.p + t0, dk2.p, deb.p, del.p, dk1.p, dm.p,
+                                                                       dGlr.p, n_atoms_total, d1.p, dH.p, ns);
+            count_launch(stream, "ex_vu");
+            check_launch("ex_vu");
         }
-        double fl = 0.0;
-        for (const ExJob &J : xj) {
-            const double n1 = hm[J.x1].n_atoms + (J.x1 != J.y1 ? hm[J.y1].n_atoms : 0);
-            const double n2 = hm[J.x2].n_atoms + (J.x2 != J.y2 ? hm[J.y2].n_atoms : 0);
-            fl += 2.0 * J.ta * J.tj * n1 * n2;
-        }
+        sync();   // the host lists above must outlive their uploads
         prof_end(slot, fl, 0.0);
-        sync();
-    }
+    };
+    if (fp32)
+        run_exchange(0.0f);
+    else
+        run_exchange(0.0);
 
     // ---- LCMO Fock blocks and one-electron LE-CT couplings ----
     // blocks F'_{xy} (x < y) of every CT pair, from the real pairs' dimer orbitals
@@ -846,17 +1106,33 @@ int Ctx::exciton_states(int n_mono, const tincr_exciton_monomer *mono, int n_pai
             o_po[p] = npo; npo += (long long)nij * nij;
             o_pe[p] = npe; npe += nij;
         }
-        std::vector<double> hPo(std::max<long long>(1, npo)), hPe(std::max<long long>(1, npe));
-        for (int p : rp) {
-            const int nij = nao[pairs[p].i] + nao[pairs[p].j];
-            check_finite(pairs[p].pair_orbs, (size_t)nij * nij, "pair orbitals");
-            check_finite(pairs[p].pair_orbe, (size_t)nij, "pair orbital energies");
-            std::copy(pairs[p].pair_orbs, pairs[p].pair_orbs + (size_t)nij * nij, hPo.begin() + o_po[p]);
-            std::copy(pairs[p].pair_orbe, pairs[p].pair_orbe + nij, hPe.begin() + o_pe[p]);
+        // dimer orbitals and energies: packed in parallel into the staging buffer, one DMA each
+        double *hPo = ex_pin.p + pin_used;
+        pin_used += npo;
+        double *hPe = ex_pin.p + pin_used;
+        pin_used += npe;
+        int bad_pair = -1;
+#pragma omp parallel for schedule(dynamic, 4) num_threads(8)
+        for (int r = 0; r < (int)rp.size(); ++r) {
+            const int p = rp[r];
+            const size_t nij = (size_t)nao[pairs[p].i] + nao[pairs[p].j];
+            const double *po = pairs[p].pair_orbs, *pe = pairs[p].pair_orbe;
+            bool ok = true;
+            for (size_t x = 0; x < nij * nij; ++x) ok = ok && std::isfinite(po[x]);
+            for (size_t x = 0; x < nij; ++x) ok = ok && std::isfinite(pe[x]);
+            if (!ok) {
+#pragma omp critical
+                bad_pair = p;
+            }
+            std::copy(po, po + nij * nij, hPo + o_po.at(p));
+            std::copy(pe, pe + nij, hPe + o_pe.at(p));
         }
+        if (bad_pair >= 0) fail(TINCR_NONFINITE, "non-finite value in pair orbitals of pair " + std::to_string(bad_pair));
         DevBuf<double> dPo, dPe, dSpr, dSpq, dFd, dFij;
-        upload_vec(stream, dPo, hPo);
-        upload_vec(stream, dPe, hPe);
+        dPo.alloc(std::max<long long>(1, npo));
+        dPe.alloc(std::max<long long>(1, npe));
+        if (npo) TINCR_CUDA(cudaMemcpyAsync(dPo.p, hPo, npo * sizeof(double), cudaMemcpyHostToDevice, stream));
+        if (npe) TINCR_CUDA(cudaMemcpyAsync(dPe.p, hPe, npe * sizeof(double), cudaMemcpyHostToDevice, stream));
         dSpr.alloc(std::max<long long>(1, nspr));
         dSpq.alloc(std::max<long long>(1, nspq));
         dFij.alloc(std::max<long long>(1, nfij));
@@ -1025,7 +1301,8 @@ int Ctx::exciton_states(int n_mono, const tincr_exciton_monomer *mono, int n_pai
     for (int x = 0; x < ns; ++x) order[x] = x;
     std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return hdiag[a] < hdiag[b]; });
     const int cap = max_space + nr;
-    DevBuf<double> dV, dAV, dAp, dY, dRitz, dRk, dU, dNrm, dT, dc;
+    DevBuf<double> dV, dAV, dAp, dY, dRitz, dRk, dU, dNrm, dT, dc, dPart;
+    dPart.alloc(ceil_div(ns, 256));
     dV.alloc((size_t)cap * ns);
     dAV.alloc((size_t)cap * ns);
     dAp.alloc((size_t)cap * cap);
@@ -1043,15 +1320,23 @@ int Ctx::exciton_states(int n_mono, const tincr_exciton_monomer *mono, int n_pai
         sync();
     }
     int m = nr, dim_sub = nr, it = 0, status = TINCR_NOT_CONVERGED;
+    int n_av = 0;   // rows of AV that hold H v_i for the current basis
     std::vector<double> ap, w(nr), yt, err(nr), u(nr);
     for (it = 0; it < max_iter; ++it) {
-        // products of every subspace vector (the dense engine has no cache) and the projection
-        TINCR_CUDA(cudaMemsetAsync(dAV.p, 0, (size_t)m * ns * sizeof(double), stream));
-        TINCR_CUDA(cudaMemsetAsync(dAp.p, 0, (size_t)m * m * sizeof(double), stream));
-        gb.gemm(m, ns, ns, dV.p, ns, 1, dH.p, ns, 1, dAV.p, ns, 1.0);
-        gb.run(*this, false, dJobs, dTiles, TINCR_KF_SUBSPACE);
-        gb.gemm(m, m, ns, dV.p, ns, 1, dAV.p, 1, ns, dAp.p, m, 1.0);
-        gb.run(*this, false, dJobs, dTiles, TINCR_KF_SUBSPACE);
+        // products of the subspace vectors and the projection.  tincr's dense engine multiplies every
+        // vector again (solvers/mod.rs:36-51); the rows of earlier vectors are unchanged (each row of the
+        // product is formed on its own, in the same order), so only the new vectors are multiplied
+        const int sub_slot = prof_begin(TINCR_KF_SUBSPACE);
+        if (n_av < m) {   // (H is symmetric: row i of V H is H v_i)
+            ex_rowprod_kernel<<<dim3(ceil_div(ns, 256), m - n_av), 256, 0, stream>>>(ns, ns, dV.p + (size_t)n_av * ns,
+                                                                                    dH.p, dAV.p + (size_t)n_av * ns);
+            count_launch(stream, "ex_rowprod");
+            n_av = m;
+        }
+        ex_dotmat_kernel<<<ceil_div((long long)m * m * 32, 256), 256, 0, stream>>>(m, m, ns, dV.p, dAV.p, dAp.p);
+        count_launch(stream, "ex_dotmat");
+        check_launch("ex_dotmat");
+        prof_end(sub_slot, 2.0 * m * (double)m * ns, 0.0);
         ap.resize((size_t)m * m);
         TINCR_CUDA(cudaMemcpyAsync(ap.data(), dAp.p, ap.size() * sizeof(double), cudaMemcpyDeviceToHost, stream));
         sync();
@@ -1061,11 +1346,11 @@ int Ctx::exciton_states(int n_mono, const tincr_exciton_monomer *mono, int n_pai
         for (int r = 0; r < nr; ++r) u[r] = w[r];
         TINCR_CUDA(cudaMemcpyAsync(dY.p, yt.data(), yt.size() * sizeof(double), cudaMemcpyHostToDevice, stream));
         TINCR_CUDA(cudaMemcpyAsync(dU.p, u.data(), nr * sizeof(double), cudaMemcpyHostToDevice, stream));
-        TINCR_CUDA(cudaMemsetAsync(dRitz.p, 0, (size_t)nr * ns * sizeof(double), stream));
-        TINCR_CUDA(cudaMemsetAsync(dRk.p, 0, (size_t)nr * ns * sizeof(double), stream));
-        gb.gemm(nr, ns, m, dY.p, m, 1, dV.p, ns, 1, dRitz.p, ns, 1.0);
-        gb.gemm(nr, ns, m, dY.p, m, 1, dAV.p, ns, 1, dRk.p, ns, 1.0);
-        gb.run(*this, false, dJobs, dTiles, TINCR_KF_SUBSPACE);
+        ex_rowprod_kernel<<<dim3(ceil_div(ns, 256), nr), 256, 0, stream>>>(ns, m, dY.p, dV.p, dRitz.p);
+        count_launch(stream, "ex_rowprod");
+        ex_rowprod_kernel<<<dim3(ceil_div(ns, 256), nr), 256, 0, stream>>>(ns, m, dY.p, dAV.p, dRk.p);
+        count_launch(stream, "ex_rowprod");
+        check_launch("ex_rowprod");
         ex_residual_kernel<<<ceil_div((long long)nr * ns, 256), 256, 0, stream>>>(nr, ns, dU.p, dRitz.p, dRk.p);
         count_launch(stream, "ex_residual");
         ex_row_norms_kernel<<<nr, 256, 0, stream>>>(nr, ns, dRk.p, dNrm.p);
@@ -1092,8 +1377,10 @@ int Ctx::exciton_states(int n_mono, const tincr_exciton_monomer *mono, int n_pai
                 count_launch(stream, "ex_precondition");
                 ex_dots_kernel<<<m, 256, 0, stream>>>(m, ns, dV.p, dT.p, dc.p);
                 count_launch(stream, "ex_dots");
-                ex_orth_update_kernel<<<1, 256, 0, stream>>>(m, ns, dV.p, dc.p, dT.p, dNrm.p + nr);
+                ex_orth_update_kernel<<<ceil_div(ns, 256), 256, 0, stream>>>(m, ns, dV.p, dc.p, dT.p, dPart.p);
                 count_launch(stream, "ex_orth_update");
+                ex_norm_finish_kernel<<<1, 32, 0, stream>>>(ceil_div(ns, 256), dPart.p, dNrm.p + nr);
+                count_launch(stream, "ex_norm_finish");
                 double nrm = 0.0;
                 TINCR_CUDA(cudaMemcpyAsync(&nrm, dNrm.p + nr, sizeof(double), cudaMemcpyDeviceToHost, stream));
                 sync();
@@ -1107,6 +1394,7 @@ int Ctx::exciton_states(int n_mono, const tincr_exciton_monomer *mono, int n_pai
             dim_sub = nr;
             TINCR_CUDA(cudaMemcpyAsync(dV.p, dRitz.p, (size_t)nr * ns * sizeof(double), cudaMemcpyDeviceToDevice, stream));
             m = nr;
+            n_av = 0;
         }
     }
     for (int r = 0; r < nr; ++r) energies[r] = u[r];

@@ -133,6 +133,7 @@ struct Ctx {
     int dg_check();
     void gemm_f64_digits(int M, int N, int K, const double *A, const double *B, double *C);
     BatchWork *batch = nullptr;
+    PinnedBuf ex_pin;                     // staging of the exciton Hamiltonian's large inputs
 
     explicit Ctx(int dev);
     ~Ctx();
