@@ -729,6 +729,12 @@ int Ctx::exciton_states(int n_mono, const tincr_exciton_monomer *mono, int n_pai
             const size_t nij = (size_t)nao[pairs[p].i] + nao[pairs[p].j];
             pin_need += nij * nij + nij;
         }
+    for (int k = 0; k < n_mono; ++k)   // LE charges and CI vectors
+        pin_need += (size_t)std::max(0, mono[k].n_le) * (mono[k].n_atoms + (size_t)no[k] * (nao[k] - no[k]));
+    for (int c = 0; c < n_ct; ++c)     // CT charges and CI vectors (states with bad indices are rejected below)
+        if (cts && cts[c].h >= 0 && cts[c].h < n_mono && cts[c].l >= 0 && cts[c].l < n_mono)
+            pin_need += (size_t)mono[cts[c].h].n_atoms + mono[cts[c].l].n_atoms +
+                        (size_t)no[cts[c].h] * (nao[cts[c].l] - no[cts[c].l]);
     ex_pin.reserve(pin_need);
     size_t pin_used = 0;
     auto stage = [&](double *dst, const double *src, size_t n, const char *what) {
@@ -812,19 +818,26 @@ int Ctx::exciton_states(int n_mono, const tincr_exciton_monomer *mono, int n_pai
     }
     gb.run(*this, false, dJobs, dTiles, TINCR_KF_OTHER);
 
-    // states in the basis order: LE (monomer-major), then the CT states as given
+    // states in the basis order: LE (monomer-major), then the CT states as given.  Offsets first, then
+    // the charges and CI vectors gathered in parallel into the staging buffer (one DMA each)
     std::vector<ExState> hst;
-    std::vector<double> hq, hX;
     std::vector<long long> xoff;
+    struct Src {
+        const double *q, *x;         // charges [atoms x n] and coefficients [o v x n], column `col` of n
+        int n, col, nq;
+        long long nx;
+    };
+    std::vector<Src> src;
+    long long nq_tot = 0, nx_tot = 0;
     for (int k = 0; k < n_mono; ++k) {
         const tincr_exciton_monomer &m = mono[k];
-        const int o = m.n_occ, v = m.n_orb - m.n_occ;
+        const long long ov = (long long)m.n_occ * (m.n_orb - m.n_occ);
         for (int r = 0; r < m.n_le; ++r) {
-            ExState s{0, k, k, atom0[k], m.n_atoms, 0, 0, (long long)hq.size(), m.le_energies[r]};
-            for (int a = 0; a < m.n_atoms; ++a) hq.push_back(m.le_q_trans[(size_t)a * m.n_le + r]);
-            xoff.push_back((long long)hX.size());
-            for (long long x = 0; x < (long long)o * v; ++x) hX.push_back(m.le_coefficients[x * m.n_le + r]);
-            hst.push_back(s);
+            hst.push_back(ExState{0, k, k, atom0[k], m.n_atoms, 0, 0, nq_tot, m.le_energies[r]});
+            xoff.push_back(nx_tot);
+            src.push_back(Src{m.le_q_trans, m.le_coefficients, m.n_le, r, m.n_atoms, ov});
+            nq_tot += m.n_atoms;
+            nx_tot += ov;
         }
     }
     for (int c = 0; c < n_ct; ++c) {
@@ -832,25 +845,45 @@ int Ctx::exciton_states(int n_mono, const tincr_exciton_monomer *mono, int n_pai
         if (q.h < 0 || q.h >= n_mono || q.l < 0 || q.l >= n_mono || q.h == q.l || q.n_ct <= 0 || q.state < 0 ||
             q.state >= q.n_ct || !q.energies || !q.coefficients || !q.q_tr)
             fail(TINCR_BAD_ARG, "exciton_states: bad CT state");
-        if (!pidx.count(PairKey{std::min(q.h, q.l), std::max(q.h, q.l)}))
-            fail(TINCR_BAD_ARG, "exciton_states: CT state of an unlisted pair");
-        const int oh = no[q.h], vl = nao[q.l] - no[q.l];
+        if (pdense[(size_t)q.h * n_mono + q.l] < 0) fail(TINCR_BAD_ARG, "exciton_states: CT state of an unlisted pair");
+        const long long ov = (long long)no[q.h] * (nao[q.l] - no[q.l]);
         const int nh = mono[q.h].n_atoms, nl = mono[q.l].n_atoms;
-        ExState s{1, q.h, q.l, atom0[q.h], nh, atom0[q.l], nl, (long long)hq.size(), q.energies[q.state]};
-        for (int a = 0; a < nh + nl; ++a) hq.push_back(q.q_tr[(size_t)a * q.n_ct + q.state]);
-        xoff.push_back((long long)hX.size());
-        for (long long x = 0; x < (long long)oh * vl; ++x) hX.push_back(q.coefficients[x * q.n_ct + q.state]);
-        hst.push_back(s);
+        hst.push_back(ExState{1, q.h, q.l, atom0[q.h], nh, atom0[q.l], nl, nq_tot, q.energies[q.state]});
+        xoff.push_back(nx_tot);
+        src.push_back(Src{q.q_tr, q.coefficients, q.n_ct, q.state, nh + nl, ov});
+        nq_tot += nh + nl;
+        nx_tot += ov;
     }
     const int ns = (int)hst.size();
     if (ns < n_roots) fail(TINCR_BAD_ARG, "exciton_states: fewer basis states than roots");
-    check_finite(hq.data(), hq.size(), "transition charges");
-    check_finite(hX.data(), hX.size(), "CI coefficients");
+    if (pin_used + nq_tot + nx_tot > ex_pin.n) {   // (counted above; growing drops the staged gamma copies)
+        sync();
+        ex_pin.reserve(pin_used + nq_tot + nx_tot);
+    }
+    double *hq = ex_pin.p + pin_used, *hX = hq + nq_tot;
+    long long bad = 0;
+#pragma omp parallel for schedule(dynamic, 8) num_threads(8) reduction(+ : bad)
+    for (int t = 0; t < ns; ++t) {
+        const Src &r = src[t];
+        double *qo = hq + hst[t].q_off, *xo = hX + xoff[t];
+        for (int a = 0; a < r.nq; ++a) {
+            qo[a] = r.q[(size_t)a * r.n + r.col];
+            bad += !std::isfinite(qo[a]);
+        }
+        for (long long x = 0; x < r.nx; ++x) {
+            xo[x] = r.x[x * r.n + r.col];
+            bad += !std::isfinite(xo[x]);
+        }
+    }
+    if (bad) fail(TINCR_NONFINITE, "non-finite value in transition charges or CI coefficients");
     DevBuf<ExState> dst;
     DevBuf<double> dq, dX, dW, dH;
     upload_vec(stream, dst, hst);
-    upload_vec(stream, dq, hq);
-    upload_vec(stream, dX, hX);
+    dq.alloc(std::max<long long>(1, nq_tot));
+    dX.alloc(std::max<long long>(1, nx_tot));
+    if (nq_tot) TINCR_CUDA(cudaMemcpyAsync(dq.p, hq, nq_tot * sizeof(double), cudaMemcpyHostToDevice, stream));
+    if (nx_tot) TINCR_CUDA(cudaMemcpyAsync(dX.p, hX, nx_tot * sizeof(double), cudaMemcpyHostToDevice, stream));
+    pin_used += nq_tot + nx_tot;
     dW.alloc((size_t)ns * n_atoms_total);
     dH.alloc((size_t)ns * ns);
 
