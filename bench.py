@@ -21,6 +21,8 @@ the FMO work list is timed in full.  `--impl reference` runs the complete CPU st
 (Davidson to convergence with its own iteration count, then the S1 gradients), and the whole FMO work
 list.  `parity` holds the per-root errors against the oracle's results on the same inputs
 (tests/golden/water128.npz, acene64.npz).
+`--mode acene512` runs the 512-acene aggregate (8 x 8 x 8 lattice: batched TDA, exciton states,
+the LE terms of the lowest exciton state's gradient) once per form with sampled oracle checks.
 Under torchrun (N > 1) every rank runs an independent replica (the path does not shard one
 system); rank 0 prints the JSON line with the max over ranks.
 """
@@ -740,6 +742,156 @@ def run_fmo_once(args):
     ctx.close()
 
 
+def fmo512_workload(workers):
+    """512-acene FMO aggregate: the 64-acene recipe on an 8 x 8 x 8 lattice (13812 atoms)."""
+    from tincr_gb300 import fmo
+    from tincr_gb300 import geometry as G
+    from tincr_gb300 import groundstate as gs
+    z, x, mono = G.acene_lattice(8, 8, 8)
+    mons = fmo.build_monomers(z, G.to_bohr(x), mono, lc=True, workers=workers)
+    pairs = fmo.close_pairs(mons, 4.5 / gs.P.BOHR_TO_ANGS)
+    inst, labels = fmo.aggregate_instances(mons, pairs, FMO_N_LE, FMO_N_CT)
+    return mons, pairs, inst, labels
+
+
+def acene512_parity(mons, setup, inst, labels, r64, rmx, h64, hmx, e64, emx, n_sample=32, n_elem=100, seed=512):
+    """Sampled checks of the 512-acene step against the oracle (too large for it in full):
+    the TDA of n_sample random instances (oracle engines); n_elem random matrix elements of each kind
+    (LE-LE, LE-CT, CT-CT) among those that carry an exchange term, plus n_elem random pairs of
+    states, from the oracle couplings (LCMO Fock block by block) on the GPU roots of the same form;
+    the lowest roots of the GPU FP64 matrix by dense diagonalisation against the GPU Davidson's."""
+    cases, OG, OT = _cpu_helpers()
+    from oracle import exciton as OX
+    rng = np.random.default_rng(seed)
+    out = {}
+    case = dict(monomers=mons, labels=labels, lc=True)
+    n_mon = len(mons)
+    pick = np.concatenate([rng.choice(n_mon, n_sample // 4, replace=False),
+                           n_mon + rng.choice(len(inst) - n_mon, n_sample - n_sample // 4, replace=False)])
+    d64, dmx = 0.0, 0.0
+    for k in pick:
+        eng, xyz = cases.fmo_oracle_engine(case, int(k))
+        r = OT.run_tda_engine(eng, xyz, inst[k]["n_roots"], FMO_MAX_ITER, FMO_TOL)
+        d64 = max(d64, float(np.abs(r64[k]["energies"] - r["energies"]).max()))
+        dmx = max(dmx, float(np.abs(rmx[k]["energies"] - r["energies"]).max()))
+    out["tda_sample"] = {"instances": int(len(pick)), "fp64_max_energy_err_eh": d64, "mixed_max_energy_err_eh": dmx}
+    agg = OX.aggregate_of(mons, setup)
+    states = OX.basis_of(agg, labels, r64, setup.ct_pairs, FMO_N_LE, FMO_N_CT)
+    # the mixed matrix is built from the mixed roots: near-degenerate roots of an instance can come
+    # out as another rotation of the same subspace, so its elements are checked on those roots
+    states_mx = OX.basis_of(agg, labels, rmx, setup.ct_pairs, FMO_N_LE, FMO_N_CT)
+    fb = OX.LcmoFockBlocks(agg)
+    near = lambda a, b: a == b or agg.type_of_pair(a, b) == "pair"
+    le = [i for i, st in enumerate(states) if isinstance(st, OX.LE)]
+    ct = [i for i, st in enumerate(states) if isinstance(st, OX.CT)]
+    mon = lambda st: (st.m,) if isinstance(st, OX.LE) else (st.m_h, st.m_l)
+    chosen = {"le_le": [], "le_ct": [], "ct_ct": [], "any": []}
+    tries = 0
+    while min(len(v) for v in chosen.values()) < n_elem and tries < 200000:
+        tries += 1
+        i, j = (int(v) for v in rng.choice(len(states), 2, replace=False))
+        a, b = states[i], states[j]
+        if len(chosen["any"]) < n_elem:
+            chosen["any"].append((i, j))
+        if isinstance(a, OX.LE) and isinstance(b, OX.LE):
+            kind, ok = "le_le", a.m != b.m and near(a.m, b.m)
+        elif isinstance(a, OX.LE) or isinstance(b, OX.LE):
+            L, C = (a, b) if isinstance(a, OX.LE) else (b, a)
+            kind, ok = "le_ct", near(L.m, C.m_h) or near(L.m, C.m_l)
+        else:
+            kind, ok = "ct_ct", mon(a) != mon(b) and near(a.m_h, b.m_h) and near(a.m_l, b.m_l)
+        if ok and len(chosen[kind]) < n_elem:
+            chosen[kind].append((i, j))
+    # targeted draws for kinds that random pairs rarely hit
+    for _ in range(20 * n_elem):
+        if len(chosen["le_le"]) >= n_elem:
+            break
+        i = int(rng.choice(le))
+        nb = [j for j in le if states[j].m != states[i].m and near(states[j].m, states[i].m)]
+        if nb:
+            chosen["le_le"].append((i, int(rng.choice(nb))))
+    for _ in range(20 * n_elem):
+        if len(chosen["ct_ct"]) >= n_elem:
+            break
+        i = int(rng.choice(ct))
+        nb = [j for j in ct if mon(states[j]) != mon(states[i]) and near(states[j].m_h, states[i].m_h)
+              and near(states[j].m_l, states[i].m_l)]
+        if nb:
+            chosen["ct_ct"].append((i, int(rng.choice(nb))))
+    el = {}
+    for kind, pairs_ in chosen.items():
+        e64k, emxk = 0.0, 0.0
+        for i, j in pairs_:
+            e64k = max(e64k, abs(h64[i, j] - OX.exciton_coupling(agg, fb, None, states[i], states[j])))
+            emxk = max(emxk, abs(hmx[i, j] - OX.exciton_coupling(agg, fb, None, states_mx[i], states_mx[j])))
+        el[kind] = {"elements": len(pairs_), "fp64_max_err_eh": e64k, "mixed_max_err_eh": emxk}
+    out["matrix_sample"] = el
+    w = np.linalg.eigvalsh(h64)[:FMO_N_EXCITON]
+    out["roots"] = {"dense_eigenvalues_of_gpu_fp64_matrix_eh": [float(x) for x in w],
+                    "fp64_davidson_max_err_eh": float(np.abs(e64 - w).max()),
+                    "mixed_davidson_max_err_eh": float(np.abs(emx - w).max())}
+    return out
+
+
+def run_fmo512(args):
+    """--mode acene512: the 512-acene aggregate once per form (batched TDA of the work list, the
+    exciton Hamiltonian and its lowest 10 states, the LE terms of the lowest exciton state's
+    gradient), with sampled oracle checks (`acene512_parity`).  Prints one JSON line."""
+    from tincr_gb300 import _lib, build
+    from tincr_gb300 import fmo
+    build.build()
+    workers = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    mons, pairs, inst, labels = fmo512_workload(workers)
+    t_w = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    # the 8 x 8 x 8 lattice puts some acenes into each other (H-H contacts down to 0.2 A); the SCC of
+    # 8 of those dimers has no stable stationary point, and they take the isolated monomers' orbitals
+    setup = fmo.ExcitonSetup(mons, pairs, workers=workers, unconverged="isolated")
+    t_s = time.perf_counter() - t0
+    ctx = _lib.Context(0)
+    gctxs = [_lib.Context(0) for _ in range(8)]
+    n_mon = len(mons)
+    out = {"mode": "acene512", "workload": "acene512-fmo-le4-ct1-exciton10", "monomers": n_mon,
+           "atoms": int(sum(m.system.n_atoms for m in mons)), "ct_pairs": len(pairs), "instances": len(inst),
+           "real_pairs": len(setup.real_pairs), "dimers_without_scc_solution": [list(k) for k in setup.unconverged_pairs],
+           "host_setup_s": t_w, "host_exciton_setup_s": t_s}
+    runs = {}
+    for name, prec in (("bf16x3", _lib.PREC_BF16X3), ("fp64", _lib.PREC_FP64)):
+        fmo.solve_batch(ctx, inst, FMO_MAX_ITER, FMO_TOL, prec)   # warm-up (tile autotuner, graphs)
+        t0 = time.perf_counter()
+        rc, r = fmo.solve_batch(ctx, inst, FMO_MAX_ITER, FMO_TOL, prec)
+        t_b = ctx.last_timing()[0]
+        ex = fmo.exciton_states(ctx, setup, r, labels, FMO_N_LE, FMO_N_CT, n_roots=FMO_N_EXCITON, tol=FMO_EX_TOL,
+                                max_iter=FMO_EX_MAX_ITER, precision=prec, want_matrix=True)
+        t_e = ctx.last_timing()[0]
+        g, n_le_t, n_ct_t = fmo.exciton_le_gradient(mons, r, ex["vectors"][:, 0], FMO_N_LE,
+                                                    n_ct_states=len(ex["vectors"]) - n_mon * FMO_N_LE,
+                                                    contexts=gctxs, precision=prec)
+        wall = time.perf_counter() - t0
+        runs[name] = (rc, r, ex, g)
+        out[name] = {"batch_tda_ms": t_b, "exciton_ms": t_e, "wall_s": wall, "status_ok": rc == _lib.OK,
+                     "exciton_states": int(len(ex["vectors"])), "exciton_iterations": int(ex["iterations"]),
+                     "exciton_energies_eh": [float(e) for e in ex["energies"]],
+                     "lowest_state_le_gradient_terms": n_le_t, "lowest_state_ct_terms_not_built": n_ct_t,
+                     "le_gradient_norm": float(np.linalg.norm(g))}
+    for c in gctxs:
+        c.close()
+    ctx.close()
+    (_, r64, ex64, g64), (_, rmx, exmx, gmx) = runs["fp64"], runs["bf16x3"]
+    out["mixed_vs_fp64"] = {
+        "max_instance_energy_err_eh": float(max(np.abs(a["energies"] - b["energies"]).max() for a, b in zip(rmx, r64))),
+        "max_exciton_energy_err_eh": float(np.abs(exmx["energies"] - ex64["energies"]).max()),
+        "max_le_gradient_err_eh_per_bohr": float(np.abs(gmx - g64).max()),
+        "speedup_batch_plus_exciton": (out["fp64"]["batch_tda_ms"] + out["fp64"]["exciton_ms"]) /
+                                      (out["bf16x3"]["batch_tda_ms"] + out["bf16x3"]["exciton_ms"])}
+    t0 = time.perf_counter()
+    out["parity"] = acene512_parity(mons, setup, inst, labels, r64, rmx, ex64["matrix"], exmx["matrix"],
+                                    ex64["energies"], exmx["energies"])
+    out["parity"]["oracle_s"] = time.perf_counter() - t0
+    print(json.dumps(out))
+
+
 def run_products(args):
     """Profiling helper: set up the workload and evaluate A.X for `--k` random trial vectors once
     (used for ncu captures of the product kernels on the full-size system)."""
@@ -773,7 +925,7 @@ def main():
     ap.add_argument("--ref-products", type=int, default=None)
     ap.add_argument("--ref-iters", type=int, default=None)
     ap.add_argument("--ref-cg", type=int, default=None)
-    ap.add_argument("--mode", default="solve", choices=["solve", "products", "fmo", "cpu-sample"])
+    ap.add_argument("--mode", default="solve", choices=["solve", "products", "fmo", "cpu-sample", "acene512"])
     ap.add_argument("--k", type=int, default=4)
     args = ap.parse_args()
     if args.mode == "products":
@@ -781,6 +933,9 @@ def main():
         return
     if args.mode == "fmo":
         run_fmo_once(args)
+        return
+    if args.mode == "acene512":
+        run_fmo512(args)
         return
     if args.mode == "cpu-sample":
         if None in (args.ref_products, args.ref_iters, args.ref_cg):

@@ -152,6 +152,82 @@ def lcmo_fock(agg):
     return (x.T @ fock) @ x, off
 
 
+class LcmoFockBlocks:
+    """Blocks of the LCMO Fock matrix F' = x^T F x (`lcmo_fock`) without the dense matrix, for
+    aggregates whose MO space is too large to hold it: x = I - 1/2 S_off, with S_off and F nonzero only
+    on the diagonal blocks and between the monomers of real pairs, so
+        F'_xy = sum_{k in {x} + nb(x)} sum_{m in {y} + nb(y)} x_kx^T F_km x_my,
+    x_kx = I for k == x and -1/2 S_kx otherwise (nb = real-pair neighbours).  The same sums of the
+    same pair quantities as the dense form (hamiltonian.rs:12-152), block by block; blocks cached."""
+
+    def __init__(self, agg):
+        self.agg = agg
+        n = len(agg.frags)
+        self.nb = [[] for _ in range(n)]
+        for (i, j), t in agg.pair_types.items():
+            if t == "pair":
+                self.nb[i].append(j)
+                self.nb[j].append(i)
+        self._pair = {}
+        self._f = {}
+        self._fp = {}
+
+    def _pair_terms(self, i, j):
+        """(s_pq, f_aa, f_bb, f_ab) of the real pair i < j (hamiltonian.rs:46-110)."""
+        key = (i, j)
+        if key not in self._pair:
+            agg = self.agg
+            fi, fj = agg.frags[i], agg.frags[j]
+            orbs_ij, orbe_ij = agg.pair_scc[(i, j)]
+            ni = fi.n_orb
+            s_pair = np.block([[fi.s, agg.s_block(i, j)], [agg.s_block(j, i), fj.s]])
+            s_pr = (fi.orbs.T @ s_pair[:ni, :]) @ orbs_ij
+            s_qr = (fj.orbs.T @ s_pair[ni:, :]) @ orbs_ij
+            s_pq = (fi.orbs.T @ s_pair[:ni, ni:]) @ fj.orbs
+            self._pair[key] = (s_pq, (s_pr * orbe_ij) @ s_pr.T, (s_qr * orbe_ij) @ s_qr.T,
+                               (s_pr * orbe_ij) @ s_qr.T)
+        return self._pair[key]
+
+    def s(self, k, m):
+        """MO overlap block S_km of a real pair (k != m)."""
+        s_pq = self._pair_terms(min(k, m), max(k, m))[0]
+        return s_pq if k < m else s_pq.T
+
+    def f(self, k, m):
+        """Block F_km before the transformation (zero unless k == m or k, m is a real pair)."""
+        key = (k, m)
+        if key not in self._f:
+            frags = self.agg.frags
+            if k == m:
+                out = np.diag(frags[k].orbe).astype(float)
+                for o in self.nb[k]:
+                    _, f_aa, f_bb, _ = self._pair_terms(min(k, o), max(k, o))
+                    out = out + (f_aa if k < o else f_bb) - np.diag(frags[k].orbe)
+            elif m in self.nb[k]:
+                f_ab = self._pair_terms(min(k, m), max(k, m))[3]
+                out = f_ab if k < m else f_ab.T
+            else:
+                out = None
+            self._f[key] = out
+        return self._f[key]
+
+    def __call__(self, x, y):
+        key = (x, y)
+        if key not in self._fp:
+            frags = self.agg.frags
+            out = np.zeros((frags[x].n_orb, frags[y].n_orb))
+            for k in [x] + self.nb[x]:
+                xk = None if k == x else -0.5 * self.s(k, x)
+                for m in [y] + self.nb[y]:
+                    fkm = self.f(k, m)
+                    if fkm is None:
+                        continue
+                    t = fkm if m == y else fkm @ (-0.5 * self.s(m, y))
+                    out += t if xk is None else xk.T @ t
+            self._fp[key] = out
+        return self._fp[key]
+
+
 # ----------------------------------------------------------------------------------------------
 # diabatic basis states
 # ----------------------------------------------------------------------------------------------
@@ -273,6 +349,14 @@ def le_le(agg, a, b):
     return 2.0 * coulomb - exchange
 
 
+def fock_block(fock, off, i, j):
+    """MO block (monomer i, monomer j) of the LCMO Fock matrix: `fock` is the dense matrix of
+    `lcmo_fock` (with its offsets `off`) or a callable (i, j) -> block, such as `LcmoFockBlocks`."""
+    if callable(fock):
+        return fock(i, j)
+    return fock[off[i]:off[i + 1], off[j]:off[j + 1]]
+
+
 def le_ct_1e(agg, fock, off, le, ct):
     """`le_ct_1e_new` (integrals.rs:542-600): one-electron coupling through the LCMO Fock matrix
     when the LE monomer carries the CT state's electron (occupied block, minus sign) or hole
@@ -280,12 +364,12 @@ def le_ct_1e(agg, fock, off, le, ct):
     fi = agg.frags[le.m]
     if le.m == ct.m_l:
         fh = agg.frags[ct.m_h]
-        f_ij = fock[off[le.m]:off[le.m] + fi.n_occ, off[ct.m_h]:off[ct.m_h] + fh.n_occ]
+        f_ij = fock_block(fock, off, le.m, ct.m_h)[:fi.n_occ, :fh.n_occ]
         t_ij = le.tdm @ ct.tdm.T
         return -float(np.sum(f_ij * t_ij))
     if le.m == ct.m_h:
         fl = agg.frags[ct.m_l]
-        f_ab = fock[off[le.m] + fi.n_occ:off[le.m + 1], off[ct.m_l] + fl.n_occ:off[ct.m_l + 1]]
+        f_ab = fock_block(fock, off, le.m, ct.m_l)[fi.n_occ:, fl.n_occ:]
         t_ab = le.tdm.T @ ct.tdm
         return float(np.sum(f_ab * t_ab))
     return 0.0

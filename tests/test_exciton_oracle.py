@@ -136,3 +136,24 @@ def test_dimer_scc_from_monomer_densities():
     assert not gs.run_scc(sy, tol=1e-10, max_iter=2).converged
     with pytest.raises(RuntimeError):
         gs.run_scc(sy, tol=1e-10, max_iter=2, require_convergence=True)
+    # the level shift (the fallback for dimers whose occupations swap) keeps the stationary density
+    gsh = gs.run_scc(sy, tol=1e-10, p_start=p_start, level_shift=0.5, max_iter=1000, require_convergence=True)
+    assert abs(gsh.energy - ref.energy) < 1e-9
+    assert np.abs(gsh.orbe - ref.orbe).max() < 1e-8
+
+
+def test_lcmo_fock_blocks_equal_the_dense_matrix(agg3):
+    """The block-by-block LCMO Fock matrix (for aggregates too large for the dense x^T F x) equals
+    the dense one on every pair of monomers."""
+    c, setup, agg, states = agg3
+    fock, off = OX.lcmo_fock(agg)
+    fb = OX.LcmoFockBlocks(agg)
+    n = len(agg.frags)
+    for i in range(n):
+        for j in range(n):
+            assert np.abs(fb(i, j) - fock[off[i]:off[i + 1], off[j]:off[j + 1]]).max() < 1e-12
+    # and the couplings through it
+    for a in range(len(states)):
+        for b in range(len(states)):
+            assert abs(OX.exciton_coupling(agg, fb, None, states[a], states[b]) -
+                       OX.exciton_coupling(agg, fock, off, states[a], states[b])) < 1e-12

@@ -6,12 +6,13 @@
 // two monomers for every element.  Here the matrix is assembled on the GPU in a few grouped passes:
 //   * Coulomb: W = gamma Q over all atoms, then 2 q_s . W_t for every element (block-sparse Q: each
 //     state's charges live on one or two monomers);
-//   * exchange: one CTA per (element, tile of the (a, j) index pairs).  The charges are never
-//     stored: with Mulliken charges q^A_pq = 1/2 sum_{mu in A} (C_mu p (S C)_mu q + (S C)_mu p C_mu q)
-//     over the AOs of the one or two monomers involved, sum_i q^A_ij b_ia is a sum over mu in A of
-//     two outer products of per-AO rows, so each job forms four small [AO x tile] arrays from C, S C
-//     (per monomer) and S_xy C_y (per pair), then
-//       exchange = sum_{A, B} gamma_lr[A, B] sum_{a, j} U^A_aj W^B_aj;
+//   * exchange: the charges are never stored.  With Mulliken charges
+//     q^A_pq = 1/2 sum_{mu in A} (C_mu p (S C)_mu q + (S C)_mu p C_mu q) over the AOs of the one or
+//     two monomers involved, sum_i q^A_ij b_ia is a sum over mu in A of two outer products of per-AO
+//     rows, and exchange = sum_{A, B} gamma_lr[A, B] sum_{a, j} U^A_aj W^B_aj.  The state-dependent
+//     rows come from batched small GEMMs; V = gamma_lr W is formed once per group of elements that
+//     share their second state and monomers, in one CTA per tile of (a, j), which then serves the
+//     group's elements (see "exchange integrals" below);
 //   * one-electron LE-CT terms through the LCMO Fock matrix (src/fmo/lcmo/hamiltonian.rs:12-152),
 //     whose needed blocks F'_{xy} = (x^T F x)_{xy}, x = 3/2 I - 1/2 S_total, come from block-sparse
 //     products over the real pairs around x and y (batched small GEMMs);

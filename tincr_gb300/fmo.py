@@ -36,14 +36,44 @@ class Monomer:
         self.ground = ground
 
 
-def build_monomers(numbers, xyz_bohr, monomer_of_atom, lc=True, r_lr=gs.LONG_RANGE_RADIUS, scc_tol=1e-10):
-    """Monomers by construction (one per distinct `monomer_of_atom` value), each with a host SCC."""
-    mons = []
+def _monomer_scc(args):
+    """Host SCC of one monomer (top-level for a spawn process pool)."""
+    sy, tol = args
+    return gs.run_scc(sy, tol=tol, require_convergence=True)
+
+
+def build_monomers(numbers, xyz_bohr, monomer_of_atom, lc=True, r_lr=gs.LONG_RANGE_RADIUS, scc_tol=1e-10, workers=1):
+    """Monomers by construction (one per distinct `monomer_of_atom` value), each with a host SCC
+    (`workers` > 1: in a spawn process pool, one BLAS thread per worker)."""
+    systems = []
     for k in np.unique(monomer_of_atom):
         at = np.nonzero(monomer_of_atom == k)[0]
-        sy = gs.build_system(numbers[at], xyz_bohr[at], lc=lc, r_lr=r_lr)
-        mons.append(Monomer(int(k), at, sy, gs.run_scc(sy, tol=scc_tol, require_convergence=True)))
-    return mons
+        systems.append((int(k), at, gs.build_system(numbers[at], xyz_bohr[at], lc=lc, r_lr=r_lr)))
+    jobs = [(sy, scc_tol) for _, _, sy in systems]
+    grounds = _pool_map(_monomer_scc, jobs, workers)
+    return [Monomer(k, at, sy, g) for (k, at, sy), g in zip(systems, grounds)]
+
+
+def _pool_map(fn, jobs, workers, chunksize=4):
+    """map(fn, jobs), in a spawn process pool when workers > 1 (the caller needs a __main__
+    guard).  One BLAS thread per worker: the workers already fill the cores, and a full-width BLAS
+    pool in each of them would oversubscribe the host."""
+    if workers <= 1 or len(jobs) <= 1:
+        return [fn(a) for a in jobs]
+    import multiprocessing as mp
+    from concurrent.futures import ProcessPoolExecutor
+    names = ("OMP_NUM_THREADS", "OPENBLAS_NUM_THREADS", "MKL_NUM_THREADS")
+    saved = {k: os.environ.get(k) for k in names}
+    os.environ.update({k: "1" for k in names})
+    try:
+        with ProcessPoolExecutor(max_workers=workers, mp_context=mp.get_context("spawn")) as ex:
+            return list(ex.map(fn, jobs, chunksize=chunksize))
+    finally:
+        for k, v in saved.items():
+            if v is None:
+                os.environ.pop(k, None)
+            else:
+                os.environ[k] = v
 
 
 def candidate_pairs(monomers, reach_bohr):
@@ -325,6 +355,41 @@ def le_gradients(monomers, results, states, n_streams=8, variant="reference", co
     return out
 
 
+def exciton_le_gradient(monomers, results, vector, n_le, threshold=0.05, n_ct_states=0, **kw):
+    """The LE terms of tincr's exciton-state gradient (`SuperSystem::fmo_cis_gradient`,
+    src/fmo/lcmo/cis_gradient.rs:10-166): for every LE basis state with |c| > threshold in the
+    exciton eigenvector `vector` (basis order: n_le LE states per monomer first), c^2 times that LE
+    state's excitation gradient, added on the monomer's atoms.  The CT basis states' terms
+    (`ct_gradient_new`, cis_gradient.rs:127-163) are not part of this function; their number above
+    the threshold is returned so that a caller can report it.
+
+    `results` are the batch TDA results of the monomers (LE instances, monomer order); the keyword
+    arguments go to `le_gradients`.  Returns (gradient [3 N_total] in the aggregate's atom order,
+    number of LE terms, number of CT terms above the threshold)."""
+    n_mon = len(monomers)
+    terms = []
+    for b, c in enumerate(np.asarray(vector)):
+        if abs(c) > threshold and b < n_mon * n_le:
+            terms.append((b // n_le, b % n_le, float(c) ** 2))
+    n_ct = int(np.sum(np.abs(np.asarray(vector)[n_mon * n_le:n_mon * n_le + n_ct_states]) > threshold))
+    offs = np.concatenate([[0], np.cumsum([m.system.n_atoms for m in monomers])])
+    grad = np.zeros(3 * int(offs[-1]))
+    pending = list(terms)
+    while pending:   # one state per monomer per round
+        seen, batch, rest = set(), [], []
+        for t in pending:
+            (rest if t[0] in seen else batch).append(t)
+            seen.add(t[0])
+        pending = rest
+        states = [None] * n_mon
+        for k, r, _ in batch:
+            states[k] = r
+        g = le_gradients(monomers, results[:n_mon], states, **kw)
+        for k, r, w in batch:
+            grad[3 * offs[k]:3 * offs[k + 1]] += w * g[k]
+    return grad, len(terms), n_ct
+
+
 # ----------------------------------------------------------------------------------------------
 # exciton Hamiltonian inputs (upstream of the couplings: pair types, overlaps, gamma, pair SCC)
 # ----------------------------------------------------------------------------------------------
@@ -351,10 +416,23 @@ def _dimer_scc(args):
     panics, pair.rs:234-240): from the neutral-atom density a few dimers of a dense aggregate stall
     past the iteration limit, and an unconverged dimer would hand machine-dependent orbitals to the
     LCMO Fock matrix."""
-    z, xyz, lc, r_lr, tol, p_start = args
+    z, xyz, lc, r_lr, tol, p_start, isolated = args
     sy = gs.build_system(z, xyz, lc=lc, r_lr=r_lr)
-    g = gs.run_scc(sy, tol=tol, p_start=p_start, require_convergence=True)
-    return g.orbs, g.orbe
+    g = gs.run_scc(sy, tol=tol, p_start=p_start)
+    if not g.converged:
+        # some dimers of the benchmark lattices overlap (H-H contacts under 0.5 A) and their DIIS swaps
+        # occupations; a level shift of the virtual space settles some of them on a stationary density
+        g = gs.run_scc(sy, tol=tol, p_start=p_start, level_shift=0.5, max_iter=1000,
+                       require_convergence=isolated is None)
+    if not g.converged:
+        # the caller's policy for a dimer without a stationary ground state: the isolated monomers'
+        # orbitals (block diagonal) and energies as its pair ground state
+        (ca, ea), (cb, eb) = isolated
+        orbs = np.zeros((len(ea) + len(eb), len(ea) + len(eb)))
+        orbs[:len(ea), :len(ea)] = ca
+        orbs[len(ea):, len(ea):] = cb
+        return orbs, np.concatenate([ea, eb]), False
+    return g.orbs, g.orbe, True
 
 
 class ExcitonSetup:
@@ -366,9 +444,12 @@ class ExcitonSetup:
     * the atomwise gamma and gamma_lr of the whole aggregate;
     * the ground state (MO coefficients, energies) of every real pair's dimer, for the LCMO Fock
       matrix (tincr's FMO pair SCC; here the isolated dimer, like the monomers).
-    `workers` > 1 runs the dimer SCCs in a spawn process pool."""
+    `workers` > 1 runs the dimer SCCs in a spawn process pool.  A dimer SCC that does not converge,
+    neither by DIIS from the monomers' densities nor with a level shift, raises (tincr panics) unless
+    `unconverged="isolated"`, which gives such a dimer the isolated monomers' orbitals and energies as
+    its pair ground state; `unconverged_pairs` lists those dimers."""
 
-    def __init__(self, monomers, ct_pairs, lc=True, scc_tol=1e-10, workers=1):
+    def __init__(self, monomers, ct_pairs, lc=True, scc_tol=1e-10, workers=1, unconverged="raise"):
         self.monomers = monomers
         self.ct_pairs = list(ct_pairs)
         n = len(monomers)
@@ -401,28 +482,13 @@ class ExcitonSetup:
             p_start = np.zeros((ni + nj, ni + nj))
             p_start[:ni, :ni] = mi.ground.p
             p_start[ni:, ni:] = mj.ground.p
+            iso = ((mi.ground.orbs, mi.ground.orbe), (mj.ground.orbs, mj.ground.orbe)) \
+                if unconverged == "isolated" else None
             jobs.append((np.concatenate([mi.system.numbers, mj.system.numbers]),
-                         np.concatenate([mi.system.xyz, mj.system.xyz]), lc, self.r_lr, scc_tol, p_start))
-        if workers > 1 and len(jobs) > 1:
-            import multiprocessing as mp
-            from concurrent.futures import ProcessPoolExecutor
-            # one BLAS thread per worker: the workers already fill the cores, and a full-width BLAS
-            # pool in each of them oversubscribes the host by workers x cores threads
-            names = ("OMP_NUM_THREADS", "OPENBLAS_NUM_THREADS", "MKL_NUM_THREADS")
-            saved = {k: os.environ.get(k) for k in names}
-            os.environ.update({k: "1" for k in names})
-            try:
-                with ProcessPoolExecutor(max_workers=workers, mp_context=mp.get_context("spawn")) as ex:
-                    out = list(ex.map(_dimer_scc, jobs, chunksize=4))
-            finally:
-                for k, v in saved.items():
-                    if v is None:
-                        os.environ.pop(k, None)
-                    else:
-                        os.environ[k] = v
-        else:
-            out = [_dimer_scc(a) for a in jobs]
-        self.pair_scc = {k: o for k, o in zip(self.real_pairs, out)}
+                         np.concatenate([mi.system.xyz, mj.system.xyz]), lc, self.r_lr, scc_tol, p_start, iso))
+        out = _pool_map(_dimer_scc, jobs, workers)
+        self.pair_scc = {k: (o[0], o[1]) for k, o in zip(self.real_pairs, out)}
+        self.unconverged_pairs = [k for k, o in zip(self.real_pairs, out) if not o[2]]
 
     def s_block(self, i, j):
         """AO overlap between monomers i and j (rows i).  Pairs without a stored block are ESD pairs

@@ -272,13 +272,18 @@ class GroundState:
     energy: float
     iterations: int
     converged: bool = True
+    residual: float = 0.0      # largest |[F, P]| element (orthogonalised basis) of the last iterate
 
 
-def run_scc(sysm, tol=1e-10, max_iter=250, s_h0=None, p_start=None, require_convergence=False):
+def run_scc(sysm, tol=1e-10, max_iter=250, s_h0=None, p_start=None, require_convergence=False, level_shift=0.0):
     """Restricted closed-shell SCC to ||[F, P]|| < tol, from the reference (neutral-atom) density or
     from `p_start` (tincr starts a pair SCC from its monomers' charges, src/fmo/scc/pair.rs:112-124).
     The result's `converged` says whether the test was met within max_iter iterations; with
-    `require_convergence` a miss raises RuntimeError (tincr panics there, pair.rs:234-240)."""
+    `require_convergence` a miss raises RuntimeError (tincr panics there, pair.rs:234-240).
+    `level_shift` > 0 raises the virtual orbitals of the matrix that is diagonalised by that much
+    (F + shift (S - S P S / 2) for the current density P): a stationary density is unchanged, but
+    an aufbau occupation that swaps between near-degenerate orbitals from one iteration to the next
+    settles."""
     s, h0 = s_h0 if s_h0 is not None else h0_and_s(sysm)
     gamma = gamma_atomwise(sysm, 0.0)
     gamma_lr = gamma_atomwise(sysm, sysm.r_lr) if sysm.lc else np.zeros_like(gamma)
@@ -326,6 +331,8 @@ def run_scc(sysm, tol=1e-10, max_iter=250, s_h0=None, p_start=None, require_conv
                 f_use = f
         else:
             f_use = f
+        if level_shift:
+            f_use = f_use + level_shift * (s - 0.5 * s @ p @ s)
         orbe, cp = np.linalg.eigh(x.T @ f_use @ x)
         orbs = x @ cp
         occ_c = orbs[:, :n_occ]
@@ -344,4 +351,4 @@ def run_scc(sysm, tol=1e-10, max_iter=250, s_h0=None, p_start=None, require_conv
         e_el += -0.125 * float(np.sum((s @ dp @ s) * dp * g_lr_ao) + np.sum((s @ dp) * (dp @ s) * g_lr_ao))
     return GroundState(s=s, h0=h0, gamma=gamma, gamma_lr=gamma_lr, orbs=np.ascontiguousarray(orbs),
                        orbe=orbe, p=p, p0=p0, dq=dq, h_coul_x=f, energy=e_el + repulsive_energy(sysm),
-                       iterations=it, converged=converged)
+                       iterations=it, converged=converged, residual=float(errn))
