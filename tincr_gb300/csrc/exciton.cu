@@ -556,28 +556,6 @@ __global__ void ex_row_norms_kernel(int k, int n, const double *__restrict__ a, 
     }
 }
 
-// v -= c^T V (c: m coefficients), one thread per component; each CTA's sum of squares into part[]
-__global__ void ex_orth_update_kernel(int m, int n, const double *__restrict__ V, const double *__restrict__ c,
-                                      double *v, double *part) {
-    __shared__ double red[8];
-    const int x = blockIdx.x * blockDim.x + threadIdx.x;
-    double s = 0.0;
-    if (x < n) {
-        double y = v[x];
-        for (int i = 0; i < m; ++i) y -= c[i] * V[(long long)i * n + x];
-        v[x] = y;
-        s = y * y;
-    }
-    for (int off = 16; off; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
-    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        double t = 0.0;
-        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w];
-        part[blockIdx.x] = t;
-    }
-}
-
 // *nrm = sqrt(sum of the k partial sums), added in a fixed order
 __global__ void ex_norm_finish_kernel(int k, const double *__restrict__ part, double *nrm) {
     if (threadIdx.x == 0) {
@@ -613,8 +591,10 @@ __global__ void ex_dotmat_kernel(int M, int N, int K, const double *__restrict__
     if (lane == 0) C[(long long)i * N + j] = acc;
 }
 
-// c[i] = V_i . v (one CTA per i)
-__global__ void ex_dots_kernel(int m, int n, const double *__restrict__ V, const double *__restrict__ v, double *c) {
+// the Davidson's growing basis with its size m in device memory: c[i] = V_i . v for i < *m
+__global__ void ex_dots_dev_kernel(const int *__restrict__ m, int n, const double *__restrict__ V,
+                                   const double *__restrict__ v, double *c) {
+    if ((int)blockIdx.x >= *m) return;
     __shared__ double red[8];
     const double *row = V + (long long)blockIdx.x * n;
     double s = 0.0;
@@ -629,9 +609,46 @@ __global__ void ex_dots_kernel(int m, int n, const double *__restrict__ V, const
     }
 }
 
-__global__ void ex_scale_kernel(int n, double f, const double *__restrict__ in, double *out) {
+// v -= c^T V for i < *m, one thread per component; each CTA's sum of squares into part[]
+__global__ void ex_orth_update_dev_kernel(const int *__restrict__ m, int n, const double *__restrict__ V,
+                                          const double *__restrict__ c, double *v, double *part) {
+    __shared__ double red[8];
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, mm = *m;
+    double s = 0.0;
+    if (x < n) {
+        double y = v[x];
+        for (int i = 0; i < mm; ++i) y -= c[i] * V[(long long)i * n + x];
+        v[x] = y;
+        s = y * y;
+    }
+    for (int off = 16; off; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w];
+        part[blockIdx.x] = t;
+    }
+}
+
+// tincr's drop rule (davidson.rs:162-168): the correction joins the basis as row *m when its norm
+// exceeds 1e-8 (and the basis has room); ex_count_kernel then advances *m
+__global__ void ex_append_kernel(int n, const double *__restrict__ nrm, const int *__restrict__ m, int cap,
+                                 const double *__restrict__ t, double *V) {
+    const double r = *nrm;
+    const int mm = *m;
+    if (!(r > 1.0e-8) || mm >= cap) return;
+    const double f = 1.0 / r;
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
-    if (x < n) out[x] = in[x] * f;
+    if (x < n) V[(long long)mm * n + x] = t[x] * f;
+}
+
+__global__ void ex_count_kernel(const double *__restrict__ nrm, int *m, int cap) {
+    if (threadIdx.x == 0 && *nrm > 1.0e-8 && *m < cap) ++*m;
+}
+
+__global__ void ex_set_int_kernel(int *p, int v) {
+    if (threadIdx.x == 0) *p = v;
 }
 
 __global__ void ex_diag_kernel(int n, const double *__restrict__ H, double *d) {
@@ -724,7 +741,7 @@ int Ctx::exciton_states(int n_mono, const tincr_exciton_monomer *mono, int n_pai
     // the large inputs (gamma, gamma_lr, the real pairs' dimer orbitals) go through the context's
     // page-locked staging buffer: parallel host copies, then one DMA each
     const size_t n_g = (size_t)n_atoms_total * n_atoms_total;
-    size_t pin_need = 2 * n_g;
+    size_t pin_need = 2 * n_g + 1;   // (+1: the Davidson's basis size read back)
     for (int p = 0; p < n_pairs; ++p)   // (pairs with bad indices are rejected below)
         if (pairs[p].real && pairs[p].i >= 0 && pairs[p].i < n_mono && pairs[p].j >= 0 && pairs[p].j < n_mono) {
             const size_t nij = (size_t)nao[pairs[p].i] + nao[pairs[p].j];
@@ -986,48 +1003,80 @@ int Ctx::exciton_states(int n_mono, const tincr_exciton_monomer *mono, int n_pai
         return id;
     };
     auto listed = [&](int a, int b) { return a == b || cross(a, b) != nullptr; };
-    auto near = [&](int a, int b) { return a == b || is_real(a, b); };   // pair type Pair or None
-    for (int s = 0; s < ns; ++s)
-        for (int t = s + 1; t < ns; ++t) {
-            const ExState &A = hst[s], &B = hst[t];
-            const double *Xs = dX.p + xoff[s], *Xt = dX.p + xoff[t];
-            if (A.kind == 0 && B.kind == 0) {
-                // le_le (integrals.rs:81-169): exchange for real pairs, full orbital spaces
-                if (A.hole == B.hole || !is_real(A.hole, B.hole)) continue;
-                const int I = A.hole, Jm = B.hole, oI = no[I], vI = nao[I] - oI, oJ = no[Jm], vJ = nao[Jm] - oJ;
-                const int k1 = k1_cached(0, s, Jm, 0, I, Jm, 0, oI, 0, vI, Xs, vI, 0);
-                const int k2 = k2_of(1, t, I, 0, I, Jm, I, Jm, oI, vI, oJ, vJ, oJ, Xt, vJ, 0);
-                elv.push_back(ExEl{s, t, k1, k2});
-            } else if (A.kind == 0 || B.kind == 0) {
-                // le_ct_2e_new (integrals.rs:602-727): exchange when the LE monomer is the hole, the
-                // electron or a real-pair neighbour of either; restricted active spaces.  A pair that
-                // is not listed is an ESD pair, whose AO overlap is zero (its atoms are farther apart
-                // than the Slater-Koster tables reach): its charges, and the integral, vanish.
-                const int le = A.kind == 0 ? s : t, ct = A.kind == 0 ? t : s;
-                const ExState &L = hst[le], &C = hst[ct];
-                const int I = L.hole, h = C.hole, l = C.elec;
-                if (!(near(I, h) || near(I, l)) || !listed(I, h) || !listed(I, l)) continue;
-                const int oI = no[I], vI = nao[I] - oI, oh = no[h], vl = nao[l] - no[l];
+    // the elements that carry an exchange term, from neighbour lists (real pairs) rather than from all
+    // pairs of states
+    std::vector<std::vector<int>> nbr(n_mono);
+    for (int p = 0; p < n_pairs; ++p)
+        if (pairs[p].real) {
+            nbr[pairs[p].i].push_back(pairs[p].j);
+            nbr[pairs[p].j].push_back(pairs[p].i);
+        }
+    for (auto &v : nbr) std::sort(v.begin(), v.end());
+    std::vector<int> le0(n_mono + 1, 0);   // LE states of monomer k: [le0[k], le0[k + 1])
+    for (int k = 0; k < n_mono; ++k) le0[k + 1] = le0[k] + mono[k].n_le;
+    const int n_le_states = le0[n_mono];
+    std::unordered_map<long long, std::vector<int>> ct_at;   // (hole, electron) -> CT states
+    for (int t = n_le_states; t < ns; ++t) ct_at[(long long)hst[t].hole * n_mono + hst[t].elec].push_back(t);
+    // le_le (integrals.rs:81-169): exchange for real pairs, full orbital spaces
+    for (int I = 0; I < n_mono; ++I)
+        for (int Jm : nbr[I]) {
+            if (Jm < I) continue;
+            const int oI = no[I], vI = nao[I] - oI, oJ = no[Jm], vJ = nao[Jm] - oJ;
+            for (int s = le0[I]; s < le0[I + 1]; ++s)
+                for (int t = le0[Jm]; t < le0[Jm + 1]; ++t) {
+                    const int k1 = k1_cached(0, s, Jm, 0, I, Jm, 0, oI, 0, vI, dX.p + xoff[s], vI, 0);
+                    const int k2 = k2_of(1, t, I, 0, I, Jm, I, Jm, oI, vI, oJ, vJ, oJ, dX.p + xoff[t], vJ, 0);
+                    elv.push_back(ExEl{s, t, k1, k2});
+                }
+        }
+    // le_ct_2e_new (integrals.rs:602-727): exchange when the LE monomer is the hole, the electron or a
+    // real-pair neighbour of either; restricted active spaces.  A pair that is not listed is an ESD
+    // pair, whose AO overlap is zero (its atoms are farther apart than the Slater-Koster tables
+    // reach): its charges, and the integral, vanish.
+    std::vector<int> cand;
+    for (int ct = n_le_states; ct < ns; ++ct) {
+        const int h = hst[ct].hole, l = hst[ct].elec;
+        cand.assign({h, l});
+        cand.insert(cand.end(), nbr[h].begin(), nbr[h].end());
+        cand.insert(cand.end(), nbr[l].begin(), nbr[l].end());
+        std::sort(cand.begin(), cand.end());
+        cand.erase(std::unique(cand.begin(), cand.end()), cand.end());
+        const int oh = no[h], vl = nao[l] - no[l];
+        for (int I : cand) {
+            if (!listed(I, h) || !listed(I, l)) continue;
+            const int oI = no[I], vI = nao[I] - oI;
+            for (int le = le0[I]; le < le0[I + 1]; ++le) {
                 const int k1 = k1_cached(2, le, h, 1, I, h, oI - ACTIVE, ACTIVE, oh - ACTIVE, ACTIVE, dX.p + xoff[le],
                                          vI, oI - ACTIVE);
                 const int k2 = k2_of(3, ct, I, 1, I, h, I, l, oI, ACTIVE, no[l], ACTIVE, ACTIVE, dX.p + xoff[ct], vl,
                                      oh - ACTIVE);
-                elv.push_back(ExEl{std::min(le, ct), std::max(le, ct), k1, k2});
-            } else {
-                // ct_ct_new (integrals.rs:733-878): exchange when the holes and the electrons are each on
-                // the same monomer or on a real pair; restricted active spaces
-                if (A.hole == B.hole && A.elec == B.elec) continue;
-                if (!(near(A.hole, B.hole) && near(A.elec, B.elec))) continue;
-                const int h1 = A.hole, l1 = A.elec, h2 = B.hole, l2 = B.elec;
-                if (!listed(h1, h2) || !listed(l1, l2)) continue;
-                const int v1 = nao[l1] - no[l1], v2 = nao[l2] - no[l2];
-                const int k1 = k1_cached(4, s, h2, 1, h1, h2, no[h1] - ACTIVE, ACTIVE, no[h2] - ACTIVE, ACTIVE, Xs,
-                                         v1, no[h1] - ACTIVE);
-                const int k2 = k2_of(-1, t, 0, 1, h1, h2, l1, l2, no[l1], ACTIVE, no[l2], ACTIVE, ACTIVE, Xt, v2,
-                                     no[h2] - ACTIVE);
-                elv.push_back(ExEl{s, t, k1, k2});
+                elv.push_back(ExEl{le, ct, k1, k2});
             }
         }
+    }
+    // ct_ct_new (integrals.rs:733-878): exchange when the holes and the electrons are each on the same
+    // monomer or on a real pair (but not both the same pair); restricted active spaces
+    for (int s = n_le_states; s < ns; ++s) {
+        const int h1 = hst[s].hole, l1 = hst[s].elec, v1 = nao[l1] - no[l1];
+        for (int hi = -1; hi < (int)nbr[h1].size(); ++hi) {
+            const int h2 = hi < 0 ? h1 : nbr[h1][hi];
+            for (int li = -1; li < (int)nbr[l1].size(); ++li) {
+                const int l2 = li < 0 ? l1 : nbr[l1][li];
+                if (h2 == l2) continue;
+                auto it = ct_at.find((long long)h2 * n_mono + l2);
+                if (it == ct_at.end()) continue;
+                const int v2 = nao[l2] - no[l2];
+                for (int t : it->second) {
+                    if (t <= s || (h1 == h2 && l1 == l2)) continue;
+                    const int k1 = k1_cached(4, s, h2, 1, h1, h2, no[h1] - ACTIVE, ACTIVE, no[h2] - ACTIVE, ACTIVE,
+                                             dX.p + xoff[s], v1, no[h1] - ACTIVE);
+                    const int k2 = k2_of(-1, t, 0, 1, h1, h2, l1, l2, no[l1], ACTIVE, no[l2], ACTIVE, ACTIVE,
+                                         dX.p + xoff[t], v2, no[h2] - ACTIVE);
+                    elv.push_back(ExEl{s, t, k1, k2});
+                }
+            }
+        }
+    }
     for (auto &v : tab) std::vector<int>().swap(v);
     auto run_exchange = [&](auto zero) {
         using T = decltype(zero);
@@ -1337,6 +1386,9 @@ int Ctx::exciton_states(int n_mono, const tincr_exciton_monomer *mono, int n_pai
     const int cap = max_space + nr;
     DevBuf<double> dV, dAV, dAp, dY, dRitz, dRk, dU, dNrm, dT, dc, dPart;
     dPart.alloc(ceil_div(ns, 256));
+    DevBuf<int> dM;   // the basis size while corrections join it
+    dM.alloc(1);
+    int *hM = reinterpret_cast<int *>(ex_pin.p + pin_used);   // one int of the page-locked staging buffer
     dV.alloc((size_t)cap * ns);
     dAV.alloc((size_t)cap * ns);
     dAp.alloc((size_t)cap * cap);
@@ -1404,26 +1456,31 @@ int Ctx::exciton_states(int n_mono, const tincr_exciton_monomer *mono, int n_pai
         }
         if (dim_sub + lft <= max_space) {
             dim_sub += lft;
+            // the corrections in order, each orthogonalised against the basis so far (which grows on
+            // the device, so no host round trip separates them); the basis size comes back once
+            ex_set_int_kernel<<<1, 32, 0, stream>>>(dM.p, m);
+            count_launch(stream, "ex_set_int");
+            const int m_max = std::min(cap, m + lft);
             for (int r = 0; r < nr; ++r) {
                 if (!(err[r] > tol)) continue;
                 ex_precondition_kernel<<<ceil_div(ns, 256), 256, 0, stream>>>(ns, dRk.p + (size_t)r * ns, u[r], dH.p,
                                                                              dT.p);
                 count_launch(stream, "ex_precondition");
-                ex_dots_kernel<<<m, 256, 0, stream>>>(m, ns, dV.p, dT.p, dc.p);
+                ex_dots_dev_kernel<<<m_max, 256, 0, stream>>>(dM.p, ns, dV.p, dT.p, dc.p);
                 count_launch(stream, "ex_dots");
-                ex_orth_update_kernel<<<ceil_div(ns, 256), 256, 0, stream>>>(m, ns, dV.p, dc.p, dT.p, dPart.p);
+                ex_orth_update_dev_kernel<<<ceil_div(ns, 256), 256, 0, stream>>>(dM.p, ns, dV.p, dc.p, dT.p, dPart.p);
                 count_launch(stream, "ex_orth_update");
                 ex_norm_finish_kernel<<<1, 32, 0, stream>>>(ceil_div(ns, 256), dPart.p, dNrm.p + nr);
                 count_launch(stream, "ex_norm_finish");
-                double nrm = 0.0;
-                TINCR_CUDA(cudaMemcpyAsync(&nrm, dNrm.p + nr, sizeof(double), cudaMemcpyDeviceToHost, stream));
-                sync();
-                if (nrm > 1.0e-8 && m < cap) {
-                    ex_scale_kernel<<<ceil_div(ns, 256), 256, 0, stream>>>(ns, 1.0 / nrm, dT.p, dV.p + (size_t)m * ns);
-                    count_launch(stream, "ex_scale");
-                    ++m;
-                }
+                ex_append_kernel<<<ceil_div(ns, 256), 256, 0, stream>>>(ns, dNrm.p + nr, dM.p, cap, dT.p, dV.p);
+                count_launch(stream, "ex_append");
+                ex_count_kernel<<<1, 32, 0, stream>>>(dNrm.p + nr, dM.p, cap);
+                count_launch(stream, "ex_count");
             }
+            check_launch("ex_append");
+            TINCR_CUDA(cudaMemcpyAsync(hM, dM.p, sizeof(int), cudaMemcpyDeviceToHost, stream));
+            sync();
+            m = *hM;
         } else {
             dim_sub = nr;
             TINCR_CUDA(cudaMemcpyAsync(dV.p, dRitz.p, (size_t)nr * ns * sizeof(double), cudaMemcpyDeviceToDevice, stream));
