@@ -742,6 +742,26 @@ def run_fmo_once(args):
     ctx.close()
 
 
+def run_fmo_exciton_once(args):
+    """Profiling helper: the 64-acene work list solved once by the batched TDA, then the exciton
+    Hamiltonian and its lowest 10 states once (`--precision`), without kernel timing."""
+    from tincr_gb300 import _lib, build
+    from tincr_gb300 import fmo
+    build.build()
+    mons, pairs, inst, labels = fmo_workload()
+    setup = fmo.ExcitonSetup(mons, pairs, workers=os.cpu_count() or 1)
+    ctx = _lib.Context(0)
+    prec = PRECISIONS[args.precision]
+    rc, r = fmo.solve_batch(ctx, inst, FMO_MAX_ITER, FMO_TOL, prec)
+    ex = fmo.exciton_states(ctx, setup, r, labels, FMO_N_LE, FMO_N_CT, n_roots=FMO_N_EXCITON, tol=FMO_EX_TOL,
+                            max_iter=FMO_EX_MAX_ITER, precision=prec)
+    ms, nl = ctx.last_timing()
+    print(json.dumps({"mode": "fmo-exciton", "precision": args.precision, "states": int(len(ex["vectors"])),
+                      "status": ex["status"], "ms": ms, "launches": nl,
+                      "energies_eh": [float(e) for e in ex["energies"]]}))
+    ctx.close()
+
+
 def fmo512_workload(workers):
     """512-acene FMO aggregate: the 64-acene recipe on an 8 x 8 x 8 lattice (13812 atoms)."""
     from tincr_gb300 import fmo
@@ -929,7 +949,8 @@ def main():
     ap.add_argument("--ref-products", type=int, default=None)
     ap.add_argument("--ref-iters", type=int, default=None)
     ap.add_argument("--ref-cg", type=int, default=None)
-    ap.add_argument("--mode", default="solve", choices=["solve", "products", "fmo", "cpu-sample", "acene512"])
+    ap.add_argument("--mode", default="solve",
+                    choices=["solve", "products", "fmo", "fmo-exciton", "cpu-sample", "acene512"])
     ap.add_argument("--k", type=int, default=4)
     args = ap.parse_args()
     if args.mode == "products":
@@ -940,6 +961,9 @@ def main():
         return
     if args.mode == "acene512":
         run_fmo512(args)
+        return
+    if args.mode == "fmo-exciton":
+        run_fmo_exciton_once(args)
         return
     if args.mode == "cpu-sample":
         if None in (args.ref_products, args.ref_iters, args.ref_cg):

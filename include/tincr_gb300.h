@@ -299,7 +299,12 @@ typedef enum {
     TINCR_GRAD_REFERENCE = 0,
     /* derivative of the energies tincr computes: (A+B) Z-vector and H+[Z] for LC, SK derivatives
      * in the centre order H0 is built with (lower index first for same-element pairs) */
-    TINCR_GRAD_EXACT = 1
+    TINCR_GRAD_EXACT = 1,
+    /* flag, OR-ed into either variant: the Slater-Koster splines beyond their grid up to 30 bohr are
+     * the boundary polynomial piece (FITPACK splev with ext = 0, which tincr's splev_uniform
+     * evaluates there, h0_and_s.rs:110, :215) instead of zero; the caller's S, H0 and SCC must
+     * follow the same rule */
+    TINCR_GRAD_SK_EXTRAPOLATE = 16
 } tincr_grad_variant;
 
 /* Parameter tables for the gradient kernels (the SK splines, gamma and repulsion tincr's

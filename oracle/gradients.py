@@ -296,10 +296,12 @@ def cg_zvector(apply, a_diag, r_matrix, conv=1.0e-19, maxiter=10000, stats=None)
 # derivative tensors of one geometry
 # ----------------------------------------------------------------------------------------------
 
-def derivative_tensors(numbers, xyz, ao_offset, ao_atom, hubbard, r_lr, params, orientation="reference"):
+def derivative_tensors(numbers, xyz, ao_offset, ao_atom, hubbard, r_lr, params, orientation="reference",
+                       sk_tail="zero"):
     """dS, dH0 [3N, n, n], dgamma (atomwise) and dgamma_AO, dgamma_lr_AO (`ground_state.rs:22-37`,
-    `:97-106`, `excited_state.rs:35-53`)."""
-    grad_s, grad_h0 = slako.h0_and_s_gradients(numbers, xyz, ao_offset, params, orientation=orientation)
+    `:97-106`, `excited_state.rs:35-53`); `sk_tail` as in `slako.sk_block`."""
+    grad_s, grad_h0 = slako.h0_and_s_gradients(numbers, xyz, ao_offset, params, orientation=orientation,
+                                               sk_tail=sk_tail)
     g1 = gamma_gradients_atomwise(xyz, gamma_c(hubbard, 0.0))
     g1_ao = gamma_gradients_ao(g1, ao_atom)
     out = dict(grad_s=grad_s, grad_h0=grad_h0, grad_gamma=g1, grad_gamma_ao=g1_ao)
@@ -497,16 +499,17 @@ class AtomRows:
     """Derivative-tensor rows of one atom at a time: the 3-row blocks of `derivative_tensors`
     (dS, dH0, dgamma, dgamma_AO, dgamma_lr_AO) for atom i, built on request."""
 
-    def __init__(self, numbers, xyz, ao_offset, ao_atom, hubbard, r_lr, params, orientation="reference"):
+    def __init__(self, numbers, xyz, ao_offset, ao_atom, hubbard, r_lr, params, orientation="reference",
+                 sk_tail="zero"):
         self.numbers, self.xyz, self.ao_offset, self.ao_atom = numbers, xyz, ao_offset, ao_atom
-        self.params, self.orientation, self.r_lr = params, orientation, r_lr
+        self.params, self.orientation, self.r_lr, self.sk_tail = params, orientation, r_lr, sk_tail
         self.c0 = gamma_c(hubbard, 0.0)
         self.clr = gamma_c(hubbard, r_lr) if r_lr > 0.0 else None
         self.v_rep = gradient_v_rep(numbers, xyz, params)
 
     def __call__(self, i):
         gs, gh = slako.h0_and_s_gradient_rows(i, self.numbers, self.xyz, self.ao_offset, self.params,
-                                              orientation=self.orientation)
+                                              orientation=self.orientation, sk_tail=self.sk_tail)
         g1 = gamma_gradient_rows(i, self.xyz, self.c0)
         out = dict(grad_s=gs, grad_h0=gh, grad_gamma=g1, grad_gamma_ao=gamma_gradient_ao_rows(i, g1, self.ao_atom))
         if self.clr is not None:

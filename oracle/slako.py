@@ -47,9 +47,11 @@ def _terms(l1, m1, l2, m2, u):
     return [(3, -p, -g), (4, p, g)]
 
 
-def sk_block(knots, coef, present, l_a, m_a, l_b, m_b, rvec, grad=False):
+def sk_block(knots, coef, present, l_a, m_a, l_b, m_b, rvec, grad=False, sk_tail="zero"):
     """Matrix elements (and gradients w.r.t. rvec) between all orbitals of centre 1 (l_a, m_a)
-    and centre 2 (l_b, m_b) for a batch of inter-centre vectors rvec [n, 3].
+    and centre 2 (l_b, m_b) for a batch of inter-centre vectors rvec [n, 3].  Beyond the spline grid
+    the integrals are zero (sk_tail="zero") or the boundary polynomial piece (sk_tail="extrapolate",
+    FITPACK splev with ext = 0, which tincr's splev_uniform evaluates up to 30 bohr).
 
     Returns val [n, na, nb] and, if grad, g [n, 3, na, nb].
     """
@@ -61,8 +63,9 @@ def sk_block(knots, coef, present, l_a, m_a, l_b, m_b, rvec, grad=False):
     slot_of = {0: 0, 2: 1, 4: 2, 5: 3, 6: 4}
     for idx in present:
         s = slot_of[idx]
-        v[s] = splev(r, (knots, coef[s], 3), ext=1)
-        dv[s] = splev(r, (knots, coef[s], 3), der=1, ext=1)
+        ext = 0 if sk_tail == "extrapolate" else 1
+        v[s] = splev(r, (knots, coef[s], 3), ext=ext)
+        dv[s] = splev(r, (knots, coef[s], 3), der=1, ext=ext)
     na, nb = len(l_a), len(l_b)
     val = np.zeros((n, na, nb))
     g = np.zeros((n, 3, na, nb)) if grad else None
@@ -77,7 +80,7 @@ def sk_block(knots, coef, present, l_a, m_a, l_b, m_b, rvec, grad=False):
     return val, g
 
 
-def h0_and_s_gradients(numbers, xyz, ao_offset, params, orientation="reference"):
+def h0_and_s_gradients(numbers, xyz, ao_offset, params, orientation="reference", sk_tail="zero"):
     """Dense dS/dR and dH0/dR [3N, n_orb, n_orb] (`src/scc/h0_and_s.rs:196-300`).
 
     Entry [3i+c, mu, nu] (and [3i+c, nu, mu]) holds d S_{mu nu} / d R_{i,c} for mu on atom i and
@@ -96,11 +99,12 @@ def h0_and_s_gradients(numbers, xyz, ao_offset, params, orientation="reference")
     gh = np.zeros((3 * n_atoms, n_orb, n_orb))
     for i in range(n_atoms):
         h0_and_s_gradient_rows(i, numbers, xyz, ao_offset, params, orientation,
-                               out_s=gs[3 * i:3 * i + 3], out_h=gh[3 * i:3 * i + 3])
+                               out_s=gs[3 * i:3 * i + 3], out_h=gh[3 * i:3 * i + 3], sk_tail=sk_tail)
     return gs, gh
 
 
-def h0_and_s_gradient_rows(i, numbers, xyz, ao_offset, params, orientation="reference", out_s=None, out_h=None):
+def h0_and_s_gradient_rows(i, numbers, xyz, ao_offset, params, orientation="reference", out_s=None, out_h=None,
+                           sk_tail="zero"):
     """Rows 3i..3i+2 of the dense dS/dR and dH0/dR of `h0_and_s_gradients` (the loop body of
     `src/scc/h0_and_s.rs:203-296` for one atom i): [3, n_orb, n_orb] each, written into out_s /
     out_h when given (zeros elsewhere).  The partner atoms j are evaluated in batches of the same
@@ -129,17 +133,17 @@ def h0_and_s_gradient_rows(i, numbers, xyz, ao_offset, params, orientation="refe
             # gradient w.r.t. r = pos_j - pos_i, turned into d/dR_i by a minus sign (`:218-248`)
             key = (zi, zj)
             _, gS = sk_block(params.sk_knots, params.sk_coef[key + ("s",)], params.sk_present[key],
-                             ei.l, ei.m, ej.l, ej.m, d, grad=True)
+                             ei.l, ei.m, ej.l, ej.m, d, grad=True, sk_tail=sk_tail)
             _, gH = sk_block(params.sk_knots, params.sk_coef[key + ("h",)], params.sk_present[key],
-                             ei.l, ei.m, ej.l, ej.m, d, grad=True)
+                             ei.l, ei.m, ej.l, ej.m, d, grad=True, sk_tail=sk_tail)
             bs_all, bh_all = -gS, -gH
         else:
             # centres swapped: r = pos_i - pos_j, orbitals (j, i) (`:249-277`)
             key = (zj, zi)
             _, gS = sk_block(params.sk_knots, params.sk_coef[key + ("s",)], params.sk_present[key],
-                             ej.l, ej.m, ei.l, ei.m, -d, grad=True)
+                             ej.l, ej.m, ei.l, ei.m, -d, grad=True, sk_tail=sk_tail)
             _, gH = sk_block(params.sk_knots, params.sk_coef[key + ("h",)], params.sk_present[key],
-                             ej.l, ej.m, ei.l, ei.m, -d, grad=True)
+                             ej.l, ej.m, ei.l, ei.m, -d, grad=True, sk_tail=sk_tail)
             bs_all, bh_all = gS.transpose(0, 1, 3, 2), gH.transpose(0, 1, 3, 2)
         for t, j in enumerate(js):
             nu = slice(ao_offset[j], ao_offset[j + 1])
@@ -151,7 +155,7 @@ def h0_and_s_gradient_rows(i, numbers, xyz, ao_offset, params, orientation="refe
     return gs, gh
 
 
-def h0_and_s(numbers, xyz, ao_offset, ao_energy, params):
+def h0_and_s(numbers, xyz, ao_offset, ao_energy, params, sk_tail="zero"):
     """Dense S and H0 (`src/scc/h0_and_s.rs:92-182`), used to cross-check the host producer and
     for finite differences of the SK gradients."""
     n_atoms = len(numbers)
@@ -168,16 +172,16 @@ def h0_and_s(numbers, xyz, ao_offset, ao_energy, params):
             if zi <= zj:
                 key = (zi, zj)
                 vs, _ = sk_block(params.sk_knots, params.sk_coef[key + ("s",)], params.sk_present[key],
-                                 ei.l, ei.m, ej.l, ej.m, d[None, :])
+                                 ei.l, ei.m, ej.l, ej.m, d[None, :], sk_tail=sk_tail)
                 vh, _ = sk_block(params.sk_knots, params.sk_coef[key + ("h",)], params.sk_present[key],
-                                 ei.l, ei.m, ej.l, ej.m, d[None, :])
+                                 ei.l, ei.m, ej.l, ej.m, d[None, :], sk_tail=sk_tail)
                 bs, bh = vs[0], vh[0]
             else:
                 key = (zj, zi)
                 vs, _ = sk_block(params.sk_knots, params.sk_coef[key + ("s",)], params.sk_present[key],
-                                 ej.l, ej.m, ei.l, ei.m, -d[None, :])
+                                 ej.l, ej.m, ei.l, ei.m, -d[None, :], sk_tail=sk_tail)
                 vh, _ = sk_block(params.sk_knots, params.sk_coef[key + ("h",)], params.sk_present[key],
-                                 ej.l, ej.m, ei.l, ei.m, -d[None, :])
+                                 ej.l, ej.m, ei.l, ei.m, -d[None, :], sk_tail=sk_tail)
                 bs, bh = vs[0].T, vh[0].T
             mu = slice(ao_offset[i], ao_offset[i + 1])
             nu = slice(ao_offset[j], ao_offset[j + 1])

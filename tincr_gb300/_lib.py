@@ -19,6 +19,7 @@ PREC_FP64, PREC_BF16X3 = 0, 1
 KF_AO_EXCHANGE, KF_AO_TRANSFORM, KF_SUBSPACE, KF_GRADIENT, KF_OTHER, KF_HOST, KF_EIGEN, KF_DIGITS = range(8)
 KF_COUNT = 8
 GRAD_REFERENCE, GRAD_EXACT = 0, 1
+GRAD_SK_EXTRAPOLATE = 16   # flag OR-ed into a variant: SK splines extrapolated beyond their grid
 
 _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int)

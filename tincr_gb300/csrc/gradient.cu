@@ -285,6 +285,7 @@ struct PairArgs {
     const double *QG, *QL;                       // N x N symmetrised atom-block adjoints (may be null)
     double r_lr;
     int orientation;                             // 0: tincr's (centre 1 by Z, then by the moving atom), 1: by index
+    int sk_extrapolate;                          // SK splines beyond the grid: boundary polynomial (1) or zero (0)
     // repulsion (ground state only)
     int rep_ntmax;
     const int *rep_nt;
@@ -316,7 +317,7 @@ __global__ void __launch_bounds__(128) pair_gradient_kernel(PairArgs a) {
             double N3[4], N2[3];
             double vS[SK_SLOTS] = {0, 0, 0, 0, 0}, dS[SK_SLOTS] = {0, 0, 0, 0, 0};
             double vH[SK_SLOTS] = {0, 0, 0, 0, 0}, dH[SK_SLOTS] = {0, 0, 0, 0, 0};
-            if (bspline3_basis(a.knots, a.n_knots, r, l, N3, N2)) {
+            if (bspline3_basis(a.knots, a.n_knots, r, l, N3, N2, a.sk_extrapolate != 0)) {
                 const double *cS = a.coef + (long long)((k1 * a.n_kinds + k2) * 2 + 0) * SK_SLOTS * a.n_knots;
                 const double *cH = a.coef + (long long)((k1 * a.n_kinds + k2) * 2 + 1) * SK_SLOTS * a.n_knots;
                 for (int s = 0; s < SK_SLOTS; ++s) {
@@ -607,6 +608,8 @@ int Ctx::gradient(const int *atom_kind, double r_lr_, const double *P, const dou
     if (!atom_kind || !P || !dq) fail(TINCR_BAD_ARG, "gradient: null input");
     if (grad_exc && (state < 0 || state >= solved_roots)) fail(TINCR_BAD_ARG, "gradient: state not solved");
     if (grad_gs && !h_coul_x) fail(TINCR_BAD_ARG, "gradient: h_coul_x needed for the ground-state gradient");
+    const bool sk_extrapolate = (variant & TINCR_GRAD_SK_EXTRAPOLATE) != 0;
+    variant &= ~TINCR_GRAD_SK_EXTRAPOLATE;
     if (variant != TINCR_GRAD_REFERENCE && variant != TINCR_GRAD_EXACT) fail(TINCR_BAD_ARG, "gradient: variant");
     for (int A = 0; A < n_atoms; ++A) {
         int k = atom_kind[A];
@@ -642,6 +645,7 @@ int Ctx::gradient(const int *atom_kind, double r_lr_, const double *P, const dou
     pa.sigma = d_sigma.p; pa.knots = d_knots.p; pa.coef = d_coef.p;
     pa.r_lr = r_lr_;
     pa.orientation = variant == TINCR_GRAD_EXACT ? 1 : 0;
+    pa.sk_extrapolate = sk_extrapolate ? 1 : 0;
     auto run_pairs = [&](bool rep, double *out_host) {
         EW(symmetrize_kernel, nn, n, PS.p, Ssym.p);
         EW(symmetrize_kernel, nn, n, PH.p, Hsym.p);

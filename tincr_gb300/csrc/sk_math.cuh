@@ -6,7 +6,8 @@
 // value and first derivative come from the Cox-de Boor recursion for the four non-zero cubic
 // B-splines on the knot interval [t_l, t_{l+1}) (de Boor, "A Practical Guide to Splines", 1978),
 // the derivative through the degree-2 basis: s'(x) = sum_i 3 (c_i - c_{i-1}) / (t_{i+3} - t_i) N_{i,2}(x).
-// Outside [t_3, t_{nt-4}] the spline is taken as zero (value and derivative).
+// Outside [t_3, t_{nt-4}] the spline is taken as zero (value and derivative), or, with `extrapolate`,
+// beyond t_{nt-4} as the polynomial piece of the last interval (FITPACK splev with ext = 0).
 //
 // SK rules: s and p orbitals, real harmonics m = -1, 0, +1 -> y, z, x, integrals in slot order
 // ss_sigma, sp_sigma, ps_sigma, pp_pi, pp_sigma (src/param/slako_transformations.rs:57-680).  The
@@ -28,11 +29,14 @@ namespace tincr {
 constexpr int SK_SLOTS = 5;
 
 // Four cubic B-spline values (and degree-2 values for the derivative) at x on interval l.
-// Returns false when x is outside the spline's support [t_3, t_{nt-4}].
-TINCR_HD bool bspline3_basis(const double *t, int nt, double x, int &l, double N3[4], double N2[3]) {
+// Returns false when x is outside the spline's support [t_3, t_{nt-4}], unless `extrapolate` and
+// x > t_{nt-4}: then the last interval's four B-splines, whose Cox-de Boor polynomials continue
+// past its end (the boundary piece of the spline).
+TINCR_HD bool bspline3_basis(const double *t, int nt, double x, int &l, double N3[4], double N2[3],
+                             bool extrapolate = false) {
     const int k = 3;
     const int lo = k, hi = nt - k - 1;          // valid intervals l in [lo, hi-1], x in [t_lo, t_hi]
-    if (!(x >= t[lo] && x <= t[hi])) return false;
+    if (!(x >= t[lo] && (x <= t[hi] || extrapolate))) return false;
     int a = lo, b = hi - 1;
     // binary search for t[l] <= x < t[l+1], with x == t[hi] in the last interval
     while (a < b) {

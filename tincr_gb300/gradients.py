@@ -99,9 +99,11 @@ class GradientSystem:
         ggs = np.empty(n3) if want_gs else None
         gex = np.empty(n3) if want_exc else None
         it = _lib.C.c_int(0)
+        code = VARIANTS[variant]
+        if getattr(self.sysm, "sk_tail", "zero") == "extrapolate":   # the ground state's SK tail rule
+            code |= _lib.GRAD_SK_EXTRAPOLATE
         rc = self.ctx.lib.tincr_gradient(self.ctx.h, iptr(self.atom_kind), self.r_lr, dptr(self.p), dptr(self.h),
-                                         dptr(self.dq), int(state), VARIANTS[variant], dptr(ggs), dptr(gex),
-                                         _lib.C.byref(it))
+                                         dptr(self.dq), int(state), code, dptr(ggs), dptr(gex), _lib.C.byref(it))
         self.ctx.check(rc, allow=(_lib.OK, _lib.CG_MAXITER))
         self.last_cg_iterations = it.value
         return ggs, gex

@@ -15,7 +15,8 @@ Conventions follow tincr:
   `splev_uniform`, whose behaviour outside the knot range no tincr fixture pins (all fixture
   distances are below 9.6 bohr).  Polynomial extrapolation of the end piece (FITPACK ext=0) grows
   to O(0.1-1) at 20-30 bohr and makes S indefinite for extended molecules, so the tail is taken as
-  zero, the rule tincr itself applies to its repulsive splines (`parameters.rs:345-372`);
+  zero by default, the rule tincr itself applies to its repulsive splines (`parameters.rs:345-372`);
+  `build_system(sk_tail="extrapolate")` evaluates the end piece instead, as FITPACK's splev does;
 * S and H0 by the Slater-Koster rules of `src/param/slako_transformations.rs:57-680` (s and p
   orbitals) on the pair ordering of `src/scc/h0_and_s.rs:92-182`: the atom with the smaller atomic
   number is centre 1 and the direction vector points from centre 1 to centre 2;
@@ -62,6 +63,10 @@ class System:
     r_lr: float                 # long-range radius (0 = LC off)
     lc: bool
     params: P.ParamSet
+    # Slater-Koster splines beyond their grid (10 bohr) up to PROXIMITY_CUTOFF: "zero", or
+    # "extrapolate" with the boundary polynomial piece, FITPACK's splev rule (ext = 0), which is what
+    # tincr's splev_uniform evaluates there (h0_and_s.rs:110)
+    sk_tail: str = "zero"
 
     @property
     def n_occ(self):
@@ -72,8 +77,10 @@ class System:
         return len(self.virt_indices)
 
 
-def build_system(numbers, xyz_bohr, lc=True, r_lr=LONG_RANGE_RADIUS, params=None):
+def build_system(numbers, xyz_bohr, lc=True, r_lr=LONG_RANGE_RADIUS, params=None, sk_tail="zero"):
     """Create a `System` from atomic numbers and bohr coordinates (`system.rs:74-240`)."""
+    if sk_tail not in ("zero", "extrapolate"):
+        raise ValueError("sk_tail must be 'zero' or 'extrapolate'")
     ps = params or P.load()
     numbers = np.asarray(numbers, dtype=np.int32)
     xyz = np.ascontiguousarray(np.asarray(xyz_bohr, dtype=np.float64).reshape(-1, 3))
@@ -95,7 +102,7 @@ def build_system(numbers, xyz_bohr, lc=True, r_lr=LONG_RANGE_RADIUS, params=None
     return System(numbers=numbers, xyz=xyz, n_atoms=n_atoms, n_orbs=n_orbs, orbs_per_atom=opa,
                   ao_offset=off, ao_atom=ao_atom, ao_l=ao_l, ao_m=ao_m, ao_energy=ao_e, ao_occ=ao_occ,
                   n_elec=n_elec, occ_indices=occ, virt_indices=virt, hubbard=hub,
-                  r_lr=float(r_lr) if lc else 0.0, lc=bool(lc), params=ps)
+                  r_lr=float(r_lr) if lc else 0.0, lc=bool(lc), params=ps, sk_tail=sk_tail)
 
 
 def system_from_symbols(symbols, xyz_angstrom, **kw):
@@ -157,6 +164,7 @@ def h0_and_s(sysm):
     a, b = _pair_list(sysm)
     za, zb = sysm.numbers[a], sysm.numbers[b]
     knots = ps.sk_knots
+    ext = 0 if sysm.sk_tail == "extrapolate" else 1
     for zA in np.unique(za):
         for zB in np.unique(zb[za == zA]):
             sel = (za == zA) & (zb == zB)
@@ -170,8 +178,8 @@ def h0_and_s(sysm):
             ch = ps.sk_coef[(int(zA), int(zB), "h")]
             for slot, idx in enumerate(P.SK_INTEGRALS):
                 if idx in ps.sk_present[(int(zA), int(zB))]:
-                    vs[slot] = splev(r, (knots, cs[slot], 3), ext=1)
-                    vh[slot] = splev(r, (knots, ch[slot], 3), ext=1)
+                    vs[slot] = splev(r, (knots, cs[slot], 3), ext=ext)
+                    vh[slot] = splev(r, (knots, ch[slot], 3), ext=ext)
             eA, eB = ps.element(zA), ps.element(zB)
             for p1 in range(eA.n_orbs):
                 for p2 in range(eB.n_orbs):
