@@ -91,3 +91,30 @@ def test_batch_struct_layouts_match_header(tmp_path):
     assert got == [ctypes.sizeof(I), I.orbs_per_atom.offset, I.xyz.offset, ctypes.sizeof(R), R.iterations.offset,
                    R.status.offset]
     assert fmo._INST_DT.itemsize == got[0] and fmo._RES_DT.itemsize == got[3]
+
+
+def test_exciton_struct_layouts_match_header(tmp_path):
+    """tincr_exciton_monomer / _pair / _ct as the C compiler lays them out equal the ctypes structures
+    `fmo.exciton_states` passes (every field's offset and the sizes)."""
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    from tincr_gb300 import fmo
+    structs = [("tincr_exciton_monomer", fmo._ExMonomer), ("tincr_exciton_pair", fmo._ExPair),
+               ("tincr_exciton_ct", fmo._ExCT)]
+    body = []
+    for cname, cls in structs:
+        body.append('printf("%%zu\\n", sizeof(%s));' % cname)
+        for f, _ in cls._fields_:
+            body.append('printf("%%zu\\n", offsetof(%s, %s));' % (cname, f))
+    src = tmp_path / "lay.c"
+    src.write_text('#include <stdio.h>\n#include <stddef.h>\n#include "tincr_gb300.h"\nint main(void) { '
+                   + " ".join(body) + " return 0; }\n")
+    exe = tmp_path / "lay"
+    subprocess.run([cc, str(src), "-I", os.path.join(ROOT, "include"), "-o", str(exe)], check=True)
+    got = [int(v) for v in subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()]
+    want = []
+    for _, cls in structs:
+        want.append(ctypes.sizeof(cls))
+        want += [getattr(cls, f).offset for f, _ in cls._fields_]
+    assert got == want
