@@ -3,7 +3,9 @@
 // C[M x N] = A[M x K] B[N x K]^T with A and B in three split-BF16 planes each (planes.cuh),
 // accumulated as the six plane products A0B0 + A0B1 + A1B0 + A0B2 + A2B0 + A1B1.
 //
-// CTA = 320 threads, one 128 x 128 output tile, K consumed in 64-element (128-byte) blocks:
+// Persistent: at most one CTA per SM, each walking the 128 x 128 output tiles t = blockIdx.x,
+// + gridDim.x, ... (all roles in the same order), so the loads and MMAs of a tile's first K blocks
+// overlap the previous tile's epilogue.  CTA = 320 threads, K consumed in 64-element (128-byte) blocks:
 //   * warp 8 / lane 0: TMA producer, six boxes (A0, A1, A2, B0, B1, B2; 128 rows x 64 bf16, 128-byte
 //     swizzle) per stage into a 2-stage ring, completion on the stage's "full" mbarrier;
 //   * warp 9 / lane 0: MMA issuer, 4 K=16 steps x 6 products per block (tcgen05.mma.cta_group::1
@@ -134,7 +136,7 @@ struct TcMaps {
 template <class Epi>
 __global__ void __launch_bounds__(TC_T, 1)
 gemm_planes_tc_kernel(const __grid_constant__ TcMaps maps, int M, int N, int Kpad, int a_batched, int b_batched,
-                      Epi epi, int *err, unsigned long long first_wait_ns) {
+                      int batch, Epi epi, int *err, unsigned long long first_wait_ns) {
     extern __shared__ unsigned char tc_raw[];
     unsigned char *smem = (unsigned char *)(((uintptr_t)tc_raw + 1023) & ~(uintptr_t)1023);
     uint64_t *full = reinterpret_cast<uint64_t *>(smem + TC_STAGES * TC_STAGE);
@@ -145,9 +147,12 @@ gemm_planes_tc_kernel(const __grid_constant__ TcMaps maps, int M, int N, int Kpa
     uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(done + 1);
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int b = blockIdx.z;
-    const int m0 = blockIdx.y * TC_M, n0 = blockIdx.x * TC_N;
     const int nk = Kpad / TC_K;
+    const int tiles_n = (N + TC_N - 1) / TC_N, tiles_m = (M + TC_M - 1) / TC_M;
+    const int n_tiles = tiles_n * tiles_m * batch;
+    // tile t = (b tiles_m + mt) tiles_n + nt; this CTA takes t = blockIdx.x, + gridDim.x, ...  Every
+    // role walks the same tiles and K blocks; g counts this CTA's K blocks over all its tiles and
+    // gives the stage (g % TC_STAGES), the accumulator pair (g & 1) and the barrier phases.
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < TC_STAGES; ++s) {
@@ -173,106 +178,122 @@ gemm_planes_tc_kernel(const __grid_constant__ TcMaps maps, int M, int N, int Kpa
 
     if (warp == TC_FOLD_WARPS) {
         if (lane == 0) {
-            int issued = 0;
+            long long g = 0, issued = 0;
             bool ok = true;
-            for (int kb = 0; kb < nk; ++kb) {
-                const int s = kb % TC_STAGES;
-                if (kb >= TC_STAGES && !mbar_wait(&empty[s], ((kb / TC_STAGES) & 1) ^ 1)) {
-                    atomicExch(err, 1);
-                    ok = false;
-                    break;
-                }
-                unsigned char *st = smem + s * TC_STAGE;
-                mbar_expect_tx(&full[s], TC_STAGE);
+            for (int t = blockIdx.x; ok && t < n_tiles; t += gridDim.x) {
+                const int nt = t % tiles_n, mt = (t / tiles_n) % tiles_m, b = t / (tiles_n * tiles_m);
+                const int m0 = mt * TC_M, n0 = nt * TC_N;
+                for (int kb = 0; kb < nk; ++kb, ++g) {
+                    const int s = (int)(g % TC_STAGES);
+                    if (g >= TC_STAGES && !mbar_wait(&empty[s], (unsigned)((g / TC_STAGES) & 1) ^ 1u)) {
+                        atomicExch(err, 1);
+                        ok = false;
+                        break;
+                    }
+                    unsigned char *st = smem + s * TC_STAGE;
+                    mbar_expect_tx(&full[s], TC_STAGE);
 #pragma unroll
-                for (int q = 0; q < N_PLANES; ++q) {
-                    tma_load_3d(st + q * TC_TILE, &maps.m[q], kb * TC_K, m0, a_batched ? b : 0, &full[s]);
-                    tma_load_3d(st + (N_PLANES + q) * TC_TILE, &maps.m[N_PLANES + q], kb * TC_K, n0,
-                                b_batched ? b : 0, &full[s]);
+                    for (int q = 0; q < N_PLANES; ++q) {
+                        tma_load_3d(st + q * TC_TILE, &maps.m[q], kb * TC_K, m0, a_batched ? b : 0, &full[s]);
+                        tma_load_3d(st + (N_PLANES + q) * TC_TILE, &maps.m[N_PLANES + q], kb * TC_K, n0,
+                                    b_batched ? b : 0, &full[s]);
+                    }
+                    issued = g + 1;
                 }
-                issued = kb + 1;
             }
             if (!ok)   // loads still in flight land before the CTA exits
-                for (int kb = (issued > TC_STAGES ? issued - TC_STAGES : 0); kb < issued; ++kb)
-                    mbar_wait(&full[kb % TC_STAGES], (kb / TC_STAGES) & 1);
+                for (long long h = (issued > TC_STAGES ? issued - TC_STAGES : 0); h < issued; ++h)
+                    mbar_wait(&full[h % TC_STAGES], (unsigned)((h / TC_STAGES) & 1));
         }
     } else if (warp == TC_FOLD_WARPS + 1) {
         if (lane == 0) {
-            for (int kb = 0; kb < nk; ++kb) {
-                const int s = kb % TC_STAGES, a = kb & 1;
-                // first_wait_ns limits the first of these waits (TC_WAIT_NS unless a test shortens it
-                // to exercise the recovery: the producer drains its loads, the fold warps give up)
-                if (!mbar_wait(&full[s], (kb / TC_STAGES) & 1, kb == 0 ? first_wait_ns : TC_WAIT_NS)) {
-                    atomicExch(err, 2);
-                    break;
-                }
-                if (kb >= 2 && !mbar_wait(&acce[a], ((kb >> 1) - 1) & 1)) {
-                    atomicExch(err, 3);
-                    break;
-                }
-                asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-                const uint32_t base = smem_u32(smem + s * TC_STAGE);
-                const uint32_t dm = tmem + (uint32_t)(a * 2 * TC_N), dx = dm + (uint32_t)TC_N;
+            long long g = 0;
+            bool ok = true;
+            for (int t = blockIdx.x; ok && t < n_tiles; t += gridDim.x) {
+                for (int kb = 0; kb < nk; ++kb, ++g) {
+                    const int s = (int)(g % TC_STAGES), a = (int)(g & 1);
+                    // first_wait_ns limits the first of these waits (TC_WAIT_NS unless a test shortens it
+                    // to exercise the recovery: the producer drains its loads, the fold warps give up)
+                    if (!mbar_wait(&full[s], (unsigned)((g / TC_STAGES) & 1), g == 0 ? first_wait_ns : TC_WAIT_NS)) {
+                        atomicExch(err, 2);
+                        ok = false;
+                        break;
+                    }
+                    if (g >= 2 && !mbar_wait(&acce[a], (unsigned)(((g >> 1) - 1) & 1))) {
+                        atomicExch(err, 3);
+                        ok = false;
+                        break;
+                    }
+                    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+                    const uint32_t base = smem_u32(smem + s * TC_STAGE);
+                    const uint32_t dm = tmem + (uint32_t)(a * 2 * TC_N), dx = dm + (uint32_t)TC_N;
 #pragma unroll
-                for (int kk = 0; kk < TC_K / 16; ++kk) {
-                    const uint32_t off = kk * 32;   // 16 bf16 = 32 bytes along K
-                    const uint64_t a0 = tc_desc(base + 0 * TC_TILE + off), a1 = tc_desc(base + 1 * TC_TILE + off),
-                                   a2 = tc_desc(base + 2 * TC_TILE + off);
-                    const uint64_t b0 = tc_desc(base + 3 * TC_TILE + off), b1 = tc_desc(base + 4 * TC_TILE + off),
-                                   b2 = tc_desc(base + 5 * TC_TILE + off);
-                    tc_mma(dm, a0, b0, kk > 0 ? 1u : 0u);
-                    tc_mma(dx, a0, b1, kk > 0 ? 1u : 0u);
-                    tc_mma(dx, a1, b0, 1u);
-                    tc_mma(dx, a0, b2, 1u);
-                    tc_mma(dx, a2, b0, 1u);
-                    tc_mma(dx, a1, b1, 1u);
+                    for (int kk = 0; kk < TC_K / 16; ++kk) {
+                        const uint32_t off = kk * 32;   // 16 bf16 = 32 bytes along K
+                        const uint64_t a0 = tc_desc(base + 0 * TC_TILE + off), a1 = tc_desc(base + 1 * TC_TILE + off),
+                                       a2 = tc_desc(base + 2 * TC_TILE + off);
+                        const uint64_t b0 = tc_desc(base + 3 * TC_TILE + off), b1 = tc_desc(base + 4 * TC_TILE + off),
+                                       b2 = tc_desc(base + 5 * TC_TILE + off);
+                        tc_mma(dm, a0, b0, kk > 0 ? 1u : 0u);
+                        tc_mma(dx, a0, b1, kk > 0 ? 1u : 0u);
+                        tc_mma(dx, a1, b0, 1u);
+                        tc_mma(dx, a0, b2, 1u);
+                        tc_mma(dx, a2, b0, 1u);
+                        tc_mma(dx, a1, b1, 1u);
+                    }
+                    tc_commit(&empty[s]);
+                    tc_commit(&accf[a]);
                 }
-                tc_commit(&empty[s]);
-                tc_commit(&accf[a]);
             }
             tc_commit(done);
             mbar_wait(done, 0);   // no MMA is in flight once the issuer leaves (also after a failure)
         }
     } else {
         // folding warps 0-7: row m0 + 32 (warp % 4) + lane (TMEM lane quarter of the warp), columns
-        // n0 + 64 (warp / 4) .. + 63: two warps per lane quarter halve the fold and epilogue per thread
+        // n0 + 64 (warp / 4) .. + 63: two warps per lane quarter halve the fold and epilogue per thread.
+        // A tile's epilogue runs while the MMAs of the next tile's first K blocks proceed.
         constexpr int HN = TC_N / 2;
         const int quarter = warp & 3, half = warp >> 2;
-        float sum[HN];
-#pragma unroll
-        for (int j = 0; j < HN; ++j) sum[j] = 0.f;
+        long long g = 0;
         bool ok = true;
-        for (int kb = 0; kb < nk; ++kb) {
-            const int a = kb & 1;
-            ok = __all_sync(0xffffffffu, mbar_wait(&accf[a], (kb >> 1) & 1));
-            if (!ok) {
-                if (lane == 0) atomicExch(err, 4);
-                break;
+        for (int t = blockIdx.x; ok && t < n_tiles; t += gridDim.x) {
+            const int nt = t % tiles_n, mt = (t / tiles_n) % tiles_m, b = t / (tiles_n * tiles_m);
+            const int m0 = mt * TC_M, n0 = nt * TC_N;
+            float sum[HN];
+#pragma unroll
+            for (int j = 0; j < HN; ++j) sum[j] = 0.f;
+            for (int kb = 0; kb < nk; ++kb, ++g) {
+                const int a = (int)(g & 1);
+                ok = __all_sync(0xffffffffu, mbar_wait(&accf[a], (unsigned)((g >> 1) & 1)));
+                if (!ok) {
+                    if (lane == 0) atomicExch(err, 4);
+                    break;
+                }
+                asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+                const uint32_t t0 =
+                    tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(a * 2 * TC_N) + (uint32_t)(half * HN);
+#pragma unroll
+                for (int c0 = 0; c0 < HN; c0 += 16) {
+                    uint32_t rm[16], rx[16];
+                    tmem_ld16(t0 + (uint32_t)c0, rm);
+                    tmem_ld16(t0 + (uint32_t)(TC_N + c0), rx);
+                    asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+#pragma unroll
+                    for (int j = 0; j < 16; ++j) sum[c0 + j] += __uint_as_float(rm[j]) + __uint_as_float(rx[j]);
+                }
+                asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+                __syncwarp();
+                if (lane == 0) mbar_arrive(&acce[a]);
             }
-            asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-            const uint32_t t0 =
-                tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(a * 2 * TC_N) + (uint32_t)(half * HN);
+            const int row = m0 + quarter * 32 + lane;
+            if (ok && row < M) {
 #pragma unroll
-            for (int c0 = 0; c0 < HN; c0 += 16) {
-                uint32_t rm[16], rx[16];
-                tmem_ld16(t0 + (uint32_t)c0, rm);
-                tmem_ld16(t0 + (uint32_t)(TC_N + c0), rx);
-                asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+                for (int c0 = 0; c0 < HN; c0 += 8) {
+                    F8 v;
 #pragma unroll
-                for (int j = 0; j < 16; ++j) sum[c0 + j] += __uint_as_float(rm[j]) + __uint_as_float(rx[j]);
-            }
-            asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
-            __syncwarp();
-            if (lane == 0) mbar_arrive(&acce[a]);
-        }
-        const int row = m0 + quarter * 32 + lane;
-        if (ok && row < M) {
-#pragma unroll
-            for (int c0 = 0; c0 < HN; c0 += 8) {
-                F8 v;
-#pragma unroll
-                for (int j = 0; j < 8; ++j) v.x[j] = sum[c0 + j];
-                epi.run8(b, row, n0 + half * HN + c0, N, v);
+                    for (int j = 0; j < 8; ++j) v.x[j] = sum[c0 + j];
+                    epi.run8(b, row, n0 + half * HN + c0, N, v);
+                }
             }
         }
     }
@@ -318,7 +339,7 @@ inline CUtensorMap plane_map(const bf16 *base, int rows, long long Kpad, long lo
 
 template <class Epi>
 void gemm_planes_tc(cudaStream_t st, int M, int N, int Kpad, PlaneOperand A, PlaneOperand B, int batch, Epi epi,
-                    int *d_err, unsigned long long first_wait_ns = TC_WAIT_NS) {
+                    int *d_err, int n_sm, unsigned long long first_wait_ns = TC_WAIT_NS) {
     if (M <= 0 || N <= 0 || batch <= 0) return;
     if (Kpad <= 0 || Kpad % TC_K) fail(TINCR_BAD_ARG, "gemm_planes_tc: K not padded to 64");
     TcMaps maps;
@@ -331,9 +352,12 @@ void gemm_planes_tc(cudaStream_t st, int M, int N, int Kpad, PlaneOperand A, Pla
         TINCR_CUDA(cudaFuncSetAttribute(gemm_planes_tc_kernel<Epi>, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM));
         attr = true;
     }
-    dim3 grid(ceil_div(N, TC_N), ceil_div(M, TC_M), batch);
-    gemm_planes_tc_kernel<Epi><<<grid, TC_T, TC_SMEM, st>>>(maps, M, N, Kpad, A.sb ? 1 : 0, B.sb ? 1 : 0, epi, d_err,
-                                                            first_wait_ns);
+    // persistent: at most one CTA per SM (the shared memory allows one), each walking its tiles
+    const long long n_tiles = (long long)ceil_div(N, TC_N) * ceil_div(M, TC_M) * batch;
+    if (n_tiles > (1LL << 31) - 1) fail(TINCR_BAD_ARG, "gemm_planes_tc: too many tiles");
+    const int grid = (int)std::min<long long>(n_tiles, std::max(1, n_sm));
+    gemm_planes_tc_kernel<Epi><<<grid, TC_T, TC_SMEM, st>>>(maps, M, N, Kpad, A.sb ? 1 : 0, B.sb ? 1 : 0, batch, epi,
+                                                            d_err, first_wait_ns);
     count_launch(st, "gemm_planes_tc");
     check_launch("gemm_planes_tc");
 }

@@ -72,7 +72,7 @@ static void plane_gemm(Ctx &c, int family, int M, int N, long long Kpad, PlaneOp
                        Epi epi, int K_alg) {
     int slot = c.prof_begin(family);
     if (c.use_tc)
-        gemm_planes_tc(c.stream, M, N, (int)Kpad, A, B, batch, epi, c.d_tc_err.p,
+        gemm_planes_tc(c.stream, M, N, (int)Kpad, A, B, batch, epi, c.d_tc_err.p, c.n_sm,
                        c.tc_first_wait_ns < 0 ? TC_WAIT_NS : (unsigned long long)c.tc_first_wait_ns);
     else gemm_planes_mma(c.stream, M, N, (int)Kpad, A, B, batch, epi);
     double nb = batch;
