@@ -47,26 +47,36 @@ struct GemmJob {
     double alpha;
 };
 
-constexpr int XG_T = 256, XG_TILE = 32;
+constexpr int XG_T = 256, XG_KC = 16;   // 256 threads; K in chunks of 16
 
-template <class T>
+// TILE x TILE output tile, (TILE / 16)^2 outputs per thread: 64 for FP32 (4 x 4 register blocks),
+// 32 for FP64 (more CTAs for the narrow FP64 pipe)
+template <class T, int TILE>
 __global__ void __launch_bounds__(XG_T) ex_gemm_kernel(const GemmJob *__restrict__ jobs, const int4 *__restrict__ tiles) {
-    __shared__ T As[XG_TILE][XG_TILE + 1], Bs[XG_TILE][XG_TILE + 1];
+    constexpr int R = TILE / 16, PER = TILE * XG_KC / XG_T;
+    __shared__ T As[XG_KC][TILE + 4], Bs[XG_KC][TILE + 4];   // [k][m], [k][n]
     const int4 tl = tiles[blockIdx.x];
     const GemmJob J = jobs[tl.x];
-    const int m0 = tl.y * XG_TILE, n0 = tl.z * XG_TILE;
-    const int tr = threadIdx.x & 31, tc = (threadIdx.x >> 5) * 4;
+    const int m0 = tl.y * TILE, n0 = tl.z * TILE;
+    const int tr = threadIdx.x >> 4, tc = threadIdx.x & 15;   // rows m0 + R tr + i, columns n0 + R tc + j
     if (!J.B) {   // elementwise add
-        for (int q = 0; q < 4; ++q) {
-            const int m = m0 + tr, n = n0 + tc + q;
+        for (int e = threadIdx.x; e < TILE * TILE; e += XG_T) {
+            const int m = m0 + e / TILE, n = n0 + e % TILE;
             if (m < J.M && n < J.N) atomicAdd(J.C + m * J.ldc + n, J.alpha * J.A[m * J.sam + n * J.sak]);
         }
         return;
     }
-    T acc[4] = {T(0), T(0), T(0), T(0)};
-    for (int k0 = 0; k0 < J.K; k0 += XG_TILE) {
-        for (int e = threadIdx.x; e < XG_TILE * XG_TILE; e += XG_T) {
-            const int mm = e >> 5, kk = e & 31;
+    T acc[R][R];
+#pragma unroll
+    for (int i = 0; i < R; ++i)
+#pragma unroll
+        for (int j = 0; j < R; ++j) acc[i][j] = T(0);
+    for (int k0 = 0; k0 < J.K; k0 += XG_KC) {
+        // A chunk [TILE m x 16 k] and B chunk [16 k x TILE n], PER elements of each per thread
+#pragma unroll
+        for (int q = 0; q < PER; ++q) {
+            const int e = threadIdx.x + q * XG_T;
+            const int mm = e >> 4, kk = e & 15;   // A: consecutive threads along k
             const int m = m0 + mm, k = k0 + kk;
             T v = T(0);
             if (m < J.M && k < J.K) {
@@ -74,24 +84,33 @@ __global__ void __launch_bounds__(XG_T) ex_gemm_kernel(const GemmJob *__restrict
                 if (J.d) x *= J.d[k];
                 v = (T)x;
             }
-            As[mm][kk] = v;
-            const int kb = e >> 5, nn = e & 31;
+            As[kk][mm] = v;
+            const int kb = e / TILE, nn = e % TILE;   // B: consecutive threads along n
             const int k2 = k0 + kb, n = n0 + nn;
             Bs[kb][nn] = (k2 < J.K && n < J.N) ? (T)J.B[k2 * J.sbk + n * J.sbn] : T(0);
         }
         __syncthreads();
-#pragma unroll 8
-        for (int kk = 0; kk < XG_TILE; ++kk) {
-            const T a = As[tr][kk];
 #pragma unroll
-            for (int q = 0; q < 4; ++q) acc[q] += a * Bs[kk][tc + q];
+        for (int kk = 0; kk < XG_KC; ++kk) {
+            T a[R], b[R];
+#pragma unroll
+            for (int i = 0; i < R; ++i) a[i] = As[kk][R * tr + i];
+#pragma unroll
+            for (int j = 0; j < R; ++j) b[j] = Bs[kk][R * tc + j];
+#pragma unroll
+            for (int i = 0; i < R; ++i)
+#pragma unroll
+                for (int j = 0; j < R; ++j) acc[i][j] += a[i] * b[j];
         }
         __syncthreads();
     }
-    for (int q = 0; q < 4; ++q) {
-        const int m = m0 + tr, n = n0 + tc + q;
-        if (m < J.M && n < J.N) atomicAdd(J.C + m * J.ldc + n, J.alpha * (double)acc[q]);
-    }
+#pragma unroll
+    for (int i = 0; i < R; ++i)
+#pragma unroll
+        for (int j = 0; j < R; ++j) {
+            const int m = m0 + R * tr + i, n = n0 + R * tc + j;
+            if (m < J.M && n < J.N) atomicAdd(J.C + m * J.ldc + n, J.alpha * (double)acc[i][j]);
+        }
 }
 
 struct GemmBatch {
@@ -100,21 +119,20 @@ struct GemmBatch {
     void gemm(int M, int N, int K, const double *A, long long sam, long long sak, const double *B, long long sbk,
               long long sbn, double *C, long long ldc, double alpha, const double *d = nullptr) {
         if (M <= 0 || N <= 0 || K <= 0) return;
-        const int j = (int)jobs.size();
         jobs.push_back(GemmJob{A, B, d, C, sam, sak, sbk, sbn, ldc, M, N, K, alpha});
-        for (int tm = 0; tm < ceil_div(M, XG_TILE); ++tm)
-            for (int tn = 0; tn < ceil_div(N, XG_TILE); ++tn) tiles.push_back(make_int4(j, tm, tn, 0));
     }
     // C[m, n] += alpha A(m, n)
     void add(int M, int N, const double *A, long long sam, long long san, double *C, long long ldc, double alpha) {
         if (M <= 0 || N <= 0) return;
-        const int j = (int)jobs.size();
         jobs.push_back(GemmJob{A, nullptr, nullptr, C, sam, san, 0, 0, ldc, M, N, 1, alpha});
-        for (int tm = 0; tm < ceil_div(M, XG_TILE); ++tm)
-            for (int tn = 0; tn < ceil_div(N, XG_TILE); ++tn) tiles.push_back(make_int4(j, tm, tn, 0));
     }
     void run(Ctx &c, bool fp32, DevBuf<GemmJob> &dj, DevBuf<int4> &dt, int family) {
-        if (tiles.empty()) return;
+        if (jobs.empty()) return;
+        const int tile = fp32 ? 64 : 32;
+        tiles.clear();
+        for (int j = 0; j < (int)jobs.size(); ++j)
+            for (int tm = 0; tm < ceil_div(jobs[j].M, tile); ++tm)
+                for (int tn = 0; tn < ceil_div(jobs[j].N, tile); ++tn) tiles.push_back(make_int4(j, tm, tn, 0));
         dj.reserve(jobs.size());
         dt.reserve(tiles.size());
         TINCR_CUDA(cudaMemcpyAsync(dj.p, jobs.data(), jobs.size() * sizeof(GemmJob), cudaMemcpyHostToDevice, c.stream));
@@ -122,11 +140,14 @@ struct GemmBatch {
         double flops = 0.0;
         for (const GemmJob &j : jobs) flops += j.B ? 2.0 * j.M * j.N * j.K : (double)j.M * j.N;
         const int slot = c.prof_begin(family);
-        if (fp32)
-            ex_gemm_kernel<float><<<(unsigned)tiles.size(), XG_T, 0, c.stream>>>(dj.p, dt.p);
-        else
-            ex_gemm_kernel<double><<<(unsigned)tiles.size(), XG_T, 0, c.stream>>>(dj.p, dt.p);
-        count_launch(c.stream, "ex_gemm");
+        for (size_t t0 = 0; t0 < tiles.size(); t0 += 1u << 20) {   // grid limit
+            const unsigned nb = (unsigned)std::min<size_t>(tiles.size() - t0, 1u << 20);
+            if (fp32)
+                ex_gemm_kernel<float, 64><<<nb, XG_T, 0, c.stream>>>(dj.p, dt.p + t0);
+            else
+                ex_gemm_kernel<double, 32><<<nb, XG_T, 0, c.stream>>>(dj.p, dt.p + t0);
+            count_launch(c.stream, "ex_gemm");
+        }
         check_launch("ex_gemm");
         c.prof_end(slot, flops, 0.0);
         // the host vectors must outlive the copies: wait before they are reused or freed
@@ -742,6 +763,9 @@ int Ctx::exciton_states(int n_mono, const tincr_exciton_monomer *mono, int n_pai
     // page-locked staging buffer: parallel host copies, then one DMA each
     const size_t n_g = (size_t)n_atoms_total * n_atoms_total;
     size_t pin_need = 2 * n_g + 1;   // (+1: the Davidson's basis size read back)
+    for (int p = 0; p < n_pairs; ++p)   // overlap blocks (pairs with bad indices are rejected below)
+        if (pairs[p].i >= 0 && pairs[p].i < n_mono && pairs[p].j >= 0 && pairs[p].j < n_mono)
+            pin_need += (size_t)nao[pairs[p].i] * nao[pairs[p].j];
     for (int p = 0; p < n_pairs; ++p)   // (pairs with bad indices are rejected below)
         if (pairs[p].real && pairs[p].i >= 0 && pairs[p].i < n_mono && pairs[p].j >= 0 && pairs[p].j < n_mono) {
             const size_t nij = (size_t)nao[pairs[p].i] + nao[pairs[p].j];
@@ -798,16 +822,34 @@ int Ctx::exciton_states(int n_mono, const tincr_exciton_monomer *mono, int n_pai
     // cross products S_xy C_y (n_x x n_y) and S_yx C_x (n_y x n_x) of every listed pair
     std::vector<long long> offX(n_pairs + 1, 0);
     for (int p = 0; p < n_pairs; ++p) offX[p + 1] = offX[p] + 2LL * nao[pairs[p].i] * nao[pairs[p].j];
-    std::vector<double> hSxy(offX[n_pairs] / 2 + 1);
     std::vector<long long> offSxy(n_pairs + 1, 0);
-    for (int p = 0; p < n_pairs; ++p) {
-        const long long sz = (long long)nao[pairs[p].i] * nao[pairs[p].j];
-        offSxy[p + 1] = offSxy[p] + sz;
-        check_finite(pairs[p].s_ij, (size_t)sz, "pair overlap");
-        std::copy(pairs[p].s_ij, pairs[p].s_ij + sz, hSxy.begin() + offSxy[p]);
+    for (int p = 0; p < n_pairs; ++p) offSxy[p + 1] = offSxy[p] + (long long)nao[pairs[p].i] * nao[pairs[p].j];
+    // the overlap blocks, packed in parallel into the staging buffer (finiteness checked there), one DMA
+    if (pin_used + offSxy[n_pairs] > ex_pin.n) {   // (counted above; growing drops the staged copies)
+        sync();
+        ex_pin.reserve(pin_used + offSxy[n_pairs] + 1);
     }
+    double *hSxy = ex_pin.p + pin_used;
+    pin_used += offSxy[n_pairs];
+    int bad_overlap = -1;
+#pragma omp parallel for schedule(dynamic, 8) num_threads(8)
+    for (int p = 0; p < n_pairs; ++p) {
+        const long long sz = offSxy[p + 1] - offSxy[p];
+        bool ok = true;
+        for (long long x = 0; x < sz; ++x) {
+            hSxy[offSxy[p] + x] = pairs[p].s_ij[x];
+            ok = ok && std::isfinite(pairs[p].s_ij[x]);
+        }
+        if (!ok) {
+#pragma omp critical
+            bad_overlap = p;
+        }
+    }
+    if (bad_overlap >= 0) fail(TINCR_NONFINITE, "non-finite value in pair overlap");
     DevBuf<double> dSxy, dCross;
-    upload_vec(stream, dSxy, hSxy);
+    dSxy.alloc(std::max<long long>(1, offSxy[n_pairs]));
+    if (offSxy[n_pairs])
+        TINCR_CUDA(cudaMemcpyAsync(dSxy.p, hSxy, offSxy[n_pairs] * sizeof(double), cudaMemcpyHostToDevice, stream));
     dCross.alloc(std::max<long long>(1, offX[n_pairs]));
     TINCR_CUDA(cudaMemsetAsync(dCross.p, 0, dCross.n * sizeof(double), stream));
     auto cross = [&](int x, int y) -> const double * {   // S_xy C_y, [n_x x n_y]
