@@ -342,6 +342,57 @@ int tincr_gradient(tincr_ctx *ctx, const int *atom_kind, double r_lr, const doub
                    const double *h_coul_x, const double *dq, int state, int variant,
                    double *grad_gs, double *grad_exc, int *cg_iterations);
 
+/* ---- SCC ground states --------------------------------------------------------------------- */
+
+typedef enum {
+    TINCR_SCC_LC = 1,              /* long-range corrected (gamma_lr with radius r_lr)                 */
+    TINCR_SCC_SK_EXTRAPOLATE = 2,  /* SK splines beyond their grid: boundary polynomial, not zero      */
+    TINCR_SCC_FP32_START = 4       /* FP32 iterations until the commutator is below 1e-5, then FP64    */
+} tincr_scc_flags;
+
+/* One system of a batched SCC.  Offsets index the packed arrays of tincr_scc_batch. */
+typedef struct {
+    int n_atoms;                   /* 1..256                                                          */
+    int n_orb;                     /* 2..256: the atoms' orbitals (kind_norb), checked                */
+    int n_occ;                     /* doubly occupied orbitals (n_elec / 2; closed shell)             */
+    int pad;
+    long long atom_off;            /* first atom in kinds[] / dq[] (xyz: 3 * atom_off)                */
+    long long orb_off;             /* first orbital energy in orbe[]                                  */
+    long long mat_off;             /* first element of the n_orb x n_orb blocks (orbs, P, S, ...)     */
+    long long pair_off;            /* first element of the n_atoms x n_atoms blocks (given gammas)    */
+} tincr_scc_system;
+
+/* Inputs the caller supplies instead of the ones tincr_scc_batch builds (each may be NULL):
+ * packed S / H0 blocks at mat_off, atomwise gamma / gamma_lr blocks at pair_off. */
+typedef struct {
+    const double *s, *h0, *gamma, *gamma_lr;
+} tincr_scc_inputs;
+
+/* Replaces tincr's SCC for many independent systems at once (System::run_scc, src/scc/
+ * scc_routine.rs:121-290, with h0_and_s, src/scc/h0_and_s.rs:92-182, the gamma matrices,
+ * src/scc/gamma_approximation.rs:75-193, and the LC exchange Hamiltonian, src/scc/helpers.rs:
+ * 111-155): FMO monomers and pairs (src/fmo/scc/), displaced geometries of a numerical gradient.
+ * Uses the context's parameter tables (tincr_set_parameters, kind indices into them).
+ *   kinds [atoms], xyz [3 * atoms] bohr; kind_energy [n_kinds*4] on-site orbital energies (H0 diagonal);
+ *   given: S, H0, gamma, gamma_lr supplied by the caller (NULL, or NULL members: built here);
+ *   p_start: packed n_orb x n_orb starting densities or NULL (the neutral-atom reference density);
+ *   flags: tincr_scc_flags; r_lr: long-range radius with TINCR_SCC_LC;
+ *   tol: convergence when the largest element of X^T (F P S - S P F) X is below tol (X = S^-1/2),
+ *   tincr's stationary density; DIIS on the Fock matrix; max_iter iterations at most;
+ *   level_shift >= 0 adds level_shift (S - S P S / 2) to the matrix that is diagonalised.
+ * Out: orbe [orbitals] ascending, orbs [n_orb x n_orb blocks] (column i = orbital i), P (or NULL),
+ *   dq [atoms] Mulliken charge differences, energy [n_sys] total SCC energy (electronic + repulsive),
+ *   s_out / h0_out / h_coul_x (converged F, the input tincr_gradient takes) or NULL;
+ *   iterations, converged (0/1) and residual (commutator of the last iterate) [n_sys].
+ * Returns TINCR_NOT_CONVERGED when some system missed tol in max_iter iterations (its outputs are
+ * those of the last Fock matrix), TINCR_NONFINITE when an iterate was not finite. */
+int tincr_scc_batch(tincr_ctx *ctx, int n_sys, const tincr_scc_system *systems, const int *kinds,
+                    const double *xyz, const double *kind_energy, const tincr_scc_inputs *given,
+                    const double *p_start, double r_lr,
+                    int flags, double tol, int max_iter, double level_shift, double *orbe, double *orbs,
+                    double *P, double *dq, double *energy, double *s_out, double *h0_out,
+                    double *h_coul_x, int *iterations, int *converged, double *residual);
+
 #ifdef __cplusplus
 }
 #endif

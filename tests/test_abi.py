@@ -118,3 +118,26 @@ def test_exciton_struct_layouts_match_header(tmp_path):
         want.append(ctypes.sizeof(cls))
         want += [getattr(cls, f).offset for f, _ in cls._fields_]
     assert got == want
+
+
+def test_scc_struct_layouts_match_header(tmp_path):
+    """tincr_scc_system as the C compiler lays it out equals the numpy record `scc.scc_batch` packs,
+    and tincr_scc_inputs the ctypes structure it passes."""
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    from tincr_gb300 import scc
+    dt = scc.SYSTEM_DTYPE
+    body = ['printf("%zu\\n", sizeof(tincr_scc_system));']
+    body += ['printf("%%zu\\n", offsetof(tincr_scc_system, %s));' % f for f in dt.names]
+    body += ['printf("%zu\\n", sizeof(tincr_scc_inputs));']
+    body += ['printf("%%zu\\n", offsetof(tincr_scc_inputs, %s));' % f for f, _ in scc._Inputs._fields_]
+    src = tmp_path / "lay.c"
+    src.write_text('#include <stdio.h>\n#include <stddef.h>\n#include "tincr_gb300.h"\nint main(void) { '
+                   + " ".join(body) + " return 0; }\n")
+    exe = tmp_path / "lay"
+    subprocess.run([cc, str(src), "-I", os.path.join(ROOT, "include"), "-o", str(exe)], check=True)
+    got = [int(v) for v in subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()]
+    want = [dt.itemsize] + [dt.fields[f][1] for f in dt.names]
+    want += [ctypes.sizeof(scc._Inputs)] + [getattr(scc._Inputs, f).offset for f, _ in scc._Inputs._fields_]
+    assert got == want

@@ -20,6 +20,7 @@ KF_AO_EXCHANGE, KF_AO_TRANSFORM, KF_SUBSPACE, KF_GRADIENT, KF_OTHER, KF_HOST, KF
 KF_COUNT = 8
 GRAD_REFERENCE, GRAD_EXACT = 0, 1
 GRAD_SK_EXTRAPOLATE = 16   # flag OR-ed into a variant: SK splines extrapolated beyond their grid
+SCC_LC, SCC_SK_EXTRAPOLATE, SCC_FP32_START = 1, 2, 4
 
 _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int)
@@ -55,6 +56,9 @@ SIGNATURES = {
     "tincr_set_parameters": (C.c_int, [C.c_void_p, C.c_int, _ip, _ip, _ip, _ip, _dp, _dp, C.c_int, _dp, _dp,
                                        C.c_int, _ip, _dp, _dp, _dp]),
     "tincr_gradient": (C.c_int, [C.c_void_p, _ip, C.c_double, _dp, _dp, _dp, C.c_int, C.c_int, _dp, _dp, _ip]),
+    "tincr_scc_batch": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, _ip, _dp, _dp, C.c_void_p, _dp, C.c_double,
+                                  C.c_int, C.c_double, C.c_int, C.c_double, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp,
+                                  _ip, _ip, _dp]),
 }
 
 _lib = None

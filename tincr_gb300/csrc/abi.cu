@@ -184,6 +184,17 @@ int tincr_exciton_states(tincr_ctx *ctx, int n_monomers, const tincr_exciton_mon
     });
 }
 
+int tincr_scc_batch(tincr_ctx *ctx, int n_sys, const tincr_scc_system *systems, const int *kinds, const double *xyz,
+                    const double *kind_energy, const tincr_scc_inputs *given, const double *p_start, double r_lr,
+                    int flags, double tol, int max_iter, double level_shift, double *orbe, double *orbs, double *P, double *dq, double *energy,
+                    double *s_out, double *h0_out, double *h_coul_x, int *iterations, int *converged,
+                    double *residual) {
+    return guarded(ctx, [&](tincr::Ctx &c) {
+        return c.scc_batch(n_sys, systems, kinds, xyz, kind_energy, given, p_start, r_lr, flags, tol, max_iter, level_shift,
+                           orbe, orbs, P, dq, energy, s_out, h0_out, h_coul_x, iterations, converged, residual);
+    });
+}
+
 int tincr_tda_products_noalloc(tincr_ctx *ctx, int k, const double *X_dev, double *AX_dev) {
     return guarded(ctx, [&](tincr::Ctx &c) {
         tincr::products_noalloc(c, k, X_dev, AX_dev);

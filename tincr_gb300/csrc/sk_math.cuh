@@ -129,6 +129,19 @@ TINCR_HD void sk_element(int l1, int m1, int l2, int m2, const double u[3], doub
     }
 }
 
+// Value of one SK matrix element (the value part of sk_element).
+TINCR_HD double sk_value(int l1, int m1, int l2, int m2, const double u[3], const double v[SK_SLOTS]) {
+    if (l1 == 0 && l2 == 0) return v[0];
+    if (l1 == 0) return u[p_axis(m2)] * v[1];
+    if (l2 == 0) return u[p_axis(m1)] * v[2];
+    const int c1 = p_axis(m1), c2 = p_axis(m2);
+    if (c1 == c2) {
+        const int o0 = c1 == 0 ? 1 : 0, o1 = c1 == 2 ? 1 : 2;   // the other two axes, ascending
+        return (u[o0] * u[o0] + u[o1] * u[o1]) * v[3] + u[c1] * u[c1] * v[4];
+    }
+    return u[c1] * u[c2] * (-v[3] + v[4]);
+}
+
 // d gamma / d r for the Gaussian gamma function, C = 1/sqrt(2 (sA^2 + sB^2 + R_lr^2 / 2))
 // (src/scc/gamma_approximation.rs:126-137).  Uses CUDA's erf and exp.
 TINCR_HD double gamma_deriv(double r, double c) {

@@ -134,6 +134,7 @@ struct Ctx {
     void gemm_f64_digits(int M, int N, int K, const double *A, const double *B, double *C);
     BatchWork *batch = nullptr;
     PinnedBuf ex_pin;                     // staging of the exciton Hamiltonian's large inputs
+    DevBuf<unsigned char> scc_ws;         // per-CTA slots of the batched SCC (scc.cu)
 
     explicit Ctx(int dev);
     ~Ctx();
@@ -180,6 +181,11 @@ struct Ctx {
     int davidson(int n_roots, int max_iter, double tol, bool from_ritz, std::vector<double> &u, int *it_out);
     int solve_batch(int n_inst, const tincr_tda_instance *inst, int max_iter, double tol, int precision,
                     tincr_tda_result *res);
+    int scc_batch(int n_sys, const tincr_scc_system *sys, const int *kinds, const double *xyz,
+                  const double *kind_energy, const tincr_scc_inputs *given, const double *p_start, double r_lr,
+                  int flags, double tol, int max_iter,
+                  double level_shift, double *orbe, double *orbs, double *p_out, double *dq, double *energy,
+                  double *s_out, double *h0_out, double *hcx_out, int *iterations, int *converged, double *residual);
     int exciton_states(int n_mono, const tincr_exciton_monomer *mono, int n_pairs, const tincr_exciton_pair *pairs,
                        int n_ct, const tincr_exciton_ct *cts, int n_atoms_total, const double *gamma,
                        const double *gamma_lr, int precision, int n_roots, double tol, int max_iter, double *h_out,
