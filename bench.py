@@ -49,6 +49,7 @@ FMO_N_LE, FMO_N_CT, FMO_TOL, FMO_MAX_ITER = 4, 1, 1e-4, 150
 # 100 iterations), the lowest 10 states
 FMO_N_EXCITON, FMO_EX_TOL, FMO_EX_MAX_ITER = 10, 1e-4, 100
 R_LR = 1.0 / 0.3
+SCC_TOL = 1e-10   # the SCC's commutator tolerance (host and GPU)
 
 
 def dist_env():
@@ -762,6 +763,101 @@ def run_fmo_exciton_once(args):
     ctx.close()
 
 
+def scc_workload():
+    """The SCCs of the 64-acene FMO set-up: 64 monomers (48-102 orbitals, from the neutral-atom
+    density) and the 529 real-pair dimers (96-204 orbitals, from their monomers' densities, as tincr
+    starts a pair SCC, src/fmo/scc/pair.rs:112-124).  The monomers' host ground states give the dimer
+    starts and the comparison."""
+    from tincr_gb300 import fmo
+    from tincr_gb300 import groundstate as gs
+    mons, pairs, inst, labels = fmo_workload()
+    reach = 2.0 * max(fmo.VDW_SUM_BOHR.values())
+    dims, starts = [], []
+    for i, j in fmo.candidate_pairs(mons, reach):
+        if not fmo.is_real_pair(mons[i], mons[j]):
+            continue
+        mi, mj = mons[i], mons[j]
+        dims.append(gs.build_system(np.concatenate([mi.system.numbers, mj.system.numbers]),
+                                    np.concatenate([mi.system.xyz, mj.system.xyz]), lc=True, r_lr=mi.system.r_lr))
+        ni, nj = mi.system.n_orbs, mj.system.n_orbs
+        p = np.zeros((ni + nj, ni + nj))
+        p[:ni, :ni] = mi.ground.p
+        p[ni:, ni:] = mj.ground.p
+        starts.append(p)
+    return mons, dims, starts
+
+
+def _scc_host_job(args):
+    from tincr_gb300 import groundstate as gs
+    sy, p = args
+    return gs.run_scc(sy, tol=SCC_TOL, p_start=p).iterations
+
+
+def _scc_gemm_flops(systems, grounds):
+    """FP64 flops of the SCC's GEMMs per system and iteration (LC: 10 n^3 for the exchange
+    Hamiltonian, 4 n^3 for X F X, 2 n^3 for F'P', 6 n^2 n_occ for the densities) over the iterations
+    run, plus the start (X, S^1/2, P': 8 n^3) and the end (orbitals, density, LC energy: 6 n^3)."""
+    f = 0.0
+    for sy, g in zip(systems, grounds):
+        n, o = float(sy.n_orbs), float(sy.n_elec // 2)
+        per = (10 * n ** 3 if sy.lc else 0.0) + 6 * n ** 3 + 6 * n * n * o
+        f += g.iterations * per + 8 * n ** 3 + 6 * n ** 3
+    return f
+
+
+def run_scc_bench(args):
+    """Batched GPU SCC (tincr_scc_batch) on the 64-acene FMO set-up: the 64 monomers, then the 529
+    real-pair dimers, in FP64 and with the FP32 start; device time (CUDA events around the kernel),
+    wall time through the Python API (host packing and copies included), the FP64 GEMM rate against
+    GB300's nominal FP64 peak (1.25 TFLOP/s: no FP64 figure is measured for this machine), agreement with
+    the host SCC, and the host SCC on all host cores (process pool) as the CPU baseline."""
+    from tincr_gb300 import _lib, build
+    from tincr_gb300 import fmo
+    from tincr_gb300 import scc as gscc
+    build.build()
+    mons, dims, starts = scc_workload()
+    ctx = _lib.Context(0)
+    sets = [("monomers", [m.system for m in mons], None)]
+    if args.scc_set == "all":
+        sets.append(("dimers", dims, starts))
+    gscc.scc_batch(ctx, sets[0][1], tol=SCC_TOL)   # warm-up: allocation of the slots
+    out = {"mode": "scc", "metric": "batched SCC wall seconds", "tol": SCC_TOL}
+    for name, systems, st in sets:
+        for fp32 in (False, True):
+            t0 = time.perf_counter()
+            g, rc = gscc.scc_batch(ctx, systems, tol=SCC_TOL, p_start=st, fp32_start=fp32)
+            wall = time.perf_counter() - t0
+            ms = ctx.last_timing()[0]
+            its = [x.iterations for x in g]
+            rec = {"systems": len(systems), "n_orb": [min(s.n_orbs for s in systems), max(s.n_orbs for s in systems)],
+                   "status": int(rc), "kernel_ms": ms, "wall_ms": 1e3 * wall, "iterations_mean": float(np.mean(its)),
+                   "iterations_max": int(max(its)), "unconverged": int(sum(not x.converged for x in g))}
+            if not fp32:
+                fl = _scc_gemm_flops(systems, g)
+                rec["fp64_gemm_tflop"] = fl / 1e12
+                rec["fp64_gemm_tflops"] = fl / (ms * 1e-3) / 1e12
+                rec["fp64_frac_of_nominal"] = rec["fp64_gemm_tflops"] / 1.25
+            if name == "monomers":
+                rec["max_abs_orbe_diff_vs_host"] = float(max(np.abs(x.orbe - m.ground.orbe).max()
+                                                             for x, m in zip(g, mons)))
+            out["%s_%s" % (name, "fp32start" if fp32 else "fp64")] = rec
+    if args.cpu_baseline:
+        # host SCC restatement on all host cores: the monomers in full, a bounded sample of dimers
+        cores = os.cpu_count() or 1
+        t0 = time.perf_counter()
+        fmo._pool_map(_scc_host_job, [(m.system, None) for m in mons], cores)
+        t_mon = time.perf_counter() - t0
+        k = min(len(dims), 4 * cores)
+        t0 = time.perf_counter()
+        fmo._pool_map(_scc_host_job, list(zip(dims[:k], starts[:k])), cores)
+        t_dim = (time.perf_counter() - t0) * len(dims) / k
+        out["cpu_baseline"] = {"kind": "port", "cores": cores, "monomers_s": t_mon, "dimers_s": t_dim,
+                               "sample": "host SCC (groundstate.run_scc, numpy) in a spawn pool of %d processes: "
+                                         "all %d monomers; %d of %d dimers, scaled" % (cores, len(mons), k, len(dims))}
+    print(json.dumps(out))
+    ctx.close()
+
+
 def fmo512_workload(workers):
     """512-acene FMO aggregate: the 64-acene recipe on an 8 x 8 x 8 lattice (13812 atoms)."""
     from tincr_gb300 import fmo
@@ -950,7 +1046,8 @@ def main():
     ap.add_argument("--ref-iters", type=int, default=None)
     ap.add_argument("--ref-cg", type=int, default=None)
     ap.add_argument("--mode", default="solve",
-                    choices=["solve", "products", "fmo", "fmo-exciton", "cpu-sample", "acene512"])
+                    choices=["solve", "products", "fmo", "fmo-exciton", "cpu-sample", "acene512", "scc"])
+    ap.add_argument("--scc-set", default="all", choices=["all", "monomers"])
     ap.add_argument("--k", type=int, default=4)
     args = ap.parse_args()
     if args.mode == "products":
@@ -964,6 +1061,9 @@ def main():
         return
     if args.mode == "fmo-exciton":
         run_fmo_exciton_once(args)
+        return
+    if args.mode == "scc":
+        run_scc_bench(args)
         return
     if args.mode == "cpu-sample":
         if None in (args.ref_products, args.ref_iters, args.ref_cg):

@@ -148,3 +148,24 @@ def test_scc_reports_failures(gpu_ctx):
     # the context still works
     out, rc = scc.scc_batch(gpu_ctx, systems[:1], tol=1e-10)
     assert rc == _lib.OK
+
+
+def test_fmo_setup_on_gpu_matches_host(gpu_ctx):
+    """build_monomers(scc="gpu") and ExcitonSetup(scc="gpu") (batched dimer SCCs from the monomers'
+    densities) give the host set-up's ground states."""
+    from cases import fmo_case
+    from tincr_gb300 import fmo
+    case = fmo_case(3, 2, 1)
+    mons = case["monomers"]
+    z = np.concatenate([m.system.numbers for m in mons])
+    x = np.concatenate([m.system.xyz for m in mons])
+    mono = np.concatenate([np.full(m.system.n_atoms, k) for k, m in enumerate(mons)])
+    gm = fmo.build_monomers(z, x, mono, lc=True, scc="gpu", ctx=gpu_ctx)
+    for a, b in zip(gm, mons):
+        assert np.abs(a.ground.orbe - b.ground.orbe).max() < 1e-9
+        assert np.abs(a.ground.p - b.ground.p).max() < 1e-8
+    host = fmo.ExcitonSetup(mons, case["pairs"])
+    dev = fmo.ExcitonSetup(mons, case["pairs"], scc="gpu", ctx=gpu_ctx)
+    assert host.real_pairs == dev.real_pairs and host.real_pairs
+    for k in host.real_pairs:
+        assert np.abs(host.pair_scc[k][1] - dev.pair_scc[k][1]).max() < 1e-9

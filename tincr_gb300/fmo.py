@@ -42,15 +42,23 @@ def _monomer_scc(args):
     return gs.run_scc(sy, tol=tol, require_convergence=True)
 
 
-def build_monomers(numbers, xyz_bohr, monomer_of_atom, lc=True, r_lr=gs.LONG_RANGE_RADIUS, scc_tol=1e-10, workers=1):
-    """Monomers by construction (one per distinct `monomer_of_atom` value), each with a host SCC
-    (`workers` > 1: in a spawn process pool, one BLAS thread per worker)."""
+def build_monomers(numbers, xyz_bohr, monomer_of_atom, lc=True, r_lr=gs.LONG_RANGE_RADIUS, scc_tol=1e-10, workers=1,
+                   scc="host", ctx=None):
+    """Monomers by construction (one per distinct `monomer_of_atom` value), each with an SCC ground
+    state: on the host (`workers` > 1: in a spawn process pool, one BLAS thread per worker) or, with
+    scc="gpu", all monomers in one batched GPU SCC on `ctx` (tincr_scc_batch)."""
     systems = []
     for k in np.unique(monomer_of_atom):
         at = np.nonzero(monomer_of_atom == k)[0]
         systems.append((int(k), at, gs.build_system(numbers[at], xyz_bohr[at], lc=lc, r_lr=r_lr)))
-    jobs = [(sy, scc_tol) for _, _, sy in systems]
-    grounds = _pool_map(_monomer_scc, jobs, workers)
+    if scc == "gpu":
+        from . import scc as gscc
+        grounds, _ = gscc.scc_batch(ctx, [sy for _, _, sy in systems], tol=scc_tol, require_convergence=True)
+    elif scc == "host":
+        jobs = [(sy, scc_tol) for _, _, sy in systems]
+        grounds = _pool_map(_monomer_scc, jobs, workers)
+    else:
+        raise ValueError("scc must be 'host' or 'gpu'")
     return [Monomer(k, at, sy, g) for (k, at, sy), g in zip(systems, grounds)]
 
 
@@ -435,6 +443,36 @@ def _dimer_scc(args):
     return g.orbs, g.orbe, True
 
 
+def _dimer_scc_gpu(ctx, jobs):
+    """The dimer SCCs of `jobs` (the arguments of `_dimer_scc`) as batched GPU SCCs: DIIS from the
+    monomers' densities, then the dimers that missed the tolerance again with a level shift of 0.5 and
+    up to 1000 iterations, then the caller's policy for the rest (the isolated monomers' orbitals, or
+    an error).  Returns (orbs, orbe, converged) per job."""
+    from . import scc as gscc
+    systems = [gs.build_system(z, xyz, lc=lc, r_lr=r_lr) for z, xyz, lc, r_lr, _, _, _ in jobs]
+    tol = jobs[0][4]
+    grounds, _ = gscc.scc_batch(ctx, systems, tol=tol, p_start=[j[5] for j in jobs])
+    retry = [k for k, g in enumerate(grounds) if not g.converged]
+    if retry:
+        again, _ = gscc.scc_batch(ctx, [systems[k] for k in retry], tol=tol, max_iter=1000, level_shift=0.5,
+                                  p_start=[jobs[k][5] for k in retry])
+        for k, g in zip(retry, again):
+            grounds[k] = g
+    out = []
+    for (z, xyz, lc, r_lr, _, _, isolated), g in zip(jobs, grounds):
+        if g.converged:
+            out.append((g.orbs, g.orbe, True))
+        elif isolated is None:
+            raise RuntimeError("dimer SCC not converged to %g with a level shift either" % tol)
+        else:
+            (ca, ea), (cb, eb) = isolated
+            orbs = np.zeros((len(ea) + len(eb), len(ea) + len(eb)))
+            orbs[:len(ea), :len(ea)] = ca
+            orbs[len(ea):, len(ea):] = cb
+            out.append((orbs, np.concatenate([ea, eb]), False))
+    return out
+
+
 class ExcitonSetup:
     """Everything the exciton Hamiltonian reads besides the LE / CT roots, produced on the host
     (tincr's SuperSystem holds the same: src/fmo/supersystem.rs:248-305, src/fmo/pair.rs):
@@ -444,12 +482,14 @@ class ExcitonSetup:
     * the atomwise gamma and gamma_lr of the whole aggregate;
     * the ground state (MO coefficients, energies) of every real pair's dimer, for the LCMO Fock
       matrix (tincr's FMO pair SCC; here the isolated dimer, like the monomers).
-    `workers` > 1 runs the dimer SCCs in a spawn process pool.  A dimer SCC that does not converge,
-    neither by DIIS from the monomers' densities nor with a level shift, raises (tincr panics) unless
-    `unconverged="isolated"`, which gives such a dimer the isolated monomers' orbitals and energies as
-    its pair ground state; `unconverged_pairs` lists those dimers."""
+    `workers` > 1 runs the dimer SCCs in a spawn process pool; scc="gpu" runs them as one batched
+    GPU SCC on `ctx` (tincr_scc_batch), with the same starts, retry and policy.  A dimer SCC that does
+    not converge, neither by DIIS from the monomers' densities nor with a level shift, raises (tincr
+    panics) unless `unconverged="isolated"`, which gives such a dimer the isolated monomers' orbitals
+    and energies as its pair ground state; `unconverged_pairs` lists those dimers."""
 
-    def __init__(self, monomers, ct_pairs, lc=True, scc_tol=1e-10, workers=1, unconverged="raise"):
+    def __init__(self, monomers, ct_pairs, lc=True, scc_tol=1e-10, workers=1, unconverged="raise", scc="host",
+                 ctx=None):
         self.monomers = monomers
         self.ct_pairs = list(ct_pairs)
         n = len(monomers)
@@ -486,7 +526,12 @@ class ExcitonSetup:
                 if unconverged == "isolated" else None
             jobs.append((np.concatenate([mi.system.numbers, mj.system.numbers]),
                          np.concatenate([mi.system.xyz, mj.system.xyz]), lc, self.r_lr, scc_tol, p_start, iso))
-        out = _pool_map(_dimer_scc, jobs, workers)
+        if scc == "gpu":
+            out = _dimer_scc_gpu(ctx, jobs)
+        elif scc == "host":
+            out = _pool_map(_dimer_scc, jobs, workers)
+        else:
+            raise ValueError("scc must be 'host' or 'gpu'")
         self.pair_scc = {k: (o[0], o[1]) for k, o in zip(self.real_pairs, out)}
         self.unconverged_pairs = [k for k, o in zip(self.real_pairs, out) if not o[2]]
 
