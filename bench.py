@@ -858,6 +858,29 @@ def run_scc_bench(args):
     ctx.close()
 
 
+def run_rpa_bench(args):
+    """RPA / Casida (tincr_rpa_solve, FP64) on the (H2O)128 LC workload: the lowest N_ROOTS roots to
+    the bench residual, timed with CUDA events, beside the FP64 TDA solve of the same roots."""
+    from tincr_gb300 import _lib, build
+    from tincr_gb300 import tda as T
+    build.build()
+    sy, g = workload()
+    ctx = _lib.Context(0)
+    es = T.ExcitedStateSystem.from_ground_state(ctx, sy, g)
+    es.prepare_tda()
+    out = {"mode": "rpa", "workload": "water128-lc-20roots", "tol": TOL}
+    for rep in range(2):
+        r = es.run_rpa(N_ROOTS, MAX_ITER, TOL)
+        out["rpa_ms"] = ctx.last_timing()[0]
+        out["rpa_iterations"] = int(r["rpa_iterations"])
+    r = es.run_tda(N_ROOTS, MAX_ITER, TOL, precision=_lib.PREC_FP64)
+    out["tda_fp64_ms"] = ctx.last_timing()[0]
+    out["tda_iterations"] = int(r["davidson_iterations"])
+    out["rpa_minus_tda_eh"] = [float(x) for x in (es.properties["rpa_eigenvalues"] - r["ci_eigenvalues"])]
+    print(json.dumps(out))
+    ctx.close()
+
+
 def fmo512_workload(workers):
     """512-acene FMO aggregate: the 64-acene recipe on an 8 x 8 x 8 lattice (13812 atoms)."""
     from tincr_gb300 import fmo
@@ -1046,7 +1069,7 @@ def main():
     ap.add_argument("--ref-iters", type=int, default=None)
     ap.add_argument("--ref-cg", type=int, default=None)
     ap.add_argument("--mode", default="solve",
-                    choices=["solve", "products", "fmo", "fmo-exciton", "cpu-sample", "acene512", "scc"])
+                    choices=["solve", "products", "fmo", "fmo-exciton", "cpu-sample", "acene512", "scc", "rpa"])
     ap.add_argument("--scc-set", default="all", choices=["all", "monomers"])
     ap.add_argument("--k", type=int, default=4)
     args = ap.parse_args()
@@ -1064,6 +1087,9 @@ def main():
         return
     if args.mode == "scc":
         run_scc_bench(args)
+        return
+    if args.mode == "rpa":
+        run_rpa_bench(args)
         return
     if args.mode == "cpu-sample":
         if None in (args.ref_products, args.ref_iters, args.ref_cg):

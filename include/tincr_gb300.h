@@ -342,6 +342,23 @@ int tincr_gradient(tincr_ctx *ctx, const int *atom_kind, double r_lr, const doub
                    const double *h_coul_x, const double *dq, int state, int variant,
                    double *grad_gs, double *grad_exc, int *cg_iterations);
 
+/* ---- RPA / Casida ----------------------------------------------------------------------------- */
+
+/* Replaces tincr's Casida solver (src/excited_states/casida.rs:6-80, with A and B from
+ * src/excited_states/a_and_b.rs:5-163: singlets, closed shell) for the system of the last
+ * tincr_tda_setup, in FP64: the lowest n_roots of (A-B)^1/2 (A+B) (A-B)^1/2 F = Omega^2 F with
+ * A = omega + 2 (ia|jb) - (ij|ab)_lr and B = 2 (ia|jb) - (ib|ja)_lr (Mulliken charges), by a Davidson
+ * on the products (A+B) V and (A-B) V (Stratmann, Scuseria, Frisch, J. Chem. Phys. 109, 8218 (1998)).
+ * Converged when both residuals (A+B)(X+Y) - Omega (X-Y) and (A-B)(X-Y) - Omega (X+Y) of every root
+ * are below tol (2-norm).  tincr's RPA path is not reachable in its current tree (casida.rs and
+ * a_and_b.rs are no longer compiled); the gradient that reads X+Y and X-Y is
+ * src/gradients/excited_state.rs:489-983.
+ * Out: energies [n_roots] Omega; xpy, xmy [ov x n_roots] (or NULL) X+Y and X-Y with
+ * (X+Y)^T (X-Y) = 1; osc [n_roots] (or NULL) 2/3 Omega |mu|^2 with mu from the transition charges of
+ * X+Y; iterations.  Returns TINCR_NOT_CONVERGED when max_iter is reached. */
+int tincr_rpa_solve(tincr_ctx *ctx, int n_roots, int max_iter, double tol, double *energies, double *xpy,
+                    double *xmy, double *osc, int *iterations);
+
 /* ---- SCC ground states --------------------------------------------------------------------- */
 
 typedef enum {

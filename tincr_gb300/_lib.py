@@ -56,6 +56,7 @@ SIGNATURES = {
     "tincr_set_parameters": (C.c_int, [C.c_void_p, C.c_int, _ip, _ip, _ip, _ip, _dp, _dp, C.c_int, _dp, _dp,
                                        C.c_int, _ip, _dp, _dp, _dp]),
     "tincr_gradient": (C.c_int, [C.c_void_p, _ip, C.c_double, _dp, _dp, _dp, C.c_int, C.c_int, _dp, _dp, _ip]),
+    "tincr_rpa_solve": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_double, _dp, _dp, _dp, _dp, _ip]),
     "tincr_scc_batch": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, _ip, _dp, _dp, C.c_void_p, _dp, C.c_double,
                                   C.c_int, C.c_double, C.c_int, C.c_double, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp,
                                   _ip, _ip, _dp]),

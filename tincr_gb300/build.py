@@ -17,7 +17,7 @@ OUT = os.path.join(HERE, "lib")
 LIB = os.path.join(OUT, "libtincr_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["abi.cu", "tda.cu", "gradient.cu", "noalloc.cu", "mixed.cu", "batch.cu", "eig_cluster.cu", "digits.cu",
-           "exciton.cu", "scc.cu", "eigen_host.cpp"]
+           "exciton.cu", "scc.cu", "rpa.cu", "eigen_host.cpp"]
 
 
 def _nvcc():

@@ -184,6 +184,11 @@ int tincr_exciton_states(tincr_ctx *ctx, int n_monomers, const tincr_exciton_mon
     });
 }
 
+int tincr_rpa_solve(tincr_ctx *ctx, int n_roots, int max_iter, double tol, double *energies, double *xpy,
+                    double *xmy, double *osc, int *iterations) {
+    return guarded(ctx, [&](tincr::Ctx &c) { return c.rpa_solve(n_roots, max_iter, tol, energies, xpy, xmy, osc, iterations); });
+}
+
 int tincr_scc_batch(tincr_ctx *ctx, int n_sys, const tincr_scc_system *systems, const int *kinds, const double *xyz,
                     const double *kind_energy, const tincr_scc_inputs *given, const double *p_start, double r_lr,
                     int flags, double tol, int max_iter, double level_shift, double *orbe, double *orbs, double *P, double *dq, double *energy,

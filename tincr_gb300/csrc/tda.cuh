@@ -135,6 +135,7 @@ struct Ctx {
     BatchWork *batch = nullptr;
     PinnedBuf ex_pin;                     // staging of the exciton Hamiltonian's large inputs
     DevBuf<unsigned char> scc_ws;         // per-CTA slots of the batched SCC (scc.cu)
+    DevBuf<double> rpa_w1, rpa_w2;        // transposed vectors and K' products of the RPA (rpa.cu)
 
     explicit Ctx(int dev);
     ~Ctx();
@@ -181,6 +182,9 @@ struct Ctx {
     int davidson(int n_roots, int max_iter, double tol, bool from_ritz, std::vector<double> &u, int *it_out);
     int solve_batch(int n_inst, const tincr_tda_instance *inst, int max_iter, double tol, int precision,
                     tincr_tda_result *res);
+    void rpa_products(int k, const double *V, double *P, double *M);
+    int rpa_solve(int n_roots, int max_iter, double tol, double *energies, double *xpy, double *xmy, double *osc,
+                  int *iterations);
     int scc_batch(int n_sys, const tincr_scc_system *sys, const int *kinds, const double *xyz,
                   const double *kind_energy, const tincr_scc_inputs *given, const double *p_start, double r_lr,
                   int flags, double tol, int max_iter,

@@ -116,3 +116,25 @@ class ExcitedStateSystem:
                                oscillator_strengths=f, davidson_iterations=it.value,
                                **self.ctx.last_solve_stats())
         return self.properties
+
+    def run_rpa(self, n_roots, max_iter, tolerance, raise_on_failure=True):
+        """RPA / Casida excited states (tincr's `casida`, src/excited_states/casida.rs:6-80, solved by
+        a Davidson on (A+B) V and (A-B) V, FP64; `tincr_rpa_solve`).  Stores and returns
+        rpa_eigenvalues [n_roots], XpY and XmY [dim x n_roots] ((X+Y)^T (X-Y) = 1, tincr's XpY / XmY)
+        and rpa_oscillator_strengths."""
+        if not self.prepared:
+            self.prepare_tda()
+        n_roots = int(n_roots)
+        e = np.empty(n_roots)
+        xpy = np.empty((self.dim, n_roots))
+        xmy = np.empty((self.dim, n_roots))
+        f = np.empty(n_roots)
+        it = _lib.C.c_int(0)
+        rc = self.ctx.lib.tincr_rpa_solve(self.ctx.h, n_roots, int(max_iter), float(tolerance), dptr(e), dptr(xpy),
+                                          dptr(xmy), dptr(f), _lib.C.byref(it))
+        self.ctx.check(rc, allow=(_lib.OK, _lib.NOT_CONVERGED))
+        if rc == _lib.NOT_CONVERGED and raise_on_failure:
+            raise DavidsonError("RPA Davidson did not converge!")
+        self.properties.update(rpa_eigenvalues=e, XpY=xpy, XmY=xmy, rpa_oscillator_strengths=f,
+                               rpa_iterations=it.value)
+        return self.properties
