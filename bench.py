@@ -881,13 +881,14 @@ def run_rpa_bench(args):
     ctx.close()
 
 
-def fmo512_workload(workers):
-    """512-acene FMO aggregate: the 64-acene recipe on an 8 x 8 x 8 lattice (13812 atoms)."""
+def fmo512_workload(workers, scc="host", ctx=None):
+    """512-acene FMO aggregate: the 64-acene recipe on an 8 x 8 x 8 lattice (13812 atoms); monomer
+    SCCs on the host (a process pool) or as one batched GPU SCC (scc="gpu")."""
     from tincr_gb300 import fmo
     from tincr_gb300 import geometry as G
     from tincr_gb300 import groundstate as gs
     z, x, mono = G.acene_lattice(8, 8, 8)
-    mons = fmo.build_monomers(z, G.to_bohr(x), mono, lc=True, workers=workers)
+    mons = fmo.build_monomers(z, G.to_bohr(x), mono, lc=True, workers=workers, scc=scc, ctx=ctx)
     pairs = fmo.close_pairs(mons, 4.5 / gs.P.BOHR_TO_ANGS)
     inst, labels = fmo.aggregate_instances(mons, pairs, FMO_N_LE, FMO_N_CT)
     return mons, pairs, inst, labels
@@ -980,21 +981,21 @@ def run_fmo512(args):
     from tincr_gb300 import fmo
     build.build()
     workers = os.cpu_count() or 1
+    ctx = _lib.Context(0)
     t0 = time.perf_counter()
-    mons, pairs, inst, labels = fmo512_workload(workers)
+    mons, pairs, inst, labels = fmo512_workload(workers, scc=args.setup_scc, ctx=ctx)
     t_w = time.perf_counter() - t0
     t0 = time.perf_counter()
     # the 8 x 8 x 8 lattice puts some acenes into each other (H-H contacts down to 0.2 A); the SCC of
-    # 8 of those dimers has no stable stationary point, and they take the isolated monomers' orbitals
-    setup = fmo.ExcitonSetup(mons, pairs, workers=workers, unconverged="isolated")
+    # 5-8 of those dimers has no stable stationary point, and they take the isolated monomers' orbitals
+    setup = fmo.ExcitonSetup(mons, pairs, workers=workers, unconverged="isolated", scc=args.setup_scc, ctx=ctx)
     t_s = time.perf_counter() - t0
-    ctx = _lib.Context(0)
     gctxs = [_lib.Context(0) for _ in range(8)]
     n_mon = len(mons)
     out = {"mode": "acene512", "workload": "acene512-fmo-le4-ct1-exciton10", "monomers": n_mon,
            "atoms": int(sum(m.system.n_atoms for m in mons)), "ct_pairs": len(pairs), "instances": len(inst),
            "real_pairs": len(setup.real_pairs), "dimers_without_scc_solution": [list(k) for k in setup.unconverged_pairs],
-           "host_setup_s": t_w, "host_exciton_setup_s": t_s}
+           "setup_scc": args.setup_scc, "host_setup_s": t_w, "host_exciton_setup_s": t_s}
     runs = {}
     for name, prec in (("bf16x3", _lib.PREC_BF16X3), ("fp64", _lib.PREC_FP64)):
         fmo.solve_batch(ctx, inst, FMO_MAX_ITER, FMO_TOL, prec)   # warm-up (tile autotuner, graphs)
@@ -1071,6 +1072,8 @@ def main():
     ap.add_argument("--mode", default="solve",
                     choices=["solve", "products", "fmo", "fmo-exciton", "cpu-sample", "acene512", "scc", "rpa"])
     ap.add_argument("--scc-set", default="all", choices=["all", "monomers"])
+    ap.add_argument("--setup-scc", default="host", choices=["host", "gpu"],
+                    help="--mode acene512: SCCs of the set-up on the host (process pool) or batched on the GPU")
     ap.add_argument("--k", type=int, default=4)
     args = ap.parse_args()
     if args.mode == "products":

@@ -451,11 +451,11 @@ def _dimer_scc_gpu(ctx, jobs):
     from . import scc as gscc
     systems = [gs.build_system(z, xyz, lc=lc, r_lr=r_lr) for z, xyz, lc, r_lr, _, _, _ in jobs]
     tol = jobs[0][4]
-    grounds, _ = gscc.scc_batch(ctx, systems, tol=tol, p_start=[j[5] for j in jobs])
+    grounds, _ = gscc.scc_batch(ctx, systems, tol=tol, p_start=[j[5] for j in jobs], full=False)
     retry = [k for k, g in enumerate(grounds) if not g.converged]
     if retry:
         again, _ = gscc.scc_batch(ctx, [systems[k] for k in retry], tol=tol, max_iter=1000, level_shift=0.5,
-                                  p_start=[jobs[k][5] for k in retry])
+                                  p_start=[jobs[k][5] for k in retry], full=False)
         for k, g in zip(retry, again):
             grounds[k] = g
     out = []

@@ -36,11 +36,13 @@ def _common(systems, attr):
 
 
 def scc_batch(ctx, systems, tol=1e-10, max_iter=250, p_start=None, level_shift=0.0, fp32_start=False,
-              given=None, require_convergence=False):
+              given=None, require_convergence=False, full=True):
     """SCC ground states of `systems` (groundstate.System, sharing parameters, LC setting and SK tail
     rule) on the GPU.  `p_start`: None or a list with a starting density (or None) per system;
     `given`: None or a list of dicts with any of "s", "h0", "gamma", "gamma_lr" per system, used
-    instead of the matrices the GPU builds.  Returns (list of GroundState, status); with
+    instead of the matrices the GPU builds.  `full=False` returns only the orbitals, orbital
+    energies, charges and energy (the density, S, H0 and Fock matrix are None and not copied back).
+    Returns (list of GroundState, status); with
     `require_convergence` a system that misses `tol` raises (tincr panics, src/fmo/scc/pair.rs:234-240)."""
     systems = list(systems)
     if not systems:
@@ -94,8 +96,8 @@ def scc_batch(ctx, systems, tol=1e-10, max_iter=250, p_start=None, level_shift=0
                 raise ValueError("scc_batch: %s given for some systems only" % key)
     flags = (_lib.SCC_LC if s0.lc else 0) | (_lib.SCC_SK_EXTRAPOLATE if s0.sk_tail == "extrapolate" else 0) | \
         (_lib.SCC_FP32_START if fp32_start else 0)
-    orbe, orbs, p, dq = np.zeros(o), np.zeros(m), np.zeros(m), np.zeros(a)
-    s_out, h0_out, hcx = np.zeros(m), np.zeros(m), np.zeros(m)
+    orbe, orbs, dq = np.zeros(o), np.zeros(m), np.zeros(a)
+    p, s_out, h0_out, hcx = (np.zeros(m), np.zeros(m), np.zeros(m), np.zeros(m)) if full else (None,) * 4
     energy, res = np.zeros(n), np.zeros(n)
     its, conv = np.zeros(n, np.int32), np.zeros(n, np.int32)
     rc = ctx.lib.tincr_scc_batch(
@@ -107,12 +109,16 @@ def scc_batch(ctx, systems, tol=1e-10, max_iter=250, p_start=None, level_shift=0
     out = []
     for i, sy in enumerate(systems):
         no, mo, ao, nb = sy.n_orbs, int(rec[i]["mat_off"]), int(rec[i]["orb_off"]), int(rec[i]["atom_off"])
-        blk = lambda x: x[mo:mo + no * no].reshape(no, no).copy()
-        if given is not None and "gamma" in given[i]:
+        blk = lambda x: None if x is None else x[mo:mo + no * no].reshape(no, no).copy()
+        if not full:
+            gam = glr = None
+        elif given is not None and "gamma" in given[i]:
             gam = np.array(given[i]["gamma"], dtype=np.float64)
         else:
             gam = gs.gamma_atomwise(sy, 0.0)
-        if not sy.lc:
+        if not full:
+            pass
+        elif not sy.lc:
             glr = np.zeros_like(gam)
         elif given is not None and "gamma_lr" in given[i]:
             glr = np.array(given[i]["gamma_lr"], dtype=np.float64)
@@ -120,7 +126,8 @@ def scc_batch(ctx, systems, tol=1e-10, max_iter=250, p_start=None, level_shift=0
             glr = gs.gamma_atomwise(sy, sy.r_lr)
         out.append(gs.GroundState(
             s=blk(s_out), h0=blk(h0_out), gamma=gam, gamma_lr=glr, orbs=blk(orbs), orbe=orbe[ao:ao + no].copy(),
-            p=blk(p), p0=np.diag(sy.ao_occ.astype(np.float64)), dq=dq[nb:nb + sy.n_atoms].copy(), h_coul_x=blk(hcx),
+            p=blk(p), p0=np.diag(sy.ao_occ.astype(np.float64)) if full else None, dq=dq[nb:nb + sy.n_atoms].copy(),
+            h_coul_x=blk(hcx),
             energy=float(energy[i]), iterations=int(its[i]), converged=bool(conv[i]), residual=float(res[i])))
     if require_convergence and rc == _lib.NOT_CONVERGED:
         bad = [i for i in range(n) if not conv[i]]
