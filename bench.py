@@ -317,7 +317,11 @@ def run_gpu(args):
     }
     out["parity"] = water_parity(g, main, ref64)
     if args.fmo:
-        out["fmo"] = run_fmo(args, ctx)
+        out["fmo"], mons = run_fmo(args, ctx)
+        if world == 1 and args.next_rows:
+            out["scc"] = _guarded(lambda: scc_measure(ctx, mons, args.cpu_baseline))
+    if world == 1 and args.next_rows:
+        out["rpa"] = _guarded(lambda: rpa_measure(ctx, sy, g))
     if ref64 is not None:
         out["fp64_gpu"] = {"value": float(np.mean(ref64["dev_ms"])) / 1e3, "unit": "s",
                            "speedup_of_mixed": float(np.mean(ref64["dev_ms"])) / max(1e-9, float(np.mean(main["dev_ms"]))),
@@ -444,7 +448,8 @@ def tile_summary(table):
 
 def run_fmo(args, ctx):
     """The 64-acene FMO step, mixed and FP64 forms (monomers/s): batched LE / CT TDA of the work
-    list, the exciton Hamiltonian and its lowest 10 states, and the S1 LE gradient."""
+    list, the exciton Hamiltonian and its lowest 10 states, and the S1 LE gradient.  Returns the
+    JSON record and the monomers (their ground states serve the SCC measurement)."""
     from tincr_gb300 import _lib
     from tincr_gb300 import fmo
     t0 = time.perf_counter()
@@ -541,7 +546,7 @@ def run_fmo(args, ctx):
         total, sample, _ = fmo_cpu_reference(mons, pairs, inst, labels, setup)
         out["cpu_baseline"] = {"value": len(mons) / total, "unit": "monomers/s", "step_s": total,
                                "cores": os.cpu_count(), "kind": "port", "sample": sample}
-    return out
+    return out, mons
 
 
 def cpu_sample(sy, g, n_products, n_iters, cg_iters, sample_vectors=2):
@@ -763,14 +768,12 @@ def run_fmo_exciton_once(args):
     ctx.close()
 
 
-def scc_workload():
-    """The SCCs of the 64-acene FMO set-up: 64 monomers (48-102 orbitals, from the neutral-atom
-    density) and the 529 real-pair dimers (96-204 orbitals, from their monomers' densities, as tincr
-    starts a pair SCC, src/fmo/scc/pair.rs:112-124).  The monomers' host ground states give the dimer
-    starts and the comparison."""
+def scc_dimers(mons):
+    """The real-pair dimers of the 64-acene FMO set-up (529 systems of 96-204 orbitals) with their
+    starting densities, the block-diagonal densities of their monomers (tincr starts a pair SCC from
+    its monomers' charges, src/fmo/scc/pair.rs:112-124)."""
     from tincr_gb300 import fmo
     from tincr_gb300 import groundstate as gs
-    mons, pairs, inst, labels = fmo_workload()
     reach = 2.0 * max(fmo.VDW_SUM_BOHR.values())
     dims, starts = [], []
     for i, j in fmo.candidate_pairs(mons, reach):
@@ -784,7 +787,7 @@ def scc_workload():
         p[:ni, :ni] = mi.ground.p
         p[ni:, ni:] = mj.ground.p
         starts.append(p)
-    return mons, dims, starts
+    return dims, starts
 
 
 def _scc_host_job(args):
@@ -805,23 +808,20 @@ def _scc_gemm_flops(systems, grounds):
     return f
 
 
-def run_scc_bench(args):
+def scc_measure(ctx, mons, cpu_baseline=True, scc_set="all"):
     """Batched GPU SCC (tincr_scc_batch) on the 64-acene FMO set-up: the 64 monomers, then the 529
     real-pair dimers, in FP64 and with the FP32 start; device time (CUDA events around the kernel),
     wall time through the Python API (host packing and copies included), the FP64 GEMM rate against
     GB300's nominal FP64 peak (1.25 TFLOP/s: no FP64 figure is measured for this machine), agreement with
     the host SCC, and the host SCC on all host cores (process pool) as the CPU baseline."""
-    from tincr_gb300 import _lib, build
     from tincr_gb300 import fmo
     from tincr_gb300 import scc as gscc
-    build.build()
-    mons, dims, starts = scc_workload()
-    ctx = _lib.Context(0)
+    dims, starts = scc_dimers(mons)
     sets = [("monomers", [m.system for m in mons], None)]
-    if args.scc_set == "all":
+    if scc_set == "all":
         sets.append(("dimers", dims, starts))
     gscc.scc_batch(ctx, sets[0][1], tol=SCC_TOL)   # warm-up: allocation of the slots
-    out = {"mode": "scc", "metric": "batched SCC wall seconds", "tol": SCC_TOL}
+    out = {"metric": "batched SCC seconds", "tol": SCC_TOL}
     for name, systems, st in sets:
         for fp32 in (False, True):
             t0 = time.perf_counter()
@@ -841,7 +841,7 @@ def run_scc_bench(args):
                 rec["max_abs_orbe_diff_vs_host"] = float(max(np.abs(x.orbe - m.ground.orbe).max()
                                                              for x, m in zip(g, mons)))
             out["%s_%s" % (name, "fp32start" if fp32 else "fp64")] = rec
-    if args.cpu_baseline:
+    if cpu_baseline:
         # host SCC restatement on all host cores: the monomers in full, a bounded sample of dimers
         cores = os.cpu_count() or 1
         t0 = time.perf_counter()
@@ -854,31 +854,58 @@ def run_scc_bench(args):
         out["cpu_baseline"] = {"kind": "port", "cores": cores, "monomers_s": t_mon, "dimers_s": t_dim,
                                "sample": "host SCC (groundstate.run_scc, numpy) in a spawn pool of %d processes: "
                                          "all %d monomers; %d of %d dimers, scaled" % (cores, len(mons), k, len(dims))}
+    return out
+
+
+def run_scc_bench(args):
+    """--mode scc: `scc_measure` on its own; prints one JSON line."""
+    from tincr_gb300 import _lib, build
+    build.build()
+    mons, pairs, inst, labels = fmo_workload()
+    ctx = _lib.Context(0)
+    out = {"mode": "scc"}
+    out.update(scc_measure(ctx, mons, args.cpu_baseline, args.scc_set))
     print(json.dumps(out))
     ctx.close()
 
 
-def run_rpa_bench(args):
+def rpa_measure(ctx, sy, g):
     """RPA / Casida (tincr_rpa_solve, FP64) on the (H2O)128 LC workload: the lowest N_ROOTS roots to
     the bench residual, timed with CUDA events, beside the FP64 TDA solve of the same roots."""
-    from tincr_gb300 import _lib, build
+    from tincr_gb300 import _lib
     from tincr_gb300 import tda as T
-    build.build()
-    sy, g = workload()
-    ctx = _lib.Context(0)
     es = T.ExcitedStateSystem.from_ground_state(ctx, sy, g)
     es.prepare_tda()
-    out = {"mode": "rpa", "workload": "water128-lc-20roots", "tol": TOL}
-    for rep in range(2):
-        r = es.run_rpa(N_ROOTS, MAX_ITER, TOL)
-        out["rpa_ms"] = ctx.last_timing()[0]
-        out["rpa_iterations"] = int(r["rpa_iterations"])
+    out = {"workload": "water128-lc-20roots", "tol": TOL}
+    r = es.run_rpa(N_ROOTS, MAX_ITER, TOL)
+    out["rpa_ms"] = ctx.last_timing()[0]
+    out["rpa_iterations"] = int(r["rpa_iterations"])
     r = es.run_tda(N_ROOTS, MAX_ITER, TOL, precision=_lib.PREC_FP64)
     out["tda_fp64_ms"] = ctx.last_timing()[0]
     out["tda_iterations"] = int(r["davidson_iterations"])
-    out["rpa_minus_tda_eh"] = [float(x) for x in (es.properties["rpa_eigenvalues"] - r["ci_eigenvalues"])]
+    d = es.properties["rpa_eigenvalues"] - r["ci_eigenvalues"]
+    out["rpa_minus_tda_eh"] = {"min": float(d.min()), "max": float(d.max())}
+    return out
+
+
+def run_rpa_bench(args):
+    """--mode rpa: `rpa_measure` on its own; prints one JSON line."""
+    from tincr_gb300 import _lib, build
+    build.build()
+    sy, g = workload()
+    ctx = _lib.Context(0)
+    out = {"mode": "rpa"}
+    out.update(rpa_measure(ctx, sy, g))
     print(json.dumps(out))
     ctx.close()
+
+
+def _guarded(fn):
+    """The result of fn(), or the error it raised (the extra measurements must not cost the main line)."""
+    try:
+        return fn()
+    except Exception as e:   # reported in the JSON line, not hidden
+        return {"error": "%s: %s" % (type(e).__name__, e)}
 
 
 def fmo512_workload(workers, scc="host", ctx=None):
@@ -1063,6 +1090,8 @@ def main():
     ap.add_argument("--precision", default="bf16x3", choices=sorted(PRECISIONS))
     ap.add_argument("--no-compare-fp64", dest="compare_fp64", action="store_false")
     ap.add_argument("--no-fmo", dest="fmo", action="store_false")
+    ap.add_argument("--no-next-rows", dest="next_rows", action="store_false",
+                    help="skip the batched SCC and RPA measurements of the single-GPU run")
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
     # counts of the step a `--mode cpu-sample` child scales its sample to (passed by the GPU arm)
