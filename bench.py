@@ -322,6 +322,7 @@ def run_gpu(args):
             out["scc"] = _guarded(lambda: scc_measure(ctx, mons, args.cpu_baseline))
     if world == 1 and args.next_rows:
         out["rpa"] = _guarded(lambda: rpa_measure(ctx, sy, g))
+        out["fd"] = _guarded(lambda: fd_measure(ctx))
     if ref64 is not None:
         out["fp64_gpu"] = {"value": float(np.mean(ref64["dev_ms"])) / 1e3, "unit": "s",
                            "speedup_of_mixed": float(np.mean(ref64["dev_ms"])) / max(1e-9, float(np.mean(main["dev_ms"]))),
@@ -898,6 +899,50 @@ def run_rpa_bench(args):
     out.update(rpa_measure(ctx, sy, g))
     print(json.dumps(out))
     ctx.close()
+
+
+def _scc_energy_job(sy):
+    from tincr_gb300 import groundstate as gs
+    return gs.run_scc(sy, tol=1e-11).energy
+
+
+def fd_measure(ctx):
+    """Numerical S1 gradient of decacene (C42H24, LC, all 198 coordinates, +-1e-4 bohr; tincr's
+    gradients/numerical.rs check): the 396 displaced SCCs as one batched GPU SCC, then each
+    geometry's TDA (3 roots, FP64) on the GPU; the host SCC of a sample of the displaced geometries
+    on all host cores beside it, and the largest difference from the analytic exact-variant gradient."""
+    from tincr_gb300 import fmo
+    from tincr_gb300 import geometry as G
+    from tincr_gb300 import gradients as GR
+    from tincr_gb300 import groundstate as gs
+    from tincr_gb300 import numerical as NUM
+    from tincr_gb300 import scc as gscc
+    from tincr_gb300 import tda as T
+    z, x = G.acene(10)
+    sy = gs.build_system(z, G.to_bohr(x), lc=True)
+    g = gs.run_scc(sy, tol=1e-11)
+    systems, _ = NUM._displaced(sy, range(sy.xyz.size), [1e-4])
+    t0 = time.perf_counter()
+    gscc.scc_batch(ctx, systems, tol=1e-11, require_convergence=True)
+    scc_wall = time.perf_counter() - t0
+    scc_ms = ctx.last_timing()[0]
+    t0 = time.perf_counter()
+    _, fd = NUM.fd_gradient(ctx, sy, n_roots=1, h=1e-4)
+    fd_wall = time.perf_counter() - t0
+    es = T.ExcitedStateSystem.from_ground_state(ctx, sy, g)
+    es.run_tda(3, 450, 1e-8)
+    ana = GR.GradientSystem(es, sy, g).tda_gradient(0, "exact")
+    cores = os.cpu_count() or 1
+    k = min(len(systems), 2 * cores)
+    t0 = time.perf_counter()
+    fmo._pool_map(_scc_energy_job, systems[:k], cores)
+    host_scc = (time.perf_counter() - t0) * len(systems) / k
+    return {"workload": "decacene-lc-s1-fd-198coords", "displaced_sccs": len(systems),
+            "scc_batch_kernel_ms": scc_ms, "scc_batch_wall_s": scc_wall, "fd_gradient_wall_s": fd_wall,
+            "max_abs_fd_minus_analytic_eh_per_bohr": float(np.abs(fd[0] - ana).max()),
+            "cpu_baseline": {"kind": "port", "cores": cores, "displaced_sccs_s": host_scc,
+                             "sample": "host SCC (groundstate.run_scc) of %d of the %d displaced geometries in a "
+                                       "spawn pool of %d processes, scaled" % (k, len(systems), cores)}}
 
 
 def _guarded(fn):

@@ -10,9 +10,10 @@ Checks:
 * "reference" variant (tincr's formulas) against the oracle's analytic gradient of the same roots
   (`gradients/excited_state.rs`, `gradients/ground_state.rs`): 1e-9 Eh/bohr.
 * "exact" variant against central finite differences (+-1e-4 bohr, every coordinate) of the
-  excitation energies, each displaced geometry solved by the host SCC and the GPU FP64 Davidson
-  (residual 1e-8; tincr's Davidson stalls near 4e-9 on decacene, where the 1e-8 drop rule of its
-  Gram-Schmidt rejects every correction): 1e-5 Eh/bohr.
+  excitation energies, each displaced geometry solved by an SCC and the GPU FP64 Davidson (residual
+  1e-8; tincr's Davidson stalls near 4e-9 on decacene, where the 1e-8 drop rule of its Gram-Schmidt
+  rejects every correction): 1e-5 Eh/bohr.  The polyene's displaced SCCs run on the host, the
+  decacene's as one batched GPU SCC.
 * mixed form: energies within 1e-6 Eh and gradients within 1e-5 Eh/bohr of the FP64 form.
 """
 
@@ -116,11 +117,13 @@ def test_decacene_reference_gradients_match_oracle(gpu_ctx, lc):
 
 @pytest.mark.parametrize("lc", [True, False])
 def test_decacene_exact_gradients_match_finite_differences(gpu_ctx, lc):
+    """All 198 coordinates: the 396 displaced SCCs as one batched GPU SCC (tincr_gb300.numerical)."""
+    from tincr_gb300 import numerical as NUM
     sy, g = _molecule("decacene", lc)
     es = _solve(gpu_ctx, sy, g, lc, 3)
     gr = GR.GradientSystem(es, sy, g)
     ana = np.array([gr.tda_gradient(s, "exact") for s in range(3)])
-    fd = _finite_differences(gpu_ctx, sy, lc, 3)
+    _, fd = NUM.fd_gradient(gpu_ctx, sy, n_roots=3, h=FD_STEP)
     err = np.abs(ana - fd).max(axis=1)
     print("decacene lc=%s exact gradient vs FD, per state:" % lc, " ".join("%.1e" % v for v in err))
     assert err.max() < 1e-5
