@@ -4,7 +4,7 @@ tincr checks its analytic gradients against numerical derivatives of the SCC ene
 excitation energies (src/gradients/numerical.rs: `gs_gradient_wrapper`, `tda_gradient_wrapper`,
 `finite_difference`, `ridders_method`): one SCC, and one TDA, per displaced geometry.  Here the
 6N displaced geometries (+h and -h along every Cartesian coordinate) run as one `tincr_scc_batch`
-call, and each geometry's TDA runs on the GPU from that ground state.  The derivatives are central
+call, and their TDAs as one batched TDA on the GPU from those ground states.  The derivatives are central
 differences with one step (tincr's `finite_difference`); `ridders` adds Ridders' extrapolation
 over a fixed ladder of steps h, h/1.4, h/1.4^2, ... (the constants of `ridders_method`), all
 levels evaluated in the same batch."""
@@ -32,11 +32,25 @@ def _displaced(sysm, coords, steps):
 
 def energies_at(ctx, systems, n_roots=0, scc_tol=1e-11, tda_tol=1e-8, max_iter=450, fp32_start=False):
     """SCC energies (batched GPU SCC) and, with n_roots > 0, the n_roots lowest TDA excitation
-    energies (GPU FP64 Davidson) of every system.  Returns (e_scc [n], e_exc [n, n_roots])."""
+    energies (FP64) of every system: all systems in one batched TDA (`tincr_tda_solve_batch`, the
+    FMO batch, tincr's Davidson per instance) for up to 6 roots, one GPU Davidson per system above.
+    Returns (e_scc [n], e_exc [n, n_roots])."""
     grounds, _ = gscc.scc_batch(ctx, systems, tol=scc_tol, fp32_start=fp32_start, require_convergence=True)
     e_scc = np.array([g.energy for g in grounds])
     e_exc = np.zeros((len(systems), n_roots))
-    if n_roots > 0:
+    if 0 < n_roots <= 6:
+        from . import fmo
+        inst = []
+        for sy, g in zip(systems, grounds):
+            no, nv = sy.n_occ, sy.n_virt
+            inst.append(dict(n_atoms=sy.n_atoms, n_orb=sy.n_orbs, n_occ=no, n_virt=nv, n_roots=n_roots,
+                             opa=sy.orbs_per_atom.astype(np.int32), c=g.orbs[:, :no + nv], s=g.s,
+                             orbe=g.orbe[:no + nv], gamma=g.gamma, gamma_lr=g.gamma_lr if sy.lc else None, xyz=sy.xyz))
+        rc, res = fmo.solve_batch(ctx, inst, max_iter, tda_tol, _lib.PREC_FP64)
+        if rc != _lib.OK:
+            raise T.DavidsonError("batched Davidson did not converge for every displaced geometry")
+        e_exc = np.array([r["energies"] for r in res])
+    elif n_roots > 6:
         for k, (sy, g) in enumerate(zip(systems, grounds)):
             es = T.ExcitedStateSystem.from_ground_state(ctx, sy, g)
             e_exc[k] = es.run_tda(n_roots, max_iter, tda_tol, precision=_lib.PREC_FP64)["ci_eigenvalues"]
