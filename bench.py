@@ -800,7 +800,8 @@ def _scc_host_job(args):
 def _scc_gemm_flops(systems, grounds):
     """FP64 flops of the SCC's GEMMs per system and iteration (LC: 10 n^3 for the exchange
     Hamiltonian, 4 n^3 for X F X, 2 n^3 for F'P', 6 n^2 n_occ for the densities) over the iterations
-    run, plus the start (X, S^1/2, P': 8 n^3) and the end (orbitals, density, LC energy: 6 n^3)."""
+    run, plus the start (X, S^1/2, P': 8 n^3) and the end (orbitals, density, LC energy: 6 n^3):
+    the dense count (the kernel forms the symmetric products from their lower-triangle tiles)."""
     f = 0.0
     for sy, g in zip(systems, grounds):
         n, o = float(sy.n_orbs), float(sy.n_elec // 2)

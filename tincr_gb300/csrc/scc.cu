@@ -138,13 +138,14 @@ __device__ void sc_sums(double *v, int m, ScShared &sm) {
 
 template <class T, int R>
 __device__ void sc_gemm(int M, int N, int K, T alpha, const T *A, int lda, bool ta, const T *B, int ldb, bool tb,
-                        T beta, T *C, int ldc, ScShared &sm) {
+                        T beta, T *C, int ldc, ScShared &sm, bool sym) {
     constexpr int TL = 16 * R;
     T(*As)[TL + 1] = reinterpret_cast<T(*)[TL + 1]>(sm.gemm);
     T(*Bs)[TL + 1] = reinterpret_cast<T(*)[TL + 1]>(reinterpret_cast<T *>(sm.gemm) + 16 * (TL + 1));
     const int tid = threadIdx.x, ty = tid >> 4, tx = tid & 15;
     const int tm = (M + TL - 1) / TL, tn = (N + TL - 1) / TL;
     for (int t = 0; t < tm * tn; ++t) {
+        if (sym && t / tn < t % tn) continue;   // symmetric result: tiles on and below the diagonal only
         const int m0 = (t / tn) * TL, n0 = (t % tn) * TL;
         T acc[R][R];
 #pragma unroll
@@ -201,6 +202,13 @@ __device__ void sc_gemm(int M, int N, int K, T alpha, const T *A, int lda, bool 
             }
     }
     __syncthreads();
+    if (sym) {   // upper triangle from the lower one (C and, with beta != 0, its old value symmetric)
+        for (long long e = tid; e < (long long)M * M; e += SC_T) {
+            const int i = (int)(e / M), j = (int)(e - (long long)i * M);
+            if (i < j) C[(long long)i * ldc + j] = C[(long long)j * ldc + i];
+        }
+        __syncthreads();
+    }
 }
 
 template <class T> struct ScTile;
@@ -210,7 +218,15 @@ template <> struct ScTile<float> { static constexpr int R = 2; };
 template <class T>
 __device__ __forceinline__ void gemm(int M, int N, int K, T alpha, const T *A, int lda, bool ta, const T *B, int ldb,
                                      bool tb, T beta, T *C, int ldc, ScShared &sm) {
-    sc_gemm<T, ScTile<T>::R>(M, N, K, alpha, A, lda, ta, B, ldb, tb, beta, C, ldc, sm);
+    sc_gemm<T, ScTile<T>::R>(M, N, K, alpha, A, lda, ta, B, ldb, tb, beta, C, ldc, sm, false);
+}
+
+// the same for a product known to be symmetric (M == N): the tiles below the diagonal are computed
+// and mirrored
+template <class T>
+__device__ __forceinline__ void gemm_sym(int M, int K, T alpha, const T *A, int lda, bool ta, const T *B, int ldb,
+                                         bool tb, T beta, T *C, int ldc, ScShared &sm) {
+    sc_gemm<T, ScTile<T>::R>(M, M, K, alpha, A, lda, ta, B, ldb, tb, beta, C, ldc, sm, true);
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -721,7 +737,7 @@ __device__ void sc_fock(int n, int N, bool lc, const ScWork<T> &w, const double 
     }
     __syncthreads();
     gemm<T>(n, n, n, T(1), tmp, n, false, w.S, n, false, T(0), w.T2, n, sm);   // (g o S dP) S
-    gemm<T>(n, n, n, T(1), w.T1, n, false, w.S, n, false, T(0), w.T3, n, sm);   // S dP S
+    gemm_sym<T>(n, n, T(1), w.T1, n, false, w.S, n, false, T(0), w.T3, n, sm);   // S dP S
     for (long long t = tid; t < nn; t += SC_T) {
         const int mu = (int)(t / n), nu = (int)(t - (long long)mu * n);
         const T g = GLR(mu, nu);
@@ -730,7 +746,7 @@ __device__ void sc_fock(int n, int N, bool lc, const ScWork<T> &w, const double 
     }
     __syncthreads();
     gemm<T>(n, n, n, T(1), w.S, n, false, tmp, n, false, T(0), w.T1, n, sm);   // S (dP o g)
-    gemm<T>(n, n, n, T(1), w.T1, n, false, w.S, n, false, T(1), hx, n, sm);    // + S (dP o g) S
+    gemm_sym<T>(n, n, T(1), w.T1, n, false, w.S, n, false, T(1), hx, n, sm);    // + S (dP o g) S
     for (long long t = tid; t < nn; t += SC_T) {
         const int mu = (int)(t / n), nu = (int)(t - (long long)mu * n);
         w.F[t] += T(-0.0625) * (hx[t] + hx[(long long)nu * n + mu]);
@@ -794,14 +810,14 @@ __device__ void sc_iterate(const ScArgs &a, const tincr_scc_system &sy, const Sc
     const long long nn = (long long)n * n;
     // P' = S^1/2 P S^1/2 of the starting density
     gemm<T>(n, n, n, T(1), w.Sh, n, false, w.P, n, false, T(0), w.T1, n, sm);
-    gemm<T>(n, n, n, T(1), w.T1, n, false, w.Sh, n, false, T(0), w.Pp, n, sm);
+    gemm_sym<T>(n, n, T(1), w.T1, n, false, w.Sh, n, false, T(0), w.Pp, n, sm);
     for (int k = 0; k < limit; ++k) {
         ++st.it;
         sc_charges<T>(n, N, w.P, w.S, w.gam, p0, sm);
         sc_fock<T>(n, N, a.lc != 0, w, p0, sm);
         // F' = X F X, E' = F' P' - P' F'
         gemm<T>(n, n, n, T(1), w.X, n, false, w.F, n, false, T(0), w.T1, n, sm);
-        gemm<T>(n, n, n, T(1), w.T1, n, false, w.X, n, false, T(0), w.Fp, n, sm);
+        gemm_sym<T>(n, n, T(1), w.T1, n, false, w.X, n, false, T(0), w.Fp, n, sm);
         gemm<T>(n, n, n, T(1), w.Fp, n, false, w.Pp, n, false, T(0), w.T1, n, sm);
         const int cur = hist % SC_DIIS;
         T *Fc = w.Fh + cur * nn, *Ec = w.Eh + cur * nn;
@@ -868,9 +884,9 @@ __device__ void sc_iterate(const ScArgs &a, const tincr_scc_system &sy, const Sc
             return;
         }
         // P' = 2 Z Z^T, C_o = X Z, P = 2 C_o C_o^T
-        gemm<T>(n, n, o, T(2), w.Z, o, false, w.Z, o, true, T(0), w.Pp, n, sm);
+        gemm_sym<T>(n, o, T(2), w.Z, o, false, w.Z, o, true, T(0), w.Pp, n, sm);
         gemm<T>(n, o, n, T(1), w.X, n, false, w.Z, o, false, T(0), w.T2, o, sm);
-        gemm<T>(n, n, o, T(2), w.T2, o, false, w.T2, o, true, T(0), w.P, n, sm);
+        gemm_sym<T>(n, o, T(2), w.T2, o, false, w.T2, o, true, T(0), w.P, n, sm);
     }
 }
 
@@ -921,8 +937,8 @@ __global__ void __launch_bounds__(SC_T, SC_SLOTS_PER_SM) scc_kernel(ScArgs a) {
                 w.T2[t] = w.Z[t] * sqrt(sm.w[r]);
             }
             __syncthreads();
-            gemm<double>(n, n, n, 1.0, w.T1, n, false, w.Z, n, true, 0.0, w.X, n, sm);
-            gemm<double>(n, n, n, 1.0, w.T2, n, false, w.Z, n, true, 0.0, w.Sh, n, sm);
+            gemm_sym<double>(n, n, 1.0, w.T1, n, false, w.Z, n, true, 0.0, w.X, n, sm);
+            gemm_sym<double>(n, n, 1.0, w.T2, n, false, w.Z, n, true, 0.0, w.Sh, n, sm);
             start_density();
         }
         int remaining = a.max_iter, hist = 0;
@@ -980,7 +996,7 @@ __global__ void __launch_bounds__(SC_T, SC_SLOTS_PER_SM) scc_kernel(ScArgs a) {
         if (ok) {
             double *C = a.orbs + sy.mat_off;
             gemm<double>(n, n, n, 1.0, w.X, n, false, w.Z, n, false, 0.0, C, n, sm);
-            gemm<double>(n, n, o, 2.0, C, n, false, C, n, true, 0.0, w.P, n, sm);
+            gemm_sym<double>(n, o, 2.0, C, n, false, C, n, true, 0.0, w.P, n, sm);
             sc_charges<double>(n, N, w.P, w.S, w.gam, p0, sm);
             // E = sum P o H0 + 1/2 dq gamma dq [- 1/8 (sum (S dP S) o dP o g_lr + sum (S dP) o (dP S) o g_lr)]
             double e1 = 0.0;
@@ -996,7 +1012,7 @@ __global__ void __launch_bounds__(SC_T, SC_SLOTS_PER_SM) scc_kernel(ScArgs a) {
                 }
                 __syncthreads();
                 gemm<double>(n, n, n, 1.0, w.S, n, false, dP, n, false, 0.0, w.T1, n, sm);
-                gemm<double>(n, n, n, 1.0, w.T1, n, false, w.S, n, false, 0.0, w.T2, n, sm);
+                gemm_sym<double>(n, n, 1.0, w.T1, n, false, w.S, n, false, 0.0, w.T2, n, sm);
                 for (long long t = tid; t < nn; t += SC_T) {
                     const int mu = (int)(t / n), nu = (int)(t - (long long)mu * n);
                     const double g = w.glr[(long long)sm.ao_atom[mu] * N + sm.ao_atom[nu]];
