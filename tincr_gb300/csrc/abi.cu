@@ -16,8 +16,10 @@ int guarded(tincr_ctx *ctx, F &&f) {
     if (!ctx || !ctx->impl) return TINCR_BAD_ARG;
     try {
         TINCR_CUDA(cudaSetDevice(ctx->impl->device));
+        ctx->impl->err.clear();
         int rc = f(*ctx->impl);
-        if (rc == TINCR_OK) ctx->err.clear();
+        // a status returned without an exception carries the message the call left, if any
+        ctx->err = rc == TINCR_OK ? std::string() : ctx->impl->err;
         return rc;
     } catch (const tincr::Error &e) {
         ctx->err = e.msg;

@@ -984,6 +984,14 @@ __global__ void __launch_bounds__(SC_T, SC_SLOTS_PER_SM) scc_kernel(ScArgs a) {
         }
         if (ok) {
             sc_iterate<double>(a, sy, w, sl.piv, p0, remaining, a.tol, st, hist, sm);
+            if (!st.finite && a.fp32_start) {
+                // the continuation from the FP32 phase failed: max_iter FP64 iterations from the
+                // start, with a fresh DIIS history (the iteration count goes on)
+                start_density();
+                hist = 0;
+                st = ScState{st.it, false, 0.0, true};
+                sc_iterate<double>(a, sy, w, sl.piv, p0, a.max_iter, a.tol, st, hist, sm);
+            }
             ok = st.finite;
         }
         double energy = 0.0;
