@@ -292,7 +292,12 @@ __device__ __forceinline__ int ex_nat(const ExMono &x, const ExMono &y, bool two
 //   A: W [0, W) | L2 / R2 staging [W, W + ST)
 //   B: W [0, W) | gamma block [W, W + G) | V [W + G, W + G + V)
 //   C: L1 / R1 staging [0, ST) | V
+// The staged rows hold (C, S C) pairs side by side, so one vector load fetches both.
 // FP64: 215 KB, FP32: 108 KB.
+template <class T> struct ExPair;
+template <> struct ExPair<float> { using type = float2; };
+template <> struct ExPair<double> { using type = double2; };
+
 template <class T>
 struct ExVUSmem {
     static constexpr size_t W_BYTES = sizeof(T) * XJ_ATOMS * XJ_T;
@@ -319,17 +324,14 @@ __global__ void __launch_bounds__(XJ_T) ex_vu_kernel(const int4 *__restrict__ ti
     constexpr int CH = sizeof(T) == 4 ? 16 : 8;   // atoms A per register block
     using L = ExVUSmem<T>;
     extern __shared__ __align__(16) unsigned char xv_raw[];
+    using T2 = typename ExPair<T>::type;   // (C, S C) of one row and column
     T(*W)[XJ_T] = reinterpret_cast<T(*)[XJ_T]>(xv_raw);
-    T(*L2c)[XJ_TS] = reinterpret_cast<T(*)[XJ_TS]>(xv_raw + L::W_BYTES);
-    T(*L2s)[XJ_TS] = L2c + XJ_AO;
-    T(*R2c)[XJ_TS] = L2s + XJ_AO;
-    T(*R2s)[XJ_TS] = R2c + XJ_AO;
+    T2(*L2)[XJ_TS] = reinterpret_cast<T2(*)[XJ_TS]>(xv_raw + L::W_BYTES);
+    T2(*R2)[XJ_TS] = L2 + XJ_AO;
     T(*G)[XJ_ATOMS] = reinterpret_cast<T(*)[XJ_ATOMS]>(xv_raw + L::W_BYTES);
     T(*V)[XJ_T] = reinterpret_cast<T(*)[XJ_T]>(xv_raw + L::V_OFF);
-    T(*L1c)[XJ_TS] = reinterpret_cast<T(*)[XJ_TS]>(xv_raw);
-    T(*L1s)[XJ_TS] = L1c + XJ_AO;
-    T(*R1c)[XJ_TS] = L1s + XJ_AO;
-    T(*R1s)[XJ_TS] = R1c + XJ_AO;
+    T2(*L1)[XJ_TS] = reinterpret_cast<T2(*)[XJ_TS]>(xv_raw);
+    T2(*R1)[XJ_TS] = L1 + XJ_AO;
     double *red = reinterpret_cast<double *>(xv_raw + L::END);
 
     const int4 tl = tiles[blockIdx.x];
@@ -356,8 +358,7 @@ __global__ void __launch_bounds__(XJ_T) ex_vu_kernel(const int4 *__restrict__ ti
                 sc = (T)K.cross_yx2[(long long)(nu - m2x.n) * m2x.n + col];
             }
         }
-        L2c[nu][q] = c;
-        L2s[nu][q] = sc;
+        L2[nu][q] = T2{c, sc};
     }
     {
         const int ny2 = two2 ? m2y.n : m2x.n;   // rows held by the per-state part
@@ -378,8 +379,7 @@ __global__ void __launch_bounds__(XJ_T) ex_vu_kernel(const int4 *__restrict__ ti
                     sc = (T)rs[(long long)(nu - m2x.n) * K.nq + j];
                 }
             }
-            R2c[nu][q] = c;
-            R2s[nu][q] = sc;
+            R2[nu][q] = T2{c, sc};
         }
     }
     __syncthreads();
@@ -390,8 +390,10 @@ __global__ void __launch_bounds__(XJ_T) ex_vu_kernel(const int4 *__restrict__ ti
         const int base = onx ? 0 : m2x.n;
         T w = T(0);
         if (active)
-            for (int nu = base + mb.ao_off[bl]; nu < base + mb.ao_off[bl + 1]; ++nu)
-                w += L2c[nu][al] * R2s[nu][jl] + L2s[nu][al] * R2c[nu][jl];
+            for (int nu = base + mb.ao_off[bl]; nu < base + mb.ao_off[bl + 1]; ++nu) {
+                const T2 l = L2[nu][al], r = R2[nu][jl];
+                w += l.x * r.y + l.y * r.x;
+            }
         W[B][threadIdx.x] = T(0.5) * w;
     }
     __syncthreads();   // the staged rows are dead: the gamma block takes their place
@@ -444,8 +446,7 @@ __global__ void __launch_bounds__(XJ_T) ex_vu_kernel(const int4 *__restrict__ ti
                     sc = (T)scr[K1.crs + (long long)(mu - m1x.n) * K1.na + a];
                 }
             }
-            L1c[mu][q] = c;
-            L1s[mu][q] = sc;
+            L1[mu][q] = T2{c, sc};
         }
         if (ei == eb) {   // the same columns Q of y1 for every element of the group
 #pragma unroll 4
@@ -464,8 +465,7 @@ __global__ void __launch_bounds__(XJ_T) ex_vu_kernel(const int4 *__restrict__ ti
                         sc = (T)m1y.SC[(long long)(mu - m1x.n) * m1y.n + col];
                     }
                 }
-                R1c[mu][q] = c;
-                R1s[mu][q] = sc;
+                R1[mu][q] = T2{c, sc};
             }
         }
         __syncthreads();
@@ -477,8 +477,10 @@ __global__ void __launch_bounds__(XJ_T) ex_vu_kernel(const int4 *__restrict__ ti
                 const int aloc = onx ? A : A - m1x.n_atoms;
                 const int base = onx ? 0 : m1x.n;
                 T u = T(0);
-                for (int mu = base + ma.ao_off[aloc]; mu < base + ma.ao_off[aloc + 1]; ++mu)
-                    u += L1c[mu][al] * R1s[mu][jl] + L1s[mu][al] * R1c[mu][jl];
+                for (int mu = base + ma.ao_off[aloc]; mu < base + ma.ao_off[aloc + 1]; ++mu) {
+                    const T2 l = L1[mu][al], r = R1[mu][jl];
+                    u += l.x * r.y + l.y * r.x;
+                }
                 acc += u * V[A][threadIdx.x];
             }
             acc *= T(0.5);
