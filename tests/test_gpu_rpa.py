@@ -66,3 +66,19 @@ def test_rpa_iteration_cap(gpu_ctx):
         es.run_rpa(6, 1, 1e-9)
     r = es.run_rpa(6, 1, 1e-9, raise_on_failure=False)
     assert r["rpa_iterations"] == 1
+
+
+def test_rpa_arguments(gpu_ctx):
+    """Bad arguments come back as BAD_ARG; one root of the smallest fixture system (water) against
+    the dense Casida statement."""
+    c = synthetic_case("water8", lc=True)
+    es = _system(gpu_ctx, c)
+    for n_roots, max_iter, tol in ((0, 10, 1e-6), (3, 0, 1e-6), (3, 10, 0.0), (10 ** 6, 10, 1e-6)):
+        with pytest.raises(_lib.TincrError) as e:
+            es.run_rpa(n_roots, max_iter, tol)
+        assert e.value.status == _lib.BAD_ARG
+    o = oracle_inputs(c)
+    a, b = OR.a_b_matrices(o["omega"], o["q_ov"], o["gamma"], o["q_oo"], o["q_vv"], o["gamma_lr"], o["n_occ"],
+                           o["n_virt"])
+    om, _, _ = OR.casida(a, b)
+    assert abs(es.run_rpa(1, 100, 1e-8)["rpa_eigenvalues"][0] - om[0]) < 1e-10

@@ -45,11 +45,6 @@ def _host_with(sy, given, tol):
         gs.gamma_atomwise = orig
 
 
-def _signs(c):
-    idx = np.argmax(np.abs(c), axis=0)
-    return c * np.sign(c[idx, np.arange(c.shape[1])])
-
-
 def test_scc_reproduces_tincr_fixtures(gpu_ctx):
     items = [_fixture(m) for m in MOLS]
     out, rc = scc.scc_batch(gpu_ctx, [sy for sy, _, _ in items], tol=1e-11, given=[g for _, g, _ in items])
@@ -93,7 +88,8 @@ def _compare(g, h, tag):
     # orbitals up to sign, where the orbital energy is separated from its neighbours
     gap = np.minimum(np.diff(h.orbe, prepend=-np.inf), np.diff(h.orbe, append=np.inf))
     sep = gap > 1e-4
-    assert np.abs(_signs(g.orbs)[:, sep] - _signs(h.orbs)[:, sep]).max() < 1e-6, tag
+    sgn = np.sign(np.einsum("ij,ij->j", g.orbs, h.orbs))   # the sign of each orbital's overlap
+    assert np.abs(g.orbs[:, sep] * sgn[sep] - h.orbs[:, sep]).max() < 1e-6, tag
 
 
 @pytest.mark.parametrize("lc", [True, False])
@@ -169,3 +165,25 @@ def test_fmo_setup_on_gpu_matches_host(gpu_ctx):
     assert host.real_pairs == dev.real_pairs and host.real_pairs
     for k in host.real_pairs:
         assert np.abs(host.pair_scc[k][1] - dev.pair_scc[k][1]).max() < 1e-9
+
+
+def test_scc_edge_cases(gpu_ctx):
+    """The largest system one CTA takes (a water cluster of 252 orbitals) equals the host SCC; a
+    two-orbital system (H2); an empty batch and a non-finite starting density are rejected."""
+    z, x = G.water_cluster(7, 3, 2)            # 42 waters: 252 orbitals, 126 atoms
+    big = gs.build_system(z, G.to_bohr(x), lc=True)
+    assert big.n_orbs == 252
+    h2 = gs.build_system(np.array([1, 1], np.int32), np.array([[0.0, 0.0, 0.0], [0.0, 0.0, 1.4]]), lc=True)
+    out, rc = scc.scc_batch(gpu_ctx, [big, h2], tol=1e-10)
+    assert rc == _lib.OK
+    for sy, g in zip((big, h2), out):
+        _compare(g, gs.run_scc(sy, tol=1e-10), sy.n_orbs)
+    out, rc = scc.scc_batch(gpu_ctx, [], tol=1e-10)
+    assert out == [] and rc == _lib.OK
+    p = np.diag(h2.ao_occ.astype(np.float64))
+    p[0, 1] = np.nan
+    with pytest.raises(_lib.TincrError) as e:
+        scc.scc_batch(gpu_ctx, [h2], tol=1e-10, p_start=[p])
+    assert e.value.status == _lib.NONFINITE
+    with pytest.raises(ValueError):   # open shell
+        scc.scc_batch(gpu_ctx, [gs.build_system(np.array([1], np.int32), np.zeros((1, 3)), lc=True)])
