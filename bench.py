@@ -157,8 +157,22 @@ def run_gpu(args):
     ctx = _lib.Context(local)
     es = T.ExcitedStateSystem.from_ground_state(ctx, sy, g)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
-    # pinned host copies of the step inputs for the end-to-end leg
-    host_in = [es.orbs, es.s, es.orbe, es.gamma, es.gamma_lr, es.xyz]
+    # page-locked host copies of the step inputs for the end-to-end leg (torch's pinned allocator,
+    # viewed as numpy arrays; `keep` holds the tensors)
+    keep = []
+
+    def pinned(a):
+        a = np.ascontiguousarray(a)
+        t = torch.empty(a.shape, dtype=torch.float64 if a.dtype == np.float64 else torch.int32, pin_memory=True)
+        keep.append(t)
+        v = t.numpy()
+        v[...] = a
+        return v
+
+    host_in = [pinned(a) for a in (es.orbs, es.s, es.orbe, es.gamma, es.gamma_lr, es.xyz)]
+    opa_pin = pinned(es.opa.astype(np.int32))
+    import dataclasses
+    g_pin = dataclasses.replace(g, p=pinned(g.p), h_coul_x=pinned(g.h_coul_x), dq=pinned(g.dq))
     h2d_bytes = sum(a.nbytes for a in host_in) + es.opa.nbytes
     es.prepare_tda()
     gr = GR.GradientSystem(es, sy, g)
@@ -214,11 +228,11 @@ def run_gpu(args):
         l2_flush(flush)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        es2 = T.ExcitedStateSystem(ctx, es.opa, es.orbs, es.s, es.orbe, es.n_occ, es.n_virt, es.gamma,
-                                   es.gamma_lr, es.xyz)
+        orbs_h, s_h, orbe_h, gam_h, glr_h, xyz_h = host_in
+        es2 = T.ExcitedStateSystem(ctx, opa_pin, orbs_h, s_h, orbe_h, es.n_occ, es.n_virt, gam_h, glr_h, xyz_h)
         es2.prepare_tda()
         es2.run_tda(N_ROOTS, MAX_ITER, TOL, precision=prec)
-        gr2 = GR.GradientSystem(es2, sy, g)
+        gr2 = GR.GradientSystem(es2, sy, g_pin)
         gr2.both(0, "reference")
         e2e.append(time.perf_counter() - t0)
     # the plain FP64 form of the same step, for the mixed-vs-FP64 comparison
