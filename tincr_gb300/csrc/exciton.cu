@@ -590,14 +590,27 @@ __global__ void ex_norm_finish_kernel(int k, const double *__restrict__ part, do
 
 // out[i, x] = sum_k A[i, k] B[k, x] (k in order), one thread per output; A [M x K], B [K x N], out [M x N]
 // row-major (the Davidson's new products H v_i, Ritz vectors and Y^T AV)
-__global__ void ex_rowprod_kernel(int N, int K, const double *__restrict__ A, const double *__restrict__ B,
-                                  double *out) {
-    const int x = blockIdx.x * blockDim.x + threadIdx.x, i = blockIdx.y;
+// out[i][x] = sum_k A[i][k] B[k][x] split over K: part[s][i][x] = sum over chunk s of k (gridDim.z = S
+// chunks), then
+// ex_rowprod_sum_kernel adds the S partial sums in chunk order (fixed order: a row's value does not
+// depend on the other rows of the launch)
+__global__ void ex_rowprod_part_kernel(int N, int K, const double *__restrict__ A, const double *__restrict__ B,
+                                       double *__restrict__ part) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, i = blockIdx.y, sc = blockIdx.z, S = gridDim.z;
     if (x >= N) return;
+    const int k0 = (int)((long long)K * sc / S), k1 = (int)((long long)K * (sc + 1) / S);
     const double *a = A + (long long)i * K;
     double acc = 0.0;
-    for (int k = 0; k < K; ++k) acc += a[k] * B[(long long)k * N + x];
-    out[(long long)i * N + x] = acc;
+    for (int k = k0; k < k1; ++k) acc += a[k] * B[(long long)k * N + x];
+    part[((long long)sc * gridDim.y + i) * N + x] = acc;
+}
+
+__global__ void ex_rowprod_sum_kernel(long long len, int S, const double *__restrict__ part, double *__restrict__ out) {
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (t >= len) return;
+    double acc = 0.0;
+    for (int sc = 0; sc < S; ++sc) acc += part[(long long)sc * len + t];
+    out[t] = acc;
 }
 
 // C[i, j] = A_i . B_j (rows of length K), one warp per entry (lane-strided sums, fixed shuffle order)
@@ -633,14 +646,26 @@ __global__ void ex_dots_dev_kernel(const int *__restrict__ m, int n, const doubl
 }
 
 // v -= c^T V for i < *m, one thread per component; each CTA's sum of squares into part[]
-__global__ void ex_orth_update_dev_kernel(const int *__restrict__ m, int n, const double *__restrict__ V,
-                                          const double *__restrict__ c, double *v, double *part) {
+// part2[s][x] = sum over chunk s of i < *m of c[i] V[i][x] (gridDim.y = S chunks)
+__global__ void ex_orth_part_kernel(const int *__restrict__ m, int n, const double *__restrict__ V,
+                                    const double *__restrict__ c, double *__restrict__ part2) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, sc = blockIdx.y, S = gridDim.y, mm = *m;
+    if (x >= n) return;
+    const int i0 = (int)((long long)mm * sc / S), i1 = (int)((long long)mm * (sc + 1) / S);
+    double acc = 0.0;
+    for (int i = i0; i < i1; ++i) acc += c[i] * V[(long long)i * n + x];
+    part2[(long long)sc * n + x] = acc;
+}
+
+// v -= sum of the S partial sums (chunk order), with the block partial sums of |v|^2
+__global__ void ex_orth_finish_kernel(int n, int S, const double *__restrict__ part2, double *v, double *part) {
     __shared__ double red[8];
-    const int x = blockIdx.x * blockDim.x + threadIdx.x, mm = *m;
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
     double s = 0.0;
     if (x < n) {
-        double y = v[x];
-        for (int i = 0; i < mm; ++i) y -= c[i] * V[(long long)i * n + x];
+        double acc = 0.0;
+        for (int sc = 0; sc < S; ++sc) acc += part2[(long long)sc * n + x];
+        const double y = v[x] - acc;
         v[x] = y;
         s = y * y;
     }
@@ -986,6 +1011,9 @@ int Ctx::exciton_states(int n_mono, const tincr_exciton_monomer *mono, int n_pai
     std::vector<SideJob> sjobs;
     long long scr = 0;
     std::unordered_map<long long, long long> side_tab;
+    side_tab.reserve((size_t)8 * ns + 1024);
+    elv.reserve((size_t)64 * ns);
+    k2v.reserve((size_t)32 * ns);
     auto side_of = [&](int kind, int state, int mono_key, int variant, int x, int y, int c0, int nc, int nout,
                        const double *X, int ld, int r0, long long rows) -> long long {
         const long long key = (((long long)kind * ns + state) * (n_mono + 1) + mono_key) * 2 + variant;
@@ -1153,11 +1181,17 @@ int Ctx::exciton_states(int n_mono, const tincr_exciton_monomer *mono, int n_pai
             }
         }
         gb.run(*this, sizeof(T) == 4, dJobs, dTiles, TINCR_KF_AO_EXCHANGE);
-        // elements sorted by side-2 group; one CTA per (group, tile) forms V and serves the group's elements
-        std::stable_sort(elv.begin(), elv.end(), [](const ExEl &a, const ExEl &b) { return a.k2 < b.k2; });
+        // elements grouped by side-2 group (a stable counting sort); one CTA per (group, tile) forms V
+        // and serves the group's elements
         std::vector<int> el_begin(k2v.size() + 1, 0);
         for (const ExEl &E : elv) ++el_begin[E.k2 + 1];
         for (size_t k = 0; k < k2v.size(); ++k) el_begin[k + 1] += el_begin[k];
+        {
+            std::vector<ExEl> sorted(elv.size());
+            std::vector<int> fill(el_begin.begin(), el_begin.end() - 1);
+            for (const ExEl &E : elv) sorted[fill[E.k2]++] = E;
+            elv.swap(sorted);
+        }
         std::vector<int4> vt;
         double fl = 0.0;
         for (int k = 0; k < (int)k2v.size(); ++k) {
@@ -1428,8 +1462,24 @@ int Ctx::exciton_states(int n_mono, const tincr_exciton_monomer *mono, int n_pai
     for (int x = 0; x < ns; ++x) order[x] = x;
     std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return hdiag[a] < hdiag[b]; });
     const int cap = max_space + nr;
-    DevBuf<double> dV, dAV, dAp, dY, dRitz, dRk, dU, dNrm, dT, dc, dPart;
+    DevBuf<double> dV, dAV, dAp, dY, dRitz, dRk, dU, dNrm, dT, dc, dPart, dPart2, dRp;
     dPart.alloc(ceil_div(ns, 256));
+    // the long sums split over CTAs in chunks of at least 64 terms (at most 16 chunks); the chunk
+    // count depends on the sum's length only, so a row's value does not depend on its launch
+    const int xb = ceil_div(ns, 256);
+    auto chunks = [](int K) { return std::max(1, std::min(16, K / 64)); };
+    const int S_orth = chunks(cap);
+    dPart2.alloc((size_t)S_orth * ns);
+    auto rowprod = [&](int rows, int K, const double *A, const double *B, double *out) {
+        const int S = chunks(K);
+        dRp.reserve((size_t)S * rows * ns);
+        ex_rowprod_part_kernel<<<dim3(xb, rows, S), 256, 0, stream>>>(ns, K, A, B, dRp.p);
+        count_launch(stream, "ex_rowprod_part");
+        ex_rowprod_sum_kernel<<<ceil_div((long long)rows * ns, 256), 256, 0, stream>>>((long long)rows * ns, S, dRp.p,
+                                                                                     out);
+        count_launch(stream, "ex_rowprod_sum");
+        check_launch("ex_rowprod");
+    };
     DevBuf<int> dM;   // the basis size while corrections join it
     dM.alloc(1);
     int *hM = reinterpret_cast<int *>(ex_pin.p + pin_used);   // one int of the page-locked staging buffer
@@ -1458,9 +1508,7 @@ int Ctx::exciton_states(int n_mono, const tincr_exciton_monomer *mono, int n_pai
         // product is formed on its own, in the same order), so only the new vectors are multiplied
         const int sub_slot = prof_begin(TINCR_KF_SUBSPACE);
         if (n_av < m) {   // (H is symmetric: row i of V H is H v_i)
-            ex_rowprod_kernel<<<dim3(ceil_div(ns, 256), m - n_av), 256, 0, stream>>>(ns, ns, dV.p + (size_t)n_av * ns,
-                                                                                    dH.p, dAV.p + (size_t)n_av * ns);
-            count_launch(stream, "ex_rowprod");
+            rowprod(m - n_av, ns, dV.p + (size_t)n_av * ns, dH.p, dAV.p + (size_t)n_av * ns);
             n_av = m;
         }
         ex_dotmat_kernel<<<ceil_div((long long)m * m * 32, 256), 256, 0, stream>>>(m, m, ns, dV.p, dAV.p, dAp.p);
@@ -1476,11 +1524,8 @@ int Ctx::exciton_states(int n_mono, const tincr_exciton_monomer *mono, int n_pai
         for (int r = 0; r < nr; ++r) u[r] = w[r];
         TINCR_CUDA(cudaMemcpyAsync(dY.p, yt.data(), yt.size() * sizeof(double), cudaMemcpyHostToDevice, stream));
         TINCR_CUDA(cudaMemcpyAsync(dU.p, u.data(), nr * sizeof(double), cudaMemcpyHostToDevice, stream));
-        ex_rowprod_kernel<<<dim3(ceil_div(ns, 256), nr), 256, 0, stream>>>(ns, m, dY.p, dV.p, dRitz.p);
-        count_launch(stream, "ex_rowprod");
-        ex_rowprod_kernel<<<dim3(ceil_div(ns, 256), nr), 256, 0, stream>>>(ns, m, dY.p, dAV.p, dRk.p);
-        count_launch(stream, "ex_rowprod");
-        check_launch("ex_rowprod");
+        rowprod(nr, m, dY.p, dV.p, dRitz.p);
+        rowprod(nr, m, dY.p, dAV.p, dRk.p);
         ex_residual_kernel<<<ceil_div((long long)nr * ns, 256), 256, 0, stream>>>(nr, ns, dU.p, dRitz.p, dRk.p);
         count_launch(stream, "ex_residual");
         ex_row_norms_kernel<<<nr, 256, 0, stream>>>(nr, ns, dRk.p, dNrm.p);
@@ -1512,8 +1557,10 @@ int Ctx::exciton_states(int n_mono, const tincr_exciton_monomer *mono, int n_pai
                 count_launch(stream, "ex_precondition");
                 ex_dots_dev_kernel<<<m_max, 256, 0, stream>>>(dM.p, ns, dV.p, dT.p, dc.p);
                 count_launch(stream, "ex_dots");
-                ex_orth_update_dev_kernel<<<ceil_div(ns, 256), 256, 0, stream>>>(dM.p, ns, dV.p, dc.p, dT.p, dPart.p);
-                count_launch(stream, "ex_orth_update");
+                ex_orth_part_kernel<<<dim3(xb, S_orth), 256, 0, stream>>>(dM.p, ns, dV.p, dc.p, dPart2.p);
+                count_launch(stream, "ex_orth_part");
+                ex_orth_finish_kernel<<<xb, 256, 0, stream>>>(ns, S_orth, dPart2.p, dT.p, dPart.p);
+                count_launch(stream, "ex_orth_finish");
                 ex_norm_finish_kernel<<<1, 32, 0, stream>>>(ceil_div(ns, 256), dPart.p, dNrm.p + nr);
                 count_launch(stream, "ex_norm_finish");
                 ex_append_kernel<<<ceil_div(ns, 256), 256, 0, stream>>>(ns, dNrm.p + nr, dM.p, cap, dT.p, dV.p);
