@@ -41,7 +41,7 @@ namespace {
 constexpr int SC_T = 256, SC_W = SC_T / 32;
 constexpr int SC_NMAX = 256;           // orbitals (and atoms) per system
 constexpr int SC_DIIS = 8;             // DIIS history
-constexpr int SC_FP32_MAX = 60;        // FP32 iterations at most before the FP64 phase
+constexpr int SC_FP32_MAX = 20;        // FP32 iterations at most before the FP64 phase
 constexpr double SC_FP32_SWITCH = 1e-5;
 constexpr double SC_PROXIMITY = 30.0;  // bohr: Slater-Koster pairs farther apart are zero (tincr's PROXIMITY_CUTOFF)
 constexpr int SC_SLOTS_PER_SM = 2;
