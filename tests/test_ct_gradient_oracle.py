@@ -1,0 +1,136 @@
+"""CT-state gradient: the oracle's restatement of tincr's amplitude projection and the host side of
+`fmo.ct_state_gradients` (no GPU).
+
+* known answer: with dimer orbitals that are the two monomers' orbitals side by side (any column
+  order), the projected amplitudes are the CT amplitudes placed at the dimer's occupied orbitals of
+  the hole monomer and virtual orbitals of the electron monomer, in both hole directions;
+* the host projection of `fmo.ct_amplitudes_in_pair` equals the oracle's on a water-ammonia pair
+  with its SCC ground state (1e-13), for pair-TDA-like amplitudes and tincr's single-orbital CT;
+* two monomers beyond the Slater-Koster range: the dimer's orbitals stay on one monomer each, and
+  the projected amplitudes vanish on every orbital of the wrong monomer (1e-13);
+* tincr's single-orbital convention (HOMO - k of the hole, LUMO + l of the electron);
+* the oracle's CT gradient is translation invariant (sum over atoms below 1e-12)."""
+
+import numpy as np
+import pytest
+
+from cases import golden
+from oracle import ct_gradient as OCT
+from tincr_gb300 import fmo
+from tincr_gb300 import groundstate as gs
+from tincr_gb300.params import NUMBERS
+
+
+def test_projection_known_answer():
+    rng = np.random.default_rng(7)
+    ni, nj, oi, oj = 5, 4, 2, 1
+    c_i = np.linalg.qr(rng.standard_normal((ni, ni)))[0]
+    c_j = np.linalg.qr(rng.standard_normal((nj, nj)))[0]
+    # dimer orbitals: occupied (I occ, J occ) then virtual (J virt, I virt), in a shuffled order
+    cols = [("i", k) for k in range(oi)] + [("j", k) for k in range(oj)]
+    cols = [cols[1], cols[2], cols[0]]
+    vcols = [("j", k) for k in range(oj, nj)] + [("i", k) for k in range(oi, ni)]
+    vcols = vcols[::-1]
+    c_ij = np.zeros((ni + nj, ni + nj))
+    for n, (m, k) in enumerate(cols + vcols):
+        if m == "i":
+            c_ij[:ni, n] = c_i[:, k]
+        else:
+            c_ij[ni:, n] = c_j[:, k]
+    s = np.eye(ni + nj)
+    s_i, s_j = OCT.monomer_pair_overlaps(c_i, c_j, c_ij, s, ni)
+    no = oi + oj
+    for hole_i in (True, False):
+        oh, vl = (oi, nj - oj) if hole_i else (oj, ni - oi)
+        x_ct = rng.standard_normal((oh, vl))
+        x = OCT.ct_amplitudes_in_pair(s_i, s_j, oi, oj, no, x_ct, hole_i)
+        want = np.zeros((no, ni + nj - no))
+        hm, lm = ("i", "j") if hole_i else ("j", "i")
+        lo = oj if hole_i else oi
+        for a, col in enumerate(cols):
+            for b, vcol in enumerate(vcols):
+                if col[0] == hm and vcol[0] == lm:
+                    want[a, b] = x_ct[col[1], vcol[1] - lo]
+        assert np.abs(x - want).max() < 1e-14
+
+
+def _pair(shift_bohr):
+    mols = []
+    for name in ("h2o", "ammonia"):
+        d = golden(name)
+        mols.append((np.array([NUMBERS[s] for s in d["symbols"]], np.int32), d["xyz_angstrom"] / 0.529177210903))
+    z = np.concatenate([mols[0][0], mols[1][0]])
+    x = np.concatenate([mols[0][1], mols[1][1] + np.array([0.0, 0.0, shift_bohr])])
+    mono = np.concatenate([np.zeros(len(mols[0][0]), int), np.ones(len(mols[1][0]), int)])
+    mons = fmo.build_monomers(z, x, mono, lc=True)
+    sy = gs.build_system(z, x, lc=True)
+    g = gs.run_scc(sy, tol=1e-11,
+                   p_start=np.block([[mons[0].ground.p, np.zeros((mons[0].system.n_orbs, mons[1].system.n_orbs))],
+                                     [np.zeros((mons[1].system.n_orbs, mons[0].system.n_orbs)), mons[1].ground.p]]))
+    assert g.converged
+    return mons, sy, g
+
+
+def test_host_projection_matches_oracle():
+    mons, sy, g = _pair(5.5)
+    mi, mj = mons
+    rng = np.random.default_rng(3)
+    for hole_i in (True, False):
+        mh, ml = (mi, mj) if hole_i else (mj, mi)
+        for x_ct in (rng.standard_normal((mh.system.n_occ, ml.system.n_virt)),
+                     fmo.ct_unit_amplitudes(mons, mh.index, ml.index, 1, 0)):
+            got = fmo.ct_amplitudes_in_pair(mi, mj, sy, g, x_ct, hole_i)
+            s_i, s_j = OCT.monomer_pair_overlaps(mi.ground.orbs, mj.ground.orbs, g.orbs, g.s, mi.system.n_orbs)
+            want = OCT.ct_amplitudes_in_pair(s_i, s_j, mi.system.n_occ, mj.system.n_occ, sy.n_occ, x_ct, hole_i)
+            assert got.shape == (sy.n_occ, sy.n_virt)
+            assert np.abs(got - want).max() < 1e-13
+
+
+def test_projection_of_separated_monomers_stays_on_them():
+    mons, sy, g = _pair(60.0)
+    mi, mj = mons
+    ni = mi.system.n_orbs
+    on_i = np.abs(g.orbs[:ni, :]).max(axis=0) > 1e-10
+    on_j = np.abs(g.orbs[ni:, :]).max(axis=0) > 1e-10
+    assert not np.any(on_i & on_j)          # every dimer orbital lives on one monomer
+    no = sy.n_occ
+    x_ct = fmo.ct_unit_amplitudes(mons, 0, 1, 0, 0)
+    x = fmo.ct_amplitudes_in_pair(mi, mj, sy, g, x_ct, True)
+    assert np.abs(x[on_j[:no], :]).max() < 1e-13
+    assert np.abs(x[:, on_i[no:]]).max() < 1e-13
+    assert abs(np.linalg.norm(x) - 1.0) < 1e-3  # the monomers' orbitals barely change in the dimer
+
+
+def test_unit_amplitudes_follow_tincr():
+    mons, _, _ = _pair(5.5)
+    for h, l, k, m in ((0, 1, 0, 0), (0, 1, 2, 1), (1, 0, 1, 1)):
+        a = fmo.ct_unit_amplitudes(mons, h, l, k, m)
+        b = OCT.ct_unit_amplitudes(mons[h].system.n_occ, mons[l].system.n_virt, k, m)
+        assert np.array_equal(a, b)
+        assert a[mons[h].system.n_occ - 1 - k, m] == 1.0 and a.sum() == 1.0
+    with pytest.raises(ValueError):   # water has two virtual orbitals
+        fmo.ct_unit_amplitudes(mons, 1, 0, 0, 2)
+    with pytest.raises(ValueError):
+        fmo.ct_unit_amplitudes(mons, 0, 1, mons[0].system.n_occ, 0)
+
+
+def test_oracle_ct_gradient_is_translation_invariant():
+    """The CT gradient contracts derivatives of S, H0 and gamma, which depend on relative positions
+    only: summed over the atoms it vanishes in each direction."""
+    mons, sy, g = _pair(5.5)
+    mi, mj = mons
+    x_ct = np.random.default_rng(1).standard_normal((mi.system.n_occ, mj.system.n_virt))
+    x_ct /= np.linalg.norm(x_ct)
+    grad, x = OCT.ct_state_gradient(sy, g, mi.system.n_orbs, mi.ground.orbs, mj.ground.orbs, mi.system.n_occ,
+                                    mj.system.n_occ, x_ct, 0.4, True)
+    assert grad.shape == (3 * sy.n_atoms,) and np.abs(grad).max() > 1e-3
+    assert np.abs(grad.reshape(-1, 3).sum(axis=0)).max() < 1e-12
+
+
+def test_ct_gradient_argument_order():
+    """tincr's ct_gradient_new takes the lower monomer index first; checked before any GPU work."""
+    mons, _, _ = _pair(5.5)
+    with pytest.raises(ValueError):
+        fmo.ct_gradient(None, mons, 1, 0, 0, 0, 0.3, True)
+    grads, states = fmo.ct_state_gradients(None, mons, [])
+    assert grads == [] and states == {}

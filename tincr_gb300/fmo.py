@@ -639,3 +639,216 @@ def exciton_states(ctx, setup, results, labels, n_le, n_ct, n_roots=10, tol=1e-4
     if want_matrix:
         out["matrix"] = mat
     return out
+
+
+# ----------------------------------------------------------------------------------------------
+# CT-state gradients and the exciton-state gradient
+# ----------------------------------------------------------------------------------------------
+
+def pair_ground_states(ctx, monomers, pairs, scc_tol=1e-10):
+    """Full SCC ground states (orbitals, density, S, gammas, converged Fock matrix) of the dimers of
+    `pairs` ((i, j) with monomer i's atoms first), which the CT-state gradients differentiate: one
+    batched GPU SCC (`tincr_scc_batch`) from the block-diagonal density of the two monomers, then the
+    dimers that missed the tolerance again with a level shift of 0.5 and up to 1000 iterations (the
+    starts and retry of the exciton set-up's dimer SCCs).  tincr takes a real pair's SCC from its FMO
+    pair SCC (src/fmo/scc/pair.rs) and runs the SCC of an ESD pair for its CT gradient
+    (`new_charge_transfer_pair_gradient`, src/fmo/gradients/ct_state_new.rs:56-58).  Returns
+    {(i, j): (System, GroundState)}; a dimer without a converged ground state raises (tincr panics,
+    pair.rs:234-240)."""
+    from . import scc as gscc
+    pairs = list(dict.fromkeys((int(i), int(j)) for i, j in pairs))
+    if not pairs:
+        return {}
+    systems, starts = [], []
+    for i, j in pairs:
+        mi, mj = monomers[i], monomers[j]
+        systems.append(gs.build_system(np.concatenate([mi.system.numbers, mj.system.numbers]),
+                                       np.concatenate([mi.system.xyz, mj.system.xyz]), lc=mi.system.lc,
+                                       r_lr=mi.system.r_lr))
+        ni, nj = mi.system.n_orbs, mj.system.n_orbs
+        p = np.zeros((ni + nj, ni + nj))
+        p[:ni, :ni] = mi.ground.p
+        p[ni:, ni:] = mj.ground.p
+        starts.append(p)
+    grounds, _ = gscc.scc_batch(ctx, systems, tol=scc_tol, p_start=starts)
+    retry = [k for k, g in enumerate(grounds) if not g.converged]
+    if retry:
+        again, _ = gscc.scc_batch(ctx, [systems[k] for k in retry], tol=scc_tol, max_iter=1000, level_shift=0.5,
+                                  p_start=[starts[k] for k in retry])
+        for k, g in zip(retry, again):
+            grounds[k] = g
+    bad = [pairs[k] for k, g in enumerate(grounds) if not g.converged]
+    if bad:
+        raise RuntimeError("dimer SCC not converged to %g for the CT gradient of pairs %s" % (scc_tol, bad[:10]))
+    return {key: (sy, g) for key, sy, g in zip(pairs, systems, grounds)}
+
+
+def ct_amplitudes_in_pair(mi, mj, sy, g, x_ct, hole_i):
+    """The CT amplitudes x_ct [n_occ(hole), n_virt(electron)], given over the hole monomer's occupied
+    and the electron monomer's virtual orbitals, in the orbitals of the dimer (monomer mi's atoms
+    first; hole on mi when hole_i): X_IJ = S_h,IJ[occ_h, occ_IJ]^T x_ct S_l,IJ[virt_l, virt_IJ] with
+    S_I,IJ = C_I^T S[I rows, :] C_IJ (`Pair::prepare_charge_transfer_gradient`,
+    src/fmo/gradients/ct_state_new.rs:115-150; overlaps of src/fmo/lcmo/hamiltonian.rs:61-64).
+    Returns X_IJ [n_occ(IJ), n_virt(IJ)]."""
+    ni = mi.system.n_orbs
+    no = sy.n_occ
+    s_h = mi if hole_i else mj
+    s_l = mj if hole_i else mi
+    rows_h = slice(0, ni) if hole_i else slice(ni, None)
+    rows_l = slice(ni, None) if hole_i else slice(0, ni)
+    oh, ol = s_h.system.n_occ, s_l.system.n_occ
+    x_ct = np.asarray(x_ct, dtype=np.float64).reshape(oh, -1)
+    occ_h = s_h.ground.orbs[:, :oh].T @ g.s[rows_h, :] @ g.orbs[:, :no]         # [oh, no]
+    virt_l = s_l.ground.orbs[:, ol:].T @ g.s[rows_l, :] @ g.orbs[:, no:]        # [vl, nv]
+    return occ_h.T @ (x_ct @ virt_l)
+
+
+def ct_state_gradients(ctx, monomers, terms, pair_states=None, n_streams=8, contexts=None, variant="reference",
+                       precision=_lib.PREC_FP64, scc_tol=1e-10):
+    """Excitation-energy gradients of charge-transfer states, each the TDA gradient of its dimer at
+    one state (tincr's `new_charge_transfer_pair_gradient`, src/fmo/gradients/ct_state_new.rs:13-70,
+    and `ct_gradient_new`, src/fmo/lcmo/ct_gradient.rs:116-172: `Pair::tda_gradient_lc(0)`,
+    src/fmo/gradients/excited_state.rs:1470-1713, with ci_eigenvalues = [E_CT] and the CT amplitudes
+    in the dimer's orbitals as ci_coefficients).
+
+    terms: list of (hole, electron, x_ct, energy): monomer indices, amplitudes
+    [n_occ(hole), n_virt(electron)] and the CT energy.  The dimer of a term is the pair
+    (min, max) of its monomers, lower index first; its ground state comes from `pair_states` (as
+    `pair_ground_states` returns) or from one batched GPU SCC of all dimers needed.  The gradients
+    run on the GPU (`tincr_tda_set_states` + `tincr_gradient`), spread over `n_streams` contexts
+    driven by host threads like `le_gradients`; `precision` is the precision the amplitudes were
+    solved with.  Returns (list of gradients [3 (N_I + N_J)] in the dimer's atom order, pair_states)."""
+    from concurrent.futures import ThreadPoolExecutor
+    from . import gradients as GR
+    from . import tda as T
+    keys = [(min(int(h), int(l)), max(int(h), int(l))) for h, l, _, _ in terms]
+    need = [k for k in dict.fromkeys(keys) if pair_states is None or k not in pair_states]
+    states = dict(pair_states or {})
+    if need:
+        states.update(pair_ground_states(ctx, monomers, need, scc_tol))
+    out = [None] * len(terms)
+    if not terms:
+        return out, states
+    own = contexts is None
+    ctxs = contexts if contexts is not None else [_lib.Context(0) for _ in range(min(n_streams, len(terms)))]
+    lanes = min(len(ctxs), len(terms))
+
+    def work(lane):
+        c = ctxs[lane]
+        for k in range(lane, len(terms), lanes):
+            h, l, x_ct, energy = terms[k]
+            i, j = keys[k]
+            sy, g = states[(i, j)]
+            x = ct_amplitudes_in_pair(monomers[i], monomers[j], sy, g, x_ct, int(h) == i)
+            es = T.ExcitedStateSystem.from_ground_state(c, sy, g)
+            es.prepare_tda()
+            es.set_states(np.array([float(energy)]), x.reshape(-1, 1))
+            es.set_precision(precision)
+            out[k] = GR.GradientSystem(es, sy, g).tda_gradient(0, variant)
+
+    try:
+        with ThreadPoolExecutor(max_workers=lanes) as ex:
+            for f in [ex.submit(work, lane) for lane in range(lanes)]:
+                f.result()
+    finally:
+        if own:
+            for c in ctxs:
+                c.close()
+    return out, states
+
+
+def ct_unit_amplitudes(monomers, hole, electron, ct_ind_h, ct_ind_l):
+    """Amplitudes of the single orbital pair HOMO - ct_ind_h (hole monomer) -> LUMO + ct_ind_l
+    (electron monomer), tincr's CT basis states of `create_diab_basis` (src/fmo/lcmo/basis.rs:24-141)
+    as `Pair::prepare_ct_state` writes them (src/fmo/gradients/excited_state.rs:1176-1179)."""
+    oh, vl = monomers[hole].system.n_occ, monomers[electron].system.n_virt
+    if not (0 <= int(ct_ind_h) < oh and 0 <= int(ct_ind_l) < vl):
+        raise ValueError("ct_unit_amplitudes: orbital offsets (%d, %d) outside %d occupied / %d virtual orbitals"
+                         % (int(ct_ind_h), int(ct_ind_l), oh, vl))
+    x = np.zeros((oh, vl))
+    x[oh - 1 - int(ct_ind_h), int(ct_ind_l)] = 1.0
+    return x
+
+
+def ct_gradient(ctx, monomers, index_i, index_j, ct_ind_i, ct_ind_j, ct_energy, hole_i, **kw):
+    """tincr's `SuperSystem::ct_gradient_new(index_i, index_j, ct_ind_i, ct_ind_j, ct_energy, hole_i)`
+    (src/fmo/lcmo/ct_gradient.rs:116-172) for index_i < index_j: the gradient [3 (N_i + N_j)]
+    (monomer index_i's atoms first) of the single-orbital CT state hole -> electron, the hole on
+    index_i when hole_i (orbital HOMO - ct_ind_i of index_i -> LUMO + ct_ind_j of index_j), else on
+    index_j (HOMO - ct_ind_j of index_j -> LUMO + ct_ind_i of index_i), with excitation energy
+    ct_energy.  For an ESD pair tincr's routine takes the non-LC gradient (`tda_gradient_nolc`, :169)
+    with the pair's SCC call commented out (:164-165); here every pair has its dimer SCC and the
+    gradient follows the LC setting, as `new_charge_transfer_pair_gradient` does for both pair types.
+    Keyword arguments go to `ct_state_gradients`."""
+    if not index_i < index_j:
+        raise ValueError("ct_gradient: index_i < index_j (tincr's argument order)")
+    if hole_i:
+        term = (index_i, index_j, ct_unit_amplitudes(monomers, index_i, index_j, ct_ind_i, ct_ind_j), ct_energy)
+    else:
+        term = (index_j, index_i, ct_unit_amplitudes(monomers, index_j, index_i, ct_ind_j, ct_ind_i), ct_energy)
+    grads, _ = ct_state_gradients(ctx, monomers, [term], **kw)
+    return grads[0]
+
+
+def exciton_basis(labels, results, n_mon, n_le, n_ct, ct_pairs):
+    """The diabatic basis of `exciton_states` as a list: ("LE", monomer, root) for the n_le roots of
+    every monomer, then for every CT pair (i, j) and root n < n_ct the states ("CT", i, j, n) and
+    ("CT", j, i, n) (hole, electron, root; src/fmo/lcmo/basis.rs:180-238).  Returns the list and a
+    dict (hole, electron) -> batch TDA result of that CT direction."""
+    ct_of = {}
+    for k, lab in enumerate(labels):
+        if lab[0] == "CT":
+            ct_of[(lab[1], lab[2])] = results[k]
+    basis = [("LE", m, r) for m in range(n_mon) for r in range(n_le)]
+    for i, j in ct_pairs:
+        for n in range(n_ct):
+            basis.append(("CT", i, j, n))
+            basis.append(("CT", j, i, n))
+    return basis, ct_of
+
+
+def exciton_gradient(ctx, setup, results, labels, n_le, n_ct, vector, threshold=0.05, contexts=None,
+                     precision=_lib.PREC_FP64, variant="reference", scc_tol=1e-10, pair_states=None):
+    """Gradient of an exciton state's excitation energy, tincr's `SuperSystem::fmo_cis_gradient`
+    (src/fmo/lcmo/cis_gradient.rs:10-166) over the basis of `exciton_states`: for every basis state
+    whose coefficient in `vector` exceeds `threshold` in magnitude, c^2 times that state's gradient,
+    added on its atoms.  An LE state contributes its monomer's TDA gradient (`le_gradients`,
+    cis_gradient.rs:118-126), a CT state the gradient of its dimer at that state
+    (`ct_state_gradients`, the pair-TDA CT state with its amplitudes and energy, as
+    `new_charge_transfer_pair_gradient` takes them).  tincr's routine expands the state in the
+    single-orbital CT basis of `create_diab_basis` and reads the eigenvectors from properties that
+    neither exciton Hamiltonian stores (basis.rs:445-446), so it cannot run as written; this one
+    uses the basis the energies come from.  No CPHF term is added (tincr adds
+    `calculate_cphf_correction` only in its numerical CT test, src/fmo/gradients/numerical.rs:120).
+
+    Returns (gradient [3 N_total] in the aggregate's atom order, number of LE terms, number of CT
+    terms, pair_states)."""
+    mons = setup.monomers
+    n_mon = len(mons)
+    vector = np.asarray(vector, dtype=np.float64)
+    basis, ct_of = exciton_basis(labels, results, n_mon, n_le, n_ct, setup.ct_pairs)
+    if len(basis) != len(vector):
+        raise ValueError("exciton_gradient: vector of %d entries for a basis of %d states" % (len(vector), len(basis)))
+    offs = np.concatenate([[0], np.cumsum([m.system.n_atoms for m in mons])])
+    le_part, n_le_terms, _ = exciton_le_gradient(mons, results, vector, n_le, threshold=threshold,
+                                                 contexts=contexts, precision=precision, variant=variant)
+    terms, weights = [], []
+    for b, c in enumerate(vector):
+        st = basis[b]
+        if st[0] != "CT" or abs(c) <= threshold:
+            continue
+        _, h, l, n = st
+        r = ct_of[(h, l)]
+        oh = mons[h].system.n_occ
+        x = np.asarray(r["coefficients"])[:, n].reshape(oh, -1)
+        terms.append((h, l, x, float(np.asarray(r["energies"])[n])))
+        weights.append(float(c) ** 2)
+    grads, pair_states = ct_state_gradients(ctx, mons, terms, pair_states=pair_states, contexts=contexts,
+                                            variant=variant, precision=precision, scc_tol=scc_tol)
+    grad = le_part.copy()
+    for (h, l, _, _), w, gct in zip(terms, weights, grads):
+        i, j = min(h, l), max(h, l)
+        ni = 3 * int(offs[i + 1] - offs[i])
+        grad[3 * offs[i]:3 * offs[i + 1]] += w * gct[:ni]
+        grad[3 * offs[j]:3 * offs[j + 1]] += w * gct[ni:]
+    return grad, n_le_terms, len(terms), pair_states
