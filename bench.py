@@ -519,8 +519,9 @@ def run_fmo(args, ctx):
 
     def fmo_step(prec):
         """Batched LE / CT TDA; the exciton Hamiltonian over those states and its lowest 10 roots;
-        then the gradient of S1, the lowest LE root of the aggregate (its LE gradient, c = 1: the
-        CT and coupling terms of an exciton-state gradient are not built)."""
+        then the gradient of S1, the lowest LE root of the aggregate (its LE gradient, c = 1; the
+        lowest exciton state's gradient with its CT terms is measured after the steps,
+        `exciton_gradient_measure`)."""
         rc, r = fmo.solve_batch(ctx, inst, FMO_MAX_ITER, FMO_TOL, prec)
         t_batch = ctx.last_timing()[0] / 1e3
         ex = fmo.exciton_states(ctx, setup, r, labels, FMO_N_LE, FMO_N_CT, n_roots=FMO_N_EXCITON, tol=FMO_EX_TOL,
