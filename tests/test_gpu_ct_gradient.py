@@ -8,6 +8,7 @@ the same CT amplitudes (the GPU batch TDA, FP64, converged to 1e-8):
 * every CT direction's lowest pair-TDA state: amplitudes in the dimer's orbitals within 1e-12 of the
   oracle's projection, gradient within 1e-9 Eh/bohr; summed over the atoms it vanishes to 1e-5
   (tincr's same-element SK derivative orientation) and, in the "exact" variant, to 1e-8;
+* the same without the long-range correction;
 * tincr's `ct_gradient_new` form (single orbital pair, hole on the second monomer);
 * the exciton-state gradient of the lowest exciton state: the LE part (`exciton_le_gradient`) plus
   c^2 times the oracle's gradient of every CT basis state, within 1e-9 Eh/bohr."""
@@ -38,7 +39,7 @@ def _oracle(mons, states, h, l, x_ct, energy):
     sy, g = states[(i, j)]
     mi, mj = mons[i], mons[j]
     return OCT.ct_state_gradient(sy, g, mi.system.n_orbs, mi.ground.orbs, mj.ground.orbs, mi.system.n_occ,
-                                 mj.system.n_occ, x_ct, energy, h == i)
+                                 mj.system.n_occ, x_ct, energy, h == i, lc=sy.lc)
 
 
 def _ct_terms(c, res, root=0):
@@ -72,6 +73,19 @@ def test_ct_state_gradients_match_oracle(gpu_ctx, solved):
     ge, _ = fmo.ct_state_gradients(gpu_ctx, mons, terms[:2], pair_states=states, variant="exact", n_streams=2)
     for gr in ge:
         assert np.abs(gr.reshape(-1, 3).sum(axis=0)).max() < 1e-8
+
+
+def test_ct_state_gradients_without_lc(gpu_ctx):
+    c = fmo_case(3, 1, 1, lc=False)
+    rc, res = fmo.solve_batch(gpu_ctx, c["instances"], 150, 1e-8, _lib.PREC_FP64)
+    assert rc == _lib.OK
+    mons = c["monomers"]
+    terms = _ct_terms(c, res)
+    grads, states = fmo.ct_state_gradients(gpu_ctx, mons, terms, n_streams=3)
+    assert not states[(0, 1)][0].lc
+    for (h, l, x, e), gr in zip(terms, grads):
+        want, _ = _oracle(mons, states, h, l, x, e)
+        assert np.abs(gr - want).max() < 1e-9, (h, l)
 
 
 def test_ct_gradient_single_orbital_pair(gpu_ctx, solved):

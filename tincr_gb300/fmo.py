@@ -320,46 +320,73 @@ def solve_batch_sharded(ctx, instances, world, rank, allgather=None, solver=None
     return worst_status(p[1] for p in parts), full
 
 
+def run_gradient_jobs(jobs, n_streams=8, contexts=None, variant="reference"):
+    """Excitation-energy gradients of independent systems on the GPU.  jobs: list of (system, ground
+    state, energies [k], coefficients [o*v, k], state, precision): the roots of each system are
+    installed with `tincr_tda_set_states` (tincr's `set_ci_eigenvalues` / `set_ci_coefficients`) and
+    `tincr_gradient` gives the gradient of root `state`.  The jobs are spread over `n_streams`
+    contexts (or `contexts`), each driven by its own host thread, which take the next job from a
+    shared list ordered by system size, largest first, so that their kernels overlap on the device
+    and the longest jobs start first.  Returns a list of [3 N] arrays in job order."""
+    import threading
+    from concurrent.futures import ThreadPoolExecutor
+    from . import gradients as GR
+    from . import tda as T
+    out = [None] * len(jobs)
+    if not jobs:
+        return out
+    own = contexts is None
+    ctxs = contexts if not own else [_lib.Context(0) for _ in range(min(n_streams, len(jobs)))]
+    lanes = min(len(ctxs), len(jobs))
+    order = sorted(range(len(jobs)), key=lambda k: -jobs[k][0].n_orbs)
+    lock = threading.Lock()
+    nxt = [0]
+
+    def work(lane):
+        c = ctxs[lane]
+        while True:
+            with lock:
+                if nxt[0] >= len(order):
+                    return
+                k = order[nxt[0]]
+                nxt[0] += 1
+            sy, g, e, x, state, prec = jobs[k]
+            es = T.ExcitedStateSystem.from_ground_state(c, sy, g)
+            es.prepare_tda()
+            es.set_states(np.atleast_1d(np.asarray(e, dtype=np.float64)), np.asarray(x, dtype=np.float64))
+            es.set_precision(prec)
+            out[k] = GR.GradientSystem(es, sy, g).tda_gradient(int(state), variant)
+
+    try:
+        with ThreadPoolExecutor(max_workers=lanes) as ex:
+            for f in [ex.submit(work, lane) for lane in range(lanes)]:
+                f.result()
+    finally:
+        if own:
+            for c in ctxs:
+                c.close()
+    return out
+
+
 def le_gradients(monomers, results, states, n_streams=8, variant="reference", contexts=None,
                  precision=_lib.PREC_FP64):
     """Excitation-energy gradients of locally excited states, the LE terms of tincr's FMO exciton
     gradient (`SuperSystem::fmo_cis_gradient`, src/fmo/lcmo/cis_gradient.rs:118-126, which adds
     c^2 * `Monomer::tda_gradient_lc(n)` per contributing LE state; src/fmo/gradients/excited_state.rs:
     299-542).  For monomer k the gradient of root states[k] of results[k] (its batch TDA result) is
-    computed on the GPU; the monomers are spread over `n_streams` contexts, each driven by its own
-    host thread (tincr runs the monomers on rayon threads), so their kernels overlap on the device.
+    computed on the GPU (`run_gradient_jobs`: the monomers spread over `n_streams` contexts, each
+    driven by its own host thread, as tincr runs the monomers on rayon threads).
 
     `precision` is the precision the results were solved with; the gradients' contractions follow it.
     Entries of `states` that are None are skipped.  Returns a list of [3 N_k] arrays (Hartree/bohr,
     atom order of the monomer) or None."""
-    from concurrent.futures import ThreadPoolExecutor
-    from . import gradients as GR
-    from . import tda as T
-    own = contexts is None
-    ctxs = contexts if contexts is not None else [_lib.Context(0) for _ in range(n_streams)]
-    n_streams = min(len(ctxs), max(1, sum(1 for x in states if x is not None)))
+    ks = [k for k in range(len(monomers)) if states[k] is not None]
+    jobs = [(monomers[k].system, monomers[k].ground, results[k]["energies"], results[k]["coefficients"],
+             int(states[k]), precision) for k in ks]
+    got = run_gradient_jobs(jobs, n_streams=n_streams, contexts=contexts, variant=variant)
     out = [None] * len(monomers)
-
-    def work(lane):
-        ctx = ctxs[lane]
-        for k in range(lane, len(monomers), n_streams):
-            if states[k] is None:
-                continue
-            m = monomers[k]
-            es = T.ExcitedStateSystem.from_ground_state(ctx, m.system, m.ground)
-            es.prepare_tda()
-            es.set_states(results[k]["energies"], results[k]["coefficients"])
-            es.set_precision(precision)
-            out[k] = GR.GradientSystem(es, m.system, m.ground).tda_gradient(int(states[k]), variant)
-
-    try:
-        with ThreadPoolExecutor(max_workers=n_streams) as ex:
-            for f in [ex.submit(work, lane) for lane in range(n_streams)]:
-                f.result()
-    finally:
-        if own:
-            for c in ctxs:
-                c.close()
+    for k, g in zip(ks, got):
+        out[k] = g
     return out
 
 
@@ -703,6 +730,19 @@ def ct_amplitudes_in_pair(mi, mj, sy, g, x_ct, hole_i):
     return occ_h.T @ (x_ct @ virt_l)
 
 
+def _ct_jobs(monomers, terms, states, precision):
+    """Gradient jobs (`run_gradient_jobs`) of CT terms (hole, electron, x_ct, energy): the dimer
+    (lower monomer index first), its ground state from `states`, the CT energy and the amplitudes in
+    the dimer's orbitals as its one root."""
+    jobs = []
+    for h, l, x_ct, energy in terms:
+        i, j = min(int(h), int(l)), max(int(h), int(l))
+        sy, g = states[(i, j)]
+        x = ct_amplitudes_in_pair(monomers[i], monomers[j], sy, g, x_ct, int(h) == i)
+        jobs.append((sy, g, np.array([float(energy)]), x.reshape(-1, 1), 0, precision))
+    return jobs
+
+
 def ct_state_gradients(ctx, monomers, terms, pair_states=None, n_streams=8, contexts=None, variant="reference",
                        precision=_lib.PREC_FP64, scc_tol=1e-10):
     """Excitation-energy gradients of charge-transfer states, each the TDA gradient of its dimer at
@@ -715,46 +755,15 @@ def ct_state_gradients(ctx, monomers, terms, pair_states=None, n_streams=8, cont
     [n_occ(hole), n_virt(electron)] and the CT energy.  The dimer of a term is the pair
     (min, max) of its monomers, lower index first; its ground state comes from `pair_states` (as
     `pair_ground_states` returns) or from one batched GPU SCC of all dimers needed.  The gradients
-    run on the GPU (`tincr_tda_set_states` + `tincr_gradient`), spread over `n_streams` contexts
-    driven by host threads like `le_gradients`; `precision` is the precision the amplitudes were
-    solved with.  Returns (list of gradients [3 (N_I + N_J)] in the dimer's atom order, pair_states)."""
-    from concurrent.futures import ThreadPoolExecutor
-    from . import gradients as GR
-    from . import tda as T
+    run on the GPU (`run_gradient_jobs`); `precision` is the precision the amplitudes were solved
+    with.  Returns (list of gradients [3 (N_I + N_J)] in the dimer's atom order, pair_states)."""
     keys = [(min(int(h), int(l)), max(int(h), int(l))) for h, l, _, _ in terms]
     need = [k for k in dict.fromkeys(keys) if pair_states is None or k not in pair_states]
     states = dict(pair_states or {})
     if need:
         states.update(pair_ground_states(ctx, monomers, need, scc_tol))
-    out = [None] * len(terms)
-    if not terms:
-        return out, states
-    own = contexts is None
-    ctxs = contexts if contexts is not None else [_lib.Context(0) for _ in range(min(n_streams, len(terms)))]
-    lanes = min(len(ctxs), len(terms))
-
-    def work(lane):
-        c = ctxs[lane]
-        for k in range(lane, len(terms), lanes):
-            h, l, x_ct, energy = terms[k]
-            i, j = keys[k]
-            sy, g = states[(i, j)]
-            x = ct_amplitudes_in_pair(monomers[i], monomers[j], sy, g, x_ct, int(h) == i)
-            es = T.ExcitedStateSystem.from_ground_state(c, sy, g)
-            es.prepare_tda()
-            es.set_states(np.array([float(energy)]), x.reshape(-1, 1))
-            es.set_precision(precision)
-            out[k] = GR.GradientSystem(es, sy, g).tda_gradient(0, variant)
-
-    try:
-        with ThreadPoolExecutor(max_workers=lanes) as ex:
-            for f in [ex.submit(work, lane) for lane in range(lanes)]:
-                f.result()
-    finally:
-        if own:
-            for c in ctxs:
-                c.close()
-    return out, states
+    jobs = _ct_jobs(monomers, terms, states, precision)
+    return run_gradient_jobs(jobs, n_streams=n_streams, contexts=contexts, variant=variant), states
 
 
 def ct_unit_amplitudes(monomers, hole, electron, ct_ind_h, ct_ind_l):
@@ -812,14 +821,16 @@ def exciton_gradient(ctx, setup, results, labels, n_le, n_ct, vector, threshold=
     """Gradient of an exciton state's excitation energy, tincr's `SuperSystem::fmo_cis_gradient`
     (src/fmo/lcmo/cis_gradient.rs:10-166) over the basis of `exciton_states`: for every basis state
     whose coefficient in `vector` exceeds `threshold` in magnitude, c^2 times that state's gradient,
-    added on its atoms.  An LE state contributes its monomer's TDA gradient (`le_gradients`,
-    cis_gradient.rs:118-126), a CT state the gradient of its dimer at that state
-    (`ct_state_gradients`, the pair-TDA CT state with its amplitudes and energy, as
-    `new_charge_transfer_pair_gradient` takes them).  tincr's routine expands the state in the
-    single-orbital CT basis of `create_diab_basis` and reads the eigenvectors from properties that
-    neither exciton Hamiltonian stores (basis.rs:445-446), so it cannot run as written; this one
-    uses the basis the energies come from.  No CPHF term is added (tincr adds
-    `calculate_cphf_correction` only in its numerical CT test, src/fmo/gradients/numerical.rs:120).
+    added on its atoms.  An LE state contributes its monomer's TDA gradient at that root
+    (cis_gradient.rs:118-126), a CT state the gradient of its dimer at that state (the pair-TDA CT
+    state with its amplitudes and energy, as `new_charge_transfer_pair_gradient` takes them; the
+    dimers' ground states from `pair_states` or one batched GPU SCC).  All terms form one job list
+    for `run_gradient_jobs`.  tincr's routine expands the state in the single-orbital CT basis of
+    `create_diab_basis` and reads the eigenvectors from properties that neither exciton Hamiltonian
+    stores (basis.rs:445-446), so it cannot run as written; this one uses the basis the energies come
+    from.  No CPHF term is added, as in `fmo_cis_gradient` (tincr adds `calculate_cphf_correction` in
+    its Ehrenfest gradient, src/dynamics/helpers.rs:248, and its numerical CT test,
+    src/fmo/gradients/numerical.rs:120).
 
     Returns (gradient [3 N_total] in the aggregate's atom order, number of LE terms, number of CT
     terms, pair_states)."""
@@ -829,26 +840,37 @@ def exciton_gradient(ctx, setup, results, labels, n_le, n_ct, vector, threshold=
     basis, ct_of = exciton_basis(labels, results, n_mon, n_le, n_ct, setup.ct_pairs)
     if len(basis) != len(vector):
         raise ValueError("exciton_gradient: vector of %d entries for a basis of %d states" % (len(vector), len(basis)))
-    offs = np.concatenate([[0], np.cumsum([m.system.n_atoms for m in mons])])
-    le_part, n_le_terms, _ = exciton_le_gradient(mons, results, vector, n_le, threshold=threshold,
-                                                 contexts=contexts, precision=precision, variant=variant)
-    terms, weights = [], []
+    le_of = {lab[1]: results[k] for k, lab in enumerate(labels) if lab[0] == "LE"}
+    le_terms, ct_terms, ct_w = [], [], []
     for b, c in enumerate(vector):
-        st = basis[b]
-        if st[0] != "CT" or abs(c) <= threshold:
+        if abs(c) <= threshold:
             continue
-        _, h, l, n = st
-        r = ct_of[(h, l)]
-        oh = mons[h].system.n_occ
-        x = np.asarray(r["coefficients"])[:, n].reshape(oh, -1)
-        terms.append((h, l, x, float(np.asarray(r["energies"])[n])))
-        weights.append(float(c) ** 2)
-    grads, pair_states = ct_state_gradients(ctx, mons, terms, pair_states=pair_states, contexts=contexts,
-                                            variant=variant, precision=precision, scc_tol=scc_tol)
-    grad = le_part.copy()
-    for (h, l, _, _), w, gct in zip(terms, weights, grads):
+        st = basis[b]
+        if st[0] == "LE":
+            le_terms.append((st[1], st[2], float(c) ** 2))
+        else:
+            _, h, l, n = st
+            r = ct_of[(h, l)]
+            x = np.asarray(r["coefficients"])[:, n].reshape(mons[h].system.n_occ, -1)
+            ct_terms.append((h, l, x, float(np.asarray(r["energies"])[n])))
+            ct_w.append(float(c) ** 2)
+    keys = [(min(h, l), max(h, l)) for h, l, _, _ in ct_terms]
+    need = [k for k in dict.fromkeys(keys) if pair_states is None or k not in pair_states]
+    pair_states = dict(pair_states or {})
+    if need:
+        pair_states.update(pair_ground_states(ctx, mons, need, scc_tol))
+    # every term, LE and CT, in one job list over the same contexts
+    jobs = [(mons[m].system, mons[m].ground, le_of[mons[m].index]["energies"], le_of[mons[m].index]["coefficients"],
+             r, precision) for m, r, _ in le_terms]
+    jobs += _ct_jobs(mons, ct_terms, pair_states, precision)
+    grads = run_gradient_jobs(jobs, contexts=contexts, variant=variant)
+    offs = np.concatenate([[0], np.cumsum([m.system.n_atoms for m in mons])])
+    grad = np.zeros(3 * int(offs[-1]))
+    for (m, _, w), gle in zip(le_terms, grads):
+        grad[3 * offs[m]:3 * offs[m + 1]] += w * gle
+    for (h, l, _, _), w, gct in zip(ct_terms, ct_w, grads[len(le_terms):]):
         i, j = min(h, l), max(h, l)
         ni = 3 * int(offs[i + 1] - offs[i])
         grad[3 * offs[i]:3 * offs[i + 1]] += w * gct[:ni]
         grad[3 * offs[j]:3 * offs[j + 1]] += w * gct[ni:]
-    return grad, n_le_terms, len(terms), pair_states
+    return grad, len(le_terms), len(ct_terms), pair_states
