@@ -9,7 +9,9 @@
 * two monomers beyond the Slater-Koster range: the dimer's orbitals stay on one monomer each, and
   the projected amplitudes vanish on every orbital of the wrong monomer (1e-13);
 * tincr's single-orbital convention (HOMO - k of the hole, LUMO + l of the electron);
-* the oracle's CT gradient is translation invariant (sum over atoms below 1e-12)."""
+* the oracle's CT gradient is translation invariant (sum over atoms below 1e-12);
+* the host logic of `fmo.exciton_gradient`: the basis order of `exciton_states`, no terms below
+  the threshold, argument checks."""
 
 import numpy as np
 import pytest
@@ -134,3 +136,31 @@ def test_ct_gradient_argument_order():
         fmo.ct_gradient(None, mons, 1, 0, 0, 0, 0.3, True)
     grads, states = fmo.ct_state_gradients(None, mons, [])
     assert grads == [] and states == {}
+
+
+def test_exciton_basis_order_and_empty_gradient():
+    """The basis of `exciton_states` (n_le LE roots per monomer, then (i -> j, n), (j -> i, n) per CT
+    pair and root), and an exciton vector with every coefficient at or below the threshold: no term,
+    no GPU work, a zero gradient."""
+    from cases import fmo_case
+    c = fmo_case(3, 1, 1)
+    mons, labels = c["monomers"], c["labels"]
+    n_le, n_ct = 4, 1
+    results = [dict(energies=np.zeros(n_le if lab[0] == "LE" else n_ct), coefficients=None) for lab in labels]
+    basis, ct_of = fmo.exciton_basis(labels, results, len(mons), n_le, n_ct, c["pairs"])
+    assert len(basis) == len(mons) * n_le + 2 * n_ct * len(c["pairs"])
+    assert basis[:n_le] == [("LE", 0, r) for r in range(n_le)]
+    i, j = c["pairs"][0]
+    assert basis[len(mons) * n_le:len(mons) * n_le + 2] == [("CT", i, j, 0), ("CT", j, i, 0)]
+    assert set(ct_of) == {(a, b) for a, b in c["pairs"]} | {(b, a) for a, b in c["pairs"]}
+
+    class _Setup:
+        monomers, ct_pairs = mons, c["pairs"]
+
+    v = np.full(len(basis), 0.01)
+    grad, n_le_t, n_ct_t, states = fmo.exciton_gradient(None, _Setup, results, labels, n_le, n_ct, v)
+    assert n_le_t == 0 and n_ct_t == 0 and states == {}
+    assert grad.shape == (3 * sum(m.system.n_atoms for m in mons),) and not grad.any()
+    with pytest.raises(ValueError):
+        fmo.exciton_gradient(None, _Setup, results, labels, n_le, n_ct, v[:-1])
+    assert fmo.run_gradient_jobs([]) == []
