@@ -132,11 +132,17 @@ def test_oracle_ct_gradient_is_translation_invariant():
     assert np.abs(grad.reshape(-1, 3).sum(axis=0)).max() < 1e-12
 
 
-def test_ct_gradient_argument_order():
-    """tincr's ct_gradient_new takes the lower monomer index first; checked before any GPU work."""
-    mons, _, _ = _pair(5.5)
+def test_ct_gradient_argument_checks():
+    """tincr's ct_gradient_new takes the lower monomer index first; a CT term needs two monomers and
+    amplitudes over the hole's occupied x the electron's virtual orbitals; all checked before any
+    GPU work."""
+    mons, sy, g = _pair(5.5)
     with pytest.raises(ValueError):
         fmo.ct_gradient(None, mons, 1, 0, 0, 0, 0.3, True)
+    with pytest.raises(ValueError):
+        fmo.ct_state_gradients(None, mons, [(0, 0, np.zeros((4, 2)), 0.3)])
+    with pytest.raises(ValueError):   # water -> ammonia: 4 x 3 amplitudes, not 4 x 2
+        fmo.ct_amplitudes_in_pair(mons[0], mons[1], sy, g, np.zeros((4, 2)), True)
     grads, states = fmo.ct_state_gradients(None, mons, [])
     assert grads == [] and states == {}
 

@@ -724,7 +724,11 @@ def ct_amplitudes_in_pair(mi, mj, sy, g, x_ct, hole_i):
     rows_h = slice(0, ni) if hole_i else slice(ni, None)
     rows_l = slice(ni, None) if hole_i else slice(0, ni)
     oh, ol = s_h.system.n_occ, s_l.system.n_occ
-    x_ct = np.asarray(x_ct, dtype=np.float64).reshape(oh, -1)
+    x_ct = np.asarray(x_ct, dtype=np.float64)
+    if x_ct.size != oh * s_l.system.n_virt:
+        raise ValueError("ct_amplitudes_in_pair: %d amplitudes for %d occupied x %d virtual orbitals"
+                         % (x_ct.size, oh, s_l.system.n_virt))
+    x_ct = x_ct.reshape(oh, -1)
     occ_h = s_h.ground.orbs[:, :oh].T @ g.s[rows_h, :] @ g.orbs[:, :no]         # [oh, no]
     virt_l = s_l.ground.orbs[:, ol:].T @ g.s[rows_l, :] @ g.orbs[:, no:]        # [vl, nv]
     return occ_h.T @ (x_ct @ virt_l)
@@ -757,6 +761,8 @@ def ct_state_gradients(ctx, monomers, terms, pair_states=None, n_streams=8, cont
     `pair_ground_states` returns) or from one batched GPU SCC of all dimers needed.  The gradients
     run on the GPU (`run_gradient_jobs`); `precision` is the precision the amplitudes were solved
     with.  Returns (list of gradients [3 (N_I + N_J)] in the dimer's atom order, pair_states)."""
+    if any(int(h) == int(l) for h, l, _, _ in terms):
+        raise ValueError("ct_state_gradients: a CT term needs two different monomers")
     keys = [(min(int(h), int(l)), max(int(h), int(l))) for h, l, _, _ in terms]
     need = [k for k in dict.fromkeys(keys) if pair_states is None or k not in pair_states]
     states = dict(pair_states or {})
